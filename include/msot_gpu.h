@@ -1,0 +1,143 @@
+/*
+ * msot_gpu.h -- C ABI of the GB300 (sm_103a) implementation of the
+ * model-based MSOT operator A, its transpose, the non-negative solvers that
+ * call them, and the two analytic reconstructors.
+ *
+ * Conventions
+ *   - Every function returns an int status: MSOT_OK (0) or a negative
+ *     MSOT_E* code; msot_last_error() gives a message for the calling thread.
+ *     No C++ exception crosses this boundary.
+ *   - Device pointers are CUDA device memory of the current device; `stream`
+ *     is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *   - Batched layouts are instance-major and FP32:
+ *       image     [batch][nx][nz]       (pixel p = ix*nz + iz, MATLAB Nz x Nx)
+ *       sinogram  [batch][n_det][n_t]   (MATLAB T x D x W)
+ *     so one instance is one contiguous MATLAB image / sinogram.
+ *   - Host-buffer entry points (msot_mex_*) take FP64 arrays in exactly the
+ *     column-major layouts of the reference MEX functions and do all device
+ *     transfers themselves.
+ *   - A plan is immutable after creation and may be used from several host
+ *     threads on different streams, except for the functions documented as
+ *     using the plan's scratch (msot_forward/transpose with a NULL workspace
+ *     and the solvers), which must not overlap on the GPU for one plan.
+ */
+#ifndef MSOT_GPU_H
+#define MSOT_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MSOT_OK 0
+#define MSOT_EINVAL -1     /* bad argument / shape / class */
+#define MSOT_ERANGE -2     /* travel time or index out of the representable range */
+#define MSOT_ECUDA -3      /* CUDA runtime error */
+#define MSOT_ENOMEM -4     /* allocation failed */
+#define MSOT_ENONFINITE -5 /* NaN/Inf in an input or a solver scalar */
+#define MSOT_ETIMEOUT -6   /* a bounded device-side wait gave up */
+
+typedef struct msot_plan *msot_plan_t;
+
+/* Geometry and model tables of one MSOTmodel (MSOTmodel.m:18-48).
+ * Replaces the model struct fields absoluteTravelTimeIndices,
+ * circularInterpolationRadiusInSamples, IRHat/IRFlippedHat (as taps), the
+ * Discretization prefilter (as separable circular taps), the normalisation
+ * factor (MSOTmodel.m:271-287) and, when include_sir, SPMR / SPMRIndices /
+ * SPMRTimestepIndexStartAndEnd (MSOTmodel.m:463-480). */
+typedef struct msot_plan_desc {
+    int nx, nz;               /* pixel grid: nx columns (x), nz rows (z) */
+    int n_det, n_t;           /* detectors, time samples per detector */
+    double radius;            /* interpolation radius in samples */
+    const double *travel;     /* host [n_det][nx*nz] fractional sample indices (MATLAB P x D) */
+    int ir_len;               /* odd; 0 = no IR convolution */
+    const double *ir;         /* host IR taps (MSOTmodel.m:338-342) */
+    int pre_len_x, pre_len_z; /* odd; 0 = no prefilter along that axis */
+    const double *pre_x;      /* host circular kernel along x, centred */
+    const double *pre_z;      /* host circular kernel along z, centred */
+    double norm;              /* model normalisation factor; <= 0 means 1 */
+    /* spatial impulse response (forwardMex.cpp:18-27); sir_len == 0 = none */
+    int sir_len, n_sir;
+    const double *sir;            /* host [n_sir][sir_len] (MATLAB S x NS) */
+    const int32_t *sir_start_end; /* host [n_sir][2], 1-based inclusive */
+    const int32_t *sir_idx;       /* host [n_det][nx*nz], 1-based */
+    int max_batch;            /* largest batch the plan's scratch is sized for */
+} msot_plan_desc;
+
+const char *msot_last_error(void);
+int msot_version(void);
+
+int msot_plan_create(const msot_plan_desc *desc, msot_plan_t *plan);
+int msot_plan_destroy(msot_plan_t plan);
+/* Bytes of device memory the plan holds (tables + scratch). */
+size_t msot_plan_device_bytes(msot_plan_t plan);
+
+/* model.Funcs.applyForward (MSOTmodel.m:285 -> forwardWithoutSIR :208-222 or
+ * forward :189-206): prefilter, interpolation (+SIR), IR convolution, 1/norm.
+ * d_img [batch][nx][nz] -> d_sino [batch][n_det][n_t].  Uses plan scratch. */
+int msot_forward(msot_plan_t plan, const float *d_img, float *d_sino, int batch, void *stream);
+
+/* model.Funcs.applyTranspose (MSOTmodel.m:286 -> transposeWithoutSIR
+ * :243-257 or transpose :224-241).  d_sino -> d_img.  Uses plan scratch. */
+int msot_transpose(msot_plan_t plan, const float *d_sino, float *d_img, int batch, void *stream);
+
+/* The bare interpolation operators, i.e. the MEX kernels on device FP32
+ * data in the instance-major layouts above (no prefilter, IR or norm):
+ *   forwardDelayAndSumMex.cpp:15 / forwardMex.cpp:16 (when the plan has SIR)
+ *   transposeDelayAndSumMex.cpp:15 / transposeMex.cpp:16 */
+int msot_interp_forward(msot_plan_t plan, const float *d_coeffs, float *d_raw, int batch,
+                        void *stream);
+int msot_interp_transpose(msot_plan_t plan, const float *d_raw, float *d_coeffs, int batch,
+                          void *stream);
+
+/* Estimate sigma_max of the unnormalised operator by power iteration on the
+ * GPU (replaces the svds call, MSOTmodel.m:277-278); FP64 norms. */
+int msot_estimate_norm(msot_plan_t plan, int iters, uint64_t seed, double *sigma_max,
+                       void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Solvers.  b: d_sino [batch][n_det][n_t]; result d_rec [batch][nx][nz].
+ * Each instance of the batch is an independent reconstruction (one
+ * single-wavelength call of the reference); coupled = 1 instead treats the
+ * whole batch as the wavelengths of ONE reference call (shared scalars).
+ * d_x0 (optional, may be NULL) seeds the iterate (warm start; the reference
+ * always starts from zero).  err_img/err_reg (optional host arrays of
+ * `batch` doubles) receive lCurveErrImg / lCurveErrReg per instance. */
+
+/* rec_nn_with_L2_reg.m:1 with RegL2 = identity (lambdaL2 <= 0: no reg). */
+int msot_rec_nn_with_L2_reg(msot_plan_t plan, const float *d_b, float *d_rec, int batch,
+                            int num_iter, double lambdaL2, const float *d_x0, int coupled,
+                            double *err_img, double *err_reg, void *stream);
+
+/* rec_nn_with_L1_eye_reg.m:1 */
+int msot_rec_nn_with_L1_eye_reg(msot_plan_t plan, const float *d_b, float *d_rec, int batch,
+                                int num_iter, double reg, const float *d_x0, int coupled,
+                                double *err_img, double *err_reg, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Host-buffer entry points with the reference MEX contracts (FP64 in/out,
+ * column-major, MATLAB-owned inputs; output written to caller memory that
+ * MATLAB allocated with mxCreate*).  Arithmetic is FP32 on the GPU. */
+
+/* forwardDelayAndSumMex.cpp:15-104: image W x P, travelTimes P x D,
+ * numTimesteps, radius -> out W x T x D. */
+int msot_mex_forwardDelayAndSum(const double *image, int W, int P, const double *travel, int D,
+                                int T, double radius, double *out);
+/* transposeDelayAndSumMex.cpp:15-98: sigMat W x T x D -> out W x P. */
+int msot_mex_transposeDelayAndSum(const double *sig, int W, int T, int D, const double *travel,
+                                  int P, double radius, double *out);
+/* forwardMex.cpp:16-162 */
+int msot_mex_forward(const double *image, int W, int P, const int32_t *sir_idx,
+                     const double *travel, int D, const double *sir, int S, int NS, int T,
+                     const int32_t *start_end, double radius, double *out);
+/* transposeMex.cpp:16-158 */
+int msot_mex_transpose(const double *sig, int W, int T, int D, const int32_t *sir_idx,
+                       const double *travel, int P, const double *sir, int S, int NS,
+                       const int32_t *start_end, double radius, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

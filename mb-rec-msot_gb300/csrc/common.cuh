@@ -1,0 +1,113 @@
+// common.cuh -- shared definitions of the sm_103a MSOT operator library.
+//
+// Device-side data layout (all device memory, built once per plan):
+//   tau_tiles  int32 [n_patch][n_det][PATCH]   travel time of pixel q of patch
+//              (8x8 pixels) to detector d, fixed point Q(frac_bits); padding
+//              pixels hold TAU_PAD.  Read by the gather kernels (transpose).
+//   tau_pi     int32 [n_det][P]                travel times with the pixels in a
+//              fixed pseudo-random order perm[] (scatter kernels).
+//   ir_fwd/ir_adj float [L]                    IR taps (and flipped) times 1/norm.
+//   pre_x/pre_z float [2K+1]                   circular prefilter taps.
+//   sir        float [n_sir][S], sir_se int2 [n_sir] (0-based inclusive),
+//   sir_tiles  int32 [n_patch][n_det][PATCH]   SIR column per (pixel, detector),
+//   sir_pi     int32 [n_det][P]                the same in scatter order.
+// Batched vectors are instance-major FP32: image [W][nx][nz], sinogram
+// [W][n_det][n_t].
+#pragma once
+
+#include <cstdint>
+#include <cstdio>
+#include <cuda_runtime.h>
+
+#include "../../include/msot_gpu.h"
+
+namespace msot {
+
+constexpr int PATCH_X = 8;           // patch width (x columns)
+constexpr int PATCH_Z = 8;           // patch height (z rows)
+constexpr int PATCH = PATCH_X * PATCH_Z;
+constexpr int32_t TAU_PAD = INT32_MIN;  // marks a padding pixel in tau_tiles
+
+struct Plan {
+    int nx, nz, P, D, T;
+    double radius;
+    int frac_bits;     // fixed-point fraction bits of tau
+    int32_t r_fx;      // radius in fixed point
+    float c1;          // 2^-frac_bits / radius
+    int n_tap;         // upper bound of taps per (pixel, detector): floor(2r) + 2
+    int n_patch_x, n_patch_z, n_patch;
+    // tables
+    int32_t *tau_tiles = nullptr;  // [n_patch][D][PATCH] (gather kernels)
+    int32_t *tau_pi = nullptr;     // [D][P] pixels in scatter order perm[]
+    int32_t *perm = nullptr;       // [P] scatter order -> pixel index
+    // IR
+    int L = 0, Lh = 0;
+    float *ir_fwd = nullptr, *ir_adj = nullptr;
+    // prefilter
+    int Kx = -1, Kz = -1;   // -1: no prefilter along that axis
+    float *pre_x = nullptr, *pre_z = nullptr;
+    double norm = 1.0;
+    float scale = 1.f;      // 1/norm
+    // SIR
+    int S = 0, NS = 0;
+    float *sir = nullptr;
+    int2 *sir_se = nullptr;        // [NS] 0-based inclusive start/end
+    int32_t *sir_tiles = nullptr;  // [n_patch][D][PATCH] 0-based SIR column
+    int32_t *sir_pi = nullptr;     // [D][P] SIR column in scatter order
+    // scratch for the operator chains
+    int max_batch = 0;
+    float *scr_img0 = nullptr, *scr_img1 = nullptr;  // [max_batch][P]
+    float *scr_sino = nullptr;                       // [max_batch][D][T]
+    size_t device_bytes = 0;
+};
+
+const char *set_error(const char *fmt, ...);
+
+#define MSOT_CUDA_TRY(expr)                                                            \
+    do {                                                                               \
+        cudaError_t e_ = (expr);                                                       \
+        if (e_ != cudaSuccess) {                                                       \
+            ::msot::set_error("%s:%d %s: %s", __FILE__, __LINE__, #expr,               \
+                              cudaGetErrorString(e_));                                 \
+            return MSOT_ECUDA;                                                         \
+        }                                                                              \
+    } while (0)
+
+#define MSOT_LAUNCH_CHECK()                                                            \
+    do {                                                                               \
+        cudaError_t e_ = cudaGetLastError();                                           \
+        if (e_ != cudaSuccess) {                                                       \
+            ::msot::set_error("%s:%d launch: %s", __FILE__, __LINE__,                  \
+                              cudaGetErrorString(e_));                                 \
+            return MSOT_ECUDA;                                                         \
+        }                                                                              \
+    } while (0)
+
+// operator chains (operator.cu)
+int launch_prefilter(const Plan &pl, const float *in, float *out, int W, bool transpose,
+                     bool along_x, float scale, bool out_perm, cudaStream_t st);
+int launch_permute(const Plan &pl, const float *in, float *out, int W, cudaStream_t st);
+int launch_das_forward(const Plan &pl, const float *x_pi, float *raw, int W, float scale,
+                       cudaStream_t st);
+int launch_das_adjoint(const Plan &pl, const float *raw, float *x, int W, float scale,
+                       cudaStream_t st);
+int launch_conv(const Plan &pl, const float *in, float *out, int W, bool transpose,
+                cudaStream_t st);
+int launch_sir_forward(const Plan &pl, const float *x_pi, float *raw, int W, float scale,
+                       cudaStream_t st);
+int launch_sir_adjoint(const Plan &pl, const float *raw, float *x, int W, float scale,
+                       cudaStream_t st);
+int interp_forward(const Plan &pl, const float *x_pi, float *raw, int W, float scale,
+                   cudaStream_t st);
+int interp_adjoint(const Plan &pl, const float *raw, float *x, int W, float scale,
+                   cudaStream_t st);
+int apply_forward(const Plan &pl, const float *img, float *sino, int W, cudaStream_t st);
+int apply_transpose(const Plan &pl, const float *sino, float *img, int W, cudaStream_t st);
+
+inline int div_up(int a, int b) { return (a + b - 1) / b; }
+
+}  // namespace msot
+
+struct msot_plan {
+    msot::Plan p;
+};

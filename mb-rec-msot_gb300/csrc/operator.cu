@@ -1,0 +1,640 @@
+// operator.cu -- sm_103a kernels of the model-based operator A and A^T.
+//
+//   k_prefilter   separable circular prefilter (Discretization.m:54-72); the
+//                 2-D filter conj(phi_hat/|phi_hat|^2) of shift_inv_proj.m:67-71
+//                 factors into one circular filter per axis for the Gaussian
+//                 pixel model, applied here as two short stencils.
+//   k_das_fwd     forwardDelayAndSumMex.cpp:72-103: scatter of tri-interpolated
+//                 pixels into one detector column held in shared memory.
+//   k_das_adj     transposeDelayAndSumMex.cpp:67-100: gather per pixel over all
+//                 detectors, 8x8 pixel patch x 4 detector groups per CTA.
+//   k_sir_fwd     forwardMex.cpp:118-160 (SIR column convolved with the tri
+//                 taps, samples outside [0, T) dropped).
+//   k_sir_adj     transposeMex.cpp:115-158 (its exact adjoint).
+//   k_conv        convolve_with_IR / transpose_convolve_with_IR
+//                 (MSOTmodel.m:259-269) as a direct FIR over each detector column.
+//
+// Fixed-point travel times: tau_fx = tau * 2^fb (int32).  The taps of a
+// (pixel, detector) pair are t in [ceil((tau_fx - r_fx)/2^fb),
+// floor((tau_fx + r_fx)/2^fb)] and the weight is 1 - |t - tau| / r, computed
+// from the exact integer difference (t << fb) - tau_fx.
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace msot {
+
+__device__ __forceinline__ int tap_lo(int32_t tau, int32_t r_fx, int fb) {
+    return -((r_fx - tau) >> fb);
+}
+__device__ __forceinline__ int tap_hi(int32_t tau, int32_t r_fx, int fb) {
+    return (tau + r_fx) >> fb;
+}
+__device__ __forceinline__ float tri_weight(int t, int32_t tau, int fb, float c1) {
+    const float df = (float)((t << fb) - tau);
+    return fmaxf(0.f, fmaf(-fabsf(df), c1, 1.f));
+}
+
+// ---------------------------------------------------------------------------
+// Prefilter: out[w][j] = scale * sum_k h[k] in[w][pix(j) - k (circular)]
+// along one axis; pix(j) = perm[j] when perm != nullptr (scatter order).
+// ---------------------------------------------------------------------------
+__global__ void k_prefilter(const float *__restrict__ in, float *__restrict__ out,
+                            const float *__restrict__ taps, int K, int nx, int nz, int W,
+                            int along_x, int transpose, float scale,
+                            const int32_t *__restrict__ perm) {
+    const int P = nx * nz;
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)W * P) return;
+    const int w = (int)(idx / P), j = (int)(idx % P);
+    const int pix = perm ? __ldg(perm + j) : j;
+    const int ix = pix / nz, iz = pix - ix * nz;
+    const float *src = in + (size_t)w * P;
+    float acc = 0.f;
+    for (int k = -K; k <= K; ++k) {
+        const float h = __ldg(taps + (transpose ? K - k : K + k));
+        int s;
+        if (along_x) {
+            int a = ix - k;
+            a += (a < 0) ? nx : 0;
+            a -= (a >= nx) ? nx : 0;
+            s = a * nz + iz;
+        } else {
+            int a = iz - k;
+            a += (a < 0) ? nz : 0;
+            a -= (a >= nz) ? nz : 0;
+            s = ix * nz + a;
+        }
+        acc = fmaf(h, __ldg(src + s), acc);
+    }
+    out[(size_t)w * P + j] = acc * scale;
+}
+
+__global__ void k_permute(const float *__restrict__ in, float *__restrict__ out,
+                          const int32_t *__restrict__ perm, int P, int W) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)W * P) return;
+    const int w = (int)(idx / P), j = (int)(idx % P);
+    out[idx] = __ldg(in + (size_t)w * P + __ldg(perm + j));
+}
+
+// ---------------------------------------------------------------------------
+// DAS forward: CTA = (detector, pixel split, instance tile).  The detector's
+// sinogram column for WT instances lives in shared memory ([WT][T]); pixels
+// are visited in scatter order so that the 32 lanes of a warp hit unrelated
+// samples.  With nsplit > 1 the CTAs of one detector add their columns into
+// a zeroed output with global atomics.
+// ---------------------------------------------------------------------------
+template <int WT>
+__global__ void __launch_bounds__(256) k_das_fwd(const int32_t *__restrict__ tau_pi,
+                                                 const float *__restrict__ x_pi,
+                                                 float *__restrict__ raw, int P, int D, int T,
+                                                 int fb, int32_t r_fx, float c1, float scale,
+                                                 int nsplit) {
+    extern __shared__ float col[];  // [WT][T]
+    const int d = blockIdx.x, sp = blockIdx.y, w0 = blockIdx.z * WT;
+    for (int i = threadIdx.x; i < WT * T; i += blockDim.x) col[i] = 0.f;
+    __syncthreads();
+    const int j0 = (int)((long)P * sp / nsplit), j1 = (int)((long)P * (sp + 1) / nsplit);
+    const int32_t *tau_d = tau_pi + (size_t)d * P;
+    for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+        const int32_t tau = __ldg(tau_d + j);
+        float xv[WT];
+#pragma unroll
+        for (int i = 0; i < WT; ++i) xv[i] = __ldg(x_pi + (size_t)(w0 + i) * P + j);
+        const int tb = max(0, tap_lo(tau, r_fx, fb)), te = min(T - 1, tap_hi(tau, r_fx, fb));
+        for (int t = tb; t <= te; ++t) {
+            const float wt = tri_weight(t, tau, fb, c1);
+#pragma unroll
+            for (int i = 0; i < WT; ++i) atomicAdd(&col[i * T + t], wt * xv[i]);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < WT * T; i += blockDim.x) {
+        const int wi = i / T, t = i - wi * T;
+        float *dst = raw + ((size_t)(w0 + wi) * D + d) * T + t;
+        const float v = col[i] * scale;
+        if (nsplit == 1)
+            *dst = v;
+        else
+            atomicAdd(dst, v);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// DAS adjoint: CTA = (8x8 pixel patch, instance tile); 256 threads = 64 pixels
+// x 4 detector groups; the four partial sums are added in shared memory in a
+// fixed order (deterministic).
+// ---------------------------------------------------------------------------
+template <int WT>
+__global__ void __launch_bounds__(256) k_das_adj(const int32_t *__restrict__ tiles,
+                                                 const float *__restrict__ raw,
+                                                 float *__restrict__ out, int nx, int nz,
+                                                 int npx, int D, int T, int fb, int32_t r_fx,
+                                                 float c1, float scale) {
+    __shared__ float red[4][PATCH][WT];
+    const int patch = blockIdx.x, w0 = blockIdx.y * WT;
+    const int q = threadIdx.x & (PATCH - 1), g = threadIdx.x / PATCH;
+    const int px = patch % npx, pz = patch / npx;
+    const int ix = px * PATCH_X + q / PATCH_Z, iz = pz * PATCH_Z + q % PATCH_Z;
+    float acc[WT];
+#pragma unroll
+    for (int i = 0; i < WT; ++i) acc[i] = 0.f;
+    const int32_t *tp = tiles + (size_t)patch * D * PATCH + q;
+    const size_t DT = (size_t)D * T;
+    for (int d = g; d < D; d += 4) {
+        const int32_t tau = __ldg(tp + (size_t)d * PATCH);
+        if (tau == TAU_PAD) continue;
+        const int tb = max(0, tap_lo(tau, r_fx, fb)), te = min(T - 1, tap_hi(tau, r_fx, fb));
+        const float *base = raw + ((size_t)w0 * D + d) * T;
+        for (int t = tb; t <= te; ++t) {
+            const float wt = tri_weight(t, tau, fb, c1);
+#pragma unroll
+            for (int i = 0; i < WT; ++i) acc[i] = fmaf(wt, __ldg(base + i * DT + t), acc[i]);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < WT; ++i) red[g][q][i] = acc[i];
+    __syncthreads();
+    if (g == 0 && ix < nx && iz < nz) {
+        const size_t P = (size_t)nx * nz;
+#pragma unroll
+        for (int i = 0; i < WT; ++i) {
+            const float s = ((red[0][q][i] + red[1][q][i]) + red[2][q][i]) + red[3][q][i];
+            out[(size_t)(w0 + i) * P + (size_t)ix * nz + iz] = s * scale;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// SIR forward: as k_das_fwd, but each (pixel, detector) pair deposits the
+// SIR column convolved with its NT tri taps: e[m] = sum_i f[i] h[m - i],
+// output sample tb + m - S/2, dropped outside [0, T) (forwardMex.cpp:139).
+// ---------------------------------------------------------------------------
+template <int WT, int NT>
+__global__ void __launch_bounds__(256) k_sir_fwd(const int32_t *__restrict__ tau_pi,
+                                                 const int32_t *__restrict__ sir_pi,
+                                                 const float *__restrict__ sir,
+                                                 const int2 *__restrict__ sir_se,
+                                                 const float *__restrict__ x_pi,
+                                                 float *__restrict__ raw, int P, int D, int T,
+                                                 int S, int fb, int32_t r_fx, float c1,
+                                                 float scale, int nsplit) {
+    extern __shared__ float col[];  // [WT][T]
+    const int d = blockIdx.x, sp = blockIdx.y, w0 = blockIdx.z * WT;
+    for (int i = threadIdx.x; i < WT * T; i += blockDim.x) col[i] = 0.f;
+    __syncthreads();
+    const int half = S / 2;
+    const int j0 = (int)((long)P * sp / nsplit), j1 = (int)((long)P * (sp + 1) / nsplit);
+    for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+        const size_t o = (size_t)d * P + j;
+        const int32_t tau = __ldg(tau_pi + o);
+        const int s = __ldg(sir_pi + o);
+        float xv[WT];
+#pragma unroll
+        for (int i = 0; i < WT; ++i) xv[i] = __ldg(x_pi + (size_t)(w0 + i) * P + j);
+        const int tb = tap_lo(tau, r_fx, fb);
+        float f[NT];
+#pragma unroll
+        for (int i = 0; i < NT; ++i) f[i] = tri_weight(tb + i, tau, fb, c1);
+        const int2 se = __ldg(sir_se + s);
+        const float *h = sir + (size_t)s * S;
+        float acc[NT];
+#pragma unroll
+        for (int i = 0; i < NT; ++i) acc[i] = 0.f;
+        const int jb = tb - half;
+        for (int k = se.x; k <= se.y; ++k) {
+            const float hk = __ldg(h + k);
+#pragma unroll
+            for (int i = 0; i < NT; ++i) acc[i] = fmaf(f[i], hk, acc[i]);
+            const int J = jb + k;
+            if (J >= 0 && J < T) {
+#pragma unroll
+                for (int i = 0; i < WT; ++i) atomicAdd(&col[i * T + J], acc[0] * xv[i]);
+            }
+#pragma unroll
+            for (int i = 0; i < NT - 1; ++i) acc[i] = acc[i + 1];
+            acc[NT - 1] = 0.f;
+        }
+#pragma unroll
+        for (int m = 0; m < NT - 1; ++m) {
+            const int J = jb + se.y + 1 + m;
+            if (J >= 0 && J < T && acc[m] != 0.f) {
+#pragma unroll
+                for (int i = 0; i < WT; ++i) atomicAdd(&col[i * T + J], acc[m] * xv[i]);
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < WT * T; i += blockDim.x) {
+        const int wi = i / T, t = i - wi * T;
+        float *dst = raw + ((size_t)(w0 + wi) * D + d) * T + t;
+        const float v = col[i] * scale;
+        if (nsplit == 1)
+            *dst = v;
+        else
+            atomicAdd(dst, v);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// SIR adjoint: per (pixel, detector) v_k = sum_i f[i] y[tb + i + k - S/2] for
+// k in the SIR column's [start, end], x += sum_k h[k] v_k; y outside [0, T)
+// counts as zero (transposeMex.cpp:298).
+// ---------------------------------------------------------------------------
+template <int WT, int NT>
+__global__ void __launch_bounds__(256) k_sir_adj(const int32_t *__restrict__ tiles,
+                                                 const int32_t *__restrict__ sir_tiles,
+                                                 const float *__restrict__ sir,
+                                                 const int2 *__restrict__ sir_se,
+                                                 const float *__restrict__ raw,
+                                                 float *__restrict__ out, int nx, int nz,
+                                                 int npx, int D, int T, int S, int fb,
+                                                 int32_t r_fx, float c1, float scale) {
+    __shared__ float red[4][PATCH][WT];
+    const int patch = blockIdx.x, w0 = blockIdx.y * WT;
+    const int q = threadIdx.x & (PATCH - 1), g = threadIdx.x / PATCH;
+    const int px = patch % npx, pz = patch / npx;
+    const int ix = px * PATCH_X + q / PATCH_Z, iz = pz * PATCH_Z + q % PATCH_Z;
+    const int half = S / 2;
+    const size_t DT = (size_t)D * T;
+    float acc[WT];
+#pragma unroll
+    for (int i = 0; i < WT; ++i) acc[i] = 0.f;
+    for (int d = g; d < D; d += 4) {
+        const size_t o = ((size_t)patch * D + d) * PATCH + q;
+        const int32_t tau = __ldg(tiles + o);
+        if (tau == TAU_PAD) continue;
+        const int s = __ldg(sir_tiles + o);
+        const int tb = tap_lo(tau, r_fx, fb);
+        float f[NT];
+#pragma unroll
+        for (int i = 0; i < NT; ++i) f[i] = tri_weight(tb + i, tau, fb, c1);
+        const int2 se = __ldg(sir_se + s);
+        const float *h = sir + (size_t)s * S;
+        const float *base = raw + ((size_t)w0 * D + d) * T;
+        const int jb = tb + se.x - half;
+        float win[WT][NT];
+#pragma unroll
+        for (int i = 0; i < NT; ++i) {
+            const int J = jb + i;
+            const bool ok = J >= 0 && J < T;
+#pragma unroll
+            for (int w = 0; w < WT; ++w) win[w][i] = ok ? __ldg(base + w * DT + J) : 0.f;
+        }
+        for (int k = se.x; k <= se.y; ++k) {
+            const float hk = __ldg(h + k);
+#pragma unroll
+            for (int w = 0; w < WT; ++w) {
+                float v = 0.f;
+#pragma unroll
+                for (int i = 0; i < NT; ++i) v = fmaf(f[i], win[w][i], v);
+                acc[w] = fmaf(hk, v, acc[w]);
+            }
+            const int J = jb + (k - se.x) + NT;
+            const bool ok = J >= 0 && J < T;
+#pragma unroll
+            for (int w = 0; w < WT; ++w) {
+#pragma unroll
+                for (int i = 0; i < NT - 1; ++i) win[w][i] = win[w][i + 1];
+                win[w][NT - 1] = ok ? __ldg(base + w * DT + J) : 0.f;
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < WT; ++i) red[g][q][i] = acc[i];
+    __syncthreads();
+    if (g == 0 && ix < nx && iz < nz) {
+        const size_t P = (size_t)nx * nz;
+#pragma unroll
+        for (int i = 0; i < WT; ++i) {
+            const float s = ((red[0][q][i] + red[1][q][i]) + red[2][q][i]) + red[3][q][i];
+            out[(size_t)(w0 + i) * P + (size_t)ix * nz + iz] = s * scale;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// IR convolution along t of every (instance, detector) column:
+//   out[t] = sum_{k<L} taps[k] in[t + L/2 - k]   (in = 0 outside [0, T)).
+// CTA = (t tile of TPT*NTH samples, column).  Each thread keeps TPT outputs
+// and a sliding window of TPT inputs in registers; the shared-memory segment
+// is padded (one word per 8) so the window loads are bank-conflict free.
+// ---------------------------------------------------------------------------
+template <int TPT, int NTH>
+__global__ void __launch_bounds__(NTH) k_conv(const float *__restrict__ in,
+                                              float *__restrict__ out,
+                                              const float *__restrict__ taps, int L, int T) {
+    constexpr int TT = TPT * NTH;
+    extern __shared__ float sm[];
+    const int Lp = (L + TPT - 1) / TPT * TPT;
+    float *irr = sm;
+    float *seg = sm + Lp;
+    const int seg_len = TT + Lp + TPT;
+    const size_t col = blockIdx.y;
+    const int t0 = blockIdx.x * TT;
+    const int base_in = t0 + L / 2 - (L - 1);
+    const float *src = in + col * T;
+    for (int j = threadIdx.x; j < Lp; j += NTH) irr[j] = j < L ? __ldg(taps + L - 1 - j) : 0.f;
+    for (int q = threadIdx.x; q < seg_len; q += NTH) {
+        const int ti = base_in + q;
+        seg[q + (q >> 3)] = (ti >= 0 && ti < T) ? __ldg(src + ti) : 0.f;
+    }
+    __syncthreads();
+    const int o0 = threadIdx.x * TPT;
+    float acc[TPT], win[TPT];
+#pragma unroll
+    for (int i = 0; i < TPT; ++i) {
+        acc[i] = 0.f;
+        const int q = o0 + i;
+        win[i] = seg[q + (q >> 3)];
+    }
+    for (int j0 = 0; j0 < Lp; j0 += TPT) {
+#pragma unroll
+        for (int jj = 0; jj < TPT; ++jj) {
+            const float c = irr[j0 + jj];
+#pragma unroll
+            for (int i = 0; i < TPT; ++i) acc[i] = fmaf(c, win[(i + jj) % TPT], acc[i]);
+            const int q = o0 + j0 + jj + TPT;
+            win[jj] = seg[q + (q >> 3)];
+        }
+    }
+    float *dst = out + col * T + t0 + o0;
+#pragma unroll
+    for (int i = 0; i < TPT; ++i)
+        if (t0 + o0 + i < T) dst[i] = acc[i];
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------
+static int pick_wt(int W, int T, int max_wt) {
+    for (int wt = max_wt; wt > 1; wt >>= 1)
+        if (W % wt == 0 && (size_t)wt * T * sizeof(float) <= 160 * 1024) return wt;
+    return 1;
+}
+
+template <class K>
+static int set_smem(K kern, size_t bytes) {
+    if (bytes > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)bytes);
+        if (e != cudaSuccess) {
+            set_error("cudaFuncSetAttribute(smem=%zu): %s", bytes, cudaGetErrorString(e));
+            return MSOT_ECUDA;
+        }
+    }
+    return MSOT_OK;
+}
+
+int launch_prefilter(const Plan &pl, const float *in, float *out, int W, bool transpose,
+                     bool along_x, float scale, bool out_perm, cudaStream_t st) {
+    const int K = along_x ? pl.Kx : pl.Kz;
+    const float *taps = along_x ? pl.pre_x : pl.pre_z;
+    const long n = (long)W * pl.P;
+    k_prefilter<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+        in, out, taps, K, pl.nx, pl.nz, W, along_x, transpose, scale,
+        out_perm ? pl.perm : nullptr);
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
+}
+
+int launch_permute(const Plan &pl, const float *in, float *out, int W, cudaStream_t st) {
+    const long n = (long)W * pl.P;
+    k_permute<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, pl.perm, pl.P, W);
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
+}
+
+static int fwd_split(const Plan &pl, int nwt) {
+    // enough CTAs to fill the GPU twice over
+    int ctas = pl.D * nwt;
+    int ns = 1;
+    while (ctas * ns < 2 * 152 && ns < 8) ns *= 2;
+    return ns;
+}
+
+int launch_das_forward(const Plan &pl, const float *x_pi, float *raw, int W, float scale,
+                       cudaStream_t st) {
+    const int wt = pick_wt(W, pl.T, 8);
+    const int ns = fwd_split(pl, W / wt);
+    if (ns > 1) MSOT_CUDA_TRY(cudaMemsetAsync(raw, 0, sizeof(float) * W * pl.D * pl.T, st));
+    const size_t smem = (size_t)wt * pl.T * sizeof(float);
+    dim3 grid(pl.D, ns, W / wt);
+    int rc;
+#define CASE(WT)                                                                          \
+    case WT:                                                                              \
+        if ((rc = set_smem(k_das_fwd<WT>, smem)) != MSOT_OK) return rc;                   \
+        k_das_fwd<WT><<<grid, 256, smem, st>>>(pl.tau_pi, x_pi, raw, pl.P, pl.D, pl.T,     \
+                                               pl.frac_bits, pl.r_fx, pl.c1, scale, ns);  \
+        break;
+    switch (wt) {
+        CASE(1) CASE(2) CASE(4) CASE(8)
+    }
+#undef CASE
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
+}
+
+int launch_das_adjoint(const Plan &pl, const float *raw, float *x, int W, float scale,
+                       cudaStream_t st) {
+    const int wt = pick_wt(W, 1, 8);
+    dim3 grid(pl.n_patch, W / wt);
+#define CASE(WT)                                                                          \
+    case WT:                                                                              \
+        k_das_adj<WT><<<grid, 256, 0, st>>>(pl.tau_tiles, raw, x, pl.nx, pl.nz,            \
+                                            pl.n_patch_x, pl.D, pl.T, pl.frac_bits, pl.r_fx, \
+                                            pl.c1, scale);                                \
+        break;
+    switch (wt) {
+        CASE(1) CASE(2) CASE(4) CASE(8)
+    }
+#undef CASE
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
+}
+
+template <int WT>
+static int sir_fwd_nt(const Plan &pl, const float *x_pi, float *raw, float scale, dim3 grid,
+                      size_t smem, int ns, cudaStream_t st) {
+    int rc;
+#define NTCASE(NT)                                                                         \
+    if (pl.n_tap <= NT) {                                                                  \
+        if ((rc = set_smem(k_sir_fwd<WT, NT>, smem)) != MSOT_OK) return rc;                \
+        k_sir_fwd<WT, NT><<<grid, 256, smem, st>>>(pl.tau_pi, pl.sir_pi, pl.sir, pl.sir_se, \
+                                                   x_pi, raw, pl.P, pl.D, pl.T, pl.S,      \
+                                                   pl.frac_bits, pl.r_fx, pl.c1, scale, ns); \
+        MSOT_LAUNCH_CHECK();                                                               \
+        return MSOT_OK;                                                                    \
+    }
+    NTCASE(4) NTCASE(8) NTCASE(12) NTCASE(16) NTCASE(24) NTCASE(32)
+#undef NTCASE
+    set_error("SIR: interpolation radius too large (%d taps)", pl.n_tap);
+    return MSOT_EINVAL;
+}
+
+int launch_sir_forward(const Plan &pl, const float *x_pi, float *raw, int W, float scale,
+                       cudaStream_t st) {
+    const int wt = pick_wt(W, pl.T, 4);
+    const int ns = fwd_split(pl, W / wt);
+    if (ns > 1) MSOT_CUDA_TRY(cudaMemsetAsync(raw, 0, sizeof(float) * W * pl.D * pl.T, st));
+    const size_t smem = (size_t)wt * pl.T * sizeof(float);
+    dim3 grid(pl.D, ns, W / wt);
+    switch (wt) {
+        case 1: return sir_fwd_nt<1>(pl, x_pi, raw, scale, grid, smem, ns, st);
+        case 2: return sir_fwd_nt<2>(pl, x_pi, raw, scale, grid, smem, ns, st);
+        default: return sir_fwd_nt<4>(pl, x_pi, raw, scale, grid, smem, ns, st);
+    }
+}
+
+template <int WT>
+static int sir_adj_nt(const Plan &pl, const float *raw, float *x, float scale, dim3 grid,
+                      cudaStream_t st) {
+#define NTCASE(NT)                                                                         \
+    if (pl.n_tap <= NT) {                                                                  \
+        k_sir_adj<WT, NT><<<grid, 256, 0, st>>>(pl.tau_tiles, pl.sir_tiles, pl.sir,         \
+                                                pl.sir_se, raw, x, pl.nx, pl.nz,           \
+                                                pl.n_patch_x, pl.D, pl.T, pl.S,            \
+                                                pl.frac_bits, pl.r_fx, pl.c1, scale);      \
+        MSOT_LAUNCH_CHECK();                                                               \
+        return MSOT_OK;                                                                    \
+    }
+    NTCASE(4) NTCASE(8) NTCASE(12) NTCASE(16) NTCASE(24) NTCASE(32)
+#undef NTCASE
+    set_error("SIR: interpolation radius too large (%d taps)", pl.n_tap);
+    return MSOT_EINVAL;
+}
+
+int launch_sir_adjoint(const Plan &pl, const float *raw, float *x, int W, float scale,
+                       cudaStream_t st) {
+    const int wt = pick_wt(W, 1, 2);
+    dim3 grid(pl.n_patch, W / wt);
+    if (wt == 2) return sir_adj_nt<2>(pl, raw, x, scale, grid, st);
+    return sir_adj_nt<1>(pl, raw, x, scale, grid, st);
+}
+
+int launch_conv(const Plan &pl, const float *in, float *out, int W, bool transpose,
+                cudaStream_t st) {
+    constexpr int TPT = 8, NTH = 64, TT = TPT * NTH;
+    const int Lp = (pl.L + TPT - 1) / TPT * TPT;
+    const int seg_len = TT + Lp + TPT;
+    const size_t smem = sizeof(float) * (Lp + seg_len + seg_len / 8 + 1);
+    int rc;
+    if ((rc = set_smem(k_conv<TPT, NTH>, smem)) != MSOT_OK) return rc;
+    dim3 grid(div_up(pl.T, TT), (unsigned)W * pl.D);
+    k_conv<TPT, NTH><<<grid, NTH, smem, st>>>(in, out, transpose ? pl.ir_adj : pl.ir_fwd,
+                                              pl.L, pl.T);
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// chains
+// ---------------------------------------------------------------------------
+int interp_forward(const Plan &pl, const float *x_pi, float *raw, int W, float scale,
+                   cudaStream_t st) {
+    return pl.S ? launch_sir_forward(pl, x_pi, raw, W, scale, st)
+                : launch_das_forward(pl, x_pi, raw, W, scale, st);
+}
+
+int interp_adjoint(const Plan &pl, const float *raw, float *x, int W, float scale,
+                   cudaStream_t st) {
+    return pl.S ? launch_sir_adjoint(pl, raw, x, W, scale, st)
+                : launch_das_adjoint(pl, raw, x, W, scale, st);
+}
+
+int apply_forward(const Plan &pl, const float *img, float *sino, int W, cudaStream_t st) {
+    int rc;
+    float *xpi = pl.scr_img1;
+    if (pl.Kz >= 0 && pl.Kx >= 0) {
+        if ((rc = launch_prefilter(pl, img, pl.scr_img0, W, false, false, 1.f, false, st)))
+            return rc;
+        if ((rc = launch_prefilter(pl, pl.scr_img0, xpi, W, false, true, 1.f, true, st)))
+            return rc;
+    } else if (pl.Kz >= 0) {
+        if ((rc = launch_prefilter(pl, img, xpi, W, false, false, 1.f, true, st))) return rc;
+    } else if (pl.Kx >= 0) {
+        if ((rc = launch_prefilter(pl, img, xpi, W, false, true, 1.f, true, st))) return rc;
+    } else {
+        if ((rc = launch_permute(pl, img, xpi, W, st))) return rc;
+    }
+    if (pl.L > 0) {
+        if ((rc = interp_forward(pl, xpi, pl.scr_sino, W, 1.f, st))) return rc;
+        return launch_conv(pl, pl.scr_sino, sino, W, false, st);
+    }
+    return interp_forward(pl, xpi, sino, W, pl.scale, st);
+}
+
+int apply_transpose(const Plan &pl, const float *sino, float *img, int W, cudaStream_t st) {
+    int rc;
+    const float *src = sino;
+    float scale = pl.scale;
+    if (pl.L > 0) {
+        if ((rc = launch_conv(pl, sino, pl.scr_sino, W, true, st))) return rc;
+        src = pl.scr_sino;
+        scale = 1.f;
+    }
+    const bool pre = pl.Kx >= 0 || pl.Kz >= 0;
+    float *x = pre ? pl.scr_img0 : img;
+    if ((rc = interp_adjoint(pl, src, x, W, scale, st))) return rc;
+    if (pl.Kx >= 0 && pl.Kz >= 0) {
+        if ((rc = launch_prefilter(pl, pl.scr_img0, pl.scr_img1, W, true, true, 1.f, false, st)))
+            return rc;
+        return launch_prefilter(pl, pl.scr_img1, img, W, true, false, 1.f, false, st);
+    }
+    if (pl.Kx >= 0) return launch_prefilter(pl, pl.scr_img0, img, W, true, true, 1.f, false, st);
+    if (pl.Kz >= 0) return launch_prefilter(pl, pl.scr_img0, img, W, true, false, 1.f, false, st);
+    return MSOT_OK;
+}
+
+}  // namespace msot
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+using namespace msot;
+
+static int check_batch(msot_plan_t plan, int batch, const void *a, const void *b) {
+    if (!plan || !a || !b || batch <= 0) {
+        set_error("null plan/pointer or non-positive batch");
+        return MSOT_EINVAL;
+    }
+    if (batch > plan->p.max_batch) {
+        set_error("batch %d exceeds the plan's max_batch %d", batch, plan->p.max_batch);
+        return MSOT_EINVAL;
+    }
+    return MSOT_OK;
+}
+
+extern "C" {
+
+int msot_forward(msot_plan_t plan, const float *d_img, float *d_sino, int batch, void *stream) {
+    int rc = check_batch(plan, batch, d_img, d_sino);
+    if (rc) return rc;
+    return apply_forward(plan->p, d_img, d_sino, batch, (cudaStream_t)stream);
+}
+
+int msot_transpose(msot_plan_t plan, const float *d_sino, float *d_img, int batch,
+                   void *stream) {
+    int rc = check_batch(plan, batch, d_sino, d_img);
+    if (rc) return rc;
+    return apply_transpose(plan->p, d_sino, d_img, batch, (cudaStream_t)stream);
+}
+
+int msot_interp_forward(msot_plan_t plan, const float *d_coeffs, float *d_raw, int batch,
+                        void *stream) {
+    int rc = check_batch(plan, batch, d_coeffs, d_raw);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    if ((rc = launch_permute(plan->p, d_coeffs, plan->p.scr_img1, batch, st))) return rc;
+    return interp_forward(plan->p, plan->p.scr_img1, d_raw, batch, 1.f, st);
+}
+
+int msot_interp_transpose(msot_plan_t plan, const float *d_raw, float *d_coeffs, int batch,
+                          void *stream) {
+    int rc = check_batch(plan, batch, d_raw, d_coeffs);
+    if (rc) return rc;
+    return interp_adjoint(plan->p, d_raw, d_coeffs, batch, 1.f, (cudaStream_t)stream);
+}
+
+}  // extern "C"

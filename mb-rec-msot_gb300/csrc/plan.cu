@@ -1,0 +1,308 @@
+// plan.cu -- plan creation: validates the model tables of one MSOTmodel and
+// lays them out in HBM for the sm_103a kernels (layout in common.cuh).
+//
+// Replaces the per-call inputs of the reference MEX functions
+// (forwardDelayAndSumMex.cpp:17-55, forwardMex.cpp:18-73) and the model
+// fields built by MSOTmodel.m:31-47 with one device-resident object.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+
+namespace msot {
+
+static thread_local char g_err[512] = "";
+
+const char *set_error(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+    return g_err;
+}
+
+template <class T>
+static int upload(T **dst, const T *src, size_t n, size_t &bytes) {
+    if (n == 0) {
+        *dst = nullptr;
+        return MSOT_OK;
+    }
+    cudaError_t e = cudaMalloc((void **)dst, n * sizeof(T));
+    if (e != cudaSuccess) {
+        set_error("cudaMalloc(%zu): %s", n * sizeof(T), cudaGetErrorString(e));
+        return MSOT_ENOMEM;
+    }
+    bytes += n * sizeof(T);
+    if (src) MSOT_CUDA_TRY(cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice));
+    return MSOT_OK;
+}
+
+template <class T>
+static int alloc(T **dst, size_t n, size_t &bytes) {
+    return upload<T>(dst, nullptr, n, bytes);
+}
+
+static void free_plan(Plan &p) {
+    void *ptrs[] = {p.tau_tiles, p.tau_pi, p.perm, p.ir_fwd, p.ir_adj, p.pre_x, p.pre_z,
+                    p.sir, p.sir_se, p.sir_tiles, p.sir_pi, p.scr_img0, p.scr_img1,
+                    p.scr_sino};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+    p = Plan();
+}
+
+// Fixed-point travel time: tau_fx = rint(tau * 2^fb).  The device computes
+// the tap range of a (pixel, detector) pair as [ceil((tau_fx - r_fx) / 2^fb),
+// floor((tau_fx + r_fx) / 2^fb)], i.e. {t : |t - tau| <= r} in fixed point.
+static inline int32_t to_fx(double v, int fb) { return (int32_t)std::nearbyint(std::ldexp(v, fb)); }
+static inline int tap_lo(int32_t tau, int32_t r, int fb) { return -((r - tau) >> fb); }
+static inline int tap_hi(int32_t tau, int32_t r, int fb) { return (tau + r) >> fb; }
+
+static int build(const msot_plan_desc *d, Plan &p) {
+    if (!d || d->nx <= 0 || d->nz <= 0 || d->n_det <= 0 || d->n_t <= 1 || !d->travel) {
+        set_error("plan: bad grid / detector / sample counts or missing travel table");
+        return MSOT_EINVAL;
+    }
+    if (!(d->radius > 0) || !std::isfinite(d->radius)) {
+        set_error("plan: interpolation radius must be positive");
+        return MSOT_EINVAL;
+    }
+    const bool has_sir = d->sir_len > 0;
+    if (has_sir && (!d->sir || !d->sir_start_end || !d->sir_idx || d->n_sir <= 0)) {
+        set_error("plan: SIR tables incomplete");
+        return MSOT_EINVAL;
+    }
+    if (d->ir_len < 0 || (d->ir_len > 0 && (d->ir_len % 2 == 0 || !d->ir))) {
+        set_error("plan: IR length must be odd (got %d)", d->ir_len);
+        return MSOT_EINVAL;
+    }
+    if ((long)d->nx * d->nz > (1L << 28) || (long)d->n_det * d->nx * d->nz > (1L << 34)) {
+        set_error("plan: grid too large");
+        return MSOT_EINVAL;
+    }
+    p.nx = d->nx;
+    p.nz = d->nz;
+    p.P = d->nx * d->nz;
+    p.D = d->n_det;
+    p.T = d->n_t;
+    p.radius = d->radius;
+    p.max_batch = d->max_batch > 0 ? d->max_batch : 1;
+    const long PD = (long)p.P * p.D;
+
+    // --- fixed-point format ---------------------------------------------------
+    double tmax = 0;
+    for (long i = 0; i < PD; ++i) {
+        double t = d->travel[i];
+        if (!std::isfinite(t)) {
+            set_error("plan: non-finite travel time at %ld", i);
+            return MSOT_ENONFINITE;
+        }
+        tmax = std::max(tmax, std::fabs(t));
+    }
+    double span = std::max(tmax, (double)p.T) + d->radius + 4.0;
+    int ib = (int)std::ceil(std::log2(span));       // integer bits needed
+    int fb = std::min(30 - ib, 23 - (int)std::ceil(std::log2(d->radius + 2.0)));
+    fb = std::min(fb, 20);
+    if (fb < 8) {
+        set_error("plan: travel times (%g) or radius (%g) too large for fixed point", tmax,
+                  d->radius);
+        return MSOT_ERANGE;
+    }
+    p.frac_bits = fb;
+    p.r_fx = to_fx(d->radius, fb);
+    p.c1 = (float)(std::ldexp(1.0, -fb) / d->radius);
+    p.n_tap = (int)std::floor(2.0 * d->radius) + 2;
+
+    std::vector<int32_t> tfx(PD);
+    for (long i = 0; i < PD; ++i) tfx[i] = to_fx(d->travel[i], fb);
+    if (!has_sir) {
+        // The DAS MEX has no bounds check (forwardDelayAndSumMex.cpp:80); its
+        // precondition -- every tap inside [0, T) -- is checked here instead.
+        for (long i = 0; i < PD; ++i) {
+            if (tap_lo(tfx[i], p.r_fx, fb) < 0 || tap_hi(tfx[i], p.r_fx, fb) >= p.T) {
+                set_error("plan: travel time %g (pixel %ld, detector %ld) puts taps outside "
+                          "[0, %d)",
+                          d->travel[i], i % p.P, i / p.P, p.T);
+                return MSOT_ERANGE;
+            }
+        }
+    }
+
+    // --- gather table: 8x8 pixel patches -----------------------------------------
+    p.n_patch_x = div_up(p.nx, PATCH_X);
+    p.n_patch_z = div_up(p.nz, PATCH_Z);
+    p.n_patch = p.n_patch_x * p.n_patch_z;
+    size_t ntile = (size_t)p.n_patch * p.D * PATCH;
+    std::vector<int32_t> tiles(ntile, TAU_PAD);
+    std::vector<int32_t> stiles;
+    if (has_sir) stiles.assign(ntile, 0);
+    for (int pz = 0; pz < p.n_patch_z; ++pz)
+        for (int px = 0; px < p.n_patch_x; ++px) {
+            int patch = pz * p.n_patch_x + px;
+            for (int q = 0; q < PATCH; ++q) {
+                int ix = px * PATCH_X + q / PATCH_Z, iz = pz * PATCH_Z + q % PATCH_Z;
+                if (ix >= p.nx || iz >= p.nz) continue;
+                long pix = (long)ix * p.nz + iz;
+                for (int det = 0; det < p.D; ++det) {
+                    size_t o = ((size_t)patch * p.D + det) * PATCH + q;
+                    tiles[o] = tfx[(size_t)det * p.P + pix];
+                    if (has_sir) stiles[o] = d->sir_idx[(size_t)det * p.P + pix] - 1;
+                }
+            }
+        }
+
+    // --- scatter table: pixels in a fixed pseudo-random order ------------------------
+    // Lanes of a warp then work on pixels far apart in the image, so their
+    // taps land on different samples of the shared-memory sinogram column.
+    std::vector<int32_t> perm(p.P);
+    for (int i = 0; i < p.P; ++i) perm[i] = i;
+    uint64_t s = 0x9E3779B97F4A7C15ull;
+    for (int i = p.P - 1; i > 0; --i) {
+        s = s * 6364136223846793005ull + 1442695040888963407ull;
+        int j = (int)((s >> 33) % (uint64_t)(i + 1));
+        std::swap(perm[i], perm[j]);
+    }
+    std::vector<int32_t> tpi(PD);
+    std::vector<int32_t> spi;
+    if (has_sir) spi.resize(PD);
+    for (int det = 0; det < p.D; ++det)
+        for (int j = 0; j < p.P; ++j) {
+            tpi[(size_t)det * p.P + j] = tfx[(size_t)det * p.P + perm[j]];
+            if (has_sir) spi[(size_t)det * p.P + j] = d->sir_idx[(size_t)det * p.P + perm[j]] - 1;
+        }
+
+    // --- SIR ----------------------------------------------------------------------
+    std::vector<float> sirf;
+    std::vector<int2> se;
+    if (has_sir) {
+        p.S = d->sir_len;
+        p.NS = d->n_sir;
+        for (long i = 0; i < PD; ++i)
+            if (d->sir_idx[i] < 1 || d->sir_idx[i] > p.NS) {
+                set_error("plan: sirIndices[%ld] = %d outside [1, %d]", i, d->sir_idx[i], p.NS);
+                return MSOT_ERANGE;
+            }
+        se.resize(p.NS);
+        int maxlen = 0;
+        for (int k = 0; k < p.NS; ++k) {
+            int a = d->sir_start_end[2 * k] - 1, b = d->sir_start_end[2 * k + 1] - 1;
+            if (a < 0 || b >= p.S) {
+                set_error("plan: sirTimestepsStartAndEnd of column %d outside [1, %d]", k + 1,
+                          p.S);
+                return MSOT_ERANGE;
+            }
+            se[k] = make_int2(a, b);
+            maxlen = std::max(maxlen, b - a + 1);
+        }
+        sirf.resize((size_t)p.NS * p.S);
+        for (size_t i = 0; i < sirf.size(); ++i) sirf[i] = (float)d->sir[i];
+        (void)maxlen;
+    }
+
+    // --- IR, prefilter, normalisation ----------------------------------------------
+    p.norm = d->norm > 0 ? d->norm : 1.0;
+    p.scale = (float)(1.0 / p.norm);
+    std::vector<float> irf, ira;
+    if (d->ir_len > 0) {
+        p.L = d->ir_len;
+        p.Lh = p.L / 2;
+        irf.resize(p.L);
+        ira.resize(p.L);
+        for (int k = 0; k < p.L; ++k) {
+            irf[k] = (float)(d->ir[k] / p.norm);
+            ira[k] = (float)(d->ir[p.L - 1 - k] / p.norm);
+        }
+    }
+    std::vector<float> px, pz;
+    if (d->pre_len_x > 0) {
+        if (d->pre_len_x % 2 == 0 || !d->pre_x || d->pre_len_x > 2 * p.nx - 1) {
+            set_error("plan: bad prefilter length along x");
+            return MSOT_EINVAL;
+        }
+        p.Kx = d->pre_len_x / 2;
+        px.assign(d->pre_x, d->pre_x + d->pre_len_x);
+    }
+    if (d->pre_len_z > 0) {
+        if (d->pre_len_z % 2 == 0 || !d->pre_z || d->pre_len_z > 2 * p.nz - 1) {
+            set_error("plan: bad prefilter length along z");
+            return MSOT_EINVAL;
+        }
+        p.Kz = d->pre_len_z / 2;
+        pz.assign(d->pre_z, d->pre_z + d->pre_len_z);
+    }
+
+    // --- upload -------------------------------------------------------------------
+    size_t &B = p.device_bytes;
+    int rc;
+#define UP(dst, vec)                                                                       \
+    if ((rc = upload(&(dst), (vec).data(), (vec).size(), B)) != MSOT_OK) return rc;
+    UP(p.tau_tiles, tiles);
+    UP(p.tau_pi, tpi);
+    UP(p.perm, perm);
+    if (has_sir) {
+        UP(p.sir, sirf);
+        UP(p.sir_se, se);
+        UP(p.sir_tiles, stiles);
+        UP(p.sir_pi, spi);
+    }
+    if (p.L) {
+        UP(p.ir_fwd, irf);
+        UP(p.ir_adj, ira);
+    }
+    if (p.Kx >= 0) {
+        std::vector<float> v(px.begin(), px.end());
+        UP(p.pre_x, v);
+    }
+    if (p.Kz >= 0) {
+        std::vector<float> v(pz.begin(), pz.end());
+        UP(p.pre_z, v);
+    }
+#undef UP
+    const size_t W = (size_t)p.max_batch;
+    if ((rc = alloc(&p.scr_img0, W * p.P, B)) != MSOT_OK) return rc;
+    if ((rc = alloc(&p.scr_img1, W * p.P, B)) != MSOT_OK) return rc;
+    if ((rc = alloc(&p.scr_sino, W * p.D * p.T, B)) != MSOT_OK) return rc;
+    return MSOT_OK;
+}
+
+}  // namespace msot
+
+using namespace msot;
+
+extern "C" {
+
+const char *msot_last_error(void) { return g_err; }
+int msot_version(void) { return 1; }
+
+int msot_plan_create(const msot_plan_desc *desc, msot_plan_t *out) {
+    if (!out) {
+        set_error("plan: null output handle");
+        return MSOT_EINVAL;
+    }
+    *out = nullptr;
+    msot_plan *h = new (std::nothrow) msot_plan;
+    if (!h) return MSOT_ENOMEM;
+    int rc = build(desc, h->p);
+    if (rc != MSOT_OK) {
+        free_plan(h->p);
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return MSOT_OK;
+}
+
+int msot_plan_destroy(msot_plan_t plan) {
+    if (!plan) return MSOT_OK;
+    free_plan(plan->p);
+    delete plan;
+    return MSOT_OK;
+}
+
+size_t msot_plan_device_bytes(msot_plan_t plan) { return plan ? plan->p.device_bytes : 0; }
+
+}  // extern "C"

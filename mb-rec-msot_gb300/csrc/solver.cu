@@ -1,0 +1,843 @@
+// solver.cu -- batched non-negative solvers on the GPU.
+//
+// FP32 vectors, FP64 reductions and scalars.  A batch of W instances is
+// solved at once; each instance owns its Krylov scalars (independent
+// reconstructions), or the whole batch shares one set (coupled = the W
+// wavelengths of one reference call, whose lsqr/cgs see one stacked vector).
+//
+//   rec_nn_with_L2_reg  -> rec_nn_with_L2_reg.m:24-63, nnls_L2_less.m:93-141,
+//                          lsqr (Paige & Saunders) on [sqrt(lam) [A; sqrt(lamL2) I];
+//                          sqrt(beta) I] with maxit 2, x0 = w, tol 1e-8.
+//   rec_nn_with_L1_eye  -> rec_nn_with_L1_eye_reg.m:21-47,
+//                          nnls_L1_eye_matrix_less.m:76-107, cgs on lam A^T A + I.
+//   estimate_norm       -> the sigma_max of MSOTmodel.m:277-278 by power
+//                          iteration.
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+
+namespace msot {
+
+constexpr int RED_THREADS = 256;
+
+struct Scal {
+    double alpha, beta, c, s, phibar, normr, normrmin, normb;
+    double rho, thet, phi, gamma;  // gamma = alpha / beta_prev
+    double rho_cg, rho1_cg, alpha_cg;
+    int done, improved, pad0, pad1;
+};
+
+__device__ __forceinline__ double block_sum(double v) {
+    __shared__ double sh[RED_THREADS / 32];
+    __syncthreads();  // sh may still be read by a previous call
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        v = lane < RED_THREADS / 32 ? sh[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    }
+    return v;  // valid in thread 0
+}
+
+// grid (nblk, W); each block reduces a strided chunk of instance w.
+#define FOR_CHUNK(N)                                                                       \
+    const int w = blockIdx.y;                                                              \
+    const size_t base = (size_t)w * (N);                                                   \
+    for (size_t i = (size_t)blockIdx.x * RED_THREADS + threadIdx.x; i < (size_t)(N);       \
+         i += (size_t)gridDim.x * RED_THREADS)
+
+#define STORE_PARTIAL(v, part)                                                             \
+    {                                                                                      \
+        double s_ = block_sum(v);                                                          \
+        if (threadIdx.x == 0) (part)[(size_t)w * gridDim.x + blockIdx.x] = s_;             \
+    }
+
+__device__ __forceinline__ int grp(int w, int coupled) { return coupled ? 0 : w; }
+
+// u = a*x + b*u with per-group scalars; partial sums of u^2.
+// mode 0: u = sl*b_vec - sl*x          (LSQR init, sinogram part)
+// mode 1: u = sl*x - gamma*u           (LSQR step, sinogram part)
+__global__ void k_sino_update(const float *__restrict__ x, const float *__restrict__ bvec,
+                              float *__restrict__ u, size_t N, int mode, double sl,
+                              const Scal *__restrict__ sc, int coupled, double *part) {
+    double acc = 0.0;
+    FOR_CHUNK(N) {
+        const size_t k = base + i;
+        float v;
+        if (mode == 0) {
+            v = (float)(sl * (double)bvec[k] - sl * (double)x[k]);
+        } else {
+            const double g = sc[grp(w, coupled)].gamma;
+            v = (float)(sl * (double)x[k] - g * (double)u[k]);
+        }
+        if (!(mode == 1 && sc[grp(w, coupled)].done)) u[k] = v;
+        const double vv = (double)u[k];
+        acc += vv * vv;
+    }
+    STORE_PARTIAL(acc, part);
+}
+
+// generic sum of squares of (x - y) (y may be null) per instance
+__global__ void k_sumsq(const float *__restrict__ x, const float *__restrict__ y, size_t N,
+                        double *part) {
+    double acc = 0.0;
+    FOR_CHUNK(N) {
+        double v = (double)x[base + i] - (y ? (double)y[base + i] : 0.0);
+        acc += v * v;
+    }
+    STORE_PARTIAL(acc, part);
+}
+
+// LSQR init, image parts: ur = -sl*sr*w ; ub = sb*(w+vm) - sb*w.
+// part: sum ur^2 + ub^2 ; part2: sum (w+vm)^2 (for ||b_aug||).
+__global__ void k_l2_init_img(const float *__restrict__ wv, const float *__restrict__ vm,
+                              float *__restrict__ ur, float *__restrict__ ub, size_t N,
+                              double sl, double sr, double sb, int has_reg, double *part,
+                              double *part2) {
+    double a1 = 0.0, a2 = 0.0;
+    FOR_CHUNK(N) {
+        const size_t k = base + i;
+        const double wd = wv[k], s = wd + (double)vm[k];
+        const float r = (float)(-sl * sr * wd);
+        const float bb = (float)(sb * s - sb * wd);
+        if (has_reg) ur[k] = r;
+        ub[k] = bb;
+        a1 += (has_reg ? (double)r * r : 0.0) + (double)bb * bb;
+        a2 += s * s;
+    }
+    STORE_PARTIAL(a1, part);
+    STORE_PARTIAL(a2, part2);
+}
+
+// LSQR step, image parts: ur = sl*sr*v - gamma*ur ; ub = sb*v - gamma*ub
+__global__ void k_l2_u_img(const float *__restrict__ v, float *__restrict__ ur,
+                           float *__restrict__ ub, size_t N, double sl, double sr, double sb,
+                           int has_reg, const Scal *__restrict__ sc, int coupled,
+                           double *part) {
+    double acc = 0.0;
+    FOR_CHUNK(N) {
+        const size_t k = base + i;
+        const Scal &q = sc[grp(w, coupled)];
+        const double g = q.gamma, vd = v[k];
+        if (!q.done) {
+            if (has_reg) ur[k] = (float)(sl * sr * vd - g * (double)ur[k]);
+            ub[k] = (float)(sb * vd - g * (double)ub[k]);
+        }
+        const double r = has_reg ? (double)ur[k] : 0.0, bb = ub[k];
+        acc += r * r + bb * bb;
+    }
+    STORE_PARTIAL(acc, part);
+}
+
+// vt = (sl*(At_us + sr*ur) + sb*ub) / beta ; v = vt - beta*v_old (first: v_old = 0)
+__global__ void k_l2_v_img(const float *__restrict__ atu, const float *__restrict__ ur,
+                           const float *__restrict__ ub, float *__restrict__ v, size_t N,
+                           double sl, double sr, double sb, int has_reg, int first,
+                           const Scal *__restrict__ sc, int coupled, double *part) {
+    double acc = 0.0;
+    FOR_CHUNK(N) {
+        const size_t k = base + i;
+        const Scal &q = sc[grp(w, coupled)];
+        if (!q.done) {
+            double vt = sl * ((double)atu[k] + (has_reg ? sr * (double)ur[k] : 0.0)) +
+                        sb * (double)ub[k];
+            vt /= q.beta;
+            if (!first) vt -= q.beta * (double)v[k];
+            v[k] = (float)vt;
+        }
+        const double vv = v[k];
+        acc += vv * vv;
+    }
+    STORE_PARTIAL(acc, part);
+}
+
+__device__ double sum_parts(const double *part, int nblk, int w) {
+    double s = 0.0;
+    for (int b = 0; b < nblk; ++b) s += part[(size_t)w * nblk + b];
+    return s;
+}
+
+__device__ double group_sum(const double *p1, int n1, const double *p2, int n2, int g,
+                            int W, int coupled) {
+    double s = 0.0;
+    const int w0 = coupled ? 0 : g, w1 = coupled ? W : g + 1;
+    for (int w = w0; w < w1; ++w) {
+        if (p1) s += sum_parts(p1, n1, w);
+        if (p2) s += sum_parts(p2, n2, w);
+    }
+    return s;
+}
+
+// stage 0: beta after init; stage 1: alpha (init or step); stage 2: LSQR step scalars
+__global__ void k_l2_scalar(Scal *sc, int stage, const double *p1, int n1, const double *p2,
+                            int n2, const double *p3, int n3, const double *normb2_sino,
+                            double sl, double sb, int W, int coupled, double tol) {
+    const int G = coupled ? 1 : W;
+    for (int g = threadIdx.x; g < G; g += blockDim.x) {
+        Scal &q = sc[g];
+        if (stage == 0) {
+            const double b2 = group_sum(p1, n1, p2, n2, g, W, coupled);
+            const double wv2 = group_sum(p3, n3, nullptr, 0, g, W, coupled);
+            q.normb = sqrt(sl * sl * normb2_sino[g] + sb * sb * wv2);
+            q.beta = sqrt(b2);
+            q.normr = q.beta;
+            q.normrmin = q.beta;
+            q.phibar = q.beta;
+            q.c = 1.0;
+            q.s = 0.0;
+            q.done = !(q.beta > 0.0) || !isfinite(q.beta);
+            q.improved = 0;
+        } else if (stage == 1) {
+            const double a2 = group_sum(p1, n1, nullptr, 0, g, W, coupled);
+            if (!q.done) {
+                q.alpha = sqrt(a2);
+                if (!(q.alpha > 0.0) || !isfinite(q.alpha)) q.done = 1;
+            }
+        } else {
+            const double b2 = group_sum(p1, n1, p2, n2, g, W, coupled);
+            q.improved = 0;
+            if (q.done) continue;
+            const double beta = sqrt(b2);
+            const double thet = -q.s * q.alpha;
+            const double rhot = q.c * q.alpha;
+            const double rho = sqrt(rhot * rhot + beta * beta);
+            if (!(rho > 0.0) || !isfinite(rho)) {
+                q.done = 1;
+                continue;
+            }
+            q.c = rhot / rho;
+            q.s = -beta / rho;
+            q.phi = q.c * q.phibar;
+            q.phibar = q.s * q.phibar;
+            q.rho = rho;
+            q.thet = thet;
+            q.beta = beta;
+            q.normr = fabs(q.s) * q.normr;
+            q.improved = 2;  // x is updated this step (2 = update x, no xmin copy)
+            if (q.normr < q.normrmin) {
+                q.normrmin = q.normr;
+                q.improved = 1;  // update x and xmin
+            }
+            if (q.normr <= tol * q.normb) q.improved = 3;  // converged: x is final
+        }
+    }
+}
+
+// gamma = alpha / beta for the next u update
+__global__ void k_l2_gamma(Scal *sc, int G) {
+    for (int g = threadIdx.x; g < G; g += blockDim.x) sc[g].gamma = sc[g].alpha / sc[g].beta;
+}
+
+// v /= alpha ; on init also d = 0, x = w, xmin = w
+__global__ void k_l2_scale_v(float *v, float *d, float *x, float *xmin, const float *wv,
+                             size_t N, int init, const Scal *sc, int coupled) {
+    FOR_CHUNK(N) {
+        const size_t k = base + i;
+        const Scal &q = sc[grp(w, coupled)];
+        if (init) {
+            d[k] = 0.f;
+            x[k] = wv[k];
+            xmin[k] = wv[k];
+        }
+        if (!q.done) v[k] = (float)((double)v[k] / q.alpha);
+    }
+}
+
+// d = (v - thet*d)/rho ; x += phi*d ; xmin = x when improved
+__global__ void k_l2_dx(const float *v, float *d, float *x, float *xmin, size_t N, Scal *sc,
+                        int coupled) {
+    FOR_CHUNK(N) {
+        const size_t k = base + i;
+        const Scal &q = sc[grp(w, coupled)];
+        if (q.done || q.improved == 0) continue;
+        const double dn = ((double)v[k] - q.thet * (double)d[k]) / q.rho;
+        d[k] = (float)dn;
+        const float xn = (float)((double)x[k] + q.phi * dn);
+        x[k] = xn;
+        if (q.improved != 2) xmin[k] = xn;
+    }
+}
+
+__global__ void k_l2_mark_converged(Scal *sc, int G) {
+    for (int g = threadIdx.x; g < G; g += blockDim.x)
+        if (sc[g].improved == 3) sc[g].done = 1;
+}
+
+// w = max(xmin - vm, 0) ; vm += w - xmin
+__global__ void k_nn_outer(const float *xmin, float *wv, float *vm, size_t N) {
+    FOR_CHUNK(N) {
+        const size_t k = base + i;
+        const float u = xmin[k];
+        const float wn = fmaxf(u - vm[k], 0.f);
+        wv[k] = wn;
+        vm[k] = vm[k] + wn - u;
+    }
+}
+
+__global__ void k_copy(const float *__restrict__ a, float *__restrict__ b, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        b[i] = a[i];
+}
+
+__global__ void k_fill(float *__restrict__ b, float v, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        b[i] = v;
+}
+
+__global__ void k_group_sums(const double *part, int nblk, int W, int coupled, double *out) {
+    const int G = coupled ? 1 : W;
+    for (int g = threadIdx.x; g < G; g += blockDim.x)
+        out[g] = group_sum(part, nblk, nullptr, 0, g, W, coupled);
+}
+
+// ---------------------------------------------------------------------------
+// workspace
+// ---------------------------------------------------------------------------
+struct Work {
+    int W = 0;
+    size_t bytes = 0;
+    float *s1 = nullptr, *s2 = nullptr;                 // sinogram vectors
+    float *i[12] = {};                                  // image vectors
+    double *part = nullptr;                             // partial sums, 4 slots
+    Scal *sc = nullptr;
+    double *gsum = nullptr;
+};
+
+static int nblk_for(size_t N) {
+    size_t b = (N + RED_THREADS * 8 - 1) / (RED_THREADS * 8);
+    if (b < 1) b = 1;
+    if (b > 256) b = 256;
+    return (int)b;
+}
+
+static void free_work(Work &w) {
+    cudaFree(w.s1);
+    cudaFree(w.s2);
+    for (auto &p : w.i) cudaFree(p);
+    cudaFree(w.part);
+    cudaFree(w.sc);
+    cudaFree(w.gsum);
+    w = Work();
+}
+
+static int make_work(const Plan &pl, int W, Work &wk) {
+    const size_t NS = (size_t)W * pl.D * pl.T, NI = (size_t)W * pl.P;
+    wk.W = W;
+#define AL(p, n, T)                                                                        \
+    if (cudaMalloc((void **)&(p), (n) * sizeof(T)) != cudaSuccess) {                        \
+        free_work(wk);                                                                     \
+        set_error("solver workspace allocation failed");                                   \
+        return MSOT_ENOMEM;                                                                \
+    }
+    AL(wk.s1, NS, float);
+    AL(wk.s2, NS, float);
+    for (auto &p : wk.i) AL(p, NI, float);
+    AL(wk.part, (size_t)4 * W * 256, double);
+    AL(wk.sc, (size_t)W, Scal);
+    AL(wk.gsum, (size_t)W, double);
+#undef AL
+    return MSOT_OK;
+}
+
+struct Ctx {
+    const Plan &pl;
+    int W;
+    int coupled;
+    cudaStream_t st;
+    size_t NS, NI;
+    int nbs, nbi;
+    Work &wk;
+    double *P(int slot) const { return wk.part + (size_t)slot * W * 256; }
+};
+
+#define TRY(x)                                                                             \
+    do {                                                                                   \
+        int rc_ = (x);                                                                     \
+        if (rc_ != MSOT_OK) return rc_;                                                    \
+    } while (0)
+
+static int group_sumsq(const Ctx &c, const float *x, const float *y, size_t N, int nb,
+                       std::vector<double> &out) {
+    k_sumsq<<<dim3(nb, c.W), RED_THREADS, 0, c.st>>>(x, y, N / c.W, c.P(3));
+    MSOT_LAUNCH_CHECK();
+    k_group_sums<<<1, 256, 0, c.st>>>(c.P(3), nb, c.W, c.coupled, c.wk.gsum);
+    MSOT_LAUNCH_CHECK();
+    const int G = c.coupled ? 1 : c.W;
+    out.resize(G);
+    MSOT_CUDA_TRY(cudaMemcpyAsync(out.data(), c.wk.gsum, sizeof(double) * G,
+                                  cudaMemcpyDeviceToHost, c.st));
+    MSOT_CUDA_TRY(cudaStreamSynchronize(c.st));
+    return MSOT_OK;
+}
+
+// One outer iteration of nnls_L2_less: lsqr(maxit = 2, x0 = w), clip, multiplier.
+static int l2_outer(const Ctx &c, const float *b, float *wv, float *vm, double sr,
+                    int has_reg, const double *normb2) {
+    const double sl = 1.0, sb = std::sqrt(1e-3);
+    Work &k = c.wk;
+    float *us = k.s1, *tmp_s = k.s2;
+    float *ur = k.i[0], *ub = k.i[1], *v = k.i[2], *d = k.i[3], *x = k.i[4], *xmin = k.i[5],
+          *tmp_i = k.i[6];
+    const size_t ns = c.NS / c.W, ni = c.NI / c.W;
+    const dim3 gs(c.nbs, c.W), gi(c.nbi, c.W);
+    const int G = c.coupled ? 1 : c.W;
+    cudaStream_t st = c.st;
+    // init: u = b_aug - A_aug w
+    TRY(apply_forward(c.pl, wv, tmp_s, c.W, st));
+    k_sino_update<<<gs, RED_THREADS, 0, st>>>(tmp_s, b, us, ns, 0, sl, k.sc, c.coupled, c.P(0));
+    k_l2_init_img<<<gi, RED_THREADS, 0, st>>>(wv, vm, ur, ub, ni, sl, sr, sb, has_reg, c.P(1),
+                                              c.P(2));
+    k_l2_scalar<<<1, 256, 0, st>>>(k.sc, 0, c.P(0), c.nbs, c.P(1), c.nbi, c.P(2), c.nbi, normb2,
+                                   sl, sb, c.W, c.coupled, 1e-8);
+    MSOT_LAUNCH_CHECK();
+    // v = A_aug^T u / beta
+    TRY(apply_transpose(c.pl, us, tmp_i, c.W, st));
+    k_l2_v_img<<<gi, RED_THREADS, 0, st>>>(tmp_i, ur, ub, v, ni, sl, sr, sb, has_reg, 1, k.sc,
+                                           c.coupled, c.P(1));
+    k_l2_scalar<<<1, 256, 0, st>>>(k.sc, 1, c.P(1), c.nbi, nullptr, 0, nullptr, 0, nullptr, sl,
+                                   sb, c.W, c.coupled, 1e-8);
+    k_l2_scale_v<<<gi, RED_THREADS, 0, st>>>(v, d, x, xmin, wv, ni, 1, k.sc, c.coupled);
+    MSOT_LAUNCH_CHECK();
+    for (int it = 0; it < 2; ++it) {
+        k_l2_gamma<<<1, 256, 0, st>>>(k.sc, G);
+        TRY(apply_forward(c.pl, v, tmp_s, c.W, st));
+        k_sino_update<<<gs, RED_THREADS, 0, st>>>(tmp_s, nullptr, us, ns, 1, sl, k.sc,
+                                                  c.coupled, c.P(0));
+        k_l2_u_img<<<gi, RED_THREADS, 0, st>>>(v, ur, ub, ni, sl, sr, sb, has_reg, k.sc,
+                                               c.coupled, c.P(1));
+        k_l2_scalar<<<1, 256, 0, st>>>(k.sc, 2, c.P(0), c.nbs, c.P(1), c.nbi, nullptr, 0,
+                                       nullptr, sl, sb, c.W, c.coupled, 1e-8);
+        k_l2_dx<<<gi, RED_THREADS, 0, st>>>(v, d, x, xmin, ni, k.sc, c.coupled);
+        k_l2_mark_converged<<<1, 256, 0, st>>>(k.sc, G);
+        MSOT_LAUNCH_CHECK();
+        if (it == 1) break;  // the last A^T of lsqr only feeds its stopping test
+        TRY(apply_transpose(c.pl, us, tmp_i, c.W, st));
+        k_l2_v_img<<<gi, RED_THREADS, 0, st>>>(tmp_i, ur, ub, v, ni, sl, sr, sb, has_reg, 0,
+                                               k.sc, c.coupled, c.P(1));
+        k_l2_scalar<<<1, 256, 0, st>>>(k.sc, 1, c.P(1), c.nbi, nullptr, 0, nullptr, 0, nullptr,
+                                       sl, sb, c.W, c.coupled, 1e-8);
+        k_l2_scale_v<<<gi, RED_THREADS, 0, st>>>(v, d, x, xmin, wv, ni, 0, k.sc, c.coupled);
+        MSOT_LAUNCH_CHECK();
+    }
+    k_nn_outer<<<gi, RED_THREADS, 0, st>>>(xmin, wv, vm, ni);
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
+}
+
+static int solve_l2(const Plan &pl, const float *b, float *rec, int W, int num_iter,
+                    double lambdaL2, const float *x0, int coupled, double *err_img,
+                    double *err_reg, cudaStream_t st) {
+    Work wk;
+    TRY(make_work(pl, W, wk));
+    const size_t NS = (size_t)W * pl.D * pl.T, NI = (size_t)W * pl.P;
+    Ctx c{pl, W, coupled, st, NS, NI, nblk_for(NS / W), nblk_for(NI / W), wk};
+    const int has_reg = lambdaL2 > 0;
+    const double sr = has_reg ? std::sqrt(lambdaL2) : 0.0;
+    float *wv = wk.i[7], *vm = wk.i[8];
+    int rc = MSOT_OK;
+    do {
+        if (x0)
+            k_copy<<<256, 256, 0, st>>>(x0, wv, NI);
+        else
+            k_fill<<<256, 256, 0, st>>>(wv, 0.f, NI);
+        k_fill<<<256, 256, 0, st>>>(vm, 0.f, NI);
+        // ||b||^2 per group enters ||b_aug|| of lsqr's tolerance test
+        k_sumsq<<<dim3(c.nbs, W), RED_THREADS, 0, st>>>(b, nullptr, NS / W, c.P(3));
+        k_group_sums<<<1, 256, 0, st>>>(c.P(3), c.nbs, W, coupled, wk.gsum);
+        if (cudaGetLastError() != cudaSuccess) {
+            set_error("solver: launch failed");
+            rc = MSOT_ECUDA;
+            break;
+        }
+        for (int it = 0; it < num_iter && rc == MSOT_OK; ++it)
+            rc = l2_outer(c, b, wv, vm, sr, has_reg, wk.gsum);
+        if (rc) break;
+        k_copy<<<256, 256, 0, st>>>(wv, rec, NI);
+        if (err_img || err_reg) {
+            std::vector<double> e;
+            if ((rc = apply_forward(pl, rec, wk.s2, W, st))) break;
+            if (err_img) {
+                Ctx ci = c;
+                ci.coupled = 0;
+                if ((rc = group_sumsq(ci, wk.s2, b, NS, c.nbs, e))) break;
+                for (int w = 0; w < W; ++w) err_img[w] = e[w];
+            }
+            if (err_reg) {
+                Ctx ci = c;
+                ci.coupled = 0;
+                if ((rc = group_sumsq(ci, rec, nullptr, NI, c.nbi, e))) break;
+                for (int w = 0; w < W; ++w) err_reg[w] = has_reg ? e[w] : 0.0;
+            }
+        }
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            set_error("solver: %s", cudaGetErrorString(e));
+            rc = MSOT_ECUDA;
+        }
+    } while (0);
+    free_work(wk);
+    return rc;
+}
+
+
+// ---------------------------------------------------------------------------
+// L1 (identity) NNLS: split Bregman with cgs(lam A^T A + I, rhs, 1e-8, 2)
+// ---------------------------------------------------------------------------
+__global__ void k_dot(const float *__restrict__ a, const float *__restrict__ b, size_t N,
+                      double *part) {
+    double acc = 0.0;
+    FOR_CHUNK(N) acc += (double)a[base + i] * (double)b[base + i];
+    STORE_PARTIAL(acc, part);
+}
+
+// d = max(u - bp, 0); rhs = d + bp + lam*atb - lam*eta; cgs init: x = 0, r = rt = rhs.
+__global__ void k_l1_rhs(const float *u, const float *bp, const float *atb, float *dv,
+                         float *rhs, float *x, float *r, float *rt, float *xmin, size_t N,
+                         double lam, double eta, double *part) {
+    double acc = 0.0;
+    FOR_CHUNK(N) {
+        const size_t k = base + i;
+        const float dd = fmaxf(u[k] - bp[k], 0.f);
+        dv[k] = dd;
+        const float rh = (float)((double)fmaxf(dd, 0.f) + (double)bp[k] + lam * (double)atb[k] -
+                                 lam * eta);
+        rhs[k] = rh;
+        r[k] = rh;
+        rt[k] = rh;
+        x[k] = 0.f;
+        xmin[k] = 0.f;
+        acc += (double)rh * rh;
+    }
+    STORE_PARTIAL(acc, part);
+}
+
+// stage 0: n2b; 1: rho = rt.r; 2: alpha = rho / rt.vh; 3: normr after r update
+__global__ void k_cgs_scalar(Scal *sc, int stage, const double *p, int nb, int W, int coupled,
+                             double tol) {
+    const int G = coupled ? 1 : W;
+    for (int g = threadIdx.x; g < G; g += blockDim.x) {
+        Scal &q = sc[g];
+        const double v = group_sum(p, nb, nullptr, 0, g, W, coupled);
+        if (stage == 0) {
+            q.normb = sqrt(v);
+            q.normr = q.normb;
+            q.normrmin = q.normb;
+            q.rho_cg = 1.0;
+            q.done = !(q.normb > 0.0) || !isfinite(q.normb);
+            q.improved = 0;
+            continue;
+        }
+        if (q.done) {
+            q.improved = 0;
+            continue;
+        }
+        if (stage == 1) {
+            q.rho1_cg = q.rho_cg;
+            q.rho_cg = v;
+            if (v == 0.0 || !isfinite(v)) q.done = 1;
+        } else if (stage == 2) {
+            if (v == 0.0 || !isfinite(v)) {
+                q.done = 1;
+            } else {
+                q.alpha_cg = q.rho_cg / v;
+            }
+        } else {
+            q.normr = sqrt(v);
+            q.improved = 0;
+            if (q.normr <= tol * q.normb) {
+                q.improved = 3;
+            } else if (q.normr < q.normrmin) {
+                q.normrmin = q.normr;
+                q.improved = 1;
+            }
+        }
+    }
+}
+
+// direction: first: uc = r, p = uc; else beta = rho/rho1: uc = r + beta q,
+// p = uc + beta (q + beta p)
+__global__ void k_cgs_dir(const float *r, float *q, float *uc, float *p, size_t N, int first,
+                          const Scal *sc, int coupled) {
+    FOR_CHUNK(N) {
+        const size_t k = base + i;
+        const Scal &s = sc[grp(w, coupled)];
+        if (s.done) continue;
+        if (first) {
+            uc[k] = r[k];
+            p[k] = r[k];
+        } else {
+            const double beta = s.rho_cg / s.rho1_cg;
+            const double u = (double)r[k] + beta * (double)q[k];
+            uc[k] = (float)u;
+            p[k] = (float)(u + beta * ((double)q[k] + beta * (double)p[k]));
+        }
+    }
+}
+
+// y = lam*atav + v ; partial dot(rt, y)
+__global__ void k_cgs_op(const float *atav, const float *v, float *y, const float *rt,
+                         size_t N, double lam, double *part) {
+    double acc = 0.0;
+    FOR_CHUNK(N) {
+        const size_t k = base + i;
+        const float o = (float)(lam * (double)atav[k] + (double)v[k]);
+        y[k] = o;
+        acc += (double)rt[k] * o;
+    }
+    STORE_PARTIAL(acc, part);
+}
+
+// q = uc - alpha vh; uh = uc + q; x += alpha uh
+__global__ void k_cgs_upd(const float *uc, const float *vh, float *q, float *uh, float *x,
+                          size_t N, const Scal *sc, int coupled) {
+    FOR_CHUNK(N) {
+        const size_t k = base + i;
+        const Scal &s = sc[grp(w, coupled)];
+        if (s.done) continue;
+        const double a = s.alpha_cg;
+        const double qq = (double)uc[k] - a * (double)vh[k];
+        q[k] = (float)qq;
+        const double u = (double)uc[k] + qq;
+        uh[k] = (float)u;
+        x[k] = (float)((double)x[k] + a * u);
+    }
+}
+
+// r -= alpha (lam atau + uh); partial ||r||^2
+__global__ void k_cgs_res(const float *atau, const float *uh, float *r, size_t N, double lam,
+                          const Scal *sc, int coupled, double *part) {
+    double acc = 0.0;
+    FOR_CHUNK(N) {
+        const size_t k = base + i;
+        const Scal &s = sc[grp(w, coupled)];
+        if (!s.done) {
+            const double o = lam * (double)atau[k] + (double)uh[k];
+            r[k] = (float)((double)r[k] - s.alpha_cg * o);
+        }
+        acc += (double)r[k] * r[k];
+    }
+    STORE_PARTIAL(acc, part);
+}
+
+__global__ void k_cgs_keep(const float *x, float *xmin, size_t N, const Scal *sc, int coupled) {
+    FOR_CHUNK(N) {
+        const size_t k = base + i;
+        const Scal &s = sc[grp(w, coupled)];
+        if (s.improved) xmin[k] = x[k];
+    }
+}
+
+__global__ void k_cgs_mark(Scal *sc, int G) {
+    for (int g = threadIdx.x; g < G; g += blockDim.x)
+        if (sc[g].improved == 3) sc[g].done = 1;
+}
+
+// bp += d - u
+__global__ void k_l1_bregman(const float *dv, const float *u, float *bp, size_t N) {
+    FOR_CHUNK(N) {
+        const size_t k = base + i;
+        bp[k] = bp[k] + fmaxf(dv[k], 0.f) - u[k];
+    }
+}
+
+static int normal_op(const Ctx &c, const float *v, float *out_atav) {
+    TRY(apply_forward(c.pl, v, c.wk.s2, c.W, c.st));
+    return apply_transpose(c.pl, c.wk.s2, out_atav, c.W, c.st);
+}
+
+static int solve_l1(const Plan &pl, const float *b, float *rec, int W, int num_iter, double eta,
+                    const float *x0, int coupled, double *err_img, double *err_reg,
+                    cudaStream_t st) {
+    Work wk;
+    TRY(make_work(pl, W, wk));
+    const size_t NS = (size_t)W * pl.D * pl.T, NI = (size_t)W * pl.P;
+    Ctx c{pl, W, coupled, st, NS, NI, nblk_for(NS / W), nblk_for(NI / W), wk};
+    const size_t ni = NI / W;
+    const dim3 gi(c.nbi, W);
+    const int G = coupled ? 1 : W;
+    const double lam = 1.0;
+    float *u = wk.i[0], *bp = wk.i[1], *atb = wk.i[2], *dv = wk.i[3], *rhs = wk.i[4],
+          *x = wk.i[5], *r = wk.i[6], *rt = wk.i[7], *xmin = wk.i[8], *q = wk.i[9],
+          *uc = wk.i[10], *p = wk.i[11];
+    // vh shares storage with rhs (rhs is only needed for the cgs init)
+    float *vh = rhs;
+    int rc = MSOT_OK;
+    float *atmp = nullptr, *uh = nullptr;
+    do {
+        if (cudaMalloc(&atmp, NI * sizeof(float)) != cudaSuccess ||
+            cudaMalloc(&uh, NI * sizeof(float)) != cudaSuccess) {
+            set_error("L1 workspace allocation failed");
+            rc = MSOT_ENOMEM;
+            break;
+        }
+        // start value A^T b (rec_nn_with_L1_eye_reg.m:33) unless a warm start is given
+        if ((rc = apply_transpose(pl, b, atb, W, st))) break;
+        if (x0)
+            k_copy<<<256, 256, 0, st>>>(x0, u, NI);
+        else
+            k_copy<<<256, 256, 0, st>>>(atb, u, NI);
+        k_fill<<<256, 256, 0, st>>>(bp, 0.f, NI);
+        for (int it = 0; it < num_iter && rc == MSOT_OK; ++it) {
+            k_l1_rhs<<<gi, RED_THREADS, 0, st>>>(u, bp, atb, dv, rhs, x, r, rt, xmin, ni, lam, eta,
+                                                 c.P(0));
+            k_cgs_scalar<<<1, 256, 0, st>>>(wk.sc, 0, c.P(0), c.nbi, W, coupled, 1e-8);
+            for (int ci = 0; ci < 2 && rc == MSOT_OK; ++ci) {
+                k_dot<<<gi, RED_THREADS, 0, st>>>(rt, r, ni, c.P(0));
+                k_cgs_scalar<<<1, 256, 0, st>>>(wk.sc, 1, c.P(0), c.nbi, W, coupled, 1e-8);
+                k_cgs_dir<<<gi, RED_THREADS, 0, st>>>(r, q, uc, p, ni, ci == 0, wk.sc, coupled);
+                if ((rc = normal_op(c, p, atmp))) break;
+                k_cgs_op<<<gi, RED_THREADS, 0, st>>>(atmp, p, vh, rt, ni, lam, c.P(0));
+                k_cgs_scalar<<<1, 256, 0, st>>>(wk.sc, 2, c.P(0), c.nbi, W, coupled, 1e-8);
+                k_cgs_upd<<<gi, RED_THREADS, 0, st>>>(uc, vh, q, uh, x, ni, wk.sc, coupled);
+                if ((rc = normal_op(c, uh, atmp))) break;
+                k_cgs_res<<<gi, RED_THREADS, 0, st>>>(atmp, uh, r, ni, lam, wk.sc, coupled,
+                                                      c.P(0));
+                k_cgs_scalar<<<1, 256, 0, st>>>(wk.sc, 3, c.P(0), c.nbi, W, coupled, 1e-8);
+                k_cgs_keep<<<gi, RED_THREADS, 0, st>>>(x, xmin, ni, wk.sc, coupled);
+                k_cgs_mark<<<1, 256, 0, st>>>(wk.sc, G);
+            }
+            if (rc) break;
+            k_copy<<<256, 256, 0, st>>>(xmin, u, NI);
+            k_l1_bregman<<<gi, RED_THREADS, 0, st>>>(dv, u, bp, ni);
+            if (cudaGetLastError() != cudaSuccess) {
+                set_error("L1 solver: launch failed");
+                rc = MSOT_ECUDA;
+            }
+        }
+        if (rc) break;
+        k_copy<<<256, 256, 0, st>>>(u, rec, NI);
+        if (err_img || err_reg) {
+            std::vector<double> e;
+            Ctx ci = c;
+            ci.coupled = 0;
+            if (err_img) {
+                if ((rc = apply_forward(pl, rec, wk.s2, W, st))) break;
+                if ((rc = group_sumsq(ci, wk.s2, b, NS, c.nbs, e))) break;
+                for (int w = 0; w < W; ++w) err_img[w] = e[w];
+            }
+            if (err_reg) {
+                std::vector<float> h(NI);
+                MSOT_CUDA_TRY(cudaMemcpyAsync(h.data(), rec, NI * sizeof(float),
+                                              cudaMemcpyDeviceToHost, st));
+                MSOT_CUDA_TRY(cudaStreamSynchronize(st));
+                for (int w = 0; w < W; ++w) {
+                    double s1 = 0;
+                    for (size_t k = 0; k < ni; ++k) s1 += std::fabs((double)h[w * ni + k]);
+                    err_reg[w] = s1;
+                }
+            }
+        }
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            set_error("L1 solver: %s", cudaGetErrorString(e));
+            rc = MSOT_ECUDA;
+        }
+    } while (0);
+    cudaFree(atmp);
+    cudaFree(uh);
+    free_work(wk);
+    return rc;
+}
+
+// ---------------------------------------------------------------------------
+// sigma_max by power iteration on A^T A (FP64 norms)
+// ---------------------------------------------------------------------------
+__global__ void k_seed(float *v, size_t n, uint64_t seed) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        uint64_t z = seed + 0x9E3779B97F4A7C15ull * (i + 1);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        v[i] = (float)((double)(z >> 11) * (1.0 / 9007199254740992.0) - 0.5);
+    }
+}
+
+__global__ void k_scale_by(float *v, size_t n, const double *ss) {
+    const double f = 1.0 / sqrt(ss[0]);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        v[i] = (float)((double)v[i] * f);
+}
+
+static int estimate_norm(const Plan &pl, int iters, uint64_t seed, double *out, cudaStream_t st) {
+    Work wk;
+    TRY(make_work(pl, 1, wk));
+    const size_t NI = pl.P, NS = (size_t)pl.D * pl.T;
+    Ctx c{pl, 1, 0, st, NS, NI, nblk_for(NS), nblk_for(NI), wk};
+    int rc = MSOT_OK;
+    float *v = wk.i[0], *z = wk.i[1];
+    do {
+        k_seed<<<64, 256, 0, st>>>(v, NI, seed);
+        k_sumsq<<<dim3(c.nbi, 1), RED_THREADS, 0, st>>>(v, nullptr, NI, c.P(0));
+        k_group_sums<<<1, 32, 0, st>>>(c.P(0), c.nbi, 1, 0, wk.gsum);
+        k_scale_by<<<64, 256, 0, st>>>(v, NI, wk.gsum);
+        for (int it = 0; it < iters && rc == MSOT_OK; ++it) {
+            if ((rc = apply_forward(pl, v, wk.s1, 1, st))) break;
+            if ((rc = apply_transpose(pl, wk.s1, z, 1, st))) break;
+            k_sumsq<<<dim3(c.nbi, 1), RED_THREADS, 0, st>>>(z, nullptr, NI, c.P(0));
+            k_group_sums<<<1, 32, 0, st>>>(c.P(0), c.nbi, 1, 0, wk.gsum);
+            k_scale_by<<<64, 256, 0, st>>>(z, NI, wk.gsum);
+            std::swap(v, z);
+        }
+        if (rc) break;
+        if ((rc = apply_forward(pl, v, wk.s1, 1, st))) break;
+        std::vector<double> e;
+        if ((rc = group_sumsq(c, wk.s1, nullptr, NS, c.nbs, e))) break;
+        *out = std::sqrt(e[0]) * pl.norm;
+    } while (0);
+    free_work(wk);
+    return rc;
+}
+
+}  // namespace msot
+
+using namespace msot;
+
+extern "C" int msot_rec_nn_with_L2_reg(msot_plan_t plan, const float *d_b, float *d_rec,
+                                       int batch, int num_iter, double lambdaL2,
+                                       const float *d_x0, int coupled, double *err_img,
+                                       double *err_reg, void *stream) {
+    if (!plan || !d_b || !d_rec || batch <= 0 || num_iter < 0) {
+        set_error("rec_nn_with_L2_reg: bad arguments");
+        return MSOT_EINVAL;
+    }
+    if (batch > plan->p.max_batch) {
+        set_error("batch %d exceeds the plan's max_batch %d", batch, plan->p.max_batch);
+        return MSOT_EINVAL;
+    }
+    return solve_l2(plan->p, d_b, d_rec, batch, num_iter, lambdaL2, d_x0, coupled ? 1 : 0,
+                    err_img, err_reg, (cudaStream_t)stream);
+}
+
+extern "C" int msot_rec_nn_with_L1_eye_reg(msot_plan_t plan, const float *d_b, float *d_rec,
+                                           int batch, int num_iter, double reg,
+                                           const float *d_x0, int coupled, double *err_img,
+                                           double *err_reg, void *stream) {
+    if (!plan || !d_b || !d_rec || batch <= 0 || num_iter < 0) {
+        set_error("rec_nn_with_L1_eye_reg: bad arguments");
+        return MSOT_EINVAL;
+    }
+    if (batch > plan->p.max_batch) {
+        set_error("batch %d exceeds the plan's max_batch %d", batch, plan->p.max_batch);
+        return MSOT_EINVAL;
+    }
+    return solve_l1(plan->p, d_b, d_rec, batch, num_iter, reg, d_x0, coupled ? 1 : 0, err_img,
+                    err_reg, (cudaStream_t)stream);
+}
+
+extern "C" int msot_estimate_norm(msot_plan_t plan, int iters, uint64_t seed, double *sigma_max,
+                                  void *stream) {
+    if (!plan || !sigma_max || iters < 1) {
+        set_error("estimate_norm: bad arguments");
+        return MSOT_EINVAL;
+    }
+    return estimate_norm(plan->p, iters, seed, sigma_max, (cudaStream_t)stream);
+}

@@ -1,0 +1,78 @@
+"""Build of the CUDA library libmsotgpu.so (sm_103a) with nvcc.
+
+The translation units under csrc/ are compiled in parallel into
+build/*.o and linked into lib/libmsotgpu.so next to this package.  No cmake,
+no torch extension machinery: the library exposes a plain C ABI
+(include/msot_gpu.h).
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+
+PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))  # mb-rec-msot_gb300/
+CSRC = os.path.join(PKG_ROOT, "csrc")
+BUILD = os.path.join(PKG_ROOT, "build")
+LIBDIR = os.path.join(PKG_ROOT, "lib")
+LIB_PATH = os.path.join(LIBDIR, "libmsotgpu.so")
+
+ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise FileNotFoundError("nvcc not found")
+
+
+def sources():
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+
+
+def _stale(target: str, deps) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(verbose: bool = False, force: bool = False) -> str:
+    """Compile (incrementally) and link; returns the library path."""
+    os.makedirs(BUILD, exist_ok=True)
+    os.makedirs(LIBDIR, exist_ok=True)
+    nv = nvcc()
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    headers.append(os.path.join(os.path.dirname(PKG_ROOT), "include", "msot_gpu.h"))
+    srcs = sources()
+    objs = [os.path.join(BUILD, os.path.basename(s)[:-3] + ".o") for s in srcs]
+
+    def compile_one(pair):
+        src, obj = pair
+        if not force and not _stale(obj, [src] + headers):
+            return None
+        cmd = [nv, *ARCH_FLAGS, *NVCC_FLAGS, "-c", src, "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+        if verbose:
+            print(" ".join(cmd))
+        return obj
+
+    with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+        list(ex.map(compile_one, zip(srcs, objs)))
+    if force or _stale(LIB_PATH, objs):
+        cmd = [nv, *ARCH_FLAGS, "-shared", "-o", LIB_PATH, *objs, "-lcudart"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        if verbose:
+            print(" ".join(cmd))
+    return LIB_PATH
+
+
+if __name__ == "__main__":
+    print(build(verbose=True))

@@ -1,0 +1,112 @@
+"""ctypes binding of libmsotgpu.so (include/msot_gpu.h).
+
+The library is the only compute path: if it is missing this module raises
+(there is no CPU fallback).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import _build
+
+MSOT_OK = 0
+ERRORS = {
+    -1: "MSOT_EINVAL",
+    -2: "MSOT_ERANGE",
+    -3: "MSOT_ECUDA",
+    -4: "MSOT_ENOMEM",
+    -5: "MSOT_ENONFINITE",
+    -6: "MSOT_ETIMEOUT",
+}
+
+
+class MsotError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class PlanDesc(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("nz", C.c_int),
+        ("n_det", C.c_int), ("n_t", C.c_int),
+        ("radius", C.c_double),
+        ("travel", C.POINTER(C.c_double)),
+        ("ir_len", C.c_int),
+        ("ir", C.POINTER(C.c_double)),
+        ("pre_len_x", C.c_int), ("pre_len_z", C.c_int),
+        ("pre_x", C.POINTER(C.c_double)),
+        ("pre_z", C.POINTER(C.c_double)),
+        ("norm", C.c_double),
+        ("sir_len", C.c_int), ("n_sir", C.c_int),
+        ("sir", C.POINTER(C.c_double)),
+        ("sir_start_end", C.POINTER(C.c_int32)),
+        ("sir_idx", C.POINTER(C.c_int32)),
+        ("max_batch", C.c_int),
+    ]
+
+
+_vp = C.c_void_p
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+
+# name: (restype, argtypes)
+SIGNATURES = {
+    "msot_last_error": (C.c_char_p, []),
+    "msot_version": (C.c_int, []),
+    "msot_plan_create": (C.c_int, [C.POINTER(PlanDesc), C.POINTER(_vp)]),
+    "msot_plan_destroy": (C.c_int, [_vp]),
+    "msot_plan_device_bytes": (C.c_size_t, [_vp]),
+    "msot_forward": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp]),
+    "msot_transpose": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp]),
+    "msot_interp_forward": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp]),
+    "msot_interp_transpose": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp]),
+    "msot_estimate_norm": (C.c_int, [_vp, C.c_int, C.c_uint64, _dp, _vp]),
+    "msot_rec_nn_with_L2_reg": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_double, _vp,
+                                          C.c_int, _dp, _dp, _vp]),
+    "msot_rec_nn_with_L1_eye_reg": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_double, _vp,
+                                              C.c_int, _dp, _dp, _vp]),
+    "msot_mex_forwardDelayAndSum": (C.c_int, [_dp, C.c_int, C.c_int, _dp, C.c_int, C.c_int,
+                                              C.c_double, _dp]),
+    "msot_mex_transposeDelayAndSum": (C.c_int, [_dp, C.c_int, C.c_int, C.c_int, _dp, C.c_int,
+                                                C.c_double, _dp]),
+    "msot_mex_forward": (C.c_int, [_dp, C.c_int, C.c_int, _ip, _dp, C.c_int, _dp, C.c_int,
+                                   C.c_int, C.c_int, _ip, C.c_double, _dp]),
+    "msot_mex_transpose": (C.c_int, [_dp, C.c_int, C.c_int, C.c_int, _ip, _dp, C.c_int, _dp,
+                                     C.c_int, C.c_int, _ip, C.c_double, _dp]),
+}
+
+_LIB = None
+
+
+def lib_path() -> str:
+    return _build.LIB_PATH
+
+
+def load(build_if_missing: bool = False):
+    """Load the CUDA library (optionally building it first)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = lib_path()
+    if not os.path.exists(path):
+        if build_if_missing:
+            _build.build()
+        else:
+            raise ImportError(
+                f"{path} is missing: build it with __graft_entry__.build() or "
+                "python mb-rec-msot_gb300/msot_gb300/_build.py (no CPU fallback exists)")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def check(rc: int) -> None:
+    if rc != MSOT_OK:
+        msg = load().msot_last_error()
+        raise MsotError(rc, msg.decode() if msg else "")

@@ -1,0 +1,330 @@
+"""Host-side mirror of the reference's model classes (Probe, Discretization,
+MSOTmodel) on top of the CUDA library.
+
+The model tables are built once on the host in FP64 (geometry, IR,
+prefilter) and handed to a device-resident plan; every apply runs on the GPU.
+Tensor layouts (torch, CUDA, float32) are memory-identical to the MATLAB
+arrays of the reference:
+    image     [W, nx, nz]      == MATLAB Nz x Nx x W   (pixel p = ix*nz + iz)
+    sinogram  [W, n_det, n_t]  == MATLAB T x D x W
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+from scipy import signal as sps
+
+from . import _lib
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _iptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def _stream_ptr(stream=None):
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return C.c_void_p(stream.cuda_stream)
+
+
+# ----------------------------------------------------------------------------
+# Probe (Probe.m)
+# ----------------------------------------------------------------------------
+@dataclass
+class Probe:
+    """Arc array: elements evenly over ``angular_coverage`` degrees centred
+    on the -z axis (Probe.m:112-116).  ``eir`` None -> identity EIR of
+    ``eir_length`` taps (Probe.m:57-59)."""
+
+    n_det: int = 256
+    radius: float = 0.040
+    angular_coverage: float = 135.0
+    fs: float = 4e7
+    n_samples: int = 2030
+    delay: float = 0.0
+    eir: np.ndarray | None = None
+    eir_length: int = 257
+
+    @classmethod
+    def example_system(cls, eir=None):
+        """The reference's 'example_system' entry (Probe.m:101-127)."""
+        return cls(n_det=256, radius=0.060, angular_coverage=145.0, fs=4e7, n_samples=2030,
+                   delay=500.0, eir=eir, eir_length=201)
+
+    def detector_positions(self):
+        off = (180.0 - self.angular_coverage) / 2.0
+        step = self.angular_coverage / (self.n_det - 1)
+        ang = np.deg2rad(off + step * np.arange(self.n_det))
+        return self.radius * np.cos(ang), -self.radius * np.sin(ang)
+
+    def eir_taps(self) -> np.ndarray:
+        if self.eir is None:
+            e = np.zeros(self.eir_length)
+            e[self.eir_length // 2] = 1.0
+            return e
+        e = np.asarray(self.eir, dtype=np.float64).ravel()
+        if e.size % 2 != 1:
+            raise ValueError("EIR length must be odd")
+        return e
+
+
+# ----------------------------------------------------------------------------
+# Discretization (Discretization.m)
+# ----------------------------------------------------------------------------
+class Discretization:
+    """Pixel grid (Discretization.m:19-35) and the Gaussian pixel model's
+    shift-invariant prefilter (Discretization.m:41-51) as separable circular
+    taps."""
+
+    def __init__(self, field_of_view, size_of_pixel_grid):
+        fov = list(field_of_view)
+        if len(fov) <= 2:
+            fov = [fov[0], fov[1], fov[0], fov[1]]
+        if np.isscalar(size_of_pixel_grid):
+            size_of_pixel_grid = (size_of_pixel_grid, size_of_pixel_grid)
+        self.nx, self.nz = int(size_of_pixel_grid[0]), int(size_of_pixel_grid[1])
+        self.fov = tuple(float(v) for v in fov)
+        self.x = np.linspace(fov[0], fov[1], self.nx)
+        self.z = np.linspace(fov[2], fov[3], self.nz)
+        self.dx = self.x[1] - self.x[0]
+        self.dz = self.z[1] - self.z[0]
+        self.sigma = round(min(self.dx, self.dz) / 2 * 1e6) / 1e6
+
+    @property
+    def number_of_pixels(self) -> int:
+        return self.nx * self.nz
+
+    def pixel_model(self, r):
+        return np.exp(-np.asarray(r) ** 2 / (2 * self.sigma ** 2))
+
+    def pixel_coordinates(self):
+        """(x, z) of pixel p = ix*nz + iz."""
+        return np.repeat(self.x, self.nz), np.tile(self.z, self.nx)
+
+    def _axis_taps(self, n, h, tol=1e-13, kmax=64):
+        # 1-D factor of conj(phi_hat / F{autocorr}) with lattice [1 1]
+        lin = h * np.arange(np.floor(-n / 2), np.floor(n / 2 - 1) + 1)
+        g = np.fft.fftshift(self.pixel_model(lin))
+        gh = np.fft.fft(g)
+        pre = np.conj(gh / np.fft.fft(np.real(np.fft.ifft(np.abs(gh) ** 2))))
+        kern = np.real(np.fft.ifft(pre))
+        big = np.abs(kern) > tol * abs(kern[0])
+        K = 0
+        for k in range(1, (n - 1) // 2 + 1):
+            if big[k] or big[-k]:
+                K = k
+        K = min(K, kmax)
+        return kern[np.arange(-K, K + 1) % n].copy()
+
+    def prefilter_taps(self):
+        """(taps_x, taps_z): centred circular kernels along x and z."""
+        return self._axis_taps(self.nx, self.dx), self._axis_taps(self.nz, self.dz)
+
+
+# ----------------------------------------------------------------------------
+# Impulse response (MSOTmodel.m:320-348, filter_butter_zero_phase.m)
+# ----------------------------------------------------------------------------
+def butter_zero_phase(sig: np.ndarray, fs: float, fmin: float, fmax: float) -> np.ndarray:
+    """Zero-phase Butterworth filtering in the FFT domain along axis 0
+    (filter_butter_zero_phase.m:16-48): demean when fmin > 0, |H|^2 of an
+    order-8 low-pass (fmax) and order-2 high-pass (fmin) on the whole circle."""
+    x = np.asarray(sig, dtype=np.float64)
+    if fmin > 0:
+        x = x - x.mean(axis=0, keepdims=True)
+    zs, ps, k = [], [], 1.0
+    if fmax > 0:
+        z, p, g = sps.butter(8, 2 * fmax / fs, "low", output="zpk")
+        zs.append(z); ps.append(p); k *= g
+    if fmin > 0:
+        z, p, g = sps.butter(2, 2 * fmin / fs, "high", output="zpk")
+        zs.append(z); ps.append(p); k *= g
+    if not zs:
+        return x
+    sos = sps.zpk2sos(np.concatenate(zs), np.concatenate(ps), k)
+    _, h = sps.sosfreqz(sos, worN=x.shape[0], whole=True)
+    H2 = (np.abs(h) ** 2).reshape((-1,) + (1,) * (x.ndim - 1))
+    return np.real(np.fft.ifft(H2 * np.fft.fft(x, axis=0), axis=0))
+
+
+def model_impulse_response(probe: Probe, disc: Discretization, c: float, fmin: float,
+                           fmax: float, include_sir: bool) -> np.ndarray:
+    eir = probe.eir_taps()
+    if include_sir:
+        return butter_zero_phase(eir, probe.fs, fmin, fmax)
+    L = eir.size
+    h = (L - 1) // 2
+    t = np.arange(-h, h + 1) / probe.fs
+    pixel_response = disc.pixel_model(t * c) * (-t)  # time derivative of the pixel
+    ir = np.convolve(eir, pixel_response)[h:h + L]
+    return butter_zero_phase(ir, probe.fs, fmin, fmax)
+
+
+# ----------------------------------------------------------------------------
+# MSOTmodel
+# ----------------------------------------------------------------------------
+class _Funcs:
+    def __init__(self, model):
+        self.applyForward = model.forward
+        self.applyTranspose = model.transpose
+
+
+class MSOTmodel:
+    """MSOTmodel(probe, discretization, speed_of_sound, include_sir,
+    use_single_speed_of_sound, num_cropped_samples_at_sinogram_start,
+    filt_cutoff_min, filt_cutoff_max, model_normalization_factor)
+    (MSOTmodel.m:18) with single speed of sound.  SIR tables, when
+    include_sir, are given as ``sir_tables=(SPMR [NS, S], start_end [NS, 2]
+    1-based, SPMRIndices [n_det, P] 1-based)``.  ``max_batch`` sizes the
+    plan's scratch for batched applies and solves."""
+
+    def __init__(self, probe: Probe, discretization: Discretization, speed_of_sound: float,
+                 include_sir: bool = False, use_single_speed_of_sound: bool = True,
+                 num_cropped_samples_at_sinogram_start: int = 0, filt_cutoff_min: float = 1e5,
+                 filt_cutoff_max: float = 12e6, model_normalization_factor: float | None = None,
+                 sir_tables=None, max_batch: int = 1, norm_iterations: int = 100):
+        if not use_single_speed_of_sound:
+            raise NotImplementedError("dual speed of sound is not part of this build")
+        self.Probe = probe
+        self.Discretization = discretization
+        self.c = float(speed_of_sound)
+        self.include_sir = bool(include_sir)
+        self.n_crop = int(num_cropped_samples_at_sinogram_start)
+        self.fmin, self.fmax = float(filt_cutoff_min), float(filt_cutoff_max)
+        self.n_t = int(probe.n_samples - self.n_crop)
+        self.max_batch = int(max_batch)
+        disc = discretization
+        # travel-time indices (MSOTmodel.m:380-381; straight rays, refraction.m:327)
+        xd, zd = probe.detector_positions()
+        xp, zp = disc.pixel_coordinates()
+        dist = np.hypot(xd[:, None] - xp[None, :], zd[:, None] - zp[None, :])
+        self.travel = np.ascontiguousarray(dist / self.c * probe.fs - probe.delay - self.n_crop)
+        # interpolation radius (MSOTmodel.m:36-38)
+        self.radius = float(disc.dz / (self.c / probe.fs))
+        self.ir = model_impulse_response(probe, disc, self.c, self.fmin, self.fmax,
+                                         self.include_sir)
+        self.pre_x, self.pre_z = disc.prefilter_taps()
+        self.sir_tables = None
+        if self.include_sir:
+            if sir_tables is None:
+                raise ValueError("include_sir needs sir_tables (SPMR, start/end, indices)")
+            sir, se, idx = sir_tables
+            self.sir_tables = (np.ascontiguousarray(sir, dtype=np.float64),
+                               np.ascontiguousarray(se, dtype=np.int32),
+                               np.ascontiguousarray(idx, dtype=np.int32))
+        self._plan = None
+        self.norm = 1.0
+        self._make_plan(1.0)
+        if model_normalization_factor is None:
+            self.norm = self.estimate_sigma_max(norm_iterations)
+        else:
+            self.norm = float(model_normalization_factor)
+        self._make_plan(self.norm)
+        self.Funcs = _Funcs(self)
+
+    # --- plan -------------------------------------------------------------------
+    def _make_plan(self, norm: float):
+        L = _lib.load()
+        if self._plan:
+            L.msot_plan_destroy(self._plan)
+            self._plan = None
+        d = _lib.PlanDesc()
+        disc = self.Discretization
+        d.nx, d.nz = disc.nx, disc.nz
+        d.n_det, d.n_t = self.Probe.n_det, self.n_t
+        d.radius = self.radius
+        self._keep = [self.travel, self.ir, self.pre_x, self.pre_z]
+        d.travel = _dptr(self.travel)
+        d.ir_len = self.ir.size
+        d.ir = _dptr(self.ir)
+        d.pre_len_x, d.pre_len_z = self.pre_x.size, self.pre_z.size
+        d.pre_x, d.pre_z = _dptr(self.pre_x), _dptr(self.pre_z)
+        d.norm = norm
+        if self.sir_tables is not None:
+            sir, se, idx = self.sir_tables
+            self._keep += [sir, se, idx]
+            d.sir_len, d.n_sir = sir.shape[1], sir.shape[0]
+            d.sir, d.sir_start_end, d.sir_idx = _dptr(sir), _iptr(se), _iptr(idx)
+        d.max_batch = self.max_batch
+        h = C.c_void_p()
+        _lib.check(L.msot_plan_create(C.byref(d), C.byref(h)))
+        self._plan = h
+
+    def __del__(self):
+        try:
+            if self._plan:
+                _lib.load().msot_plan_destroy(self._plan)
+        except Exception:
+            pass
+
+    @property
+    def plan(self):
+        return self._plan
+
+    def estimate_sigma_max(self, iters: int = 100, seed: int = 0) -> float:
+        out = C.c_double()
+        _lib.check(_lib.load().msot_estimate_norm(self._plan, int(iters), int(seed),
+                                                  C.byref(out), _stream_ptr()))
+        return float(out.value)
+
+    # --- operators ----------------------------------------------------------------
+    @property
+    def image_shape(self):
+        return (self.Discretization.nx, self.Discretization.nz)
+
+    @property
+    def sinogram_shape(self):
+        return (self.Probe.n_det, self.n_t)
+
+    def _as_batch(self, x, inner):
+        t = torch.as_tensor(x)
+        if not t.is_cuda:
+            t = t.cuda()
+        t = t.to(torch.float32).reshape(-1, *inner).contiguous()
+        if t.shape[0] > self.max_batch:
+            raise ValueError(f"batch {t.shape[0]} > max_batch {self.max_batch}")
+        return t
+
+    def forward(self, p0, out=None, stream=None):
+        """Funcs.applyForward: [W, nx, nz] -> [W, n_det, n_t] (MSOTmodel.m:285)."""
+        x = self._as_batch(p0, self.image_shape)
+        W = x.shape[0]
+        if out is None:
+            out = torch.empty((W, *self.sinogram_shape), device=x.device, dtype=torch.float32)
+        _lib.check(_lib.load().msot_forward(self._plan, C.c_void_p(x.data_ptr()),
+                                            C.c_void_p(out.data_ptr()), W, _stream_ptr(stream)))
+        return out
+
+    def transpose(self, sig, out=None, stream=None):
+        """Funcs.applyTranspose: [W, n_det, n_t] -> [W, nx, nz] (MSOTmodel.m:286)."""
+        y = self._as_batch(sig, self.sinogram_shape)
+        W = y.shape[0]
+        if out is None:
+            out = torch.empty((W, *self.image_shape), device=y.device, dtype=torch.float32)
+        _lib.check(_lib.load().msot_transpose(self._plan, C.c_void_p(y.data_ptr()),
+                                              C.c_void_p(out.data_ptr()), W,
+                                              _stream_ptr(stream)))
+        return out
+
+    def interp_forward(self, coeffs, stream=None):
+        """The bare MEX operator (forwardDelayAndSumMex / forwardMex) on device."""
+        x = self._as_batch(coeffs, (self.Discretization.number_of_pixels,))
+        out = torch.empty((x.shape[0], *self.sinogram_shape), device=x.device)
+        _lib.check(_lib.load().msot_interp_forward(self._plan, C.c_void_p(x.data_ptr()),
+                                                   C.c_void_p(out.data_ptr()), x.shape[0],
+                                                   _stream_ptr(stream)))
+        return out
+
+    def interp_transpose(self, sig, stream=None):
+        y = self._as_batch(sig, self.sinogram_shape)
+        out = torch.empty((y.shape[0], self.Discretization.number_of_pixels), device=y.device)
+        _lib.check(_lib.load().msot_interp_transpose(self._plan, C.c_void_p(y.data_ptr()),
+                                                     C.c_void_p(out.data_ptr()), y.shape[0],
+                                                     _stream_ptr(stream)))
+        return out

@@ -1,0 +1,84 @@
+"""Non-negative solvers with the reference's MATLAB signatures, running on
+the GPU through the CUDA library.
+
+Inputs/outputs are torch tensors (CUDA) or numpy arrays in the layouts of
+model.py: data_filt [W, n_det, n_t], images [W, nx, nz].  By default the W
+slices are W independent reconstructions (one reference call each); with
+``coupled=True`` they are the wavelengths of ONE reference call (the
+reference's lsqr/cgs then see one stacked vector).  ``x0`` is an optional
+warm start (the reference's L2/TV cores always start from zero,
+nnls_L2_less.m:94).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from .model import MSOTmodel, _stream_ptr
+
+
+def _prep(model: MSOTmodel, data_filt, x0):
+    b = torch.as_tensor(data_filt)
+    if not b.is_cuda:
+        b = b.cuda()
+    b = b.to(torch.float32).reshape(-1, *model.sinogram_shape).contiguous()
+    W = b.shape[0]
+    if W > model.max_batch:
+        raise ValueError(f"batch {W} > model.max_batch {model.max_batch}")
+    x0p = None
+    if x0 is not None:
+        x0p = torch.as_tensor(x0).to(device=b.device, dtype=torch.float32)
+        x0p = x0p.reshape(W, *model.image_shape).contiguous()
+    rec = torch.empty((W, *model.image_shape), device=b.device, dtype=torch.float32)
+    return b, W, x0p, rec
+
+
+def rec_nn_with_L2_reg(model: MSOTmodel, data_filt, num_iter_nn_outer: int, lambdaL2: float = 0.0,
+                       RegL2="identity", RegL2T="identity", lambdaL2_2=None, RegL2_2=None,
+                       RegL2T_2=None, *, x0=None, coupled: bool = False, stream=None):
+    """rec_nn_with_L2_reg.m:1.  Returns (rec_img, lCurveErrImg, lCurveErrReg,
+    lCurveErrReg_2, err, t) like the reference; lCurveErr* are per-instance
+    numpy arrays (one value when coupled), err is empty (the reference only
+    fills it when calculate_objective_per_iter is set, which it hard-codes
+    to false) and t is the wall time of the solve in seconds."""
+    if lambdaL2 and lambdaL2 > 0 and RegL2 not in ("identity", None):
+        raise NotImplementedError("only the identity L2 regulariser is supported")
+    if lambdaL2_2 and lambdaL2_2 > 0:
+        raise NotImplementedError("the second (Laplacian) L2 term is not part of this build")
+    b, W, x0p, rec = _prep(model, data_filt, x0)
+    e1 = np.zeros(W)
+    e2 = np.zeros(W)
+    t0 = time.perf_counter()
+    _lib.check(_lib.load().msot_rec_nn_with_L2_reg(
+        model.plan, C.c_void_p(b.data_ptr()), C.c_void_p(rec.data_ptr()), W,
+        int(num_iter_nn_outer), float(lambdaL2 or 0.0),
+        C.c_void_p(x0p.data_ptr()) if x0p is not None else None, 1 if coupled else 0,
+        e1.ctypes.data_as(C.POINTER(C.c_double)), e2.ctypes.data_as(C.POINTER(C.c_double)),
+        _stream_ptr(stream)))
+    t = time.perf_counter() - t0
+    if coupled:
+        e1, e2 = np.array([e1.sum()]), np.array([e2.sum()])
+    return rec, e1, e2, np.zeros_like(e1), np.zeros(0), t
+
+
+def rec_nn_with_L1_eye_reg(model: MSOTmodel, data_filt, num_iter: int, regParam: float, *,
+                           x0=None, coupled: bool = False, stream=None):
+    """rec_nn_with_L1_eye_reg.m:1.  Returns (rec_img, lCurveErrImg,
+    lCurveErrReg, err, t); the start value is A^T b unless x0 is given."""
+    b, W, x0p, rec = _prep(model, data_filt, x0)
+    e1 = np.zeros(W)
+    e2 = np.zeros(W)
+    t0 = time.perf_counter()
+    _lib.check(_lib.load().msot_rec_nn_with_L1_eye_reg(
+        model.plan, C.c_void_p(b.data_ptr()), C.c_void_p(rec.data_ptr()), W, int(num_iter),
+        float(regParam), C.c_void_p(x0p.data_ptr()) if x0p is not None else None,
+        1 if coupled else 0, e1.ctypes.data_as(C.POINTER(C.c_double)),
+        e2.ctypes.data_as(C.POINTER(C.c_double)), _stream_ptr(stream)))
+    t = time.perf_counter() - t0
+    if coupled:
+        e1, e2 = np.array([e1.sum()]), np.array([e2.sum()])
+    return rec, e1, e2, np.zeros(0), t

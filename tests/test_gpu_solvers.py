@@ -1,0 +1,88 @@
+"""GPU solvers against the FP64 oracle solve of the same algorithm.
+Bar (the headline metric's): relative error <= 1e-3 per instance."""
+import numpy as np
+import pytest
+
+from oracle import model as M
+from oracle import solvers as S
+from pairs import make_pair, rel
+
+pytestmark = pytest.mark.gpu
+
+
+def _data(om, n, W, seed):
+    rng = np.random.default_rng(seed)
+    imgs, bs = [], []
+    for _ in range(W):
+        img = M.phantom(om.grid, rng)
+        imgs.append(img)
+        bs.append(M.noisy_sinogram(om, img, rng))
+    return np.stack(imgs), np.stack(bs)
+
+
+@pytest.fixture(scope="module")
+def norm_pair(cuda):
+    pm, om = make_pair(n=64, n_det=128, n_samples=1200, radius=0.02, fov_half=0.0063,
+                       norm=1.0, max_batch=4)
+    s = pm.estimate_sigma_max(100)
+    pm2, om2 = make_pair(n=64, n_det=128, n_samples=1200, radius=0.02, fov_half=0.0063,
+                         norm=s, max_batch=4)
+    return pm2, om2
+
+
+def test_l2_nnls_matches_fp64_oracle(norm_pair):
+    import torch
+    from msot_gb300 import rec_nn_with_L2_reg
+    pm, om = norm_pair
+    _, b = _data(om, 64, 3, 21)
+    rec, e_img, e_reg, _, _, _ = rec_nn_with_L2_reg(pm, torch.tensor(b, dtype=torch.float32),
+                                                    50, 1e-2)
+    rec = rec.cpu().numpy()
+    fwd = lambda v: om.forward(v.reshape(1, 64, 64)).ravel()
+    adj = lambda y: om.transpose(y.reshape(1, 128, -1)).ravel()
+    for w in range(3):
+        ref, ref_img, ref_reg = S.rec_nn_with_L2_reg(fwd, adj, b[w].ravel(), 64 * 64, 50, 1e-2)
+        assert rec[w].min() >= 0
+        assert rel(rec[w], ref) <= 1e-3
+        assert abs(e_img[w] - ref_img) / ref_img < 1e-3
+        assert abs(e_reg[w] - ref_reg) / ref_reg < 1e-3
+
+
+def test_l2_nnls_coupled_wavelengths(norm_pair):
+    import torch
+    from msot_gb300 import rec_nn_with_L2_reg
+    pm, om = norm_pair
+    _, b = _data(om, 64, 2, 22)
+    rec = rec_nn_with_L2_reg(pm, torch.tensor(b, dtype=torch.float32), 20, 1e-2,
+                             coupled=True)[0].cpu().numpy()
+    fwd = lambda v: om.forward(v.reshape(2, 64, 64)).ravel()
+    adj = lambda y: om.transpose(y.reshape(2, 128, -1)).ravel()
+    ref = S.rec_nn_with_L2_reg(fwd, adj, b.ravel(), 2 * 64 * 64, 20, 1e-2)[0]
+    assert rel(rec, ref) <= 1e-3
+
+
+def test_l2_warm_start_is_used(norm_pair):
+    import torch
+    from msot_gb300 import rec_nn_with_L2_reg
+    pm, om = norm_pair
+    img, b = _data(om, 64, 1, 23)
+    bt = torch.tensor(b, dtype=torch.float32)
+    cold = rec_nn_with_L2_reg(pm, bt, 2, 1e-2)[0]
+    warm = rec_nn_with_L2_reg(pm, bt, 2, 1e-2, x0=torch.tensor(img, dtype=torch.float32))[0]
+    assert rel(warm.cpu().numpy(), cold.cpu().numpy()) > 1e-2
+
+
+def test_l1_nnls_matches_fp64_oracle(norm_pair):
+    import torch
+    from msot_gb300 import rec_nn_with_L1_eye_reg
+    pm, om = norm_pair
+    _, b = _data(om, 64, 2, 24)
+    rec, e_img, e_reg, _, _ = rec_nn_with_L1_eye_reg(pm, torch.tensor(b, dtype=torch.float32),
+                                                     15, 1e-3)
+    rec = rec.cpu().numpy()
+    fwd = lambda v: om.forward(v.reshape(1, 64, 64)).ravel()
+    adj = lambda y: om.transpose(y.reshape(1, 128, -1)).ravel()
+    for w in range(2):
+        ref, ref_img, ref_reg = S.rec_nn_with_L1_eye_reg(fwd, adj, b[w].ravel(), 15, 1e-3)
+        assert rel(rec[w], ref) <= 1e-3
+        assert abs(e_img[w] - ref_img) / ref_img < 1e-3

@@ -1,0 +1,72 @@
+"""CPU tests of the product's host-side logic against the oracle, and of the
+C-ABI library's exports (no device calls)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import model as M
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_discretization_taps_match_oracle():
+    from msot_gb300 import Discretization
+    for n in (128, 200, 101):
+        d = Discretization([-0.0127, 0.0127], n)
+        tx, tz = d.prefilter_taps()
+        g = M.Grid(n, n, (-0.0127, 0.0127, -0.0127, 0.0127))
+        ox = M.separable_prefilter_taps(n, g.spacing()[0], g.sigma())
+        K = min(tx.size, ox.size) // 2
+        cx, co = tx.size // 2, ox.size // 2
+        assert np.allclose(tx[cx - K:cx + K + 1], ox[co - K:co + K + 1], rtol=0, atol=1e-15)
+
+
+def test_impulse_response_and_travel_times_match_oracle():
+    from msot_gb300 import Discretization, Probe
+    from msot_gb300.model import model_impulse_response
+    eir = M.gauss_pulse_eir()
+    p = Probe(eir=eir)
+    d = Discretization([-0.0127, 0.0127], 128)
+    ir = model_impulse_response(p, d, 1500.0, 1e5, 12e6, False)
+    op = M.config1_probe()
+    og = M.config_grid(128)
+    ref = M.impulse_response(op, og, 1500.0, 1e5, 12e6)
+    assert np.allclose(ir, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+    ir_sir = model_impulse_response(p, d, 1500.0, 1e5, 12e6, True)
+    ref_sir = M.impulse_response(op, og, 1500.0, 1e5, 12e6, include_sir=True)
+    assert np.allclose(ir_sir, ref_sir, rtol=0, atol=1e-12 * np.abs(ref_sir).max())
+    xd, zd = p.detector_positions()
+    oxd, ozd = op.positions()
+    assert np.allclose(xd, oxd, atol=1e-15) and np.allclose(zd, ozd, atol=1e-15)
+
+
+def declared_symbols():
+    with open(os.path.join(ROOT, "include", "msot_gpu.h")) as f:
+        text = f.read()
+    return sorted(set(re.findall(r"\b(msot_[A-Za-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    from msot_gb300 import _build, _lib
+    path = _lib.lib_path()
+    if not os.path.exists(path):
+        _build.build()
+    lib = ctypes.CDLL(path)
+    syms = declared_symbols()
+    assert len(syms) >= 16
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+    # every declared symbol also has a Python binding
+    assert set(syms) <= set(_lib.SIGNATURES), set(syms) - set(_lib.SIGNATURES)
+
+
+def test_library_reports_errors_without_a_device():
+    from msot_gb300 import _lib
+    L = _lib.load(build_if_missing=True)
+    assert L.msot_version() >= 1
+    h = ctypes.c_void_p()
+    rc = L.msot_plan_create(None, ctypes.byref(h))
+    assert rc == -1 and b"plan" in L.msot_last_error()

@@ -1,0 +1,156 @@
+"""CPU tests of the oracle: the C restatement against the golden vectors made
+by the reference's own MEX code, and the FP64 model/solver restatements."""
+import numpy as np
+import pytest
+
+from oracle import model as M
+from oracle import native
+from oracle import solvers as S
+
+
+@pytest.fixture(scope="module")
+def port():
+    return native.port()
+
+
+@pytest.mark.parametrize("W", [1, 5])
+def test_port_das_matches_reference_bitwise(port, golden, W):
+    tau, r, T = golden["tau"], float(golden["radius"]), int(golden["T"])
+    y = port.forward_das(golden[f"das_img_w{W}"], tau, T, r)
+    assert np.array_equal(y, golden[f"das_fwd_w{W}"])
+    x = port.transpose_das(golden[f"das_sig_w{W}"], tau, r)
+    assert np.array_equal(x, golden[f"das_adj_w{W}"])
+
+
+@pytest.mark.parametrize("W", [1, 3])
+def test_port_sir_matches_reference_bitwise(port, golden, W):
+    g = golden
+    r, T = float(g["radius"]), int(g["sir_T"])
+    y = port.forward_sir(g[f"sir_img_w{W}"], g["sir_idx"], g["sir_tau"], g["sir"], T, g["sir_se"], r)
+    assert np.array_equal(y, g[f"sir_fwd_w{W}"])
+    x = port.transpose_sir(g[f"sir_sig_w{W}"], g["sir_idx"], g["sir_tau"], g["sir"], g["sir_se"], r)
+    assert np.array_equal(x, g[f"sir_adj_w{W}"])
+
+
+@pytest.mark.skipif(not native.ref_available(), reason="reference MEX not compiled on this host")
+def test_reference_library_reproduces_golden(golden):
+    ref = native.ref()
+    tau, r, T = golden["tau"], float(golden["radius"]), int(golden["T"])
+    assert np.array_equal(ref.forward_das(golden["das_img_w5"], tau, T, r), golden["das_fwd_w5"])
+
+
+def test_port_rejects_out_of_range_taps(port, golden):
+    tau, r, T = golden["tau"], float(golden["radius"]), int(golden["T"])
+    bad = tau.copy()
+    bad[3, 7] = T - 1.0  # taps past the end of the sinogram
+    with pytest.raises(ValueError):
+        port.forward_das(golden["das_img_w1"], bad, T, r)
+    bad[3, 7] = np.nan
+    with pytest.raises(ValueError):
+        port.transpose_das(golden["das_sig_w1"], bad, r)
+
+
+def test_port_adjoint_config1_geometry(port):
+    probe, grid = M.config1_probe(eir=False), M.config_grid(128)
+    tau = M.travel_time_indices(probe, grid, 1500.0)
+    r = M.interpolation_radius(grid, probe, 1500.0)
+    rng = np.random.default_rng(0)
+    x = rng.random((grid.n_pix, 2))
+    y = rng.standard_normal((probe.n_det, probe.n_samples, 2))
+    Ax = port.forward_das(x, tau, probe.n_samples, r)
+    Aty = port.transpose_das(y, tau, r)
+    err = abs(np.vdot(Ax, y) - np.vdot(x, Aty)) / (np.linalg.norm(Ax) * np.linalg.norm(y))
+    assert err < 1e-13
+
+
+@pytest.mark.parametrize("n", [128, 101, 40])
+def test_separable_prefilter_equals_2d_fft_prefilter(n):
+    grid = M.Grid(n, n, (-0.0127, 0.0127, -0.0127, 0.0127))
+    pre = M.prefilter(grid)
+    rng = np.random.default_rng(n)
+    img = rng.random((1, n, n))
+    ref = M.project(img, pre)[0]
+    dx, dz = grid.spacing()
+    hx = M.separable_prefilter_taps(n, dx, grid.sigma())
+    hz = M.separable_prefilter_taps(n, dz, grid.sigma())
+    Kx, Kz = hx.size // 2, hz.size // 2
+    m = img[0]  # (nx, nz)
+    out = np.zeros_like(m)
+    for k in range(-Kz, Kz + 1):
+        out += hz[k + Kz] * np.roll(m, k, axis=1)
+    out2 = np.zeros_like(m)
+    for k in range(-Kx, Kx + 1):
+        out2 += hx[k + Kx] * np.roll(out, k, axis=0)
+    assert np.max(np.abs(out2 - ref)) < 1e-11 * np.max(np.abs(ref))
+
+
+def test_oracle_model_is_adjoint():
+    probe = M.ArcProbe(n_det=32, radius=0.02, coverage_deg=135, n_samples=800,
+                       eir=M.gauss_pulse_eir(n_taps=64), eir_length=65)
+    grid = M.Grid(24, 20, (-0.003, 0.003, -0.0025, 0.0025))
+    m = M.Model(probe, grid, c=1500.0)
+    rng = np.random.default_rng(1)
+    x = rng.random((2, 24, 20))
+    y = rng.standard_normal((2, 32, 800))
+    Ax, Aty = m.forward(x), m.transpose(y)
+    err = abs(np.vdot(Ax, y) - np.vdot(x, Aty)) / (np.linalg.norm(Ax) * np.linalg.norm(y))
+    assert err < 1e-12
+
+
+def test_convolve_ir_matches_direct_fir():
+    rng = np.random.default_rng(2)
+    ir = rng.standard_normal(9)
+    s = rng.standard_normal((3, 40))
+    y = M.convolve_ir(s, ir)
+    h = ir.size // 2
+    direct = np.zeros_like(s)
+    for t in range(40):
+        for k in range(ir.size):
+            u = t + h - k
+            if 0 <= u < 40:
+                direct[:, t] += ir[k] * s[:, u]
+    assert np.allclose(y, direct, rtol=0, atol=1e-12)
+
+
+def test_lsqr_restatement_matches_scipy():
+    from scipy.sparse.linalg import lsqr as sp_lsqr
+    rng = np.random.default_rng(3)
+    A = rng.standard_normal((40, 15))
+    b = rng.standard_normal(40)
+    x0 = rng.standard_normal(15)
+    ours = S.lsqr(lambda v: A @ v, lambda u: A.T @ u, b, 1e-12, 3, x0)
+    ref = sp_lsqr(A, b, atol=0, btol=0, iter_lim=3, x0=x0)[0]
+    assert np.allclose(ours, ref, rtol=1e-10, atol=1e-12)
+
+
+def test_cgs_restatement_solves_spd_system():
+    rng = np.random.default_rng(4)
+    B = rng.standard_normal((20, 20))
+    A = B @ B.T + 20 * np.eye(20)
+    b = rng.standard_normal(20)
+    x = S.cgs(lambda v: A @ v, b, 1e-12, 200)
+    assert np.linalg.norm(A @ x - b) < 1e-9 * np.linalg.norm(b)
+    # not converged after 2 steps: returns the iterate of smallest residual
+    x2 = S.cgs(lambda v: A @ v, b, 1e-12, 2)
+    assert np.linalg.norm(A @ x2 - b) <= np.linalg.norm(b)
+
+
+def test_l2_nnls_oracle_is_nonnegative_and_fits():
+    rng = np.random.default_rng(5)
+    A = rng.random((60, 30))
+    xt = np.maximum(rng.standard_normal(30), 0)
+    b = A @ xt
+    rec, e_img, e_reg = S.rec_nn_with_L2_reg(lambda v: A @ v, lambda u: A.T @ u, b, 30, 200, 1e-4)
+    assert rec.min() >= 0
+    assert e_img < 0.1 * np.linalg.norm(b) ** 2
+
+
+def test_sb_itv2_reduces_tv():
+    rng = np.random.default_rng(6)
+    n = 12
+    B, Bt, BtB = S.diff_oper(n)
+    g = np.zeros((n, n))
+    g[3:8, 4:9] = 1.0
+    g += 0.1 * rng.standard_normal((n, n))
+    u = S.sb_itv2(g, 0.05, B, Bt, BtB).reshape(n, n, order="F")
+    assert S.itv(u) < S.itv(g)
