@@ -21,10 +21,14 @@ from . import _lib
 
 
 def _dptr(a: np.ndarray):
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise TypeError("FP64 C-contiguous array required at the C ABI")
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
 def _iptr(a: np.ndarray):
+    if a.dtype != np.int32 or not a.flags.c_contiguous:
+        raise TypeError("int32 C-contiguous array required at the C ABI")
     return a.ctypes.data_as(C.POINTER(C.c_int32))
 
 
@@ -207,9 +211,11 @@ class MSOTmodel:
         self.travel = np.ascontiguousarray(dist / self.c * probe.fs - probe.delay - self.n_crop)
         # interpolation radius (MSOTmodel.m:36-38)
         self.radius = float(disc.dz / (self.c / probe.fs))
-        self.ir = model_impulse_response(probe, disc, self.c, self.fmin, self.fmax,
-                                         self.include_sir)
-        self.pre_x, self.pre_z = disc.prefilter_taps()
+        self.ir = np.ascontiguousarray(
+            model_impulse_response(probe, disc, self.c, self.fmin, self.fmax, self.include_sir),
+            dtype=np.float64)
+        self.pre_x, self.pre_z = (np.ascontiguousarray(t, dtype=np.float64)
+                                  for t in disc.prefilter_taps())
         self.sir_tables = None
         if self.include_sir:
             if sir_tables is None:
