@@ -1,0 +1,372 @@
+"""Benchmark: batched non-negative L2-regularised reconstruction
+(rec_nn_with_L2_reg) on one GB300, checked against the FP64 oracle solve.
+
+Workload (one "step" = one batched solve of --batch independent sinograms):
+  128 x 128 px at 0.2 mm pitch (25.4 mm FOV); 256-element arc, R = 40 mm,
+  135 deg; 2030 samples at 40 MHz; c = 1500 m/s; Gaussian-modulated 5 MHz EIR
+  (60 % bandwidth, 256 taps zero-padded to 257); Butterworth [0.1, 12] MHz;
+  no SIR; disk + vessel phantoms, 1 % Gaussian noise; lambdaL2 = 1e-2
+  (identity), 50 outer iterations; the model is normalised by its largest
+  singular value (power iteration on the GPU).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--batch B] [--impl ours|reference]
+
+Prints ONE JSON line (rank 0).  ``value`` is recons/s with the sinograms
+already in HBM; ``e2e`` is the same metric through the public Python API
+with pinned host buffers (H2D of the sinograms and D2H of the images inside
+the timed region).  ``--impl reference`` times the CPU implementation of the
+same path (the reference's compiled MEX when it was built on this host,
+otherwise the project's C restatement of it, inside the FP64 wrappers and
+solver) on a bounded sample of the workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import platform
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "mb-rec-msot_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "NNLS recons/s at <=1e-3 rel. error vs FP64: learned+batched vs plain, 1 GB300"
+N_GRID, N_DET, N_T, N_ITER, LAMBDA = 128, 256, 2030, 50, 1e-2
+HBM_FALLBACK_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-oracle", action="store_true", help="skip the FP64 oracle solve")
+    return ap.parse_args()
+
+
+def workload_config(batch, n_gpus):
+    return {
+        "workload": "rec_nn_with_L2_reg, 128x128 px @0.2 mm, 256-el arc R=40 mm 135 deg, "
+                    "2030 samples @40 MHz, EIR 257 taps, lambdaL2=1e-2, 50 outer iterations",
+        "grid": [N_GRID, N_GRID], "n_det": N_DET, "n_t": N_T, "iterations": N_ITER,
+        "lambdaL2": LAMBDA, "batch_per_gpu": batch, "global_batch": batch * n_gpus,
+        "parallelism": f"replicas x{n_gpus}",
+        "l2": "flushed (512 MB write) between timed steps",
+    }
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+# ----------------------------------------------------------------------------
+# clocks during the timed region
+# ----------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        self.idx = gpu_index
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-i", str(self.idx), "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax = float(parts[2])
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------
+# our implementation
+# ----------------------------------------------------------------------------
+def build_model(batch):
+    from msot_gb300 import Discretization, MSOTmodel, Probe
+    from msot_gb300.synthetic import gauss_pulse_eir
+    h = 0.2e-3 * 127 / 2
+    probe = Probe(n_det=N_DET, radius=0.040, angular_coverage=135.0, fs=4e7, n_samples=N_T,
+                  delay=0.0, eir=gauss_pulse_eir(), eir_length=257)
+    disc = Discretization([-h, h], N_GRID)
+    return MSOTmodel(probe, disc, 1500.0, False, True, 0, 1e5, 12e6, None, max_batch=batch)
+
+
+def make_data(model, batch, seed):
+    """Seeded disk + vessel phantoms -> sinograms on the GPU (+1 % noise)."""
+    import torch
+    from msot_gb300.synthetic import phantom
+    rng = np.random.default_rng(seed)
+    imgs = np.stack([phantom(model.Discretization, rng) for _ in range(batch)]).astype(np.float32)
+    x = torch.tensor(imgs, device="cuda")
+    y = model.forward(x)
+    amp = y.abs().amax(dim=(1, 2), keepdim=True)
+    gen = torch.Generator(device="cuda").manual_seed(seed)
+    y = y + 0.01 * amp * torch.randn(y.shape, device="cuda", generator=gen)
+    return x, y.contiguous()
+
+
+def oracle_solve(model, b_np, threads):
+    """CPU-baseline leg: FP64 oracle solve of one instance with the same model
+    parameters as the GPU plan; its result is also the accuracy reference."""
+    from oracle import model as M
+    from oracle import native
+    from oracle import solvers as S
+    native.port().set_threads(threads)
+    g = model.Discretization
+    p = model.Probe
+    op = M.ArcProbe(n_det=p.n_det, radius=p.radius, coverage_deg=p.angular_coverage, fs=p.fs,
+                    n_samples=p.n_samples, delay=p.delay, eir=p.eir, eir_length=p.eir_length)
+    om = M.Model(op, M.Grid(g.nx, g.nz, g.fov), c=model.c, fmin=model.fmin, fmax=model.fmax,
+                 norm=model.norm)
+    P = g.nx * g.nz
+    fwd = lambda v: om.forward(v.reshape(1, g.nx, g.nz)).ravel()
+    adj = lambda y: om.transpose(y.reshape(1, p.n_det, -1)).ravel()
+    t0 = time.perf_counter()
+    rec, _, _ = S.rec_nn_with_L2_reg(fwd, adj, b_np.astype(np.float64).ravel(), P, N_ITER, LAMBDA)
+    return rec.reshape(g.nx, g.nz), time.perf_counter() - t0
+
+
+def algorithmic_bytes(kid_name, batch):
+    P, D, T = N_GRID * N_GRID, N_DET, N_T
+    if kid_name in ("interp_forward", "interp_adjoint"):
+        return 4 * P * D + 4 * P * batch + 4 * T * D * batch
+    if kid_name == "ir_conv":
+        return 2 * 4 * T * D * batch
+    if kid_name == "prefilter":
+        return 2 * 4 * P * batch
+    if kid_name == "permute":
+        return 2 * 4 * P * batch + 4 * P
+    return None
+
+
+def run_ours(args, rank, world):
+    import torch
+    from msot_gb300 import _lib, rec_nn_with_L2_reg
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    L = _lib.load()
+    B = args.batch
+    model = build_model(B)
+    x_true, b = make_data(model, B, seed=1000 + rank)
+    flush = torch.empty(512 * 1024 * 1024 // 4, device="cuda")
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+    for _ in range(args.warmup):
+        rec = rec_nn_with_L2_reg(model, b, N_ITER, LAMBDA)[0]
+    torch.cuda.synchronize()
+    # --- timed region: K batched solves, device time by CUDA events ----------------
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    n0 = L.msot_launch_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with Clocks(torch.cuda.current_device()) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record()
+            rec = rec_nn_with_L2_reg(model, b, N_ITER, LAMBDA)[0]
+            ev[k][1].record()
+        torch.cuda.synchronize()
+    launches = L.msot_launch_count() - n0
+    ms = float(sum(a.elapsed_time(z) for a, z in ev))
+    if dist:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = B * world / (ms_per_step / 1e3)
+    # --- end to end through the public API with host buffers --------------------------
+    b_host = b.cpu().pin_memory()
+    rec_host = torch.empty((B, N_GRID, N_GRID), dtype=torch.float32).pin_memory()
+    e2e_ms = 0.0
+    for k in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = rec_nn_with_L2_reg(model, b_host, N_ITER, LAMBDA)[0]
+        rec_host.copy_(r)
+        torch.cuda.synchronize()
+        e2e_ms += (time.perf_counter() - t0) * 1e3
+    e2e_ms /= args.steps
+    if dist:
+        t = torch.tensor([e2e_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e = {"value": B * world / (e2e_ms / 1e3), "unit": "recons/s",
+           "h2d_bytes_per_step": int(b_host.numel() * 4),
+           "d2h_bytes_per_step": int(rec_host.numel() * 4)}
+    # --- live per-kernel event timing (one instrumented solve) ------------------------
+    L.msot_profile_enable(1)
+    rec_nn_with_L2_reg(model, b, N_ITER, LAMBDA)
+    torch.cuda.synchronize()
+    fam = {}
+    import ctypes as C
+    for kid in range(16):
+        name = L.msot_profile_kernel_name(kid)
+        if not name:
+            break
+        n, t = C.c_int(), C.c_double()
+        L.msot_profile_read(kid, C.byref(n), C.byref(t))
+        if n.value:
+            fam[name.decode()] = {"launches": n.value, "ms": t.value}
+    L.msot_profile_enable(0)
+    if rank != 0:
+        return None
+    peak, peak_kind = peaks()
+    dom = max(fam.items(), key=lambda kv: kv[1]["ms"]) if fam else None
+    roof = None
+    if dom:
+        name, d = dom
+        avg_s = d["ms"] / d["launches"] / 1e3
+        alg = algorithmic_bytes(name, B)
+        ach = alg / avg_s / 1e9 if alg else None
+        roof = {"bound": "hbm", "kernel": name, "achieved": ach, "peak": peak, "unit": "GB/s",
+                "frac": ach / peak if ach else None, "traffic": None,
+                "peak_source": f"{peak_kind} hbm_gbs (copy)",
+                "avg_launch_us": avg_s * 1e6, "bytes_per_launch": alg,
+                "families_ms_per_solve": {k: round(v["ms"], 3) for k, v in fam.items()}}
+    # --- FP64 oracle: accuracy of instance 0 + the CPU baseline sample ----------------
+    acc = None
+    cpu = None
+    if not args.no_oracle:
+        threads = os.cpu_count() or 1
+        ref, t_cpu = oracle_solve(model, b[0].cpu().numpy(), threads)
+        got = rec[0].cpu().numpy().astype(np.float64)
+        acc = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+        cpu = {"value": 1.0 / t_cpu, "unit": "recons/s", "cores": threads, "kind": "port",
+               "sample": "one full 50-iteration FP64 solve of instance 0 (C restatement of the "
+                         "MEX kernels + numpy FFT wrappers/LSQR)"}
+    return {
+        "metric": METRIC, "value": value, "unit": "recons/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded disk+vessel phantoms, 1% noise)",
+        "config": workload_config(B, world), "clocks": clk.summary(), "e2e": e2e,
+        "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
+        "rel_error_vs_fp64": acc, "host": platform.machine(),
+    }
+
+
+# ----------------------------------------------------------------------------
+# reference arm: the CPU implementation of the same path
+# ----------------------------------------------------------------------------
+SAMPLE_ITERS = 5
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return None
+    from oracle import model as M
+    from oracle import native
+    from oracle import solvers as S
+    threads = os.cpu_count() or 1
+    if native.ref_available() and platform.machine() in ("x86_64", "AMD64"):
+        lib, kind = native.ref(), "reference"
+    else:
+        lib, kind = native.port(), "port"
+    lib.set_threads(threads)
+    probe = M.config1_probe()
+    grid = M.config_grid(N_GRID)
+    om = M.Model(probe, grid, c=1500.0, lib=lib)
+    om.norm = 2.0243e-05  # sigma_max of this geometry (power iteration); scales time not work
+    rng = np.random.default_rng(1000)
+    img = M.phantom(grid, rng)
+    b = M.noisy_sinogram(om, img, rng).ravel()
+    fwd = lambda v: om.forward(v.reshape(1, N_GRID, N_GRID)).ravel()
+    adj = lambda y: om.transpose(y.reshape(1, N_DET, -1)).ravel()
+    times = []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        S.rec_nn_with_L2_reg(fwd, adj, b, N_GRID * N_GRID, SAMPLE_ITERS, LAMBDA)
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            times.append(dt)
+    t_step = float(np.mean(times))
+    value = (SAMPLE_ITERS / N_ITER) / t_step  # recons/s, extrapolated from the sample
+    sample = (f"{SAMPLE_ITERS} of the {N_ITER} outer iterations of one instance per step, "
+              f"{'reference MEX' if kind == 'reference' else 'C restatement of the MEX'} "
+              f"kernels in FP64 numpy wrappers; recons/s = ({SAMPLE_ITERS}/{N_ITER}) / step time")
+    return {
+        "metric": METRIC, "value": value, "unit": "recons/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(1, 1), "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "recons/s", "cores": threads, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "recons/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "host": platform.machine(),
+    }
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        out = run_reference(args, rank)
+    else:
+        if world > 1:
+            import torch
+            import torch.distributed as dist
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+            dist.init_process_group("nccl")
+        out = run_ours(args, rank, world)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -117,6 +117,20 @@ int msot_rec_nn_with_L1_eye_reg(msot_plan_t plan, const float *d_b, float *d_rec
                                 double *err_img, double *err_reg, void *stream);
 
 /* ------------------------------------------------------------------------ */
+/* Instrumentation (no counterpart in the reference, whose only timing is
+ * tic/toc, e.g. rec_nn_with_L2_reg.m:44-49). */
+
+/* Number of kernels the library has launched since it was loaded. */
+long long msot_launch_count(void);
+/* on != 0: record a CUDA event pair around every launch of the hot kernel
+ * families (reset on each call); 0 disables. */
+int msot_profile_enable(int on);
+/* Name of kernel family `kid` (0..6), NULL past the end. */
+const char *msot_profile_kernel_name(int kid);
+/* Launches and summed event time (ms) recorded for family `kid`; syncs the device. */
+int msot_profile_read(int kid, int *launches, double *total_ms);
+
+/* ------------------------------------------------------------------------ */
 /* Host-buffer entry points with the reference MEX contracts (FP64 in/out,
  * column-major, MATLAB-owned inputs; output written to caller memory that
  * MATLAB allocated with mxCreate*).  Arithmetic is FP32 on the GPU. */

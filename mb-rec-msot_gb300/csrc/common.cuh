@@ -15,6 +15,7 @@
 // [W][n_det][n_t].
 #pragma once
 
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <cuda_runtime.h>
@@ -62,6 +63,37 @@ struct Plan {
 };
 
 const char *set_error(const char *fmt, ...);
+
+// launch counter (every kernel launch of the library goes through KLAUNCH)
+extern std::atomic<long long> g_launch_count;
+#define KLAUNCH(...) (++::msot::g_launch_count, __VA_ARGS__)
+
+// kernel families timed by TimedScope when profiling is enabled
+enum KernelId {
+    KID_PREFILTER = 0,
+    KID_INTERP_FWD = 1,
+    KID_INTERP_ADJ = 2,
+    KID_CONV = 3,
+    KID_VECTOR = 4,
+    KID_PERMUTE = 5,
+    KID_TOEPLITZ = 6,
+    KID_COUNT = 7
+};
+
+// Records a CUDA event pair around the launches in its scope (on stream st)
+// when profiling is enabled (msot_profile_enable); otherwise does nothing.
+class TimedScope {
+  public:
+    TimedScope(int kid, cudaStream_t st);
+    ~TimedScope();
+    TimedScope(const TimedScope &) = delete;
+    TimedScope &operator=(const TimedScope &) = delete;
+
+  private:
+    int kid_;
+    cudaStream_t st_;
+    long slot_;
+};
 
 #define MSOT_CUDA_TRY(expr)                                                            \
     do {                                                                               \

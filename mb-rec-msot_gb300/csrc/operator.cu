@@ -389,19 +389,21 @@ static int set_smem(K kern, size_t bytes) {
 
 int launch_prefilter(const Plan &pl, const float *in, float *out, int W, bool transpose,
                      bool along_x, float scale, bool out_perm, cudaStream_t st) {
+    TimedScope ts_(KID_PREFILTER, st);
     const int K = along_x ? pl.Kx : pl.Kz;
     const float *taps = along_x ? pl.pre_x : pl.pre_z;
     const long n = (long)W * pl.P;
-    k_prefilter<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+    KLAUNCH(k_prefilter<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
         in, out, taps, K, pl.nx, pl.nz, W, along_x, transpose, scale,
-        out_perm ? pl.perm : nullptr);
+        out_perm ? pl.perm : nullptr));
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
 }
 
 int launch_permute(const Plan &pl, const float *in, float *out, int W, cudaStream_t st) {
+    TimedScope ts_(KID_PERMUTE, st);
     const long n = (long)W * pl.P;
-    k_permute<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, pl.perm, pl.P, W);
+    KLAUNCH(k_permute<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, pl.perm, pl.P, W));
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
 }
@@ -416,6 +418,7 @@ static int fwd_split(const Plan &pl, int nwt) {
 
 int launch_das_forward(const Plan &pl, const float *x_pi, float *raw, int W, float scale,
                        cudaStream_t st) {
+    TimedScope ts_(KID_INTERP_FWD, st);
     const int wt = pick_wt(W, pl.T, 8);
     const int ns = fwd_split(pl, W / wt);
     if (ns > 1) MSOT_CUDA_TRY(cudaMemsetAsync(raw, 0, sizeof(float) * W * pl.D * pl.T, st));
@@ -425,8 +428,8 @@ int launch_das_forward(const Plan &pl, const float *x_pi, float *raw, int W, flo
 #define CASE(WT)                                                                          \
     case WT:                                                                              \
         if ((rc = set_smem(k_das_fwd<WT>, smem)) != MSOT_OK) return rc;                   \
-        k_das_fwd<WT><<<grid, 256, smem, st>>>(pl.tau_pi, x_pi, raw, pl.P, pl.D, pl.T,     \
-                                               pl.frac_bits, pl.r_fx, pl.c1, scale, ns);  \
+        KLAUNCH(k_das_fwd<WT><<<grid, 256, smem, st>>>(pl.tau_pi, x_pi, raw, pl.P, pl.D, pl.T,     \
+                                               pl.frac_bits, pl.r_fx, pl.c1, scale, ns));  \
         break;
     switch (wt) {
         CASE(1) CASE(2) CASE(4) CASE(8)
@@ -438,13 +441,14 @@ int launch_das_forward(const Plan &pl, const float *x_pi, float *raw, int W, flo
 
 int launch_das_adjoint(const Plan &pl, const float *raw, float *x, int W, float scale,
                        cudaStream_t st) {
+    TimedScope ts_(KID_INTERP_ADJ, st);
     const int wt = pick_wt(W, 1, 8);
     dim3 grid(pl.n_patch, W / wt);
 #define CASE(WT)                                                                          \
     case WT:                                                                              \
-        k_das_adj<WT><<<grid, 256, 0, st>>>(pl.tau_tiles, raw, x, pl.nx, pl.nz,            \
+        KLAUNCH(k_das_adj<WT><<<grid, 256, 0, st>>>(pl.tau_tiles, raw, x, pl.nx, pl.nz,            \
                                             pl.n_patch_x, pl.D, pl.T, pl.frac_bits, pl.r_fx, \
-                                            pl.c1, scale);                                \
+                                            pl.c1, scale));                                \
         break;
     switch (wt) {
         CASE(1) CASE(2) CASE(4) CASE(8)
@@ -461,9 +465,9 @@ static int sir_fwd_nt(const Plan &pl, const float *x_pi, float *raw, float scale
 #define NTCASE(NT)                                                                         \
     if (pl.n_tap <= NT) {                                                                  \
         if ((rc = set_smem(k_sir_fwd<WT, NT>, smem)) != MSOT_OK) return rc;                \
-        k_sir_fwd<WT, NT><<<grid, 256, smem, st>>>(pl.tau_pi, pl.sir_pi, pl.sir, pl.sir_se, \
+        KLAUNCH(k_sir_fwd<WT, NT><<<grid, 256, smem, st>>>(pl.tau_pi, pl.sir_pi, pl.sir, pl.sir_se, \
                                                    x_pi, raw, pl.P, pl.D, pl.T, pl.S,      \
-                                                   pl.frac_bits, pl.r_fx, pl.c1, scale, ns); \
+                                                   pl.frac_bits, pl.r_fx, pl.c1, scale, ns)); \
         MSOT_LAUNCH_CHECK();                                                               \
         return MSOT_OK;                                                                    \
     }
@@ -475,6 +479,7 @@ static int sir_fwd_nt(const Plan &pl, const float *x_pi, float *raw, float scale
 
 int launch_sir_forward(const Plan &pl, const float *x_pi, float *raw, int W, float scale,
                        cudaStream_t st) {
+    TimedScope ts_(KID_INTERP_FWD, st);
     const int wt = pick_wt(W, pl.T, 4);
     const int ns = fwd_split(pl, W / wt);
     if (ns > 1) MSOT_CUDA_TRY(cudaMemsetAsync(raw, 0, sizeof(float) * W * pl.D * pl.T, st));
@@ -492,10 +497,10 @@ static int sir_adj_nt(const Plan &pl, const float *raw, float *x, float scale, d
                       cudaStream_t st) {
 #define NTCASE(NT)                                                                         \
     if (pl.n_tap <= NT) {                                                                  \
-        k_sir_adj<WT, NT><<<grid, 256, 0, st>>>(pl.tau_tiles, pl.sir_tiles, pl.sir,         \
+        KLAUNCH(k_sir_adj<WT, NT><<<grid, 256, 0, st>>>(pl.tau_tiles, pl.sir_tiles, pl.sir,         \
                                                 pl.sir_se, raw, x, pl.nx, pl.nz,           \
                                                 pl.n_patch_x, pl.D, pl.T, pl.S,            \
-                                                pl.frac_bits, pl.r_fx, pl.c1, scale);      \
+                                                pl.frac_bits, pl.r_fx, pl.c1, scale));      \
         MSOT_LAUNCH_CHECK();                                                               \
         return MSOT_OK;                                                                    \
     }
@@ -507,6 +512,7 @@ static int sir_adj_nt(const Plan &pl, const float *raw, float *x, float scale, d
 
 int launch_sir_adjoint(const Plan &pl, const float *raw, float *x, int W, float scale,
                        cudaStream_t st) {
+    TimedScope ts_(KID_INTERP_ADJ, st);
     const int wt = pick_wt(W, 1, 2);
     dim3 grid(pl.n_patch, W / wt);
     if (wt == 2) return sir_adj_nt<2>(pl, raw, x, scale, grid, st);
@@ -515,6 +521,7 @@ int launch_sir_adjoint(const Plan &pl, const float *raw, float *x, int W, float 
 
 int launch_conv(const Plan &pl, const float *in, float *out, int W, bool transpose,
                 cudaStream_t st) {
+    TimedScope ts_(KID_CONV, st);
     constexpr int TPT = 8, NTH = 64, TT = TPT * NTH;
     const int Lp = (pl.L + TPT - 1) / TPT * TPT;
     const int seg_len = TT + Lp + TPT;
@@ -522,8 +529,8 @@ int launch_conv(const Plan &pl, const float *in, float *out, int W, bool transpo
     int rc;
     if ((rc = set_smem(k_conv<TPT, NTH>, smem)) != MSOT_OK) return rc;
     dim3 grid(div_up(pl.T, TT), (unsigned)W * pl.D);
-    k_conv<TPT, NTH><<<grid, NTH, smem, st>>>(in, out, transpose ? pl.ir_adj : pl.ir_fwd,
-                                              pl.L, pl.T);
+    KLAUNCH(k_conv<TPT, NTH><<<grid, NTH, smem, st>>>(in, out, transpose ? pl.ir_adj : pl.ir_fwd,
+                                              pl.L, pl.T));
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
 }

@@ -365,9 +365,9 @@ struct Ctx {
 
 static int group_sumsq(const Ctx &c, const float *x, const float *y, size_t N, int nb,
                        std::vector<double> &out) {
-    k_sumsq<<<dim3(nb, c.W), RED_THREADS, 0, c.st>>>(x, y, N / c.W, c.P(3));
+    KLAUNCH(k_sumsq<<<dim3(nb, c.W), RED_THREADS, 0, c.st>>>(x, y, N / c.W, c.P(3)));
     MSOT_LAUNCH_CHECK();
-    k_group_sums<<<1, 256, 0, c.st>>>(c.P(3), nb, c.W, c.coupled, c.wk.gsum);
+    KLAUNCH(k_group_sums<<<1, 256, 0, c.st>>>(c.P(3), nb, c.W, c.coupled, c.wk.gsum));
     MSOT_LAUNCH_CHECK();
     const int G = c.coupled ? 1 : c.W;
     out.resize(G);
@@ -391,42 +391,42 @@ static int l2_outer(const Ctx &c, const float *b, float *wv, float *vm, double s
     cudaStream_t st = c.st;
     // init: u = b_aug - A_aug w
     TRY(apply_forward(c.pl, wv, tmp_s, c.W, st));
-    k_sino_update<<<gs, RED_THREADS, 0, st>>>(tmp_s, b, us, ns, 0, sl, k.sc, c.coupled, c.P(0));
-    k_l2_init_img<<<gi, RED_THREADS, 0, st>>>(wv, vm, ur, ub, ni, sl, sr, sb, has_reg, c.P(1),
-                                              c.P(2));
-    k_l2_scalar<<<1, 256, 0, st>>>(k.sc, 0, c.P(0), c.nbs, c.P(1), c.nbi, c.P(2), c.nbi, normb2,
-                                   sl, sb, c.W, c.coupled, 1e-8);
+    KLAUNCH(k_sino_update<<<gs, RED_THREADS, 0, st>>>(tmp_s, b, us, ns, 0, sl, k.sc, c.coupled, c.P(0)));
+    KLAUNCH(k_l2_init_img<<<gi, RED_THREADS, 0, st>>>(wv, vm, ur, ub, ni, sl, sr, sb, has_reg, c.P(1),
+                                              c.P(2)));
+    KLAUNCH(k_l2_scalar<<<1, 256, 0, st>>>(k.sc, 0, c.P(0), c.nbs, c.P(1), c.nbi, c.P(2), c.nbi, normb2,
+                                   sl, sb, c.W, c.coupled, 1e-8));
     MSOT_LAUNCH_CHECK();
     // v = A_aug^T u / beta
     TRY(apply_transpose(c.pl, us, tmp_i, c.W, st));
-    k_l2_v_img<<<gi, RED_THREADS, 0, st>>>(tmp_i, ur, ub, v, ni, sl, sr, sb, has_reg, 1, k.sc,
-                                           c.coupled, c.P(1));
-    k_l2_scalar<<<1, 256, 0, st>>>(k.sc, 1, c.P(1), c.nbi, nullptr, 0, nullptr, 0, nullptr, sl,
-                                   sb, c.W, c.coupled, 1e-8);
-    k_l2_scale_v<<<gi, RED_THREADS, 0, st>>>(v, d, x, xmin, wv, ni, 1, k.sc, c.coupled);
+    KLAUNCH(k_l2_v_img<<<gi, RED_THREADS, 0, st>>>(tmp_i, ur, ub, v, ni, sl, sr, sb, has_reg, 1, k.sc,
+                                           c.coupled, c.P(1)));
+    KLAUNCH(k_l2_scalar<<<1, 256, 0, st>>>(k.sc, 1, c.P(1), c.nbi, nullptr, 0, nullptr, 0, nullptr, sl,
+                                   sb, c.W, c.coupled, 1e-8));
+    KLAUNCH(k_l2_scale_v<<<gi, RED_THREADS, 0, st>>>(v, d, x, xmin, wv, ni, 1, k.sc, c.coupled));
     MSOT_LAUNCH_CHECK();
     for (int it = 0; it < 2; ++it) {
-        k_l2_gamma<<<1, 256, 0, st>>>(k.sc, G);
+        KLAUNCH(k_l2_gamma<<<1, 256, 0, st>>>(k.sc, G));
         TRY(apply_forward(c.pl, v, tmp_s, c.W, st));
-        k_sino_update<<<gs, RED_THREADS, 0, st>>>(tmp_s, nullptr, us, ns, 1, sl, k.sc,
-                                                  c.coupled, c.P(0));
-        k_l2_u_img<<<gi, RED_THREADS, 0, st>>>(v, ur, ub, ni, sl, sr, sb, has_reg, k.sc,
-                                               c.coupled, c.P(1));
-        k_l2_scalar<<<1, 256, 0, st>>>(k.sc, 2, c.P(0), c.nbs, c.P(1), c.nbi, nullptr, 0,
-                                       nullptr, sl, sb, c.W, c.coupled, 1e-8);
-        k_l2_dx<<<gi, RED_THREADS, 0, st>>>(v, d, x, xmin, ni, k.sc, c.coupled);
-        k_l2_mark_converged<<<1, 256, 0, st>>>(k.sc, G);
+        KLAUNCH(k_sino_update<<<gs, RED_THREADS, 0, st>>>(tmp_s, nullptr, us, ns, 1, sl, k.sc,
+                                                  c.coupled, c.P(0)));
+        KLAUNCH(k_l2_u_img<<<gi, RED_THREADS, 0, st>>>(v, ur, ub, ni, sl, sr, sb, has_reg, k.sc,
+                                               c.coupled, c.P(1)));
+        KLAUNCH(k_l2_scalar<<<1, 256, 0, st>>>(k.sc, 2, c.P(0), c.nbs, c.P(1), c.nbi, nullptr, 0,
+                                       nullptr, sl, sb, c.W, c.coupled, 1e-8));
+        KLAUNCH(k_l2_dx<<<gi, RED_THREADS, 0, st>>>(v, d, x, xmin, ni, k.sc, c.coupled));
+        KLAUNCH(k_l2_mark_converged<<<1, 256, 0, st>>>(k.sc, G));
         MSOT_LAUNCH_CHECK();
         if (it == 1) break;  // the last A^T of lsqr only feeds its stopping test
         TRY(apply_transpose(c.pl, us, tmp_i, c.W, st));
-        k_l2_v_img<<<gi, RED_THREADS, 0, st>>>(tmp_i, ur, ub, v, ni, sl, sr, sb, has_reg, 0,
-                                               k.sc, c.coupled, c.P(1));
-        k_l2_scalar<<<1, 256, 0, st>>>(k.sc, 1, c.P(1), c.nbi, nullptr, 0, nullptr, 0, nullptr,
-                                       sl, sb, c.W, c.coupled, 1e-8);
-        k_l2_scale_v<<<gi, RED_THREADS, 0, st>>>(v, d, x, xmin, wv, ni, 0, k.sc, c.coupled);
+        KLAUNCH(k_l2_v_img<<<gi, RED_THREADS, 0, st>>>(tmp_i, ur, ub, v, ni, sl, sr, sb, has_reg, 0,
+                                               k.sc, c.coupled, c.P(1)));
+        KLAUNCH(k_l2_scalar<<<1, 256, 0, st>>>(k.sc, 1, c.P(1), c.nbi, nullptr, 0, nullptr, 0, nullptr,
+                                       sl, sb, c.W, c.coupled, 1e-8));
+        KLAUNCH(k_l2_scale_v<<<gi, RED_THREADS, 0, st>>>(v, d, x, xmin, wv, ni, 0, k.sc, c.coupled));
         MSOT_LAUNCH_CHECK();
     }
-    k_nn_outer<<<gi, RED_THREADS, 0, st>>>(xmin, wv, vm, ni);
+    KLAUNCH(k_nn_outer<<<gi, RED_THREADS, 0, st>>>(xmin, wv, vm, ni));
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
 }
@@ -444,13 +444,13 @@ static int solve_l2(const Plan &pl, const float *b, float *rec, int W, int num_i
     int rc = MSOT_OK;
     do {
         if (x0)
-            k_copy<<<256, 256, 0, st>>>(x0, wv, NI);
+            KLAUNCH(k_copy<<<256, 256, 0, st>>>(x0, wv, NI));
         else
-            k_fill<<<256, 256, 0, st>>>(wv, 0.f, NI);
-        k_fill<<<256, 256, 0, st>>>(vm, 0.f, NI);
+            KLAUNCH(k_fill<<<256, 256, 0, st>>>(wv, 0.f, NI));
+        KLAUNCH(k_fill<<<256, 256, 0, st>>>(vm, 0.f, NI));
         // ||b||^2 per group enters ||b_aug|| of lsqr's tolerance test
-        k_sumsq<<<dim3(c.nbs, W), RED_THREADS, 0, st>>>(b, nullptr, NS / W, c.P(3));
-        k_group_sums<<<1, 256, 0, st>>>(c.P(3), c.nbs, W, coupled, wk.gsum);
+        KLAUNCH(k_sumsq<<<dim3(c.nbs, W), RED_THREADS, 0, st>>>(b, nullptr, NS / W, c.P(3)));
+        KLAUNCH(k_group_sums<<<1, 256, 0, st>>>(c.P(3), c.nbs, W, coupled, wk.gsum));
         if (cudaGetLastError() != cudaSuccess) {
             set_error("solver: launch failed");
             rc = MSOT_ECUDA;
@@ -459,7 +459,7 @@ static int solve_l2(const Plan &pl, const float *b, float *rec, int W, int num_i
         for (int it = 0; it < num_iter && rc == MSOT_OK; ++it)
             rc = l2_outer(c, b, wv, vm, sr, has_reg, wk.gsum);
         if (rc) break;
-        k_copy<<<256, 256, 0, st>>>(wv, rec, NI);
+        KLAUNCH(k_copy<<<256, 256, 0, st>>>(wv, rec, NI));
         if (err_img || err_reg) {
             std::vector<double> e;
             if ((rc = apply_forward(pl, rec, wk.s2, W, st))) break;
@@ -680,39 +680,39 @@ static int solve_l1(const Plan &pl, const float *b, float *rec, int W, int num_i
         // start value A^T b (rec_nn_with_L1_eye_reg.m:33) unless a warm start is given
         if ((rc = apply_transpose(pl, b, atb, W, st))) break;
         if (x0)
-            k_copy<<<256, 256, 0, st>>>(x0, u, NI);
+            KLAUNCH(k_copy<<<256, 256, 0, st>>>(x0, u, NI));
         else
-            k_copy<<<256, 256, 0, st>>>(atb, u, NI);
-        k_fill<<<256, 256, 0, st>>>(bp, 0.f, NI);
+            KLAUNCH(k_copy<<<256, 256, 0, st>>>(atb, u, NI));
+        KLAUNCH(k_fill<<<256, 256, 0, st>>>(bp, 0.f, NI));
         for (int it = 0; it < num_iter && rc == MSOT_OK; ++it) {
-            k_l1_rhs<<<gi, RED_THREADS, 0, st>>>(u, bp, atb, dv, rhs, x, r, rt, xmin, ni, lam, eta,
-                                                 c.P(0));
-            k_cgs_scalar<<<1, 256, 0, st>>>(wk.sc, 0, c.P(0), c.nbi, W, coupled, 1e-8);
+            KLAUNCH(k_l1_rhs<<<gi, RED_THREADS, 0, st>>>(u, bp, atb, dv, rhs, x, r, rt, xmin, ni, lam, eta,
+                                                 c.P(0)));
+            KLAUNCH(k_cgs_scalar<<<1, 256, 0, st>>>(wk.sc, 0, c.P(0), c.nbi, W, coupled, 1e-8));
             for (int ci = 0; ci < 2 && rc == MSOT_OK; ++ci) {
-                k_dot<<<gi, RED_THREADS, 0, st>>>(rt, r, ni, c.P(0));
-                k_cgs_scalar<<<1, 256, 0, st>>>(wk.sc, 1, c.P(0), c.nbi, W, coupled, 1e-8);
-                k_cgs_dir<<<gi, RED_THREADS, 0, st>>>(r, q, uc, p, ni, ci == 0, wk.sc, coupled);
+                KLAUNCH(k_dot<<<gi, RED_THREADS, 0, st>>>(rt, r, ni, c.P(0)));
+                KLAUNCH(k_cgs_scalar<<<1, 256, 0, st>>>(wk.sc, 1, c.P(0), c.nbi, W, coupled, 1e-8));
+                KLAUNCH(k_cgs_dir<<<gi, RED_THREADS, 0, st>>>(r, q, uc, p, ni, ci == 0, wk.sc, coupled));
                 if ((rc = normal_op(c, p, atmp))) break;
-                k_cgs_op<<<gi, RED_THREADS, 0, st>>>(atmp, p, vh, rt, ni, lam, c.P(0));
-                k_cgs_scalar<<<1, 256, 0, st>>>(wk.sc, 2, c.P(0), c.nbi, W, coupled, 1e-8);
-                k_cgs_upd<<<gi, RED_THREADS, 0, st>>>(uc, vh, q, uh, x, ni, wk.sc, coupled);
+                KLAUNCH(k_cgs_op<<<gi, RED_THREADS, 0, st>>>(atmp, p, vh, rt, ni, lam, c.P(0)));
+                KLAUNCH(k_cgs_scalar<<<1, 256, 0, st>>>(wk.sc, 2, c.P(0), c.nbi, W, coupled, 1e-8));
+                KLAUNCH(k_cgs_upd<<<gi, RED_THREADS, 0, st>>>(uc, vh, q, uh, x, ni, wk.sc, coupled));
                 if ((rc = normal_op(c, uh, atmp))) break;
-                k_cgs_res<<<gi, RED_THREADS, 0, st>>>(atmp, uh, r, ni, lam, wk.sc, coupled,
-                                                      c.P(0));
-                k_cgs_scalar<<<1, 256, 0, st>>>(wk.sc, 3, c.P(0), c.nbi, W, coupled, 1e-8);
-                k_cgs_keep<<<gi, RED_THREADS, 0, st>>>(x, xmin, ni, wk.sc, coupled);
-                k_cgs_mark<<<1, 256, 0, st>>>(wk.sc, G);
+                KLAUNCH(k_cgs_res<<<gi, RED_THREADS, 0, st>>>(atmp, uh, r, ni, lam, wk.sc, coupled,
+                                                      c.P(0)));
+                KLAUNCH(k_cgs_scalar<<<1, 256, 0, st>>>(wk.sc, 3, c.P(0), c.nbi, W, coupled, 1e-8));
+                KLAUNCH(k_cgs_keep<<<gi, RED_THREADS, 0, st>>>(x, xmin, ni, wk.sc, coupled));
+                KLAUNCH(k_cgs_mark<<<1, 256, 0, st>>>(wk.sc, G));
             }
             if (rc) break;
-            k_copy<<<256, 256, 0, st>>>(xmin, u, NI);
-            k_l1_bregman<<<gi, RED_THREADS, 0, st>>>(dv, u, bp, ni);
+            KLAUNCH(k_copy<<<256, 256, 0, st>>>(xmin, u, NI));
+            KLAUNCH(k_l1_bregman<<<gi, RED_THREADS, 0, st>>>(dv, u, bp, ni));
             if (cudaGetLastError() != cudaSuccess) {
                 set_error("L1 solver: launch failed");
                 rc = MSOT_ECUDA;
             }
         }
         if (rc) break;
-        k_copy<<<256, 256, 0, st>>>(u, rec, NI);
+        KLAUNCH(k_copy<<<256, 256, 0, st>>>(u, rec, NI));
         if (err_img || err_reg) {
             std::vector<double> e;
             Ctx ci = c;
@@ -775,16 +775,16 @@ static int estimate_norm(const Plan &pl, int iters, uint64_t seed, double *out, 
     int rc = MSOT_OK;
     float *v = wk.i[0], *z = wk.i[1];
     do {
-        k_seed<<<64, 256, 0, st>>>(v, NI, seed);
-        k_sumsq<<<dim3(c.nbi, 1), RED_THREADS, 0, st>>>(v, nullptr, NI, c.P(0));
-        k_group_sums<<<1, 32, 0, st>>>(c.P(0), c.nbi, 1, 0, wk.gsum);
-        k_scale_by<<<64, 256, 0, st>>>(v, NI, wk.gsum);
+        KLAUNCH(k_seed<<<64, 256, 0, st>>>(v, NI, seed));
+        KLAUNCH(k_sumsq<<<dim3(c.nbi, 1), RED_THREADS, 0, st>>>(v, nullptr, NI, c.P(0)));
+        KLAUNCH(k_group_sums<<<1, 32, 0, st>>>(c.P(0), c.nbi, 1, 0, wk.gsum));
+        KLAUNCH(k_scale_by<<<64, 256, 0, st>>>(v, NI, wk.gsum));
         for (int it = 0; it < iters && rc == MSOT_OK; ++it) {
             if ((rc = apply_forward(pl, v, wk.s1, 1, st))) break;
             if ((rc = apply_transpose(pl, wk.s1, z, 1, st))) break;
-            k_sumsq<<<dim3(c.nbi, 1), RED_THREADS, 0, st>>>(z, nullptr, NI, c.P(0));
-            k_group_sums<<<1, 32, 0, st>>>(c.P(0), c.nbi, 1, 0, wk.gsum);
-            k_scale_by<<<64, 256, 0, st>>>(z, NI, wk.gsum);
+            KLAUNCH(k_sumsq<<<dim3(c.nbi, 1), RED_THREADS, 0, st>>>(z, nullptr, NI, c.P(0)));
+            KLAUNCH(k_group_sums<<<1, 32, 0, st>>>(c.P(0), c.nbi, 1, 0, wk.gsum));
+            KLAUNCH(k_scale_by<<<64, 256, 0, st>>>(z, NI, wk.gsum));
             std::swap(v, z);
         }
         if (rc) break;
