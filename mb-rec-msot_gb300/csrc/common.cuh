@@ -39,8 +39,18 @@ struct Plan {
     int n_patch_x, n_patch_z, n_patch;
     // tables
     int32_t *tau_tiles = nullptr;  // [n_patch][D][PATCH] (gather kernels)
-    int32_t *tau_pi = nullptr;     // [D][P] pixels in scatter order perm[]
-    int32_t *perm = nullptr;       // [P] scatter order -> pixel index
+    int32_t *tau_pi = nullptr;     // [D][P] pixels in scatter order perm[] (SIR)
+    int32_t *perm = nullptr;       // [P] scatter order -> pixel index (SIR)
+    // bucket decomposition of the tri interpolation (no SIR): for tau = b + f
+    // (b integer, 0 <= f < 1) the weights of taps b-F+1 .. b+F are exactly
+    // linear in f and only taps b-F and b+F+1 need the clamp at zero.
+    int F = 0;                     // floor(radius)
+    float inv_r = 0.f;             // 1 / radius
+    float ce1 = 0.f, ce2 = 0.f;    // (r - F)/r and (F + 1 - r)/r
+    int32_t *fwd_off = nullptr;    // [D][T+1] CSR offsets of bucket b = floor(tau)
+    int2 *fwd_ent = nullptr;       // [D][P] (tau fixed point, pixel) sorted by bucket
+    int wc_max = 0;                // instances per adjoint table chunk
+    float4 *scr_q = nullptr;       // [D][T][wc_max] adjoint bucket table
     // IR
     int L = 0, Lh = 0;
     float *ir_fwd = nullptr, *ir_adj = nullptr;
@@ -117,7 +127,8 @@ class TimedScope {
 
 // operator chains (operator.cu)
 int launch_prefilter(const Plan &pl, const float *in, float *out, int W, bool transpose,
-                     bool along_x, float scale, bool out_perm, cudaStream_t st);
+                     bool along_x, float scale, int out_mode, cudaStream_t st);
+int launch_to_pixmajor(const Plan &pl, const float *in, float *out, int W, cudaStream_t st);
 int launch_permute(const Plan &pl, const float *in, float *out, int W, cudaStream_t st);
 int launch_das_forward(const Plan &pl, const float *x_pi, float *raw, int W, float scale,
                        cudaStream_t st);

@@ -74,7 +74,9 @@ int run_mex(bool forward, const double *in, int W, int P, int D, int T, const do
         for (int p = 0; p < P; ++p)
             for (int w = 0; w < W; ++w) h[(size_t)w * P + p] = (float)in[(size_t)p * W + w];
         MSOT_CUDA_TRY(cudaMemcpy(dimg.p, h.data(), NI * sizeof(float), cudaMemcpyHostToDevice));
-        if ((rc = launch_permute(pl, (float *)dimg.p, pl.scr_img1, W, st))) return rc;
+        if ((rc = pl.S ? launch_permute(pl, (float *)dimg.p, pl.scr_img1, W, st)
+                       : launch_to_pixmajor(pl, (float *)dimg.p, pl.scr_img1, W, st)))
+            return rc;
         if ((rc = interp_forward(pl, pl.scr_img1, (float *)dsino.p, W, 1.f, st))) return rc;
         std::vector<float> o(NS_);
         MSOT_CUDA_TRY(cudaMemcpy(o.data(), dsino.p, NS_ * sizeof(float), cudaMemcpyDeviceToHost));

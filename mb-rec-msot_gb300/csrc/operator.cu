@@ -36,18 +36,19 @@ __device__ __forceinline__ float tri_weight(int t, int32_t tau, int fb, float c1
 }
 
 // ---------------------------------------------------------------------------
-// Prefilter: out[w][j] = scale * sum_k h[k] in[w][pix(j) - k (circular)]
-// along one axis; pix(j) = perm[j] when perm != nullptr (scatter order).
+// Prefilter: out = scale * sum_k h[k] in[w][pix - k (circular)] along one
+// axis.  Output layout: out_mode 0 = [W][P]; 1 = [W][P] with pixel perm[j] at
+// position j (scatter order); 2 = pixel-major [P][W].
 // ---------------------------------------------------------------------------
 __global__ void k_prefilter(const float *__restrict__ in, float *__restrict__ out,
                             const float *__restrict__ taps, int K, int nx, int nz, int W,
                             int along_x, int transpose, float scale,
-                            const int32_t *__restrict__ perm) {
+                            const int32_t *__restrict__ perm, int out_mode) {
     const int P = nx * nz;
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long)W * P) return;
     const int w = (int)(idx / P), j = (int)(idx % P);
-    const int pix = perm ? __ldg(perm + j) : j;
+    const int pix = out_mode == 1 ? __ldg(perm + j) : j;
     const int ix = pix / nz, iz = pix - ix * nz;
     const float *src = in + (size_t)w * P;
     float acc = 0.f;
@@ -67,9 +68,22 @@ __global__ void k_prefilter(const float *__restrict__ in, float *__restrict__ ou
         }
         acc = fmaf(h, __ldg(src + s), acc);
     }
-    out[(size_t)w * P + j] = acc * scale;
+    if (out_mode == 2)
+        out[(size_t)j * W + w] = acc * scale;
+    else
+        out[(size_t)w * P + j] = acc * scale;
 }
 
+// [W][P] -> pixel-major [P][W]
+__global__ void k_to_pixmajor(const float *__restrict__ in, float *__restrict__ out, int P,
+                              int W) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)W * P) return;
+    const int w = (int)(idx / P), j = (int)(idx % P);
+    out[(size_t)j * W + w] = __ldg(in + idx);
+}
+
+// [W][P] -> [W][P] in scatter order (out[w][j] = in[w][perm[j]])
 __global__ void k_permute(const float *__restrict__ in, float *__restrict__ out,
                           const int32_t *__restrict__ perm, int P, int W) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -79,90 +93,207 @@ __global__ void k_permute(const float *__restrict__ in, float *__restrict__ out,
 }
 
 // ---------------------------------------------------------------------------
-// DAS forward: CTA = (detector, pixel split, instance tile).  The detector's
-// sinogram column for WT instances lives in shared memory ([WT][T]); pixels
-// are visited in scatter order so that the 32 lanes of a warp hit unrelated
-// samples.  With nsplit > 1 the CTAs of one detector add their columns into
-// a zeroed output with global atomics.
+// Bucket decomposition of the tri interpolation (no SIR).
+// For tau = b + f, taps t = b + k, k in [-(F-1), F], have weight
+// alpha_k + beta_k f with alpha_k = 1 - |k|/r, beta_k = -1/r (k <= 0) or
+// +1/r (k >= 1); tap b - F has weight e1(f) = max(0, (r - F - f)/r) and tap
+// b + F + 1 has e2(f) = max(0, (f - (F + 1 - r))/r); no other tap is non-zero.
+// This is exactly the reference's tap set ceil(tau - r) .. floor(tau + r).
+//
+// Forward: per detector the pixels are bucketed by b = floor(tau); each
+// bucket reduces four moments sum x, sum f x, sum e1 x, sum e2 x over its
+// pixels, and the output is a (2F+2)-tap filter over the moments.
+// Adjoint: the sinogram is filtered once per bucket into
+// Q_b = (U_b, V_b, s[b-F], s[b+F+1]), U_b = sum alpha_k s[b+k],
+// V_b = sum beta_k s[b+k]; each (pixel, detector) then adds
+// U + f V + e1 s[b-F] + e2 s[b+F+1].
 // ---------------------------------------------------------------------------
 template <int WT>
-__global__ void __launch_bounds__(256) k_das_fwd(const int32_t *__restrict__ tau_pi,
-                                                 const float *__restrict__ x_pi,
-                                                 float *__restrict__ raw, int P, int D, int T,
-                                                 int fb, int32_t r_fx, float c1, float scale,
-                                                 int nsplit) {
-    extern __shared__ float col[];  // [WT][T]
-    const int d = blockIdx.x, sp = blockIdx.y, w0 = blockIdx.z * WT;
-    for (int i = threadIdx.x; i < WT * T; i += blockDim.x) col[i] = 0.f;
-    __syncthreads();
-    const int j0 = (int)((long)P * sp / nsplit), j1 = (int)((long)P * (sp + 1) / nsplit);
-    const int32_t *tau_d = tau_pi + (size_t)d * P;
-    for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
-        const int32_t tau = __ldg(tau_d + j);
-        float xv[WT];
+__global__ void __launch_bounds__(256) k_das_fwd2(const int32_t *__restrict__ off,
+                                                  const int2 *__restrict__ ent,
+                                                  const float *__restrict__ xpm,
+                                                  float *__restrict__ raw, int P, int D, int T,
+                                                  int W, int fb, int F, float inv_r, float ce1,
+                                                  float ce2, float scale) {
+    extern __shared__ float mom[];  // [4][WT][NB], bucket fastest
+    const int NB = blockDim.x;
+    const int TB = NB - 2 * F - 2;
+    const int d = blockIdx.y, w0 = blockIdx.z * WT;
+    const int t0 = blockIdx.x * TB;
+    const int b_lo = t0 - F - 1;
+    {
+        float m0[WT], m1[WT], m2[WT], m3[WT];
 #pragma unroll
-        for (int i = 0; i < WT; ++i) xv[i] = __ldg(x_pi + (size_t)(w0 + i) * P + j);
-        const int tb = max(0, tap_lo(tau, r_fx, fb)), te = min(T - 1, tap_hi(tau, r_fx, fb));
-        for (int t = tb; t <= te; ++t) {
-            const float wt = tri_weight(t, tau, fb, c1);
+        for (int i = 0; i < WT; ++i) m0[i] = m1[i] = m2[i] = m3[i] = 0.f;
+        const int b = b_lo + (int)threadIdx.x;
+        if (b >= 0 && b < T) {
+            const int32_t *o = off + (size_t)d * (T + 1);
+            const int j0 = __ldg(o + b), j1 = __ldg(o + b + 1);
+            const int2 *e = ent + (size_t)d * P;
+            const int mask = (1 << fb) - 1;
+            const float step = __int_as_float((127 - fb) << 23);  // 2^-fb
+            auto load_x = [&](int pix, float (&xv)[WT]) {
+                const float *xp = xpm + (size_t)pix * W + w0;
+                if constexpr (WT % 4 == 0) {
 #pragma unroll
-            for (int i = 0; i < WT; ++i) atomicAdd(&col[i * T + t], wt * xv[i]);
+                    for (int i = 0; i < WT; i += 4) {
+                        const float4 v = __ldg(reinterpret_cast<const float4 *>(xp + i));
+                        xv[i] = v.x; xv[i + 1] = v.y; xv[i + 2] = v.z; xv[i + 3] = v.w;
+                    }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < WT; ++i) xv[i] = __ldg(xp + i);
+                }
+            };
+            auto accumulate = [&](int32_t tau, const float (&xv)[WT]) {
+                const float f = (float)(tau & mask) * step;
+                const float e1 = fmaxf(0.f, fmaf(-f, inv_r, ce1));
+                const float e2 = fmaxf(0.f, fmaf(f, inv_r, -ce2));
+#pragma unroll
+                for (int i = 0; i < WT; ++i) {
+                    m0[i] += xv[i];
+                    m1[i] = fmaf(f, xv[i], m1[i]);
+                    m2[i] = fmaf(e1, xv[i], m2[i]);
+                    m3[i] = fmaf(e2, xv[i], m3[i]);
+                }
+            };
+            // batches of UNR independent (entry, pixel) loads keep several L2
+            // requests in flight per thread
+            constexpr int UNR = WT >= 8 ? 2 : 4;
+            int j = j0;
+            for (; j + UNR <= j1; j += UNR) {
+                int2 q[UNR];
+#pragma unroll
+                for (int u = 0; u < UNR; ++u) q[u] = __ldg(e + j + u);
+                float xv[UNR][WT];
+#pragma unroll
+                for (int u = 0; u < UNR; ++u) load_x(q[u].y, xv[u]);
+#pragma unroll
+                for (int u = 0; u < UNR; ++u) accumulate(q[u].x, xv[u]);
+            }
+            for (; j < j1; ++j) {
+                const int2 q = __ldg(e + j);
+                float xv[WT];
+                load_x(q.y, xv);
+                accumulate(q.x, xv);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < WT; ++i) {
+            mom[(0 * WT + i) * NB + threadIdx.x] = m0[i];
+            mom[(1 * WT + i) * NB + threadIdx.x] = m1[i];
+            mom[(2 * WT + i) * NB + threadIdx.x] = m2[i];
+            mom[(3 * WT + i) * NB + threadIdx.x] = m3[i];
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < WT * T; i += blockDim.x) {
-        const int wi = i / T, t = i - wi * T;
-        float *dst = raw + ((size_t)(w0 + wi) * D + d) * T + t;
-        const float v = col[i] * scale;
-        if (nsplit == 1)
-            *dst = v;
-        else
-            atomicAdd(dst, v);
-    }
-}
-
-// ---------------------------------------------------------------------------
-// DAS adjoint: CTA = (8x8 pixel patch, instance tile); 256 threads = 64 pixels
-// x 4 detector groups; the four partial sums are added in shared memory in a
-// fixed order (deterministic).
-// ---------------------------------------------------------------------------
-template <int WT>
-__global__ void __launch_bounds__(256) k_das_adj(const int32_t *__restrict__ tiles,
-                                                 const float *__restrict__ raw,
-                                                 float *__restrict__ out, int nx, int nz,
-                                                 int npx, int D, int T, int fb, int32_t r_fx,
-                                                 float c1, float scale) {
-    __shared__ float red[4][PATCH][WT];
-    const int patch = blockIdx.x, w0 = blockIdx.y * WT;
-    const int q = threadIdx.x & (PATCH - 1), g = threadIdx.x / PATCH;
-    const int px = patch % npx, pz = patch / npx;
-    const int ix = px * PATCH_X + q / PATCH_Z, iz = pz * PATCH_Z + q % PATCH_Z;
+    const int ti = threadIdx.x;
+    const int t = t0 + ti;
+    if (ti >= TB || t >= T) return;
     float acc[WT];
 #pragma unroll
     for (int i = 0; i < WT; ++i) acc[i] = 0.f;
-    const int32_t *tp = tiles + (size_t)patch * D * PATCH + q;
-    const size_t DT = (size_t)D * T;
-    for (int d = g; d < D; d += 4) {
-        const int32_t tau = __ldg(tp + (size_t)d * PATCH);
-        if (tau == TAU_PAD) continue;
-        const int tb = max(0, tap_lo(tau, r_fx, fb)), te = min(T - 1, tap_hi(tau, r_fx, fb));
-        const float *base = raw + ((size_t)w0 * D + d) * T;
-        for (int t = tb; t <= te; ++t) {
-            const float wt = tri_weight(t, tau, fb, c1);
+    const int base = t - b_lo;  // local index of bucket t
+    for (int k = -(F - 1); k <= F; ++k) {
+        const int bl = base - k;
+        const float a = fmaf(-fabsf((float)k), inv_r, 1.f);
+        const float be = k <= 0 ? -inv_r : inv_r;
 #pragma unroll
-            for (int i = 0; i < WT; ++i) acc[i] = fmaf(wt, __ldg(base + i * DT + t), acc[i]);
-        }
+        for (int i = 0; i < WT; ++i)
+            acc[i] = fmaf(a, mom[(0 * WT + i) * NB + bl],
+                          fmaf(be, mom[(1 * WT + i) * NB + bl], acc[i]));
     }
 #pragma unroll
-    for (int i = 0; i < WT; ++i) red[g][q][i] = acc[i];
-    __syncthreads();
-    if (g == 0 && ix < nx && iz < nz) {
-        const size_t P = (size_t)nx * nz;
-#pragma unroll
-        for (int i = 0; i < WT; ++i) {
-            const float s = ((red[0][q][i] + red[1][q][i]) + red[2][q][i]) + red[3][q][i];
-            out[(size_t)(w0 + i) * P + (size_t)ix * nz + iz] = s * scale;
+    for (int i = 0; i < WT; ++i) {
+        acc[i] += mom[(2 * WT + i) * NB + base + F];
+        acc[i] += mom[(3 * WT + i) * NB + base - F - 1];
+        raw[((size_t)(w0 + i) * D + d) * T + t] = acc[i] * scale;
+    }
+}
+
+// Q[d][b][c] = (U_b, V_b, s[b-F], s[b+F+1]) for the WC instances c0.. of s
+template <int WC>
+__global__ void __launch_bounds__(256) k_adj_table(const float *__restrict__ s,
+                                                   float4 *__restrict__ Q, int D, int T, int c0,
+                                                   int F, float inv_r) {
+    extern __shared__ float seg[];  // [WC][256 + 2F + 2]
+    const int SL = 256 + 2 * F + 2;
+    const int d = blockIdx.y, b0 = blockIdx.x * 256;
+    for (int c = 0; c < WC; ++c) {
+        const float *src = s + ((size_t)(c0 + c) * D + d) * T;
+        for (int q = threadIdx.x; q < SL; q += blockDim.x) {
+            const int t = b0 - F + q;
+            seg[c * SL + q] = (t >= 0 && t < T) ? __ldg(src + t) : 0.f;
         }
+    }
+    __syncthreads();
+    const int b = b0 + threadIdx.x;
+    if (b >= T) return;
+    float4 *dst = Q + ((size_t)d * T + b) * WC;
+#pragma unroll
+    for (int c = 0; c < WC; ++c) {
+        const float *g = seg + c * SL + threadIdx.x + F;  // g[k] = s[b + k]
+        float U = 0.f, V = 0.f;
+        for (int k = -(F - 1); k <= F; ++k) {
+            const float a = fmaf(-fabsf((float)k), inv_r, 1.f);
+            U = fmaf(a, g[k], U);
+            V += k <= 0 ? -g[k] : g[k];
+        }
+        dst[c] = make_float4(U, V * inv_r, g[-F], g[F + 1]);
+    }
+}
+
+constexpr int ADJ_GROUPS = 16;  // detector groups per CTA of the bucket-table gather
+
+template <int WC>
+__global__ void __launch_bounds__(PATCH *ADJ_GROUPS) k_das_adj2(
+    const int32_t *__restrict__ tiles, const float4 *__restrict__ Q, float *__restrict__ out,
+    int nx, int nz, int npx, int D, int T, int c0, int fb, float inv_r, float ce1, float ce2,
+    float scale) {
+    __shared__ float red[ADJ_GROUPS][WC][PATCH];
+    const int patch = blockIdx.x;
+    const int q = threadIdx.x & (PATCH - 1), g = threadIdx.x / PATCH;
+    const int px = patch % npx, pz = patch / npx;
+    const int ix = px * PATCH_X + q / PATCH_Z, iz = pz * PATCH_Z + q % PATCH_Z;
+    float acc[WC];
+#pragma unroll
+    for (int i = 0; i < WC; ++i) acc[i] = 0.f;
+    const int32_t *tp = tiles + (size_t)patch * D * PATCH + q;
+    const int mask = (1 << fb) - 1;
+    const float step = __int_as_float((127 - fb) << 23);
+    auto add = [&](int32_t tau, const float4 (&v)[WC]) {
+        const float f = (float)(tau & mask) * step;
+        const float e1 = fmaxf(0.f, fmaf(-f, inv_r, ce1));
+        const float e2 = fmaxf(0.f, fmaf(f, inv_r, -ce2));
+#pragma unroll
+        for (int i = 0; i < WC; ++i)
+            acc[i] = fmaf(e2, v[i].w, fmaf(e1, v[i].z, fmaf(f, v[i].y, acc[i] + v[i].x)));
+    };
+    for (int d = g; d < D; d += 2 * ADJ_GROUPS) {
+        const int d2 = d + ADJ_GROUPS;
+        const int32_t t1 = __ldg(tp + (size_t)d * PATCH);
+        const int32_t t2 = d2 < D ? __ldg(tp + (size_t)d2 * PATCH) : TAU_PAD;
+        float4 v1[WC], v2[WC];
+        const bool ok1 = t1 != TAU_PAD, ok2 = t2 != TAU_PAD;
+        const float4 *q1 = Q + ((size_t)d * T + min(max(t1 >> fb, 0), T - 1)) * WC;
+        const float4 *q2 = Q + ((size_t)(ok2 ? d2 : d) * T + min(max(t2 >> fb, 0), T - 1)) * WC;
+#pragma unroll
+        for (int i = 0; i < WC; ++i) {
+            v1[i] = ok1 ? __ldg(q1 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+            v2[i] = ok2 ? __ldg(q2 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        if (ok1) add(t1, v1);
+        if (ok2) add(t2, v2);
+    }
+#pragma unroll
+    for (int i = 0; i < WC; ++i) red[g][i][q] = acc[i];
+    __syncthreads();
+    if (g < WC && ix < nx && iz < nz) {
+        float v = 0.f;
+#pragma unroll
+        for (int k = 0; k < ADJ_GROUPS; ++k) v += red[k][g][q];
+        const size_t P = (size_t)nx * nz;
+        out[(size_t)(c0 + g) * P + (size_t)ix * nz + iz] = v * scale;
     }
 }
 
@@ -388,14 +519,13 @@ static int set_smem(K kern, size_t bytes) {
 }
 
 int launch_prefilter(const Plan &pl, const float *in, float *out, int W, bool transpose,
-                     bool along_x, float scale, bool out_perm, cudaStream_t st) {
+                     bool along_x, float scale, int out_mode, cudaStream_t st) {
     TimedScope ts_(KID_PREFILTER, st);
     const int K = along_x ? pl.Kx : pl.Kz;
     const float *taps = along_x ? pl.pre_x : pl.pre_z;
     const long n = (long)W * pl.P;
     KLAUNCH(k_prefilter<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
-        in, out, taps, K, pl.nx, pl.nz, W, along_x, transpose, scale,
-        out_perm ? pl.perm : nullptr));
+        in, out, taps, K, pl.nx, pl.nz, W, along_x, transpose, scale, pl.perm, out_mode));
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
 }
@@ -416,20 +546,28 @@ static int fwd_split(const Plan &pl, int nwt) {
     return ns;
 }
 
-int launch_das_forward(const Plan &pl, const float *x_pi, float *raw, int W, float scale,
+int launch_to_pixmajor(const Plan &pl, const float *in, float *out, int W, cudaStream_t st) {
+    TimedScope ts_(KID_PERMUTE, st);
+    const long n = (long)W * pl.P;
+    KLAUNCH(k_to_pixmajor<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, pl.P, W));
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
+}
+
+// DAS forward by bucket moments; xpm is pixel-major [P][W].
+int launch_das_forward(const Plan &pl, const float *xpm, float *raw, int W, float scale,
                        cudaStream_t st) {
     TimedScope ts_(KID_INTERP_FWD, st);
-    const int wt = pick_wt(W, pl.T, 8);
-    const int ns = fwd_split(pl, W / wt);
-    if (ns > 1) MSOT_CUDA_TRY(cudaMemsetAsync(raw, 0, sizeof(float) * W * pl.D * pl.T, st));
-    const size_t smem = (size_t)wt * pl.T * sizeof(float);
-    dim3 grid(pl.D, ns, W / wt);
-    int rc;
+    const int wt = pick_wt(W, 1, 8);
+    constexpr int NB = 256;
+    const int TB = NB - 2 * pl.F - 2;
+    dim3 grid(div_up(pl.T, TB), pl.D, W / wt);
+    const size_t smem = (size_t)4 * wt * NB * sizeof(float);
 #define CASE(WT)                                                                          \
     case WT:                                                                              \
-        if ((rc = set_smem(k_das_fwd<WT>, smem)) != MSOT_OK) return rc;                   \
-        KLAUNCH(k_das_fwd<WT><<<grid, 256, smem, st>>>(pl.tau_pi, x_pi, raw, pl.P, pl.D, pl.T,     \
-                                               pl.frac_bits, pl.r_fx, pl.c1, scale, ns));  \
+        KLAUNCH(k_das_fwd2<WT><<<grid, NB, smem, st>>>(pl.fwd_off, pl.fwd_ent, xpm, raw, pl.P,  \
+                                                       pl.D, pl.T, W, pl.frac_bits, pl.F,  \
+                                                       pl.inv_r, pl.ce1, pl.ce2, scale));  \
         break;
     switch (wt) {
         CASE(1) CASE(2) CASE(4) CASE(8)
@@ -439,22 +577,29 @@ int launch_das_forward(const Plan &pl, const float *x_pi, float *raw, int W, flo
     return MSOT_OK;
 }
 
+// DAS adjoint by bucket table; raw [W][D][T] -> x [W][P], W in chunks of
+// pl.wc_max instances (the table of one chunk stays L2-resident).
 int launch_das_adjoint(const Plan &pl, const float *raw, float *x, int W, float scale,
                        cudaStream_t st) {
     TimedScope ts_(KID_INTERP_ADJ, st);
-    const int wt = pick_wt(W, 1, 8);
-    dim3 grid(pl.n_patch, W / wt);
-#define CASE(WT)                                                                          \
-    case WT:                                                                              \
-        KLAUNCH(k_das_adj<WT><<<grid, 256, 0, st>>>(pl.tau_tiles, raw, x, pl.nx, pl.nz,            \
-                                            pl.n_patch_x, pl.D, pl.T, pl.frac_bits, pl.r_fx, \
-                                            pl.c1, scale));                                \
+    const int wc = pick_wt(W, 1, pl.wc_max);
+    const size_t tsmem = (size_t)wc * (256 + 2 * pl.F + 2) * sizeof(float);
+    dim3 tgrid(div_up(pl.T, 256), pl.D);
+    for (int c0 = 0; c0 < W; c0 += wc) {
+#define CASE(WC)                                                                           \
+    case WC:                                                                               \
+        KLAUNCH(k_adj_table<WC><<<tgrid, 256, tsmem, st>>>(raw, pl.scr_q, pl.D, pl.T, c0,   \
+                                                           pl.F, pl.inv_r));               \
+        KLAUNCH(k_das_adj2<WC><<<pl.n_patch, PATCH * ADJ_GROUPS, 0, st>>>(                 \
+            pl.tau_tiles, pl.scr_q, x, pl.nx, pl.nz, pl.n_patch_x, pl.D, pl.T, c0,          \
+            pl.frac_bits, pl.inv_r, pl.ce1, pl.ce2, scale));                                \
         break;
-    switch (wt) {
-        CASE(1) CASE(2) CASE(4) CASE(8)
-    }
+        switch (wc) {
+            CASE(1) CASE(2) CASE(4)
+        }
 #undef CASE
-    MSOT_LAUNCH_CHECK();
+        MSOT_LAUNCH_CHECK();
+    }
     return MSOT_OK;
 }
 
@@ -553,17 +698,20 @@ int interp_adjoint(const Plan &pl, const float *raw, float *x, int W, float scal
 int apply_forward(const Plan &pl, const float *img, float *sino, int W, cudaStream_t st) {
     int rc;
     float *xpi = pl.scr_img1;
+    const int mode = pl.S ? 1 : 2;  // scatter order (SIR) or pixel-major (bucket moments)
     if (pl.Kz >= 0 && pl.Kx >= 0) {
-        if ((rc = launch_prefilter(pl, img, pl.scr_img0, W, false, false, 1.f, false, st)))
+        if ((rc = launch_prefilter(pl, img, pl.scr_img0, W, false, false, 1.f, 0, st)))
             return rc;
-        if ((rc = launch_prefilter(pl, pl.scr_img0, xpi, W, false, true, 1.f, true, st)))
+        if ((rc = launch_prefilter(pl, pl.scr_img0, xpi, W, false, true, 1.f, mode, st)))
             return rc;
     } else if (pl.Kz >= 0) {
-        if ((rc = launch_prefilter(pl, img, xpi, W, false, false, 1.f, true, st))) return rc;
+        if ((rc = launch_prefilter(pl, img, xpi, W, false, false, 1.f, mode, st))) return rc;
     } else if (pl.Kx >= 0) {
-        if ((rc = launch_prefilter(pl, img, xpi, W, false, true, 1.f, true, st))) return rc;
-    } else {
+        if ((rc = launch_prefilter(pl, img, xpi, W, false, true, 1.f, mode, st))) return rc;
+    } else if (pl.S) {
         if ((rc = launch_permute(pl, img, xpi, W, st))) return rc;
+    } else {
+        if ((rc = launch_to_pixmajor(pl, img, xpi, W, st))) return rc;
     }
     if (pl.L > 0) {
         if ((rc = interp_forward(pl, xpi, pl.scr_sino, W, 1.f, st))) return rc;
@@ -585,12 +733,12 @@ int apply_transpose(const Plan &pl, const float *sino, float *img, int W, cudaSt
     float *x = pre ? pl.scr_img0 : img;
     if ((rc = interp_adjoint(pl, src, x, W, scale, st))) return rc;
     if (pl.Kx >= 0 && pl.Kz >= 0) {
-        if ((rc = launch_prefilter(pl, pl.scr_img0, pl.scr_img1, W, true, true, 1.f, false, st)))
+        if ((rc = launch_prefilter(pl, pl.scr_img0, pl.scr_img1, W, true, true, 1.f, 0, st)))
             return rc;
-        return launch_prefilter(pl, pl.scr_img1, img, W, true, false, 1.f, false, st);
+        return launch_prefilter(pl, pl.scr_img1, img, W, true, false, 1.f, 0, st);
     }
-    if (pl.Kx >= 0) return launch_prefilter(pl, pl.scr_img0, img, W, true, true, 1.f, false, st);
-    if (pl.Kz >= 0) return launch_prefilter(pl, pl.scr_img0, img, W, true, false, 1.f, false, st);
+    if (pl.Kx >= 0) return launch_prefilter(pl, pl.scr_img0, img, W, true, true, 1.f, 0, st);
+    if (pl.Kz >= 0) return launch_prefilter(pl, pl.scr_img0, img, W, true, false, 1.f, 0, st);
     return MSOT_OK;
 }
 
@@ -633,7 +781,11 @@ int msot_interp_forward(msot_plan_t plan, const float *d_coeffs, float *d_raw, i
     int rc = check_batch(plan, batch, d_coeffs, d_raw);
     if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    if ((rc = launch_permute(plan->p, d_coeffs, plan->p.scr_img1, batch, st))) return rc;
+    if (plan->p.S) {
+        if ((rc = launch_permute(plan->p, d_coeffs, plan->p.scr_img1, batch, st))) return rc;
+    } else {
+        if ((rc = launch_to_pixmajor(plan->p, d_coeffs, plan->p.scr_img1, batch, st))) return rc;
+    }
     return interp_forward(plan->p, plan->p.scr_img1, d_raw, batch, 1.f, st);
 }
 

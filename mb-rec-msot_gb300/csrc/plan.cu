@@ -49,7 +49,7 @@ static int alloc(T **dst, size_t n, size_t &bytes) {
 static void free_plan(Plan &p) {
     void *ptrs[] = {p.tau_tiles, p.tau_pi, p.perm, p.ir_fwd, p.ir_adj, p.pre_x, p.pre_z,
                     p.sir, p.sir_se, p.sir_tiles, p.sir_pi, p.scr_img0, p.scr_img1,
-                    p.scr_sino};
+                    p.scr_sino, p.fwd_off, p.fwd_ent, p.scr_q};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     p = Plan();
@@ -116,6 +116,14 @@ static int build(const msot_plan_desc *d, Plan &p) {
     p.r_fx = to_fx(d->radius, fb);
     p.c1 = (float)(std::ldexp(1.0, -fb) / d->radius);
     p.n_tap = (int)std::floor(2.0 * d->radius) + 2;
+    p.F = (int)std::floor(d->radius);
+    p.inv_r = (float)(1.0 / d->radius);
+    p.ce1 = (float)((d->radius - p.F) / d->radius);
+    p.ce2 = (float)((p.F + 1 - d->radius) / d->radius);
+    if (!has_sir && 2 * p.F + 2 >= 256) {
+        set_error("plan: interpolation radius %g too large (max 126 samples)", d->radius);
+        return MSOT_EINVAL;
+    }
 
     std::vector<int32_t> tfx(PD);
     for (long i = 0; i < PD; ++i) tfx[i] = to_fx(d->travel[i], fb);
@@ -129,6 +137,23 @@ static int build(const msot_plan_desc *d, Plan &p) {
                           d->travel[i], i % p.P, i / p.P, p.T);
                 return MSOT_ERANGE;
             }
+        }
+    }
+
+    // --- forward table: pixels of each detector bucketed by floor(tau) ---------------
+    std::vector<int32_t> foff;
+    std::vector<int2> fent;
+    if (!has_sir) {
+        foff.assign((size_t)p.D * (p.T + 1), 0);
+        fent.resize(PD);
+        for (int det = 0; det < p.D; ++det) {
+            int32_t *o = foff.data() + (size_t)det * (p.T + 1);
+            const int32_t *tf = tfx.data() + (size_t)det * p.P;
+            for (int q = 0; q < p.P; ++q) ++o[(tf[q] >> fb) + 1];
+            for (int b = 0; b < p.T; ++b) o[b + 1] += o[b];
+            std::vector<int32_t> fill(o, o + p.T);
+            int2 *e = fent.data() + (size_t)det * p.P;
+            for (int q = 0; q < p.P; ++q) e[fill[tf[q] >> fb]++] = make_int2(tf[q], q);
         }
     }
 
@@ -243,6 +268,10 @@ static int build(const msot_plan_desc *d, Plan &p) {
     UP(p.tau_tiles, tiles);
     UP(p.tau_pi, tpi);
     UP(p.perm, perm);
+    if (!has_sir) {
+        UP(p.fwd_off, foff);
+        UP(p.fwd_ent, fent);
+    }
     if (has_sir) {
         UP(p.sir, sirf);
         UP(p.sir_se, se);
@@ -266,6 +295,11 @@ static int build(const msot_plan_desc *d, Plan &p) {
     if ((rc = alloc(&p.scr_img0, W * p.P, B)) != MSOT_OK) return rc;
     if ((rc = alloc(&p.scr_img1, W * p.P, B)) != MSOT_OK) return rc;
     if ((rc = alloc(&p.scr_sino, W * p.D * p.T, B)) != MSOT_OK) return rc;
+    if (!has_sir) {
+        p.wc_max = 1;
+        while (p.wc_max < 4 && (size_t)p.wc_max * 2 <= W) p.wc_max *= 2;
+        if ((rc = alloc(&p.scr_q, (size_t)p.D * p.T * p.wc_max, B)) != MSOT_OK) return rc;
+    }
     return MSOT_OK;
 }
 

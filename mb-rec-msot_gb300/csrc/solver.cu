@@ -1,6 +1,9 @@
 // solver.cu -- batched non-negative solvers on the GPU.
 //
-// FP32 vectors, FP64 reductions and scalars.  A batch of W instances is
+// FP32 vectors and element-wise arithmetic; inner products and norms are
+// FP64 sums of per-thread FP32 partial sums (each thread adds at most a few
+// dozen elements in FP32), and every Krylov scalar, step size and stopping
+// test is FP64.  A batch of W instances is
 // solved at once; each instance owns its Krylov scalars (independent
 // reconstructions), or the whole batch shares one set (coupled = the W
 // wavelengths of one reference call, whose lsqr/cgs see one stacked vector).
@@ -65,32 +68,34 @@ __device__ __forceinline__ int grp(int w, int coupled) { return coupled ? 0 : w;
 __global__ void k_sino_update(const float *__restrict__ x, const float *__restrict__ bvec,
                               float *__restrict__ u, size_t N, int mode, double sl,
                               const Scal *__restrict__ sc, int coupled, double *part) {
-    double acc = 0.0;
+    float facc = 0.f;
+    const float slf = (float)sl;
+    const float g = (float)sc[grp(blockIdx.y, coupled)].gamma;
+    const bool done = mode == 1 && sc[grp(blockIdx.y, coupled)].done;
     FOR_CHUNK(N) {
         const size_t k = base + i;
         float v;
         if (mode == 0) {
-            v = (float)(sl * (double)bvec[k] - sl * (double)x[k]);
+            v = fmaf(slf, bvec[k], -slf * x[k]);
         } else {
-            const double g = sc[grp(w, coupled)].gamma;
-            v = (float)(sl * (double)x[k] - g * (double)u[k]);
+            v = fmaf(slf, x[k], -g * u[k]);
+            if (done) v = u[k];
         }
-        if (!(mode == 1 && sc[grp(w, coupled)].done)) u[k] = v;
-        const double vv = (double)u[k];
-        acc += vv * vv;
+        u[k] = v;
+        facc = fmaf(v, v, facc);
     }
-    STORE_PARTIAL(acc, part);
+    STORE_PARTIAL((double)facc, part);
 }
 
 // generic sum of squares of (x - y) (y may be null) per instance
 __global__ void k_sumsq(const float *__restrict__ x, const float *__restrict__ y, size_t N,
                         double *part) {
-    double acc = 0.0;
+    float facc = 0.f;
     FOR_CHUNK(N) {
-        double v = (double)x[base + i] - (y ? (double)y[base + i] : 0.0);
-        acc += v * v;
+        const float v = x[base + i] - (y ? y[base + i] : 0.f);
+        facc = fmaf(v, v, facc);
     }
-    STORE_PARTIAL(acc, part);
+    STORE_PARTIAL((double)facc, part);
 }
 
 // LSQR init, image parts: ur = -sl*sr*w ; ub = sb*(w+vm) - sb*w.
@@ -99,19 +104,20 @@ __global__ void k_l2_init_img(const float *__restrict__ wv, const float *__restr
                               float *__restrict__ ur, float *__restrict__ ub, size_t N,
                               double sl, double sr, double sb, int has_reg, double *part,
                               double *part2) {
-    double a1 = 0.0, a2 = 0.0;
+    float a1 = 0.f, a2 = 0.f;
+    const float c_r = (float)(-sl * sr), c_b = (float)sb;
     FOR_CHUNK(N) {
         const size_t k = base + i;
-        const double wd = wv[k], s = wd + (double)vm[k];
-        const float r = (float)(-sl * sr * wd);
-        const float bb = (float)(sb * s - sb * wd);
+        const float wd = wv[k], s = wd + vm[k];
+        const float r = c_r * wd;
+        const float bb = fmaf(c_b, s, -c_b * wd);
         if (has_reg) ur[k] = r;
         ub[k] = bb;
-        a1 += (has_reg ? (double)r * r : 0.0) + (double)bb * bb;
-        a2 += s * s;
+        a1 = fmaf(bb, bb, has_reg ? fmaf(r, r, a1) : a1);
+        a2 = fmaf(s, s, a2);
     }
-    STORE_PARTIAL(a1, part);
-    STORE_PARTIAL(a2, part2);
+    STORE_PARTIAL((double)a1, part);
+    STORE_PARTIAL((double)a2, part2);
 }
 
 // LSQR step, image parts: ur = sl*sr*v - gamma*ur ; ub = sb*v - gamma*ub
@@ -119,19 +125,23 @@ __global__ void k_l2_u_img(const float *__restrict__ v, float *__restrict__ ur,
                            float *__restrict__ ub, size_t N, double sl, double sr, double sb,
                            int has_reg, const Scal *__restrict__ sc, int coupled,
                            double *part) {
-    double acc = 0.0;
+    float acc = 0.f;
+    const Scal &q = sc[grp(blockIdx.y, coupled)];
+    const float g = (float)q.gamma, c_r = (float)(sl * sr), c_b = (float)sb;
+    const bool done = q.done;
     FOR_CHUNK(N) {
         const size_t k = base + i;
-        const Scal &q = sc[grp(w, coupled)];
-        const double g = q.gamma, vd = v[k];
-        if (!q.done) {
-            if (has_reg) ur[k] = (float)(sl * sr * vd - g * (double)ur[k]);
-            ub[k] = (float)(sb * vd - g * (double)ub[k]);
+        const float vd = v[k];
+        float r = has_reg ? ur[k] : 0.f, bb = ub[k];
+        if (!done) {
+            r = fmaf(c_r, vd, -g * r);
+            bb = fmaf(c_b, vd, -g * bb);
+            if (has_reg) ur[k] = r;
+            ub[k] = bb;
         }
-        const double r = has_reg ? (double)ur[k] : 0.0, bb = ub[k];
-        acc += r * r + bb * bb;
+        acc = fmaf(bb, bb, fmaf(r, r, acc));
     }
-    STORE_PARTIAL(acc, part);
+    STORE_PARTIAL((double)acc, part);
 }
 
 // vt = (sl*(At_us + sr*ur) + sb*ub) / beta ; v = vt - beta*v_old (first: v_old = 0)
@@ -139,21 +149,23 @@ __global__ void k_l2_v_img(const float *__restrict__ atu, const float *__restric
                            const float *__restrict__ ub, float *__restrict__ v, size_t N,
                            double sl, double sr, double sb, int has_reg, int first,
                            const Scal *__restrict__ sc, int coupled, double *part) {
-    double acc = 0.0;
+    float acc = 0.f;
+    const Scal &q = sc[grp(blockIdx.y, coupled)];
+    const bool done = q.done;
+    const float ib = (float)(1.0 / q.beta), be = (float)q.beta;
+    const float c_l = (float)sl, c_r = (float)(sl * sr), c_b = (float)sb;
     FOR_CHUNK(N) {
         const size_t k = base + i;
-        const Scal &q = sc[grp(w, coupled)];
-        if (!q.done) {
-            double vt = sl * ((double)atu[k] + (has_reg ? sr * (double)ur[k] : 0.0)) +
-                        sb * (double)ub[k];
-            vt /= q.beta;
-            if (!first) vt -= q.beta * (double)v[k];
-            v[k] = (float)vt;
+        float vv = v[k];
+        if (!done) {
+            float vt = fmaf(c_l, atu[k], fmaf(c_b, ub[k], has_reg ? c_r * ur[k] : 0.f)) * ib;
+            if (!first) vt = fmaf(-be, vv, vt);
+            vv = vt;
+            v[k] = vv;
         }
-        const double vv = v[k];
-        acc += vv * vv;
+        acc = fmaf(vv, vv, acc);
     }
-    STORE_PARTIAL(acc, part);
+    STORE_PARTIAL((double)acc, part);
 }
 
 __device__ double sum_parts(const double *part, int nblk, int w) {
@@ -244,7 +256,7 @@ __global__ void k_l2_scale_v(float *v, float *d, float *x, float *xmin, const fl
             x[k] = wv[k];
             xmin[k] = wv[k];
         }
-        if (!q.done) v[k] = (float)((double)v[k] / q.alpha);
+        if (!q.done) v[k] = v[k] * (float)(1.0 / q.alpha);
     }
 }
 
@@ -255,9 +267,9 @@ __global__ void k_l2_dx(const float *v, float *d, float *x, float *xmin, size_t 
         const size_t k = base + i;
         const Scal &q = sc[grp(w, coupled)];
         if (q.done || q.improved == 0) continue;
-        const double dn = ((double)v[k] - q.thet * (double)d[k]) / q.rho;
-        d[k] = (float)dn;
-        const float xn = (float)((double)x[k] + q.phi * dn);
+        const float dn = fmaf(-(float)q.thet, d[k], v[k]) * (float)(1.0 / q.rho);
+        d[k] = dn;
+        const float xn = fmaf((float)q.phi, dn, x[k]);
         x[k] = xn;
         if (q.improved != 2) xmin[k] = xn;
     }
@@ -492,30 +504,30 @@ static int solve_l2(const Plan &pl, const float *b, float *rec, int W, int num_i
 // ---------------------------------------------------------------------------
 __global__ void k_dot(const float *__restrict__ a, const float *__restrict__ b, size_t N,
                       double *part) {
-    double acc = 0.0;
-    FOR_CHUNK(N) acc += (double)a[base + i] * (double)b[base + i];
-    STORE_PARTIAL(acc, part);
+    float acc = 0.f;
+    FOR_CHUNK(N) acc = fmaf(a[base + i], b[base + i], acc);
+    STORE_PARTIAL((double)acc, part);
 }
 
 // d = max(u - bp, 0); rhs = d + bp + lam*atb - lam*eta; cgs init: x = 0, r = rt = rhs.
 __global__ void k_l1_rhs(const float *u, const float *bp, const float *atb, float *dv,
                          float *rhs, float *x, float *r, float *rt, float *xmin, size_t N,
                          double lam, double eta, double *part) {
-    double acc = 0.0;
+    float acc = 0.f;
+    const float lf = (float)lam, le = (float)(lam * eta);
     FOR_CHUNK(N) {
         const size_t k = base + i;
         const float dd = fmaxf(u[k] - bp[k], 0.f);
         dv[k] = dd;
-        const float rh = (float)((double)fmaxf(dd, 0.f) + (double)bp[k] + lam * (double)atb[k] -
-                                 lam * eta);
+        const float rh = fmaf(lf, atb[k], fmaxf(dd, 0.f) + bp[k]) - le;
         rhs[k] = rh;
         r[k] = rh;
         rt[k] = rh;
         x[k] = 0.f;
         xmin[k] = 0.f;
-        acc += (double)rh * rh;
+        acc = fmaf(rh, rh, acc);
     }
-    STORE_PARTIAL(acc, part);
+    STORE_PARTIAL((double)acc, part);
 }
 
 // stage 0: n2b; 1: rho = rt.r; 2: alpha = rho / rt.vh; 3: normr after r update
@@ -573,10 +585,10 @@ __global__ void k_cgs_dir(const float *r, float *q, float *uc, float *p, size_t 
             uc[k] = r[k];
             p[k] = r[k];
         } else {
-            const double beta = s.rho_cg / s.rho1_cg;
-            const double u = (double)r[k] + beta * (double)q[k];
-            uc[k] = (float)u;
-            p[k] = (float)(u + beta * ((double)q[k] + beta * (double)p[k]));
+            const float beta = (float)(s.rho_cg / s.rho1_cg);
+            const float u = fmaf(beta, q[k], r[k]);
+            uc[k] = u;
+            p[k] = fmaf(beta, fmaf(beta, p[k], q[k]), u);
         }
     }
 }
@@ -584,14 +596,15 @@ __global__ void k_cgs_dir(const float *r, float *q, float *uc, float *p, size_t 
 // y = lam*atav + v ; partial dot(rt, y)
 __global__ void k_cgs_op(const float *atav, const float *v, float *y, const float *rt,
                          size_t N, double lam, double *part) {
-    double acc = 0.0;
+    float acc = 0.f;
+    const float lf = (float)lam;
     FOR_CHUNK(N) {
         const size_t k = base + i;
-        const float o = (float)(lam * (double)atav[k] + (double)v[k]);
+        const float o = fmaf(lf, atav[k], v[k]);
         y[k] = o;
-        acc += (double)rt[k] * o;
+        acc = fmaf(rt[k], o, acc);
     }
-    STORE_PARTIAL(acc, part);
+    STORE_PARTIAL((double)acc, part);
 }
 
 // q = uc - alpha vh; uh = uc + q; x += alpha uh
@@ -601,29 +614,32 @@ __global__ void k_cgs_upd(const float *uc, const float *vh, float *q, float *uh,
         const size_t k = base + i;
         const Scal &s = sc[grp(w, coupled)];
         if (s.done) continue;
-        const double a = s.alpha_cg;
-        const double qq = (double)uc[k] - a * (double)vh[k];
-        q[k] = (float)qq;
-        const double u = (double)uc[k] + qq;
-        uh[k] = (float)u;
-        x[k] = (float)((double)x[k] + a * u);
+        const float a = (float)s.alpha_cg;
+        const float qq = fmaf(-a, vh[k], uc[k]);
+        q[k] = qq;
+        const float u = uc[k] + qq;
+        uh[k] = u;
+        x[k] = fmaf(a, u, x[k]);
     }
 }
 
 // r -= alpha (lam atau + uh); partial ||r||^2
 __global__ void k_cgs_res(const float *atau, const float *uh, float *r, size_t N, double lam,
                           const Scal *sc, int coupled, double *part) {
-    double acc = 0.0;
+    float acc = 0.f;
+    const Scal &s = sc[grp(blockIdx.y, coupled)];
+    const float lf = (float)lam, a = (float)s.alpha_cg;
+    const bool done = s.done;
     FOR_CHUNK(N) {
         const size_t k = base + i;
-        const Scal &s = sc[grp(w, coupled)];
-        if (!s.done) {
-            const double o = lam * (double)atau[k] + (double)uh[k];
-            r[k] = (float)((double)r[k] - s.alpha_cg * o);
+        float rr = r[k];
+        if (!done) {
+            rr = fmaf(-a, fmaf(lf, atau[k], uh[k]), rr);
+            r[k] = rr;
         }
-        acc += (double)r[k] * r[k];
+        acc = fmaf(rr, rr, acc);
     }
-    STORE_PARTIAL(acc, part);
+    STORE_PARTIAL((double)acc, part);
 }
 
 __global__ void k_cgs_keep(const float *x, float *xmin, size_t N, const Scal *sc, int coupled) {
