@@ -28,6 +28,7 @@ constexpr int PATCH_X = 8;           // patch width (x columns)
 constexpr int PATCH_Z = 8;           // patch height (z rows)
 constexpr int PATCH = PATCH_X * PATCH_Z;
 constexpr int32_t TAU_PAD = INT32_MIN;  // marks a padding pixel in tau_tiles
+constexpr int REG_X = 32, REG_Z = 32, REG = REG_X * REG_Z;  // adjoint region
 
 struct Plan {
     int nx, nz, P, D, T;
@@ -49,8 +50,11 @@ struct Plan {
     float ce1 = 0.f, ce2 = 0.f;    // (r - F)/r and (F + 1 - r)/r
     int32_t *fwd_off = nullptr;    // [D][T+1] CSR offsets of bucket b = floor(tau)
     int2 *fwd_ent = nullptr;       // [D][P] (tau fixed point, pixel) sorted by bucket
-    int wc_max = 0;                // instances per adjoint table chunk
-    float4 *scr_q = nullptr;       // [D][T][wc_max] adjoint bucket table
+    // adjoint regions: 32x32 pixels (REG_Z rows of z x REG_X columns of x)
+    int n_reg_x = 0, n_reg_z = 0, n_reg = 0;
+    int32_t *reg_tau = nullptr;    // [n_reg][D][REG] tau per region pixel (TAU_PAD outside)
+    int2 *reg_span = nullptr;      // [n_reg][D] first / last bucket of the region
+    int reg_span_max = 0;          // largest last - first + 1
     // IR
     int L = 0, Lh = 0;
     float *ir_fwd = nullptr, *ir_adj = nullptr;

@@ -108,6 +108,8 @@ __global__ void k_permute(const float *__restrict__ in, float *__restrict__ out,
 // V_b = sum beta_k s[b+k]; each (pixel, detector) then adds
 // U + f V + e1 s[b-F] + e2 s[b+F+1].
 // ---------------------------------------------------------------------------
+constexpr int FWD_DG = 8;  // detectors per CTA of the bucket-moment forward
+
 template <int WT>
 __global__ void __launch_bounds__(256) k_das_fwd2(const int32_t *__restrict__ off,
                                                   const int2 *__restrict__ ent,
@@ -118,9 +120,15 @@ __global__ void __launch_bounds__(256) k_das_fwd2(const int32_t *__restrict__ of
     extern __shared__ float mom[];  // [4][WT][NB], bucket fastest
     const int NB = blockDim.x;
     const int TB = NB - 2 * F - 2;
-    const int d = blockIdx.y, w0 = blockIdx.z * WT;
+    const int w0 = blockIdx.z * WT;
     const int t0 = blockIdx.x * TB;
     const int b_lo = t0 - F - 1;
+    // FWD_DG adjacent detectors per CTA: their pixel bands overlap, so the
+    // pixel gathers of the later ones mostly hit L1
+    for (int dd = 0; dd < FWD_DG; ++dd) {
+    const int d = blockIdx.y * FWD_DG + dd;
+    if (d >= D) break;
+    if (dd) __syncthreads();  // mom of the previous detector fully consumed
     {
         float m0[WT], m1[WT], m2[WT], m3[WT];
 #pragma unroll
@@ -189,7 +197,7 @@ __global__ void __launch_bounds__(256) k_das_fwd2(const int32_t *__restrict__ of
     __syncthreads();
     const int ti = threadIdx.x;
     const int t = t0 + ti;
-    if (ti >= TB || t >= T) return;
+    if (ti >= TB || t >= T) continue;
     float acc[WT];
 #pragma unroll
     for (int i = 0; i < WT; ++i) acc[i] = 0.f;
@@ -209,91 +217,80 @@ __global__ void __launch_bounds__(256) k_das_fwd2(const int32_t *__restrict__ of
         acc[i] += mom[(3 * WT + i) * NB + base - F - 1];
         raw[((size_t)(w0 + i) * D + d) * T + t] = acc[i] * scale;
     }
-}
-
-// Q[d][b][c] = (U_b, V_b, s[b-F], s[b+F+1]) for the WC instances c0.. of s
-template <int WC>
-__global__ void __launch_bounds__(256) k_adj_table(const float *__restrict__ s,
-                                                   float4 *__restrict__ Q, int D, int T, int c0,
-                                                   int F, float inv_r) {
-    extern __shared__ float seg[];  // [WC][256 + 2F + 2]
-    const int SL = 256 + 2 * F + 2;
-    const int d = blockIdx.y, b0 = blockIdx.x * 256;
-    for (int c = 0; c < WC; ++c) {
-        const float *src = s + ((size_t)(c0 + c) * D + d) * T;
-        for (int q = threadIdx.x; q < SL; q += blockDim.x) {
-            const int t = b0 - F + q;
-            seg[c * SL + q] = (t >= 0 && t < T) ? __ldg(src + t) : 0.f;
-        }
-    }
-    __syncthreads();
-    const int b = b0 + threadIdx.x;
-    if (b >= T) return;
-    float4 *dst = Q + ((size_t)d * T + b) * WC;
-#pragma unroll
-    for (int c = 0; c < WC; ++c) {
-        const float *g = seg + c * SL + threadIdx.x + F;  // g[k] = s[b + k]
-        float U = 0.f, V = 0.f;
-        for (int k = -(F - 1); k <= F; ++k) {
-            const float a = fmaf(-fabsf((float)k), inv_r, 1.f);
-            U = fmaf(a, g[k], U);
-            V += k <= 0 ? -g[k] : g[k];
-        }
-        dst[c] = make_float4(U, V * inv_r, g[-F], g[F + 1]);
     }
 }
 
-constexpr int ADJ_GROUPS = 16;  // detector groups per CTA of the bucket-table gather
-
-template <int WC>
-__global__ void __launch_bounds__(PATCH *ADJ_GROUPS) k_das_adj2(
-    const int32_t *__restrict__ tiles, const float4 *__restrict__ Q, float *__restrict__ out,
-    int nx, int nz, int npx, int D, int T, int c0, int fb, float inv_r, float ce1, float ce2,
-    float scale) {
-    __shared__ float red[ADJ_GROUPS][WC][PATCH];
-    const int patch = blockIdx.x;
-    const int q = threadIdx.x & (PATCH - 1), g = threadIdx.x / PATCH;
-    const int px = patch % npx, pz = patch / npx;
-    const int ix = px * PATCH_X + q / PATCH_Z, iz = pz * PATCH_Z + q % PATCH_Z;
-    float acc[WC];
-#pragma unroll
-    for (int i = 0; i < WC; ++i) acc[i] = 0.f;
-    const int32_t *tp = tiles + (size_t)patch * D * PATCH + q;
+// Adjoint by regions: CTA = (32x32 pixel region, instance tile).  For each
+// detector the sinogram samples spanned by the region (plus F+1 on each
+// side) are staged in shared memory, the bucket table
+// Q_b = (U_b, V_b, s[b-F], s[b+F+1]) of that span is built there, and every
+// pixel adds U + f V + e1 s[b-F] + e2 s[b+F+1].
+template <int WT>
+__global__ void __launch_bounds__(REG) k_das_adj3(const int32_t *__restrict__ rtau,
+                                                  const int2 *__restrict__ rspan,
+                                                  const float *__restrict__ s,
+                                                  float *__restrict__ out, int nx, int nz,
+                                                  int nrx, int D, int T, int fb, int F,
+                                                  float inv_r, float ce1, float ce2,
+                                                  float scale, int span_max) {
+    extern __shared__ float sm[];
+    const int SL = span_max + 2 * F + 2;
+    float *seg = sm;                                           // [WT][SL]
+    float4 *Q = reinterpret_cast<float4 *>(sm + ((WT * SL + 3) & ~3));  // [WT][span_max]
+    const int reg = blockIdx.x, w0 = blockIdx.y * WT;
+    const int q = threadIdx.x;
+    const int rx = reg % nrx, rz = reg / nrx;
+    const int ix = rx * REG_X + q / REG_Z, iz = rz * REG_Z + q % REG_Z;
     const int mask = (1 << fb) - 1;
     const float step = __int_as_float((127 - fb) << 23);
-    auto add = [&](int32_t tau, const float4 (&v)[WC]) {
-        const float f = (float)(tau & mask) * step;
-        const float e1 = fmaxf(0.f, fmaf(-f, inv_r, ce1));
-        const float e2 = fmaxf(0.f, fmaf(f, inv_r, -ce2));
+    float acc[WT];
 #pragma unroll
-        for (int i = 0; i < WC; ++i)
-            acc[i] = fmaf(e2, v[i].w, fmaf(e1, v[i].z, fmaf(f, v[i].y, acc[i] + v[i].x)));
-    };
-    for (int d = g; d < D; d += 2 * ADJ_GROUPS) {
-        const int d2 = d + ADJ_GROUPS;
-        const int32_t t1 = __ldg(tp + (size_t)d * PATCH);
-        const int32_t t2 = d2 < D ? __ldg(tp + (size_t)d2 * PATCH) : TAU_PAD;
-        float4 v1[WC], v2[WC];
-        const bool ok1 = t1 != TAU_PAD, ok2 = t2 != TAU_PAD;
-        const float4 *q1 = Q + ((size_t)d * T + min(max(t1 >> fb, 0), T - 1)) * WC;
-        const float4 *q2 = Q + ((size_t)(ok2 ? d2 : d) * T + min(max(t2 >> fb, 0), T - 1)) * WC;
-#pragma unroll
-        for (int i = 0; i < WC; ++i) {
-            v1[i] = ok1 ? __ldg(q1 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
-            v2[i] = ok2 ? __ldg(q2 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int i = 0; i < WT; ++i) acc[i] = 0.f;
+    const int32_t *tp = rtau + (size_t)reg * D * REG + q;
+    const int2 *spp = rspan + (size_t)reg * D;
+    int32_t tau_next = __ldg(tp);
+    for (int d = 0; d < D; ++d) {
+        const int32_t tau = tau_next;
+        if (d + 1 < D) tau_next = __ldg(tp + (size_t)(d + 1) * REG);
+        const int2 sp = __ldg(spp + d);
+        const int nb = sp.y - sp.x + 1;
+        if (nb <= 0) continue;  // region outside the grid (uniform across the CTA)
+        const int L = nb + 2 * F + 2;
+        for (int i = threadIdx.x; i < WT * L; i += blockDim.x) {
+            const int w = i / L, k = i - w * L;
+            const int t = sp.x - F + k;
+            seg[w * SL + k] =
+                (t >= 0 && t < T) ? __ldg(s + ((size_t)(w0 + w) * D + d) * T + t) : 0.f;
         }
-        if (ok1) add(t1, v1);
-        if (ok2) add(t2, v2);
+        __syncthreads();
+        for (int i = threadIdx.x; i < WT * nb; i += blockDim.x) {
+            const int w = i / nb, bl = i - w * nb;
+            const float *g = seg + w * SL + bl + F;  // g[k] = s[b + k]
+            float U = 0.f, V = 0.f;
+            for (int k = -(F - 1); k <= F; ++k) {
+                U = fmaf(fmaf(-fabsf((float)k), inv_r, 1.f), g[k], U);
+                V += k <= 0 ? -g[k] : g[k];
+            }
+            Q[w * span_max + bl] = make_float4(U, V * inv_r, g[-F], g[F + 1]);
+        }
+        __syncthreads();
+        if (tau != TAU_PAD) {
+            const int bl = (tau >> fb) - sp.x;
+            const float f = (float)(tau & mask) * step;
+            const float e1 = fmaxf(0.f, fmaf(-f, inv_r, ce1));
+            const float e2 = fmaxf(0.f, fmaf(f, inv_r, -ce2));
+#pragma unroll
+            for (int i = 0; i < WT; ++i) {
+                const float4 v = Q[i * span_max + bl];
+                acc[i] = fmaf(e2, v.w, fmaf(e1, v.z, fmaf(f, v.y, acc[i] + v.x)));
+            }
+        }
+        __syncthreads();
     }
-#pragma unroll
-    for (int i = 0; i < WC; ++i) red[g][i][q] = acc[i];
-    __syncthreads();
-    if (g < WC && ix < nx && iz < nz) {
-        float v = 0.f;
-#pragma unroll
-        for (int k = 0; k < ADJ_GROUPS; ++k) v += red[k][g][q];
+    if (ix < nx && iz < nz) {
         const size_t P = (size_t)nx * nz;
-        out[(size_t)(c0 + g) * P + (size_t)ix * nz + iz] = v * scale;
+#pragma unroll
+        for (int i = 0; i < WT; ++i) out[(size_t)(w0 + i) * P + (size_t)ix * nz + iz] = acc[i] * scale;
     }
 }
 
@@ -561,7 +558,7 @@ int launch_das_forward(const Plan &pl, const float *xpm, float *raw, int W, floa
     const int wt = pick_wt(W, 1, 8);
     constexpr int NB = 256;
     const int TB = NB - 2 * pl.F - 2;
-    dim3 grid(div_up(pl.T, TB), pl.D, W / wt);
+    dim3 grid(div_up(pl.T, TB), div_up(pl.D, FWD_DG), W / wt);
     const size_t smem = (size_t)4 * wt * NB * sizeof(float);
 #define CASE(WT)                                                                          \
     case WT:                                                                              \
@@ -577,29 +574,28 @@ int launch_das_forward(const Plan &pl, const float *xpm, float *raw, int W, floa
     return MSOT_OK;
 }
 
-// DAS adjoint by bucket table; raw [W][D][T] -> x [W][P], W in chunks of
-// pl.wc_max instances (the table of one chunk stays L2-resident).
+// DAS adjoint by regions; raw [W][D][T] -> x [W][P].
 int launch_das_adjoint(const Plan &pl, const float *raw, float *x, int W, float scale,
                        cudaStream_t st) {
     TimedScope ts_(KID_INTERP_ADJ, st);
-    const int wc = pick_wt(W, 1, pl.wc_max);
-    const size_t tsmem = (size_t)wc * (256 + 2 * pl.F + 2) * sizeof(float);
-    dim3 tgrid(div_up(pl.T, 256), pl.D);
-    for (int c0 = 0; c0 < W; c0 += wc) {
-#define CASE(WC)                                                                           \
-    case WC:                                                                               \
-        KLAUNCH(k_adj_table<WC><<<tgrid, 256, tsmem, st>>>(raw, pl.scr_q, pl.D, pl.T, c0,   \
-                                                           pl.F, pl.inv_r));               \
-        KLAUNCH(k_das_adj2<WC><<<pl.n_patch, PATCH * ADJ_GROUPS, 0, st>>>(                 \
-            pl.tau_tiles, pl.scr_q, x, pl.nx, pl.nz, pl.n_patch_x, pl.D, pl.T, c0,          \
-            pl.frac_bits, pl.inv_r, pl.ce1, pl.ce2, scale));                                \
+    const int wt = pick_wt(W, 1, 4);
+    const int SL = pl.reg_span_max + 2 * pl.F + 2;
+    const size_t smem = (size_t)((wt * SL + 3) & ~3) * sizeof(float) +
+                        (size_t)wt * pl.reg_span_max * sizeof(float4);
+    dim3 grid(pl.n_reg, W / wt);
+    int rc;
+#define CASE(WT)                                                                          \
+    case WT:                                                                              \
+        if ((rc = set_smem(k_das_adj3<WT>, smem)) != MSOT_OK) return rc;                  \
+        KLAUNCH(k_das_adj3<WT><<<grid, REG, smem, st>>>(                                  \
+            pl.reg_tau, pl.reg_span, raw, x, pl.nx, pl.nz, pl.n_reg_x, pl.D, pl.T,         \
+            pl.frac_bits, pl.F, pl.inv_r, pl.ce1, pl.ce2, scale, pl.reg_span_max));       \
         break;
-        switch (wc) {
-            CASE(1) CASE(2) CASE(4)
-        }
-#undef CASE
-        MSOT_LAUNCH_CHECK();
+    switch (wt) {
+        CASE(1) CASE(2) CASE(4)
     }
+#undef CASE
+    MSOT_LAUNCH_CHECK();
     return MSOT_OK;
 }
 

@@ -49,7 +49,7 @@ static int alloc(T **dst, size_t n, size_t &bytes) {
 static void free_plan(Plan &p) {
     void *ptrs[] = {p.tau_tiles, p.tau_pi, p.perm, p.ir_fwd, p.ir_adj, p.pre_x, p.pre_z,
                     p.sir, p.sir_se, p.sir_tiles, p.sir_pi, p.scr_img0, p.scr_img1,
-                    p.scr_sino, p.fwd_off, p.fwd_ent, p.scr_q};
+                    p.scr_sino, p.fwd_off, p.fwd_ent, p.reg_tau, p.reg_span};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     p = Plan();
@@ -157,11 +157,41 @@ static int build(const msot_plan_desc *d, Plan &p) {
         }
     }
 
+    // --- adjoint regions: 32x32 pixels, travel times and bucket span per detector ------
+    std::vector<int32_t> rtau;
+    std::vector<int2> rspan;
+    if (!has_sir) {
+        p.n_reg_x = div_up(p.nx, REG_X);
+        p.n_reg_z = div_up(p.nz, REG_Z);
+        p.n_reg = p.n_reg_x * p.n_reg_z;
+        rtau.assign((size_t)p.n_reg * p.D * REG, TAU_PAD);
+        rspan.assign((size_t)p.n_reg * p.D, make_int2(0, -1));
+        for (int rz = 0; rz < p.n_reg_z; ++rz)
+            for (int rx = 0; rx < p.n_reg_x; ++rx) {
+                const int reg = rz * p.n_reg_x + rx;
+                for (int det = 0; det < p.D; ++det) {
+                    int bmin = INT32_MAX, bmax = INT32_MIN;
+                    for (int q = 0; q < REG; ++q) {
+                        const int ix = rx * REG_X + q / REG_Z, iz = rz * REG_Z + q % REG_Z;
+                        if (ix >= p.nx || iz >= p.nz) continue;
+                        const int32_t t = tfx[(size_t)det * p.P + (size_t)ix * p.nz + iz];
+                        rtau[((size_t)reg * p.D + det) * REG + q] = t;
+                        bmin = std::min(bmin, t >> fb);
+                        bmax = std::max(bmax, t >> fb);
+                    }
+                    if (bmax >= bmin) {
+                        rspan[(size_t)reg * p.D + det] = make_int2(bmin, bmax);
+                        p.reg_span_max = std::max(p.reg_span_max, bmax - bmin + 1);
+                    }
+                }
+            }
+    }
+
     // --- gather table: 8x8 pixel patches -----------------------------------------
     p.n_patch_x = div_up(p.nx, PATCH_X);
     p.n_patch_z = div_up(p.nz, PATCH_Z);
     p.n_patch = p.n_patch_x * p.n_patch_z;
-    size_t ntile = (size_t)p.n_patch * p.D * PATCH;
+    size_t ntile = has_sir ? (size_t)p.n_patch * p.D * PATCH : 0;  // SIR gather only
     std::vector<int32_t> tiles(ntile, TAU_PAD);
     std::vector<int32_t> stiles;
     if (has_sir) stiles.assign(ntile, 0);
@@ -172,7 +202,7 @@ static int build(const msot_plan_desc *d, Plan &p) {
                 int ix = px * PATCH_X + q / PATCH_Z, iz = pz * PATCH_Z + q % PATCH_Z;
                 if (ix >= p.nx || iz >= p.nz) continue;
                 long pix = (long)ix * p.nz + iz;
-                for (int det = 0; det < p.D; ++det) {
+                for (int det = 0; det < p.D && has_sir; ++det) {
                     size_t o = ((size_t)patch * p.D + det) * PATCH + q;
                     tiles[o] = tfx[(size_t)det * p.P + pix];
                     if (has_sir) stiles[o] = d->sir_idx[(size_t)det * p.P + pix] - 1;
@@ -191,10 +221,10 @@ static int build(const msot_plan_desc *d, Plan &p) {
         int j = (int)((s >> 33) % (uint64_t)(i + 1));
         std::swap(perm[i], perm[j]);
     }
-    std::vector<int32_t> tpi(PD);
+    std::vector<int32_t> tpi(has_sir ? PD : 0);
     std::vector<int32_t> spi;
     if (has_sir) spi.resize(PD);
-    for (int det = 0; det < p.D; ++det)
+    for (int det = 0; det < p.D && has_sir; ++det)
         for (int j = 0; j < p.P; ++j) {
             tpi[(size_t)det * p.P + j] = tfx[(size_t)det * p.P + perm[j]];
             if (has_sir) spi[(size_t)det * p.P + j] = d->sir_idx[(size_t)det * p.P + perm[j]] - 1;
@@ -271,6 +301,8 @@ static int build(const msot_plan_desc *d, Plan &p) {
     if (!has_sir) {
         UP(p.fwd_off, foff);
         UP(p.fwd_ent, fent);
+        UP(p.reg_tau, rtau);
+        UP(p.reg_span, rspan);
     }
     if (has_sir) {
         UP(p.sir, sirf);
@@ -295,11 +327,7 @@ static int build(const msot_plan_desc *d, Plan &p) {
     if ((rc = alloc(&p.scr_img0, W * p.P, B)) != MSOT_OK) return rc;
     if ((rc = alloc(&p.scr_img1, W * p.P, B)) != MSOT_OK) return rc;
     if ((rc = alloc(&p.scr_sino, W * p.D * p.T, B)) != MSOT_OK) return rc;
-    if (!has_sir) {
-        p.wc_max = 1;
-        while (p.wc_max < 4 && (size_t)p.wc_max * 2 <= W) p.wc_max *= 2;
-        if ((rc = alloc(&p.scr_q, (size_t)p.D * p.T * p.wc_max, B)) != MSOT_OK) return rc;
-    }
+
     return MSOT_OK;
 }
 
