@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-oracle", action="store_true", help="skip the FP64 oracle solve")
+    ap.add_argument("--op", action="store_true",
+                    help="time the operator alone: one step = A then A^T on the batch")
     return ap.parse_args()
 
 
@@ -129,14 +131,14 @@ class Clocks:
 # ----------------------------------------------------------------------------
 # our implementation
 # ----------------------------------------------------------------------------
-def build_model(batch):
+def build_model(batch, norm=None):
     from msot_gb300 import Discretization, MSOTmodel, Probe
     from msot_gb300.synthetic import gauss_pulse_eir
     h = 0.2e-3 * 127 / 2
     probe = Probe(n_det=N_DET, radius=0.040, angular_coverage=135.0, fs=4e7, n_samples=N_T,
                   delay=0.0, eir=gauss_pulse_eir(), eir_length=257)
     disc = Discretization([-h, h], N_GRID)
-    return MSOTmodel(probe, disc, 1500.0, False, True, 0, 1e5, 12e6, None, max_batch=batch)
+    return MSOTmodel(probe, disc, 1500.0, False, True, 0, 1e5, 12e6, norm, max_batch=batch)
 
 
 def make_data(model, batch, seed):
@@ -185,6 +187,30 @@ def algorithmic_bytes(kid_name, batch):
     if kid_name == "permute":
         return 2 * 4 * P * batch + 4 * P
     return None
+
+
+def run_operator(args):
+    """Operator-only step (A then A^T on --batch images); prints a JSON line
+    with applies/s.  Used for profiling the operator kernels."""
+    import torch
+    from msot_gb300 import _lib
+    L = _lib.load()
+    B = args.batch
+    model = build_model(B, norm=2.0243e-05)  # fixed sigma_max: no estimation launches
+    x, b = make_data(model, B, seed=7)
+    for _ in range(args.warmup):
+        model.transpose(model.forward(x))
+    torch.cuda.synchronize()
+    a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(args.steps):
+        model.transpose(model.forward(x))
+    z.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(z) / args.steps
+    return {"metric": "A + A^T pairs/s (instances)", "value": B / (ms / 1e3), "unit": "pairs/s",
+            "ms_per_step": ms, "batch": B, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "impl": "ours-operator"}
 
 
 def run_ours(args, rank, world):
@@ -354,6 +380,10 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
         out = run_reference(args, rank)
+    elif args.op:
+        import torch
+        torch.cuda.set_device(0)
+        out = run_operator(args)
     else:
         if world > 1:
             import torch

@@ -108,7 +108,7 @@ __global__ void k_permute(const float *__restrict__ in, float *__restrict__ out,
 // V_b = sum beta_k s[b+k]; each (pixel, detector) then adds
 // U + f V + e1 s[b-F] + e2 s[b+F+1].
 // ---------------------------------------------------------------------------
-constexpr int FWD_DG = 8;  // detectors per CTA of the bucket-moment forward
+constexpr int FWD_DG = 1;  // detectors per CTA of the bucket-moment forward
 
 template <int WT>
 __global__ void __launch_bounds__(256) k_das_fwd2(const int32_t *__restrict__ off,
@@ -220,23 +220,49 @@ __global__ void __launch_bounds__(256) k_das_fwd2(const int32_t *__restrict__ of
     }
 }
 
-// Adjoint by regions: CTA = (32x32 pixel region, instance tile).  For each
-// detector the sinogram samples spanned by the region (plus F+1 on each
-// side) are staged in shared memory, the bucket table
-// Q_b = (U_b, V_b, s[b-F], s[b+F+1]) of that span is built there, and every
-// pixel adds U + f V + e1 s[b-F] + e2 s[b+F+1].
-template <int WT>
-__global__ void __launch_bounds__(REG) k_das_adj3(const int32_t *__restrict__ rtau,
-                                                  const int2 *__restrict__ rspan,
-                                                  const float *__restrict__ s,
-                                                  float *__restrict__ out, int nx, int nz,
-                                                  int nrx, int D, int T, int fb, int F,
-                                                  float inv_r, float ce1, float ce2,
-                                                  float scale, int span_max) {
+// Adjoint by regions: CTA = (32x32 pixel region, instance tile).  Per phase
+// of ADJ_DPH detectors, the sinogram samples spanned by the region (plus F+1
+// on each side) are staged in shared memory, the bucket table
+// Q_b = (U_b, V_b, s[b-F], s[b+F+1]) of each span is built there (each thread
+// filters ADJ_BPT consecutive buckets from a register window), and every
+// pixel adds U + f V + e1 s[b-F] + e2 s[b+F+1] for the phase's detectors.
+constexpr int ADJ_DPH = 4;  // detectors per shared-memory phase
+constexpr int ADJ_BPT = 4;  // buckets per thread when building Q
+
+template <int F>
+__device__ __forceinline__ void build_q(const float *g, float4 *q, int nb_here, float inv_r) {
+    // g[j] = s[b0 - F + j]; outputs buckets b0 .. b0 + nb_here - 1
+    constexpr int NW = ADJ_BPT + 2 * F + 2;
+    float win[NW];
+#pragma unroll
+    for (int j = 0; j < NW; ++j) win[j] = g[j];
+#pragma unroll
+    for (int o = 0; o < ADJ_BPT; ++o) {
+        if (o >= nb_here) break;
+        float U = 0.f, V = 0.f;
+#pragma unroll
+        for (int k = -(F - 1); k <= F; ++k) {
+            const float sv = win[o + F + k];
+            U = fmaf(1.f - (float)(k < 0 ? -k : k) * inv_r, sv, U);
+            V += k <= 0 ? -sv : sv;
+        }
+        q[o] = make_float4(U, V * inv_r, win[o], win[o + 2 * F + 1]);
+    }
+}
+
+template <int WT, int F>
+__global__ void __launch_bounds__(REG, 1) k_das_adj3(const int32_t *__restrict__ rtau,
+                                                     const int2 *__restrict__ rspan,
+                                                     const float *__restrict__ s,
+                                                     float *__restrict__ out, int nx, int nz,
+                                                     int nrx, int D, int T, int fb,
+                                                     float inv_r, float ce1, float ce2,
+                                                     float scale, int span_max) {
     extern __shared__ float sm[];
-    const int SL = span_max + 2 * F + 2;
-    float *seg = sm;                                           // [WT][SL]
-    float4 *Q = reinterpret_cast<float4 *>(sm + ((WT * SL + 3) & ~3));  // [WT][span_max]
+    const int SL = ((span_max + ADJ_BPT - 1) / ADJ_BPT) * ADJ_BPT + 2 * F + 2;
+    float *seg = sm;  // [ADJ_DPH][WT][SL]
+    float4 *Q = reinterpret_cast<float4 *>(sm + ((ADJ_DPH * WT * SL + 3) & ~3));
+    // Q: [ADJ_DPH][WT][span_max]
     const int reg = blockIdx.x, w0 = blockIdx.y * WT;
     const int q = threadIdx.x;
     const int rx = reg % nrx, rz = reg / nrx;
@@ -248,40 +274,53 @@ __global__ void __launch_bounds__(REG) k_das_adj3(const int32_t *__restrict__ rt
     for (int i = 0; i < WT; ++i) acc[i] = 0.f;
     const int32_t *tp = rtau + (size_t)reg * D * REG + q;
     const int2 *spp = rspan + (size_t)reg * D;
-    int32_t tau_next = __ldg(tp);
-    for (int d = 0; d < D; ++d) {
-        const int32_t tau = tau_next;
-        if (d + 1 < D) tau_next = __ldg(tp + (size_t)(d + 1) * REG);
-        const int2 sp = __ldg(spp + d);
-        const int nb = sp.y - sp.x + 1;
-        if (nb <= 0) continue;  // region outside the grid (uniform across the CTA)
-        const int L = nb + 2 * F + 2;
-        for (int i = threadIdx.x; i < WT * L; i += blockDim.x) {
-            const int w = i / L, k = i - w * L;
-            const int t = sp.x - F + k;
-            seg[w * SL + k] =
-                (t >= 0 && t < T) ? __ldg(s + ((size_t)(w0 + w) * D + d) * T + t) : 0.f;
+    for (int d0 = 0; d0 < D; d0 += ADJ_DPH) {
+        int32_t tau[ADJ_DPH];
+        int2 sp[ADJ_DPH];
+#pragma unroll
+        for (int j = 0; j < ADJ_DPH; ++j) {
+            const int d = min(d0 + j, D - 1);
+            tau[j] = d0 + j < D ? __ldg(tp + (size_t)d * REG) : TAU_PAD;
+            sp[j] = d0 + j < D ? __ldg(spp + d) : make_int2(0, -1);
         }
-        __syncthreads();
-        for (int i = threadIdx.x; i < WT * nb; i += blockDim.x) {
-            const int w = i / nb, bl = i - w * nb;
-            const float *g = seg + w * SL + bl + F;  // g[k] = s[b + k]
-            float U = 0.f, V = 0.f;
-            for (int k = -(F - 1); k <= F; ++k) {
-                U = fmaf(fmaf(-fabsf((float)k), inv_r, 1.f), g[k], U);
-                V += k <= 0 ? -g[k] : g[k];
+        // stage the spans of the phase's detectors
+#pragma unroll
+        for (int j = 0; j < ADJ_DPH; ++j) {
+            const int nb = sp[j].y - sp[j].x + 1;
+            if (nb <= 0) continue;
+            const int L = ((nb + ADJ_BPT - 1) / ADJ_BPT) * ADJ_BPT + 2 * F + 2;
+            const int d = d0 + j;
+            for (int i = threadIdx.x; i < WT * L; i += blockDim.x) {
+                const int w = i / L, k = i - w * L;
+                const int t = sp[j].x - F + k;
+                seg[(j * WT + w) * SL + k] =
+                    (t >= 0 && t < T) ? __ldg(s + ((size_t)(w0 + w) * D + d) * T + t) : 0.f;
             }
-            Q[w * span_max + bl] = make_float4(U, V * inv_r, g[-F], g[F + 1]);
         }
         __syncthreads();
-        if (tau != TAU_PAD) {
-            const int bl = (tau >> fb) - sp.x;
-            const float f = (float)(tau & mask) * step;
+        // bucket tables
+#pragma unroll
+        for (int j = 0; j < ADJ_DPH; ++j) {
+            const int nb = sp[j].y - sp[j].x + 1;
+            const int nch = (nb + ADJ_BPT - 1) / ADJ_BPT;
+            for (int i = threadIdx.x; i < WT * nch; i += blockDim.x) {
+                const int w = i / nch, c = i - w * nch;
+                build_q<F>(seg + (j * WT + w) * SL + c * ADJ_BPT,
+                           Q + (size_t)(j * WT + w) * span_max + c * ADJ_BPT,
+                           nb - c * ADJ_BPT, inv_r);
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < ADJ_DPH; ++j) {
+            if (tau[j] == TAU_PAD) continue;
+            const int bl = (tau[j] >> fb) - sp[j].x;
+            const float f = (float)(tau[j] & mask) * step;
             const float e1 = fmaxf(0.f, fmaf(-f, inv_r, ce1));
             const float e2 = fmaxf(0.f, fmaf(f, inv_r, -ce2));
 #pragma unroll
             for (int i = 0; i < WT; ++i) {
-                const float4 v = Q[i * span_max + bl];
+                const float4 v = Q[(size_t)(j * WT + i) * span_max + bl];
                 acc[i] = fmaf(e2, v.w, fmaf(e1, v.z, fmaf(f, v.y, acc[i] + v.x)));
             }
         }
@@ -290,7 +329,8 @@ __global__ void __launch_bounds__(REG) k_das_adj3(const int32_t *__restrict__ rt
     if (ix < nx && iz < nz) {
         const size_t P = (size_t)nx * nz;
 #pragma unroll
-        for (int i = 0; i < WT; ++i) out[(size_t)(w0 + i) * P + (size_t)ix * nz + iz] = acc[i] * scale;
+        for (int i = 0; i < WT; ++i)
+            out[(size_t)(w0 + i) * P + (size_t)ix * nz + iz] = acc[i] * scale;
     }
 }
 
@@ -575,28 +615,49 @@ int launch_das_forward(const Plan &pl, const float *xpm, float *raw, int W, floa
 }
 
 // DAS adjoint by regions; raw [W][D][T] -> x [W][P].
+template <int WT, int F>
+static int das_adj_launch(const Plan &pl, const float *raw, float *x, int W, float scale,
+                          cudaStream_t st) {
+    const int SL = div_up(pl.reg_span_max, ADJ_BPT) * ADJ_BPT + 2 * F + 2;
+    const size_t smem = (size_t)((ADJ_DPH * WT * SL + 3) & ~3) * sizeof(float) +
+                        (size_t)ADJ_DPH * WT * pl.reg_span_max * sizeof(float4);
+    int rc;
+    if ((rc = set_smem(k_das_adj3<WT, F>, smem)) != MSOT_OK) return rc;
+    dim3 grid(pl.n_reg, W / WT);
+    KLAUNCH(k_das_adj3<WT, F><<<grid, REG, smem, st>>>(
+        pl.reg_tau, pl.reg_span, raw, x, pl.nx, pl.nz, pl.n_reg_x, pl.D, pl.T, pl.frac_bits,
+        pl.inv_r, pl.ce1, pl.ce2, scale, pl.reg_span_max));
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
+}
+
+template <int WT>
+static int das_adj_f(const Plan &pl, const float *raw, float *x, int W, float scale,
+                     cudaStream_t st) {
+    switch (pl.F) {
+        case 0: return das_adj_launch<WT, 0>(pl, raw, x, W, scale, st);
+        case 1: return das_adj_launch<WT, 1>(pl, raw, x, W, scale, st);
+        case 2: return das_adj_launch<WT, 2>(pl, raw, x, W, scale, st);
+        case 3: return das_adj_launch<WT, 3>(pl, raw, x, W, scale, st);
+        case 4: return das_adj_launch<WT, 4>(pl, raw, x, W, scale, st);
+        case 5: return das_adj_launch<WT, 5>(pl, raw, x, W, scale, st);
+        case 6: return das_adj_launch<WT, 6>(pl, raw, x, W, scale, st);
+        case 7: return das_adj_launch<WT, 7>(pl, raw, x, W, scale, st);
+        case 8: return das_adj_launch<WT, 8>(pl, raw, x, W, scale, st);
+        default:
+            set_error("DAS adjoint: interpolation radius %g above 9 samples is not supported",
+                      pl.radius);
+            return MSOT_EINVAL;
+    }
+}
+
 int launch_das_adjoint(const Plan &pl, const float *raw, float *x, int W, float scale,
                        cudaStream_t st) {
     TimedScope ts_(KID_INTERP_ADJ, st);
     const int wt = pick_wt(W, 1, 4);
-    const int SL = pl.reg_span_max + 2 * pl.F + 2;
-    const size_t smem = (size_t)((wt * SL + 3) & ~3) * sizeof(float) +
-                        (size_t)wt * pl.reg_span_max * sizeof(float4);
-    dim3 grid(pl.n_reg, W / wt);
-    int rc;
-#define CASE(WT)                                                                          \
-    case WT:                                                                              \
-        if ((rc = set_smem(k_das_adj3<WT>, smem)) != MSOT_OK) return rc;                  \
-        KLAUNCH(k_das_adj3<WT><<<grid, REG, smem, st>>>(                                  \
-            pl.reg_tau, pl.reg_span, raw, x, pl.nx, pl.nz, pl.n_reg_x, pl.D, pl.T,         \
-            pl.frac_bits, pl.F, pl.inv_r, pl.ce1, pl.ce2, scale, pl.reg_span_max));       \
-        break;
-    switch (wt) {
-        CASE(1) CASE(2) CASE(4)
-    }
-#undef CASE
-    MSOT_LAUNCH_CHECK();
-    return MSOT_OK;
+    if (wt == 4) return das_adj_f<4>(pl, raw, x, W, scale, st);
+    if (wt == 2) return das_adj_f<2>(pl, raw, x, W, scale, st);
+    return das_adj_f<1>(pl, raw, x, W, scale, st);
 }
 
 template <int WT>

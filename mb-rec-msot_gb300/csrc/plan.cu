@@ -120,8 +120,9 @@ static int build(const msot_plan_desc *d, Plan &p) {
     p.inv_r = (float)(1.0 / d->radius);
     p.ce1 = (float)((d->radius - p.F) / d->radius);
     p.ce2 = (float)((p.F + 1 - d->radius) / d->radius);
-    if (!has_sir && 2 * p.F + 2 >= 256) {
-        set_error("plan: interpolation radius %g too large (max 126 samples)", d->radius);
+    if (!has_sir && p.F > 8) {
+        set_error("plan: interpolation radius %g too large (at most 9 samples without SIR)",
+                  d->radius);
         return MSOT_EINVAL;
     }
 
