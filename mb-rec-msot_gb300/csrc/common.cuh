@@ -28,7 +28,8 @@ constexpr int PATCH_X = 8;           // patch width (x columns)
 constexpr int PATCH_Z = 8;           // patch height (z rows)
 constexpr int PATCH = PATCH_X * PATCH_Z;
 constexpr int32_t TAU_PAD = INT32_MIN;  // marks a padding pixel in tau_tiles
-constexpr int REG_X = 32, REG_Z = 32, REG = REG_X * REG_Z;  // adjoint region
+constexpr int BLK_X = 64, BLK_Z = 64, BLK = BLK_X * BLK_Z;  // adjoint pixel block
+constexpr int BLK_THREADS = 256, BLK_PPT = BLK / BLK_THREADS;  // 16 pixels per thread
 
 struct Plan {
     int nx, nz, P, D, T;
@@ -50,11 +51,14 @@ struct Plan {
     float ce1 = 0.f, ce2 = 0.f;    // (r - F)/r and (F + 1 - r)/r
     int32_t *fwd_off = nullptr;    // [D][T+1] CSR offsets of bucket b = floor(tau)
     int2 *fwd_ent = nullptr;       // [D][P] (tau fixed point, pixel) sorted by bucket
-    // adjoint regions: 32x32 pixels (REG_Z rows of z x REG_X columns of x)
-    int n_reg_x = 0, n_reg_z = 0, n_reg = 0;
-    int32_t *reg_tau = nullptr;    // [n_reg][D][REG] tau per region pixel (TAU_PAD outside)
-    int2 *reg_span = nullptr;      // [n_reg][D] first / last bucket of the region
-    int reg_span_max = 0;          // largest last - first + 1
+    // adjoint pixel blocks of BLK_Z x BLK_X pixels; thread t of a CTA owns
+    // the pixels (iz = t % BLK_Z, ix = t / BLK_Z + 4k), k < BLK_PPT
+    int n_blk_x = 0, n_blk_z = 0, n_blk = 0;
+    int32_t *blk_tau = nullptr;    // [n_blk][D][BLK_PPT][BLK_THREADS] (TAU_PAD outside)
+    int2 *blk_span = nullptr;      // [n_blk][D] first / last bucket of the block
+    int blk_span_max = 0;          // largest last - first + 1
+    int adj_groups_max = 0;        // detector groups the partial buffer is sized for
+    float *scr_part = nullptr;     // [adj_groups_max][max_batch][P] adjoint partial sums
     // IR
     int L = 0, Lh = 0;
     float *ir_fwd = nullptr, *ir_adj = nullptr;

@@ -220,13 +220,13 @@ __global__ void __launch_bounds__(256) k_das_fwd2(const int32_t *__restrict__ of
     }
 }
 
-// Adjoint by regions: CTA = (32x32 pixel region, instance tile).  Per phase
-// of ADJ_DPH detectors, the sinogram samples spanned by the region (plus F+1
-// on each side) are staged in shared memory, the bucket table
-// Q_b = (U_b, V_b, s[b-F], s[b+F+1]) of each span is built there (each thread
-// filters ADJ_BPT consecutive buckets from a register window), and every
-// pixel adds U + f V + e1 s[b-F] + e2 s[b+F+1] for the phase's detectors.
-constexpr int ADJ_DPH = 4;  // detectors per shared-memory phase
+// Adjoint by pixel blocks: CTA = (64x64 pixel block, instance tile of WT,
+// detector group).  For each detector of its group the CTA stages the
+// sinogram samples spanned by the block (plus F+1 on each side) in shared
+// memory, builds the bucket table Q_b = (U_b, V_b, s[b-F], s[b+F+1]) of the
+// span there (each thread filters ADJ_BPT consecutive buckets from a register
+// window), and every thread adds U + f V + e1 s[b-F] + e2 s[b+F+1] to its 16
+// pixels.  Groups write partial images; k_sum_parts adds them in fixed order.
 constexpr int ADJ_BPT = 4;  // buckets per thread when building Q
 
 template <int F>
@@ -250,87 +250,85 @@ __device__ __forceinline__ void build_q(const float *g, float4 *q, int nb_here, 
     }
 }
 
+
 template <int WT, int F>
-__global__ void __launch_bounds__(REG, 1) k_das_adj3(const int32_t *__restrict__ rtau,
-                                                     const int2 *__restrict__ rspan,
-                                                     const float *__restrict__ s,
-                                                     float *__restrict__ out, int nx, int nz,
-                                                     int nrx, int D, int T, int fb,
-                                                     float inv_r, float ce1, float ce2,
-                                                     float scale, int span_max) {
+__global__ void __launch_bounds__(BLK_THREADS, 2) k_das_adj4(
+    const int32_t *__restrict__ btau, const int2 *__restrict__ bspan,
+    const float *__restrict__ s, float *__restrict__ part, int nx, int nz, int nbx, int D,
+    int T, int fb, float inv_r, float ce1, float ce2, int span_max, int det_per_group,
+    size_t part_stride) {
     extern __shared__ float sm[];
     const int SL = ((span_max + ADJ_BPT - 1) / ADJ_BPT) * ADJ_BPT + 2 * F + 2;
-    float *seg = sm;  // [ADJ_DPH][WT][SL]
-    float4 *Q = reinterpret_cast<float4 *>(sm + ((ADJ_DPH * WT * SL + 3) & ~3));
-    // Q: [ADJ_DPH][WT][span_max]
-    const int reg = blockIdx.x, w0 = blockIdx.y * WT;
-    const int q = threadIdx.x;
-    const int rx = reg % nrx, rz = reg / nrx;
-    const int ix = rx * REG_X + q / REG_Z, iz = rz * REG_Z + q % REG_Z;
+    float *seg = sm;  // [WT][SL]
+    float4 *Q = reinterpret_cast<float4 *>(sm + ((WT * SL + 3) & ~3));  // [WT][span_max]
+    const int blk = blockIdx.x, w0 = blockIdx.y * WT, grp = blockIdx.z;
+    const int t = threadIdx.x;
+    const int bxi = blk % nbx, bzi = blk / nbx;
     const int mask = (1 << fb) - 1;
     const float step = __int_as_float((127 - fb) << 23);
-    float acc[WT];
+    float acc[BLK_PPT][WT];
 #pragma unroll
-    for (int i = 0; i < WT; ++i) acc[i] = 0.f;
-    const int32_t *tp = rtau + (size_t)reg * D * REG + q;
-    const int2 *spp = rspan + (size_t)reg * D;
-    for (int d0 = 0; d0 < D; d0 += ADJ_DPH) {
-        int32_t tau[ADJ_DPH];
-        int2 sp[ADJ_DPH];
+    for (int k = 0; k < BLK_PPT; ++k)
 #pragma unroll
-        for (int j = 0; j < ADJ_DPH; ++j) {
-            const int d = min(d0 + j, D - 1);
-            tau[j] = d0 + j < D ? __ldg(tp + (size_t)d * REG) : TAU_PAD;
-            sp[j] = d0 + j < D ? __ldg(spp + d) : make_int2(0, -1);
-        }
-        // stage the spans of the phase's detectors
-#pragma unroll
-        for (int j = 0; j < ADJ_DPH; ++j) {
-            const int nb = sp[j].y - sp[j].x + 1;
-            if (nb <= 0) continue;
-            const int L = ((nb + ADJ_BPT - 1) / ADJ_BPT) * ADJ_BPT + 2 * F + 2;
-            const int d = d0 + j;
-            for (int i = threadIdx.x; i < WT * L; i += blockDim.x) {
-                const int w = i / L, k = i - w * L;
-                const int t = sp[j].x - F + k;
-                seg[(j * WT + w) * SL + k] =
-                    (t >= 0 && t < T) ? __ldg(s + ((size_t)(w0 + w) * D + d) * T + t) : 0.f;
+        for (int i = 0; i < WT; ++i) acc[k][i] = 0.f;
+    const int d_begin = grp * det_per_group, d_end = min(D, d_begin + det_per_group);
+    for (int d = d_begin; d < d_end; ++d) {
+        const int2 sp = __ldg(bspan + (size_t)blk * D + d);
+        const int nb = sp.y - sp.x + 1;
+        if (nb <= 0) continue;  // block outside the grid: uniform across the CTA
+        const int L = ((nb + ADJ_BPT - 1) / ADJ_BPT) * ADJ_BPT + 2 * F + 2;
+        for (int w = 0; w < WT; ++w) {
+            const float *src = s + ((size_t)(w0 + w) * D + d) * T;
+            for (int k = t; k < L; k += BLK_THREADS) {
+                const int tt = sp.x - F + k;
+                seg[w * SL + k] = (tt >= 0 && tt < T) ? __ldg(src + tt) : 0.f;
             }
         }
         __syncthreads();
-        // bucket tables
-#pragma unroll
-        for (int j = 0; j < ADJ_DPH; ++j) {
-            const int nb = sp[j].y - sp[j].x + 1;
-            const int nch = (nb + ADJ_BPT - 1) / ADJ_BPT;
-            for (int i = threadIdx.x; i < WT * nch; i += blockDim.x) {
-                const int w = i / nch, c = i - w * nch;
-                build_q<F>(seg + (j * WT + w) * SL + c * ADJ_BPT,
-                           Q + (size_t)(j * WT + w) * span_max + c * ADJ_BPT,
-                           nb - c * ADJ_BPT, inv_r);
-            }
+        const int nch = (nb + ADJ_BPT - 1) / ADJ_BPT;
+        for (int i = t; i < WT * nch; i += BLK_THREADS) {
+            const int w = i / nch, c = i - w * nch;
+            build_q<F>(seg + w * SL + c * ADJ_BPT, Q + (size_t)w * span_max + c * ADJ_BPT,
+                       nb - c * ADJ_BPT, inv_r);
         }
         __syncthreads();
+        const int32_t *tp = btau + ((size_t)blk * D + d) * BLK + t;
 #pragma unroll
-        for (int j = 0; j < ADJ_DPH; ++j) {
-            if (tau[j] == TAU_PAD) continue;
-            const int bl = (tau[j] >> fb) - sp[j].x;
-            const float f = (float)(tau[j] & mask) * step;
+        for (int k = 0; k < BLK_PPT; ++k) {
+            const int32_t tau = __ldg(tp + k * BLK_THREADS);
+            if (tau == TAU_PAD) continue;
+            const int bl = (tau >> fb) - sp.x;
+            const float f = (float)(tau & mask) * step;
             const float e1 = fmaxf(0.f, fmaf(-f, inv_r, ce1));
             const float e2 = fmaxf(0.f, fmaf(f, inv_r, -ce2));
 #pragma unroll
             for (int i = 0; i < WT; ++i) {
-                const float4 v = Q[(size_t)(j * WT + i) * span_max + bl];
-                acc[i] = fmaf(e2, v.w, fmaf(e1, v.z, fmaf(f, v.y, acc[i] + v.x)));
+                const float4 v = Q[(size_t)i * span_max + bl];
+                acc[k][i] = fmaf(e2, v.w, fmaf(e1, v.z, fmaf(f, v.y, acc[k][i] + v.x)));
             }
         }
         __syncthreads();
     }
-    if (ix < nx && iz < nz) {
-        const size_t P = (size_t)nx * nz;
+    const size_t P = (size_t)nx * nz;
+    float *dst = part + (size_t)grp * part_stride;
+    const int iz = bzi * BLK_Z + t % BLK_Z;
 #pragma unroll
-        for (int i = 0; i < WT; ++i)
-            out[(size_t)(w0 + i) * P + (size_t)ix * nz + iz] = acc[i] * scale;
+    for (int k = 0; k < BLK_PPT; ++k) {
+        const int ix = bxi * BLK_X + t / BLK_Z + (BLK_THREADS / BLK_Z) * k;
+        if (ix >= nx || iz >= nz) continue;
+#pragma unroll
+        for (int i = 0; i < WT; ++i) dst[(size_t)(w0 + i) * P + (size_t)ix * nz + iz] = acc[k][i];
+    }
+}
+
+// x[w][p] = scale * sum_g part[g][w][p]   (groups added in order)
+__global__ void k_sum_parts(const float *__restrict__ part, float *__restrict__ x, size_t n,
+                            int groups, size_t stride, float scale) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        float v = 0.f;
+        for (int g = 0; g < groups; ++g) v += __ldg(part + g * stride + i);
+        x[i] = v * scale;
     }
 }
 
@@ -614,19 +612,29 @@ int launch_das_forward(const Plan &pl, const float *xpm, float *raw, int W, floa
     return MSOT_OK;
 }
 
-// DAS adjoint by regions; raw [W][D][T] -> x [W][P].
+// DAS adjoint by pixel blocks; raw [W][D][T] -> x [W][P].
 template <int WT, int F>
 static int das_adj_launch(const Plan &pl, const float *raw, float *x, int W, float scale,
                           cudaStream_t st) {
-    const int SL = div_up(pl.reg_span_max, ADJ_BPT) * ADJ_BPT + 2 * F + 2;
-    const size_t smem = (size_t)((ADJ_DPH * WT * SL + 3) & ~3) * sizeof(float) +
-                        (size_t)ADJ_DPH * WT * pl.reg_span_max * sizeof(float4);
+    const int SL = div_up(pl.blk_span_max, ADJ_BPT) * ADJ_BPT + 2 * F + 2;
+    const size_t smem = (size_t)((WT * SL + 3) & ~3) * sizeof(float) +
+                        (size_t)WT * pl.blk_span_max * sizeof(float4);
     int rc;
-    if ((rc = set_smem(k_das_adj3<WT, F>, smem)) != MSOT_OK) return rc;
-    dim3 grid(pl.n_reg, W / WT);
-    KLAUNCH(k_das_adj3<WT, F><<<grid, REG, smem, st>>>(
-        pl.reg_tau, pl.reg_span, raw, x, pl.nx, pl.nz, pl.n_reg_x, pl.D, pl.T, pl.frac_bits,
-        pl.inv_r, pl.ce1, pl.ce2, scale, pl.reg_span_max));
+    if ((rc = set_smem(k_das_adj4<WT, F>, smem)) != MSOT_OK) return rc;
+    const int base = pl.n_blk * (W / WT);
+    int groups = std::max(1, std::min(pl.D, div_up(2 * 152, base)));
+    groups = std::min(groups, std::max(1, pl.adj_groups_max * pl.max_batch / W));
+    groups = std::min(groups, pl.adj_groups_max);
+    const int dpg = div_up(pl.D, groups);
+    groups = div_up(pl.D, dpg);
+    const size_t stride = (size_t)W * pl.P;
+    dim3 grid(pl.n_blk, W / WT, groups);
+    KLAUNCH(k_das_adj4<WT, F><<<grid, BLK_THREADS, smem, st>>>(
+        pl.blk_tau, pl.blk_span, raw, pl.scr_part, pl.nx, pl.nz, pl.n_blk_x, pl.D, pl.T,
+        pl.frac_bits, pl.inv_r, pl.ce1, pl.ce2, pl.blk_span_max, dpg, stride));
+    MSOT_LAUNCH_CHECK();
+    KLAUNCH(k_sum_parts<<<(unsigned)std::min<size_t>(4096, div_up((int)stride, 256)), 256, 0,
+                          st>>>(pl.scr_part, x, stride, groups, stride, scale));
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
 }

@@ -49,7 +49,8 @@ static int alloc(T **dst, size_t n, size_t &bytes) {
 static void free_plan(Plan &p) {
     void *ptrs[] = {p.tau_tiles, p.tau_pi, p.perm, p.ir_fwd, p.ir_adj, p.pre_x, p.pre_z,
                     p.sir, p.sir_se, p.sir_tiles, p.sir_pi, p.scr_img0, p.scr_img1,
-                    p.scr_sino, p.fwd_off, p.fwd_ent, p.reg_tau, p.reg_span};
+                    p.scr_sino, p.fwd_off, p.fwd_ent, p.blk_tau, p.blk_span,
+                    p.scr_part};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     p = Plan();
@@ -158,31 +159,34 @@ static int build(const msot_plan_desc *d, Plan &p) {
         }
     }
 
-    // --- adjoint regions: 32x32 pixels, travel times and bucket span per detector ------
-    std::vector<int32_t> rtau;
-    std::vector<int2> rspan;
+    // --- adjoint blocks: 64x64 pixels, travel times and bucket span per detector --------
+    std::vector<int32_t> btau;
+    std::vector<int2> bspan;
     if (!has_sir) {
-        p.n_reg_x = div_up(p.nx, REG_X);
-        p.n_reg_z = div_up(p.nz, REG_Z);
-        p.n_reg = p.n_reg_x * p.n_reg_z;
-        rtau.assign((size_t)p.n_reg * p.D * REG, TAU_PAD);
-        rspan.assign((size_t)p.n_reg * p.D, make_int2(0, -1));
-        for (int rz = 0; rz < p.n_reg_z; ++rz)
-            for (int rx = 0; rx < p.n_reg_x; ++rx) {
-                const int reg = rz * p.n_reg_x + rx;
+        p.n_blk_x = div_up(p.nx, BLK_X);
+        p.n_blk_z = div_up(p.nz, BLK_Z);
+        p.n_blk = p.n_blk_x * p.n_blk_z;
+        btau.assign((size_t)p.n_blk * p.D * BLK, TAU_PAD);
+        bspan.assign((size_t)p.n_blk * p.D, make_int2(0, -1));
+        for (int bz = 0; bz < p.n_blk_z; ++bz)
+            for (int bx = 0; bx < p.n_blk_x; ++bx) {
+                const int blk = bz * p.n_blk_x + bx;
                 for (int det = 0; det < p.D; ++det) {
                     int bmin = INT32_MAX, bmax = INT32_MIN;
-                    for (int q = 0; q < REG; ++q) {
-                        const int ix = rx * REG_X + q / REG_Z, iz = rz * REG_Z + q % REG_Z;
-                        if (ix >= p.nx || iz >= p.nz) continue;
-                        const int32_t t = tfx[(size_t)det * p.P + (size_t)ix * p.nz + iz];
-                        rtau[((size_t)reg * p.D + det) * REG + q] = t;
-                        bmin = std::min(bmin, t >> fb);
-                        bmax = std::max(bmax, t >> fb);
-                    }
+                    int32_t *dst = btau.data() + ((size_t)blk * p.D + det) * BLK;
+                    for (int k = 0; k < BLK_PPT; ++k)
+                        for (int t = 0; t < BLK_THREADS; ++t) {
+                            const int iz = bz * BLK_Z + t % BLK_Z;
+                            const int ix = bx * BLK_X + t / BLK_Z + (BLK_THREADS / BLK_Z) * k;
+                            if (ix >= p.nx || iz >= p.nz) continue;
+                            const int32_t v = tfx[(size_t)det * p.P + (size_t)ix * p.nz + iz];
+                            dst[k * BLK_THREADS + t] = v;
+                            bmin = std::min(bmin, v >> fb);
+                            bmax = std::max(bmax, v >> fb);
+                        }
                     if (bmax >= bmin) {
-                        rspan[(size_t)reg * p.D + det] = make_int2(bmin, bmax);
-                        p.reg_span_max = std::max(p.reg_span_max, bmax - bmin + 1);
+                        bspan[(size_t)blk * p.D + det] = make_int2(bmin, bmax);
+                        p.blk_span_max = std::max(p.blk_span_max, bmax - bmin + 1);
                     }
                 }
             }
@@ -302,8 +306,8 @@ static int build(const msot_plan_desc *d, Plan &p) {
     if (!has_sir) {
         UP(p.fwd_off, foff);
         UP(p.fwd_ent, fent);
-        UP(p.reg_tau, rtau);
-        UP(p.reg_span, rspan);
+        UP(p.blk_tau, btau);
+        UP(p.blk_span, bspan);
     }
     if (has_sir) {
         UP(p.sir, sirf);
@@ -328,6 +332,13 @@ static int build(const msot_plan_desc *d, Plan &p) {
     if ((rc = alloc(&p.scr_img0, W * p.P, B)) != MSOT_OK) return rc;
     if ((rc = alloc(&p.scr_img1, W * p.P, B)) != MSOT_OK) return rc;
     if ((rc = alloc(&p.scr_sino, W * p.D * p.T, B)) != MSOT_OK) return rc;
+    if (!has_sir) {
+        // detector groups of the adjoint: enough CTAs to fill the GPU twice,
+        // at most 512 partial images in flight
+        p.adj_groups_max = std::max(1, std::min(p.D, (int)std::min<size_t>(32, 512 / W)));
+        if ((rc = alloc(&p.scr_part, (size_t)p.adj_groups_max * W * p.P, B)) != MSOT_OK)
+            return rc;
+    }
 
     return MSOT_OK;
 }
