@@ -62,6 +62,12 @@ struct Plan {
     // IR
     int L = 0, Lh = 0;
     float *ir_fwd = nullptr, *ir_adj = nullptr;
+    // overlap-save FFT convolution: N-point complex FFTs (N = 4^log4n), two real
+    // columns per transform; spectra of the (flipped) taps scaled by 1/(N norm)
+    int fft_log4n = 0;
+    float2 *fft_tw = nullptr;    // [N] exp(-2 pi i t / N)
+    float2 *fft_hf = nullptr;    // [N] spectrum of ir_fwd / N
+    float2 *fft_ha = nullptr;    // [N] spectrum of ir_adj / N
     // prefilter
     int Kx = -1, Kz = -1;   // -1: no prefilter along that axis
     float *pre_x = nullptr, *pre_z = nullptr;

@@ -229,30 +229,8 @@ __global__ void __launch_bounds__(256) k_das_fwd2(const int32_t *__restrict__ of
 // pixels.  Groups write partial images; k_sum_parts adds them in fixed order.
 constexpr int ADJ_BPT = 4;  // buckets per thread when building Q
 
-template <int F>
-__device__ __forceinline__ void build_q(const float *g, float4 *q, int nb_here, float inv_r) {
-    // g[j] = s[b0 - F + j]; outputs buckets b0 .. b0 + nb_here - 1
-    constexpr int NW = ADJ_BPT + 2 * F + 2;
-    float win[NW];
-#pragma unroll
-    for (int j = 0; j < NW; ++j) win[j] = g[j];
-#pragma unroll
-    for (int o = 0; o < ADJ_BPT; ++o) {
-        if (o >= nb_here) break;
-        float U = 0.f, V = 0.f;
-#pragma unroll
-        for (int k = -(F - 1); k <= F; ++k) {
-            const float sv = win[o + F + k];
-            U = fmaf(1.f - (float)(k < 0 ? -k : k) * inv_r, sv, U);
-            V += k <= 0 ? -sv : sv;
-        }
-        q[o] = make_float4(U, V * inv_r, win[o], win[o + 2 * F + 1]);
-    }
-}
-
-
 template <int WT, int F>
-__global__ void __launch_bounds__(BLK_THREADS, 2) k_das_adj4(
+__global__ void __launch_bounds__(BLK_THREADS, 3) k_das_adj4(
     const int32_t *__restrict__ btau, const int2 *__restrict__ bspan,
     const float *__restrict__ s, float *__restrict__ part, int nx, int nz, int nbx, int D,
     int T, int fb, float inv_r, float ce1, float ce2, int span_max, int det_per_group,
@@ -285,11 +263,17 @@ __global__ void __launch_bounds__(BLK_THREADS, 2) k_das_adj4(
             }
         }
         __syncthreads();
-        const int nch = (nb + ADJ_BPT - 1) / ADJ_BPT;
-        for (int i = t; i < WT * nch; i += BLK_THREADS) {
-            const int w = i / nch, c = i - w * nch;
-            build_q<F>(seg + w * SL + c * ADJ_BPT, Q + (size_t)w * span_max + c * ADJ_BPT,
-                       nb - c * ADJ_BPT, inv_r);
+        // one bucket per thread: consecutive threads read consecutive samples
+        for (int i = t; i < WT * nb; i += BLK_THREADS) {
+            const int w = i / nb, bl = i - w * nb;
+            const float *g = seg + w * SL + bl + F;  // g[k] = s[b + k]
+            float U = 0.f, V = 0.f;
+#pragma unroll
+            for (int k = -(F - 1); k <= F; ++k) {
+                U = fmaf(1.f - (float)(k < 0 ? -k : k) * inv_r, g[k], U);
+                V += k <= 0 ? -g[k] : g[k];
+            }
+            Q[(size_t)w * span_max + bl] = make_float4(U, V * inv_r, g[-F], g[F + 1]);
         }
         __syncthreads();
         const int32_t *tp = btau + ((size_t)blk * D + d) * BLK + t;
@@ -532,6 +516,91 @@ __global__ void __launch_bounds__(NTH) k_conv(const float *__restrict__ in,
 }
 
 // ---------------------------------------------------------------------------
+// IR convolution by overlap-save FFT.  Two real columns c1, c2 ride in one
+// complex transform: y1 + i y2 = IFFT(FFT(x1 + i x2) H) since the taps are
+// real.  CTA = (output block of V = N - L + 1 samples, column pair); N-point
+// radix-4 Stockham FFTs in shared memory (N/4 threads, one butterfly each
+// per stage); H already holds the 1/N of the inverse transform.
+// ---------------------------------------------------------------------------
+template <int SIGN>
+__device__ __forceinline__ void radix4_stage(const float2 *__restrict__ A, float2 *__restrict__ B,
+                                             const float2 *__restrict__ tw, int N, int L,
+                                             int tw_step, int j) {
+    const int k = j & (L - 1), q = j / L;
+    const int Q = N >> 2;
+    float2 a[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        float2 v = A[j + r * Q];
+        if (r) {
+            float2 w = __ldg(tw + r * k * tw_step);
+            if (SIGN > 0) w.y = -w.y;
+            v = make_float2(v.x * w.x - v.y * w.y, v.x * w.y + v.y * w.x);
+        }
+        a[r] = v;
+    }
+    const float2 t0 = make_float2(a[0].x + a[2].x, a[0].y + a[2].y);
+    const float2 t1 = make_float2(a[0].x - a[2].x, a[0].y - a[2].y);
+    const float2 t2 = make_float2(a[1].x + a[3].x, a[1].y + a[3].y);
+    const float2 d = make_float2(a[1].x - a[3].x, a[1].y - a[3].y);
+    // t3 = (a1 - a3) * (SIGN * i)
+    const float2 t3 = SIGN < 0 ? make_float2(d.y, -d.x) : make_float2(-d.y, d.x);
+    float2 *o = B + q * 4 * L + k;
+    o[0] = make_float2(t0.x + t2.x, t0.y + t2.y);
+    o[L] = make_float2(t1.x + t3.x, t1.y + t3.y);
+    o[2 * L] = make_float2(t0.x - t2.x, t0.y - t2.y);
+    o[3 * L] = make_float2(t1.x - t3.x, t1.y - t3.y);
+}
+
+template <int LOG4N>
+__global__ void __launch_bounds__(1 << (2 * LOG4N - 2)) k_conv_fft(
+    const float *__restrict__ in, float *__restrict__ out, const float2 *__restrict__ tw,
+    const float2 *__restrict__ H, int C, int T, int L) {
+    constexpr int N = 1 << (2 * LOG4N), NT = N / 4;
+    extern __shared__ float2 fbuf[];
+    float2(*buf)[N] = reinterpret_cast<float2(*)[N]>(fbuf);
+    const int V = N - L + 1;
+    const int t0 = blockIdx.x * V;
+    const int c1 = 2 * blockIdx.y, c2 = c1 + 1;
+    const bool has2 = c2 < C;
+    const int u0 = t0 + L / 2 - (L - 1);
+    const float *x1 = in + (size_t)c1 * T;
+    const float *x2 = in + (size_t)(has2 ? c2 : c1) * T;
+    for (int n = threadIdx.x; n < N; n += NT) {
+        const int u = u0 + n;
+        const bool ok = u >= 0 && u < T;
+        buf[0][n] = make_float2(ok ? __ldg(x1 + u) : 0.f, (ok && has2) ? __ldg(x2 + u) : 0.f);
+    }
+    __syncthreads();
+    int cur = 0;
+#pragma unroll
+    for (int s = 0, Ls = 1; s < LOG4N; ++s, Ls *= 4) {
+        radix4_stage<-1>(buf[cur], buf[cur ^ 1], tw, N, Ls, N / (4 * Ls), threadIdx.x);
+        cur ^= 1;
+        __syncthreads();
+    }
+    for (int n = threadIdx.x; n < N; n += NT) {
+        const float2 v = buf[cur][n], h = __ldg(H + n);
+        buf[cur][n] = make_float2(v.x * h.x - v.y * h.y, v.x * h.y + v.y * h.x);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0, Ls = 1; s < LOG4N; ++s, Ls *= 4) {
+        radix4_stage<1>(buf[cur], buf[cur ^ 1], tw, N, Ls, N / (4 * Ls), threadIdx.x);
+        cur ^= 1;
+        __syncthreads();
+    }
+    float *y1 = out + (size_t)c1 * T, *y2 = out + (size_t)c2 * T;
+    for (int i = threadIdx.x; i < V; i += NT) {
+        const int t = t0 + i;
+        if (t >= T) break;
+        const float2 r = buf[cur][L - 1 + i];
+        y1[t] = r.x;
+        if (has2) y2[t] = r.y;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------
 static int pick_wt(int W, int T, int max_wt) {
@@ -662,8 +731,7 @@ static int das_adj_f(const Plan &pl, const float *raw, float *x, int W, float sc
 int launch_das_adjoint(const Plan &pl, const float *raw, float *x, int W, float scale,
                        cudaStream_t st) {
     TimedScope ts_(KID_INTERP_ADJ, st);
-    const int wt = pick_wt(W, 1, 4);
-    if (wt == 4) return das_adj_f<4>(pl, raw, x, W, scale, st);
+    const int wt = pick_wt(W, 1, 2);
     if (wt == 2) return das_adj_f<2>(pl, raw, x, W, scale, st);
     return das_adj_f<1>(pl, raw, x, W, scale, st);
 }
@@ -732,6 +800,25 @@ int launch_sir_adjoint(const Plan &pl, const float *raw, float *x, int W, float 
 int launch_conv(const Plan &pl, const float *in, float *out, int W, bool transpose,
                 cudaStream_t st) {
     TimedScope ts_(KID_CONV, st);
+    if (pl.fft_log4n) {
+        const int C = W * pl.D;
+        const int N = 1 << (2 * pl.fft_log4n), V = N - pl.L + 1;
+        dim3 grid(div_up(pl.T, V), div_up(C, 2));
+        const float2 *H = transpose ? pl.fft_ha : pl.fft_hf;
+        const size_t smem = 2 * (size_t)N * sizeof(float2);
+        int rc;
+        if (pl.fft_log4n == 5) {
+            if ((rc = set_smem(k_conv_fft<5>, smem)) != MSOT_OK) return rc;
+            KLAUNCH(k_conv_fft<5><<<grid, N / 4, smem, st>>>(in, out, pl.fft_tw, H, C, pl.T,
+                                                             pl.L));
+        } else {
+            if ((rc = set_smem(k_conv_fft<6>, smem)) != MSOT_OK) return rc;
+            KLAUNCH(k_conv_fft<6><<<grid, N / 4, smem, st>>>(in, out, pl.fft_tw, H, C, pl.T,
+                                                             pl.L));
+        }
+        MSOT_LAUNCH_CHECK();
+        return MSOT_OK;
+    }
     constexpr int TPT = 8, NTH = 64, TT = TPT * NTH;
     const int Lp = (pl.L + TPT - 1) / TPT * TPT;
     const int seg_len = TT + Lp + TPT;

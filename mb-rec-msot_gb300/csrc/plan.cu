@@ -50,7 +50,7 @@ static void free_plan(Plan &p) {
     void *ptrs[] = {p.tau_tiles, p.tau_pi, p.perm, p.ir_fwd, p.ir_adj, p.pre_x, p.pre_z,
                     p.sir, p.sir_se, p.sir_tiles, p.sir_pi, p.scr_img0, p.scr_img1,
                     p.scr_sino, p.fwd_off, p.fwd_ent, p.blk_tau, p.blk_span,
-                    p.scr_part};
+                    p.scr_part, p.fft_tw, p.fft_hf, p.fft_ha};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     p = Plan();
@@ -277,6 +277,31 @@ static int build(const msot_plan_desc *d, Plan &p) {
             ira[k] = (float)(d->ir[p.L - 1 - k] / p.norm);
         }
     }
+    // FFT convolution tables (FP64 on the host, rounded once to FP32)
+    std::vector<float2> ftw, fhf, fha;
+    if (p.L > 0 && p.L <= 2049) {
+        p.fft_log4n = p.L <= 513 ? 5 : 6;
+        const int N = 1 << (2 * p.fft_log4n);
+        ftw.resize(N);
+        fhf.resize(N);
+        fha.resize(N);
+        const double two_pi = 6.283185307179586476925286766559;
+        for (int t = 0; t < N; ++t)
+            ftw[t] = make_float2((float)std::cos(two_pi * t / N), (float)-std::sin(two_pi * t / N));
+        // direct DFT of the short tap vectors: H[f] = sum_k h[k] e^{-2 pi i f k / N} / N
+        for (int f = 0; f < N; ++f) {
+            double fr = 0, fi = 0, ar = 0, ai = 0;
+            for (int k = 0; k < p.L; ++k) {
+                const double ang = -two_pi * (double)(((long)f * k) % N) / N;
+                const double c = std::cos(ang), sn = std::sin(ang);
+                const double hf = d->ir[k] / p.norm, ha = d->ir[p.L - 1 - k] / p.norm;
+                fr += hf * c; fi += hf * sn;
+                ar += ha * c; ai += ha * sn;
+            }
+            fhf[f] = make_float2((float)(fr / N), (float)(fi / N));
+            fha[f] = make_float2((float)(ar / N), (float)(ai / N));
+        }
+    }
     std::vector<float> px, pz;
     if (d->pre_len_x > 0) {
         if (d->pre_len_x % 2 == 0 || !d->pre_x || d->pre_len_x > 2 * p.nx - 1) {
@@ -318,6 +343,11 @@ static int build(const msot_plan_desc *d, Plan &p) {
     if (p.L) {
         UP(p.ir_fwd, irf);
         UP(p.ir_adj, ira);
+    }
+    if (p.fft_log4n) {
+        UP(p.fft_tw, ftw);
+        UP(p.fft_hf, fhf);
+        UP(p.fft_ha, fha);
     }
     if (p.Kx >= 0) {
         std::vector<float> v(px.begin(), px.end());
