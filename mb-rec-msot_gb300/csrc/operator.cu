@@ -552,6 +552,123 @@ __device__ __forceinline__ void radix4_stage(const float2 *__restrict__ A, float
     o[3 * L] = make_float2(t1.x - t3.x, t1.y - t3.y);
 }
 
+// 32-point FFT in registers: radix-2 decimation in frequency, then the
+// bit-reversal permutation (register renaming).  w32[k] = exp(-2 pi i k/32).
+__constant__ float2 c_w32[16] = {
+    {1.000000000e+00f, 0.000000000e+00f},   {9.807852804e-01f, -1.950903220e-01f},
+    {9.238795325e-01f, -3.826834324e-01f},  {8.314696123e-01f, -5.555702330e-01f},
+    {7.071067812e-01f, -7.071067812e-01f},  {5.555702330e-01f, -8.314696123e-01f},
+    {3.826834324e-01f, -9.238795325e-01f},  {1.950903220e-01f, -9.807852804e-01f},
+    {0.000000000e+00f, -1.000000000e+00f},  {-1.950903220e-01f, -9.807852804e-01f},
+    {-3.826834324e-01f, -9.238795325e-01f}, {-5.555702330e-01f, -8.314696123e-01f},
+    {-7.071067812e-01f, -7.071067812e-01f}, {-8.314696123e-01f, -5.555702330e-01f},
+    {-9.238795325e-01f, -3.826834324e-01f}, {-9.807852804e-01f, -1.950903220e-01f}};
+
+__host__ __device__ constexpr int brev5(int i) {
+    return ((i & 1) << 4) | ((i & 2) << 2) | (i & 4) | ((i & 8) >> 2) | ((i & 16) >> 4);
+}
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+template <int SIGN>
+__device__ __forceinline__ void fft32(float2 (&v)[32]) {
+#pragma unroll
+    for (int len = 32; len >= 2; len >>= 1) {
+        const int half = len >> 1, step = 32 / len;
+#pragma unroll
+        for (int b = 0; b < 32; b += len) {
+#pragma unroll
+            for (int j = 0; j < half; ++j) {
+                const float2 u = v[b + j], w = v[b + j + half];
+                v[b + j] = make_float2(u.x + w.x, u.y + w.y);
+                const float2 d = make_float2(u.x - w.x, u.y - w.y);
+                const int ti = j * step;
+                if (ti == 0) {
+                    v[b + j + half] = d;
+                } else if (ti == 8) {
+                    v[b + j + half] = SIGN < 0 ? make_float2(d.y, -d.x) : make_float2(-d.y, d.x);
+                } else {
+                    float2 tw = c_w32[ti];
+                    if (SIGN > 0) tw.y = -tw.y;
+                    v[b + j + half] = cmul(d, tw);
+                }
+            }
+        }
+    }
+    float2 t[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) t[i] = v[brev5(i)];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = t[i];
+}
+
+// 1024-point overlap-save convolution by the four-step FFT 1024 = 32 x 32:
+// one warp per transform (two real columns), 32-point FFTs in registers and
+// two warp-local transposes through padded shared memory per direction.
+template <int FPC>
+__global__ void __launch_bounds__(32 * FPC) k_conv_fft1k(const float *__restrict__ in,
+                                                         float *__restrict__ out,
+                                                         const float2 *__restrict__ tw,
+                                                         const float2 *__restrict__ H, int C,
+                                                         int T, int L) {
+    __shared__ float2 S[FPC][32][33];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int pair = blockIdx.y * FPC + warp;
+    const int c1 = 2 * pair, c2 = c1 + 1;
+    if (c1 >= C) return;  // whole warp; no CTA-wide barriers below
+    const bool has2 = c2 < C;
+    const int V = 1024 - L + 1;
+    const int t0 = blockIdx.x * V;
+    const int u0 = t0 + L / 2 - (L - 1);
+    const float *x1 = in + (size_t)c1 * T;
+    const float *x2 = in + (size_t)(has2 ? c2 : c1) * T;
+    float2 v[32];
+#pragma unroll
+    for (int n1 = 0; n1 < 32; ++n1) {
+        const int u = u0 + 32 * n1 + lane;
+        const bool ok = u >= 0 && u < T;
+        v[n1] = make_float2(ok ? __ldg(x1 + u) : 0.f, (ok && has2) ? __ldg(x2 + u) : 0.f);
+    }
+    fft32<-1>(v);  // over n1, this lane is n2
+#pragma unroll
+    for (int k1 = 1; k1 < 32; ++k1) v[k1] = cmul(v[k1], __ldg(tw + lane * k1));
+    float2(*Sw)[33] = S[warp];
+#pragma unroll
+    for (int k1 = 0; k1 < 32; ++k1) Sw[k1][lane] = v[k1];
+    __syncwarp();
+#pragma unroll
+    for (int n2 = 0; n2 < 32; ++n2) v[n2] = Sw[lane][n2];
+    __syncwarp();
+    fft32<-1>(v);  // over n2, this lane is k1: v[k2] = X[k1 + 32 k2]
+#pragma unroll
+    for (int k2 = 0; k2 < 32; ++k2) v[k2] = cmul(v[k2], __ldg(H + lane + 32 * k2));
+    fft32<1>(v);  // over k2: v[n1'] for this k1
+#pragma unroll
+    for (int n1 = 1; n1 < 32; ++n1) {
+        float2 w = __ldg(tw + lane * n1);
+        w.y = -w.y;
+        v[n1] = cmul(v[n1], w);
+    }
+#pragma unroll
+    for (int n1 = 0; n1 < 32; ++n1) Sw[n1][lane] = v[n1];
+    __syncwarp();
+#pragma unroll
+    for (int k1 = 0; k1 < 32; ++k1) v[k1] = Sw[lane][k1];
+    fft32<1>(v);  // over k1, this lane is n1': v[n2'] = y[n1' + 32 n2']
+    float *y1 = out + (size_t)c1 * T, *y2 = out + (size_t)c2 * T;
+#pragma unroll
+    for (int n2 = 0; n2 < 32; ++n2) {
+        const int n = lane + 32 * n2;
+        const int t = t0 + n - (L - 1);
+        if (n >= L - 1 && t < T) {
+            y1[t] = v[n2].x;
+            if (has2) y2[t] = v[n2].y;
+        }
+    }
+}
+
 template <int LOG4N>
 __global__ void __launch_bounds__(1 << (2 * LOG4N - 2)) k_conv_fft(
     const float *__restrict__ in, float *__restrict__ out, const float2 *__restrict__ tw,
@@ -808,9 +925,10 @@ int launch_conv(const Plan &pl, const float *in, float *out, int W, bool transpo
         const size_t smem = 2 * (size_t)N * sizeof(float2);
         int rc;
         if (pl.fft_log4n == 5) {
-            if ((rc = set_smem(k_conv_fft<5>, smem)) != MSOT_OK) return rc;
-            KLAUNCH(k_conv_fft<5><<<grid, N / 4, smem, st>>>(in, out, pl.fft_tw, H, C, pl.T,
-                                                             pl.L));
+            constexpr int FPC = 4;
+            dim3 g1(div_up(pl.T, V), div_up(div_up(C, 2), FPC));
+            KLAUNCH(k_conv_fft1k<FPC><<<g1, 32 * FPC, 0, st>>>(in, out, pl.fft_tw, H, C, pl.T,
+                                                               pl.L));
         } else {
             if ((rc = set_smem(k_conv_fft<6>, smem)) != MSOT_OK) return rc;
             KLAUNCH(k_conv_fft<6><<<grid, N / 4, smem, st>>>(in, out, pl.fft_tw, H, C, pl.T,
