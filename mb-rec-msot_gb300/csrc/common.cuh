@@ -59,6 +59,7 @@ struct Plan {
     int blk_span_max = 0;          // largest last - first + 1
     int adj_groups_max = 0;        // detector groups the partial buffer is sized for
     float *scr_part = nullptr;     // [adj_groups_max][max_batch][P] adjoint partial sums
+    struct SolverCache *solver = nullptr;  // solver workspace and captured CUDA graphs
     // IR
     int L = 0, Lh = 0;
     float *ir_fwd = nullptr, *ir_adj = nullptr;
@@ -159,6 +160,8 @@ int interp_forward(const Plan &pl, const float *x_pi, float *raw, int W, float s
 int interp_adjoint(const Plan &pl, const float *raw, float *x, int W, float scale,
                    cudaStream_t st);
 int apply_forward(const Plan &pl, const float *img, float *sino, int W, cudaStream_t st);
+void solver_cache_free(Plan &pl);  // solver.cu
+bool profiling_enabled();          // timing.cu
 int apply_transpose(const Plan &pl, const float *sino, float *img, int W, cudaStream_t st);
 
 inline int div_up(int a, int b) { return (a + b - 1) / b; }

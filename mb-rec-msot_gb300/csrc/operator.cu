@@ -108,115 +108,108 @@ __global__ void k_permute(const float *__restrict__ in, float *__restrict__ out,
 // V_b = sum beta_k s[b+k]; each (pixel, detector) then adds
 // U + f V + e1 s[b-F] + e2 s[b+F+1].
 // ---------------------------------------------------------------------------
-constexpr int FWD_DG = 1;  // detectors per CTA of the bucket-moment forward
+// CTA = (tile of TB = 256 - 2F - 2 output samples, detector, WT instances).
+// Phase 0 copies the CTA's contiguous range of (tau, pixel) entries to shared
+// memory (in chunks of FWD_CHUNK); phase 1: one bucket per thread reduces the
+// four moments of its pixels, issuing FWD_UNR independent pixel gathers at a
+// time; phase 2: each output sample applies the (2F+2)-tap filter.
+constexpr int FWD_CHUNK = 2048;
+constexpr int FWD_UNR = 4;
 
-template <int WT>
-__global__ void __launch_bounds__(256) k_das_fwd2(const int32_t *__restrict__ off,
+template <int WT, int F>
+__global__ void __launch_bounds__(256) k_das_fwd3(const int32_t *__restrict__ off,
                                                   const int2 *__restrict__ ent,
                                                   const float *__restrict__ xpm,
                                                   float *__restrict__ raw, int P, int D, int T,
-                                                  int W, int fb, int F, float inv_r, float ce1,
+                                                  int W, int fb, float inv_r, float ce1,
                                                   float ce2, float scale) {
-    extern __shared__ float mom[];  // [4][WT][NB], bucket fastest
-    const int NB = blockDim.x;
-    const int TB = NB - 2 * F - 2;
-    const int w0 = blockIdx.z * WT;
+    constexpr int NB = 256;
+    constexpr int TB = NB - 2 * F - 2;
+    extern __shared__ float smf[];
+    float *mom = smf;                                            // [4][WT][NB]
+    int2 *es = reinterpret_cast<int2 *>(smf + 4 * WT * NB);     // [FWD_CHUNK]
+    const int d = blockIdx.y, w0 = blockIdx.z * WT;
     const int t0 = blockIdx.x * TB;
     const int b_lo = t0 - F - 1;
-    // FWD_DG adjacent detectors per CTA: their pixel bands overlap, so the
-    // pixel gathers of the later ones mostly hit L1
-    for (int dd = 0; dd < FWD_DG; ++dd) {
-    const int d = blockIdx.y * FWD_DG + dd;
-    if (d >= D) break;
-    if (dd) __syncthreads();  // mom of the previous detector fully consumed
-    {
-        float m0[WT], m1[WT], m2[WT], m3[WT];
+    const int32_t *o = off + (size_t)d * (T + 1);
+    const int2 *e = ent + (size_t)d * P;
+    const int b = b_lo + (int)threadIdx.x;
+    const bool valid = b >= 0 && b < T;
+    const int j0 = valid ? __ldg(o + b) : 0, j1 = valid ? __ldg(o + b + 1) : 0;
+    const int J0 = __ldg(o + max(b_lo, 0)), J1 = __ldg(o + min(b_lo + NB, T));
+    const int mask = (1 << fb) - 1;
+    const float step = __int_as_float((127 - fb) << 23);  // 2^-fb
+    float m0[WT], m1[WT], m2[WT], m3[WT];
 #pragma unroll
-        for (int i = 0; i < WT; ++i) m0[i] = m1[i] = m2[i] = m3[i] = 0.f;
-        const int b = b_lo + (int)threadIdx.x;
-        if (b >= 0 && b < T) {
-            const int32_t *o = off + (size_t)d * (T + 1);
-            const int j0 = __ldg(o + b), j1 = __ldg(o + b + 1);
-            const int2 *e = ent + (size_t)d * P;
-            const int mask = (1 << fb) - 1;
-            const float step = __int_as_float((127 - fb) << 23);  // 2^-fb
-            auto load_x = [&](int pix, float (&xv)[WT]) {
-                const float *xp = xpm + (size_t)pix * W + w0;
-                if constexpr (WT % 4 == 0) {
+    for (int i = 0; i < WT; ++i) m0[i] = m1[i] = m2[i] = m3[i] = 0.f;
+    for (int c0 = J0; c0 < J1; c0 += FWD_CHUNK) {
+        const int c1 = min(J1, c0 + FWD_CHUNK);
+        if (c0 > J0) __syncthreads();  // previous chunk fully consumed
+        for (int j = c0 + (int)threadIdx.x; j < c1; j += NB) es[j - c0] = __ldg(e + j);
+        __syncthreads();
+        const int a0 = max(j0, c0), a1 = min(j1, c1);
+        for (int j = a0; j < a1; j += FWD_UNR) {
+            int2 q[FWD_UNR];
+            float xv[FWD_UNR][WT];
 #pragma unroll
-                    for (int i = 0; i < WT; i += 4) {
-                        const float4 v = __ldg(reinterpret_cast<const float4 *>(xp + i));
-                        xv[i] = v.x; xv[i + 1] = v.y; xv[i + 2] = v.z; xv[i + 3] = v.w;
+            for (int u = 0; u < FWD_UNR; ++u) {
+                q[u] = j + u < a1 ? es[j + u - c0] : make_int2(0, -1);
+                if (q[u].y >= 0) {
+                    const float *xp = xpm + (size_t)q[u].y * W + w0;
+                    if constexpr (WT % 4 == 0) {
+#pragma unroll
+                        for (int i = 0; i < WT; i += 4) {
+                            const float4 v = __ldg(reinterpret_cast<const float4 *>(xp + i));
+                            xv[u][i] = v.x; xv[u][i + 1] = v.y; xv[u][i + 2] = v.z; xv[u][i + 3] = v.w;
+                        }
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < WT; ++i) xv[u][i] = __ldg(xp + i);
                     }
                 } else {
 #pragma unroll
-                    for (int i = 0; i < WT; ++i) xv[i] = __ldg(xp + i);
+                    for (int i = 0; i < WT; ++i) xv[u][i] = 0.f;
                 }
-            };
-            auto accumulate = [&](int32_t tau, const float (&xv)[WT]) {
-                const float f = (float)(tau & mask) * step;
+            }
+#pragma unroll
+            for (int u = 0; u < FWD_UNR; ++u) {
+                const float f = (float)(q[u].x & mask) * step;
                 const float e1 = fmaxf(0.f, fmaf(-f, inv_r, ce1));
                 const float e2 = fmaxf(0.f, fmaf(f, inv_r, -ce2));
 #pragma unroll
                 for (int i = 0; i < WT; ++i) {
-                    m0[i] += xv[i];
-                    m1[i] = fmaf(f, xv[i], m1[i]);
-                    m2[i] = fmaf(e1, xv[i], m2[i]);
-                    m3[i] = fmaf(e2, xv[i], m3[i]);
+                    m0[i] += xv[u][i];
+                    m1[i] = fmaf(f, xv[u][i], m1[i]);
+                    m2[i] = fmaf(e1, xv[u][i], m2[i]);
+                    m3[i] = fmaf(e2, xv[u][i], m3[i]);
                 }
-            };
-            // batches of UNR independent (entry, pixel) loads keep several L2
-            // requests in flight per thread
-            constexpr int UNR = WT >= 8 ? 2 : 4;
-            int j = j0;
-            for (; j + UNR <= j1; j += UNR) {
-                int2 q[UNR];
-#pragma unroll
-                for (int u = 0; u < UNR; ++u) q[u] = __ldg(e + j + u);
-                float xv[UNR][WT];
-#pragma unroll
-                for (int u = 0; u < UNR; ++u) load_x(q[u].y, xv[u]);
-#pragma unroll
-                for (int u = 0; u < UNR; ++u) accumulate(q[u].x, xv[u]);
-            }
-            for (; j < j1; ++j) {
-                const int2 q = __ldg(e + j);
-                float xv[WT];
-                load_x(q.y, xv);
-                accumulate(q.x, xv);
             }
         }
+    }
 #pragma unroll
-        for (int i = 0; i < WT; ++i) {
-            mom[(0 * WT + i) * NB + threadIdx.x] = m0[i];
-            mom[(1 * WT + i) * NB + threadIdx.x] = m1[i];
-            mom[(2 * WT + i) * NB + threadIdx.x] = m2[i];
-            mom[(3 * WT + i) * NB + threadIdx.x] = m3[i];
-        }
+    for (int i = 0; i < WT; ++i) {
+        mom[(0 * WT + i) * NB + threadIdx.x] = m0[i];
+        mom[(1 * WT + i) * NB + threadIdx.x] = m1[i];
+        mom[(2 * WT + i) * NB + threadIdx.x] = m2[i];
+        mom[(3 * WT + i) * NB + threadIdx.x] = m3[i];
     }
     __syncthreads();
     const int ti = threadIdx.x;
     const int t = t0 + ti;
-    if (ti >= TB || t >= T) continue;
-    float acc[WT];
-#pragma unroll
-    for (int i = 0; i < WT; ++i) acc[i] = 0.f;
+    if (ti >= TB || t >= T) return;
     const int base = t - b_lo;  // local index of bucket t
-    for (int k = -(F - 1); k <= F; ++k) {
-        const int bl = base - k;
-        const float a = fmaf(-fabsf((float)k), inv_r, 1.f);
-        const float be = k <= 0 ? -inv_r : inv_r;
-#pragma unroll
-        for (int i = 0; i < WT; ++i)
-            acc[i] = fmaf(a, mom[(0 * WT + i) * NB + bl],
-                          fmaf(be, mom[(1 * WT + i) * NB + bl], acc[i]));
-    }
 #pragma unroll
     for (int i = 0; i < WT; ++i) {
-        acc[i] += mom[(2 * WT + i) * NB + base + F];
-        acc[i] += mom[(3 * WT + i) * NB + base - F - 1];
-        raw[((size_t)(w0 + i) * D + d) * T + t] = acc[i] * scale;
-    }
+        const float *M0 = mom + (0 * WT + i) * NB + base;
+        const float *M1 = mom + (1 * WT + i) * NB + base;
+        float acc = mom[(2 * WT + i) * NB + base + F] + mom[(3 * WT + i) * NB + base - F - 1];
+#pragma unroll
+        for (int k = -(F - 1); k <= F; ++k) {
+            const float a = 1.f - (float)(k < 0 ? -k : k) * inv_r;
+            acc = fmaf(a, M0[-k], acc);
+            acc = k <= 0 ? acc - inv_r * M1[-k] : fmaf(inv_r, M1[-k], acc);
+        }
+        raw[((size_t)(w0 + i) * D + d) * T + t] = acc * scale;
     }
 }
 
@@ -776,26 +769,51 @@ int launch_to_pixmajor(const Plan &pl, const float *in, float *out, int W, cudaS
 }
 
 // DAS forward by bucket moments; xpm is pixel-major [P][W].
+template <int WT, int F>
+static int das_fwd_launch(const Plan &pl, const float *xpm, float *raw, int W, float scale,
+                          cudaStream_t st) {
+    constexpr int NB = 256, TB = NB - 2 * F - 2;
+    const size_t smem = (size_t)4 * WT * NB * sizeof(float) + FWD_CHUNK * sizeof(int2);
+    int rc;
+    if ((rc = set_smem(k_das_fwd3<WT, F>, smem)) != MSOT_OK) return rc;
+    dim3 grid(div_up(pl.T, TB), pl.D, W / WT);
+    KLAUNCH(k_das_fwd3<WT, F><<<grid, NB, smem, st>>>(pl.fwd_off, pl.fwd_ent, xpm, raw, pl.P,
+                                                      pl.D, pl.T, W, pl.frac_bits, pl.inv_r,
+                                                      pl.ce1, pl.ce2, scale));
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
+}
+
+template <int WT>
+static int das_fwd_f(const Plan &pl, const float *xpm, float *raw, int W, float scale,
+                     cudaStream_t st) {
+    switch (pl.F) {
+        case 0: return das_fwd_launch<WT, 0>(pl, xpm, raw, W, scale, st);
+        case 1: return das_fwd_launch<WT, 1>(pl, xpm, raw, W, scale, st);
+        case 2: return das_fwd_launch<WT, 2>(pl, xpm, raw, W, scale, st);
+        case 3: return das_fwd_launch<WT, 3>(pl, xpm, raw, W, scale, st);
+        case 4: return das_fwd_launch<WT, 4>(pl, xpm, raw, W, scale, st);
+        case 5: return das_fwd_launch<WT, 5>(pl, xpm, raw, W, scale, st);
+        case 6: return das_fwd_launch<WT, 6>(pl, xpm, raw, W, scale, st);
+        case 7: return das_fwd_launch<WT, 7>(pl, xpm, raw, W, scale, st);
+        case 8: return das_fwd_launch<WT, 8>(pl, xpm, raw, W, scale, st);
+        default:
+            set_error("DAS forward: interpolation radius %g above 9 samples is not supported",
+                      pl.radius);
+            return MSOT_EINVAL;
+    }
+}
+
 int launch_das_forward(const Plan &pl, const float *xpm, float *raw, int W, float scale,
                        cudaStream_t st) {
     TimedScope ts_(KID_INTERP_FWD, st);
     const int wt = pick_wt(W, 1, 8);
-    constexpr int NB = 256;
-    const int TB = NB - 2 * pl.F - 2;
-    dim3 grid(div_up(pl.T, TB), div_up(pl.D, FWD_DG), W / wt);
-    const size_t smem = (size_t)4 * wt * NB * sizeof(float);
-#define CASE(WT)                                                                          \
-    case WT:                                                                              \
-        KLAUNCH(k_das_fwd2<WT><<<grid, NB, smem, st>>>(pl.fwd_off, pl.fwd_ent, xpm, raw, pl.P,  \
-                                                       pl.D, pl.T, W, pl.frac_bits, pl.F,  \
-                                                       pl.inv_r, pl.ce1, pl.ce2, scale));  \
-        break;
     switch (wt) {
-        CASE(1) CASE(2) CASE(4) CASE(8)
+        case 8: return das_fwd_f<8>(pl, xpm, raw, W, scale, st);
+        case 4: return das_fwd_f<4>(pl, xpm, raw, W, scale, st);
+        case 2: return das_fwd_f<2>(pl, xpm, raw, W, scale, st);
+        default: return das_fwd_f<1>(pl, xpm, raw, W, scale, st);
     }
-#undef CASE
-    MSOT_LAUNCH_CHECK();
-    return MSOT_OK;
 }
 
 // DAS adjoint by pixel blocks; raw [W][D][T] -> x [W][P].

@@ -47,6 +47,7 @@ static int alloc(T **dst, size_t n, size_t &bytes) {
 }
 
 static void free_plan(Plan &p) {
+    solver_cache_free(p);
     void *ptrs[] = {p.tau_tiles, p.tau_pi, p.perm, p.ir_fwd, p.ir_adj, p.pre_x, p.pre_z,
                     p.sir, p.sir_se, p.sir_tiles, p.sir_pi, p.scr_img0, p.scr_img1,
                     p.scr_sino, p.fwd_off, p.fwd_ent, p.blk_tau, p.blk_span,

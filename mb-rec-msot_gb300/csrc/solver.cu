@@ -315,7 +315,7 @@ __global__ void k_group_sums(const double *part, int nblk, int W, int coupled, d
 struct Work {
     int W = 0;
     size_t bytes = 0;
-    float *s1 = nullptr, *s2 = nullptr;                 // sinogram vectors
+    float *s1 = nullptr, *s2 = nullptr, *s3 = nullptr;  // sinogram vectors
     float *i[12] = {};                                  // image vectors
     double *part = nullptr;                             // partial sums, 4 slots
     Scal *sc = nullptr;
@@ -332,6 +332,7 @@ static int nblk_for(size_t N) {
 static void free_work(Work &w) {
     cudaFree(w.s1);
     cudaFree(w.s2);
+    cudaFree(w.s3);
     for (auto &p : w.i) cudaFree(p);
     cudaFree(w.part);
     cudaFree(w.sc);
@@ -350,6 +351,7 @@ static int make_work(const Plan &pl, int W, Work &wk) {
     }
     AL(wk.s1, NS, float);
     AL(wk.s2, NS, float);
+    AL(wk.s3, NS, float);
     for (auto &p : wk.i) AL(p, NI, float);
     AL(wk.part, (size_t)4 * W * 256, double);
     AL(wk.sc, (size_t)W, Scal);
@@ -443,18 +445,68 @@ static int l2_outer(const Ctx &c, const float *b, float *wv, float *vm, double s
     return MSOT_OK;
 }
 
-static int solve_l2(const Plan &pl, const float *b, float *rec, int W, int num_iter,
+// Per-plan solver state: the workspace (grown to the largest batch seen) and
+// one captured CUDA graph of an outer L2 iteration for the last
+// (batch, regulariser, coupling) combination; the graph reads the right-hand
+// side from the workspace, so each call copies b there first.
+struct SolverCache {
+    Work wk;
+    cudaGraphExec_t l2_exec = nullptr;
+    int l2_W = -1, l2_has_reg = -1, l2_coupled = -1;
+    double l2_sr = -1.0;
+    long l2_kernels = 0;  // kernel nodes in the captured iteration
+};
+
+static SolverCache *cache_for(Plan &pl, int W, int &rc) {
+    rc = MSOT_OK;
+    if (!pl.solver) pl.solver = new SolverCache();
+    SolverCache *sc = pl.solver;
+    if (sc->wk.W < W) {
+        if (sc->l2_exec) cudaGraphExecDestroy(sc->l2_exec);
+        sc->l2_exec = nullptr;
+        sc->l2_W = -1;
+        free_work(sc->wk);
+        rc = make_work(pl, W, sc->wk);
+    }
+    return sc;
+}
+
+void solver_cache_free(Plan &pl) {
+    if (!pl.solver) return;
+    if (pl.solver->l2_exec) cudaGraphExecDestroy(pl.solver->l2_exec);
+    free_work(pl.solver->wk);
+    delete pl.solver;
+    pl.solver = nullptr;
+}
+
+static long count_kernel_nodes(cudaGraph_t g) {
+    size_t n = 0;
+    if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess || n == 0) return 0;
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) return 0;
+    long k = 0;
+    for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+    }
+    return k;
+}
+
+static int solve_l2(Plan &pl, const float *b_in, float *rec, int W, int num_iter,
                     double lambdaL2, const float *x0, int coupled, double *err_img,
                     double *err_reg, cudaStream_t st) {
-    Work wk;
-    TRY(make_work(pl, W, wk));
+    int rc;
+    SolverCache *sc = cache_for(pl, W, rc);
+    if (rc) return rc;
+    Work &wk = sc->wk;
     const size_t NS = (size_t)W * pl.D * pl.T, NI = (size_t)W * pl.P;
     Ctx c{pl, W, coupled, st, NS, NI, nblk_for(NS / W), nblk_for(NI / W), wk};
     const int has_reg = lambdaL2 > 0;
     const double sr = has_reg ? std::sqrt(lambdaL2) : 0.0;
     float *wv = wk.i[7], *vm = wk.i[8];
-    int rc = MSOT_OK;
+    const float *b = wk.s3;
     do {
+        MSOT_CUDA_TRY(cudaMemcpyAsync(wk.s3, b_in, NS * sizeof(float), cudaMemcpyDeviceToDevice, st));
         if (x0)
             KLAUNCH(k_copy<<<256, 256, 0, st>>>(x0, wv, NI));
         else
@@ -468,9 +520,54 @@ static int solve_l2(const Plan &pl, const float *b, float *rec, int W, int num_i
             rc = MSOT_ECUDA;
             break;
         }
-        for (int it = 0; it < num_iter && rc == MSOT_OK; ++it)
+        int it = 0;
+        const bool use_graph = !profiling_enabled() && num_iter > 1;
+        const bool have = sc->l2_exec && sc->l2_W == W && sc->l2_has_reg == has_reg &&
+                          sc->l2_coupled == coupled && sc->l2_sr == sr;
+        if (use_graph && !have) {
+            // first iteration eagerly (sets kernel attributes), then capture one
+            if ((rc = l2_outer(c, b, wv, vm, sr, has_reg, wk.gsum))) break;
+            ++it;
+            if (sc->l2_exec) cudaGraphExecDestroy(sc->l2_exec);
+            sc->l2_exec = nullptr;
+            cudaGraph_t g = nullptr;
+            MSOT_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+            const long before = g_launch_count.load();
             rc = l2_outer(c, b, wv, vm, sr, has_reg, wk.gsum);
-        if (rc) break;
+            g_launch_count -= g_launch_count.load() - before;  // counted per replay below
+            cudaError_t ce = cudaStreamEndCapture(st, &g);
+            if (rc || ce != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                if (!rc) {
+                    set_error("solver: graph capture failed: %s", cudaGetErrorString(ce));
+                    rc = MSOT_ECUDA;
+                }
+                break;
+            }
+            ce = cudaGraphInstantiate(&sc->l2_exec, g, 0);
+            sc->l2_kernels = count_kernel_nodes(g);
+            cudaGraphDestroy(g);
+            if (ce != cudaSuccess) {
+                set_error("solver: graph instantiation failed: %s", cudaGetErrorString(ce));
+                sc->l2_exec = nullptr;
+                rc = MSOT_ECUDA;
+                break;
+            }
+            sc->l2_W = W;
+            sc->l2_has_reg = has_reg;
+            sc->l2_coupled = coupled;
+            sc->l2_sr = sr;
+        }
+        if (use_graph) {
+            for (; it < num_iter; ++it) {
+                MSOT_CUDA_TRY(cudaGraphLaunch(sc->l2_exec, st));
+                g_launch_count += sc->l2_kernels;
+            }
+        } else {
+            for (; it < num_iter && rc == MSOT_OK; ++it)
+                rc = l2_outer(c, b, wv, vm, sr, has_reg, wk.gsum);
+            if (rc) break;
+        }
         KLAUNCH(k_copy<<<256, 256, 0, st>>>(wv, rec, NI));
         if (err_img || err_reg) {
             std::vector<double> e;
@@ -494,10 +591,8 @@ static int solve_l2(const Plan &pl, const float *b, float *rec, int W, int num_i
             rc = MSOT_ECUDA;
         }
     } while (0);
-    free_work(wk);
     return rc;
 }
-
 
 // ---------------------------------------------------------------------------
 // L1 (identity) NNLS: split Bregman with cgs(lam A^T A + I, rhs, 1e-8, 2)

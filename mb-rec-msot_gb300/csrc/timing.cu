@@ -34,6 +34,8 @@ static Registry &reg() {
 
 static constexpr size_t kPoolMax = 1 << 16;
 
+bool profiling_enabled() { return reg().enabled; }
+
 TimedScope::TimedScope(int kid, cudaStream_t st) : kid_(kid), st_(st), slot_(-1) {
     Registry &r = reg();
     if (!r.enabled) return;
