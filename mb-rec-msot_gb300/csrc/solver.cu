@@ -451,6 +451,8 @@ static int l2_outer(const Ctx &c, const float *b, float *wv, float *vm, double s
 // side from the workspace, so each call copies b there first.
 struct SolverCache {
     Work wk;
+    cudaStream_t stream = nullptr;  // non-blocking stream the graphs are captured on
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
     cudaGraphExec_t l2_exec = nullptr;
     int l2_W = -1, l2_has_reg = -1, l2_coupled = -1;
     double l2_sr = -1.0;
@@ -461,6 +463,15 @@ static SolverCache *cache_for(Plan &pl, int W, int &rc) {
     rc = MSOT_OK;
     if (!pl.solver) pl.solver = new SolverCache();
     SolverCache *sc = pl.solver;
+    if (!sc->stream) {
+        if (cudaStreamCreateWithFlags(&sc->stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&sc->ev_in, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&sc->ev_out, cudaEventDisableTiming) != cudaSuccess) {
+            set_error("solver: stream creation failed");
+            rc = MSOT_ECUDA;
+            return sc;
+        }
+    }
     if (sc->wk.W < W) {
         if (sc->l2_exec) cudaGraphExecDestroy(sc->l2_exec);
         sc->l2_exec = nullptr;
@@ -474,6 +485,9 @@ static SolverCache *cache_for(Plan &pl, int W, int &rc) {
 void solver_cache_free(Plan &pl) {
     if (!pl.solver) return;
     if (pl.solver->l2_exec) cudaGraphExecDestroy(pl.solver->l2_exec);
+    if (pl.solver->stream) cudaStreamDestroy(pl.solver->stream);
+    if (pl.solver->ev_in) cudaEventDestroy(pl.solver->ev_in);
+    if (pl.solver->ev_out) cudaEventDestroy(pl.solver->ev_out);
     free_work(pl.solver->wk);
     delete pl.solver;
     pl.solver = nullptr;
@@ -494,10 +508,14 @@ static long count_kernel_nodes(cudaGraph_t g) {
 
 static int solve_l2(Plan &pl, const float *b_in, float *rec, int W, int num_iter,
                     double lambdaL2, const float *x0, int coupled, double *err_img,
-                    double *err_reg, cudaStream_t st) {
+                    double *err_reg, cudaStream_t user) {
     int rc;
     SolverCache *sc = cache_for(pl, W, rc);
     if (rc) return rc;
+    // run on the plan's own stream (capturable), ordered after the caller's work
+    cudaStream_t st = sc->stream;
+    MSOT_CUDA_TRY(cudaEventRecord(sc->ev_in, user));
+    MSOT_CUDA_TRY(cudaStreamWaitEvent(st, sc->ev_in, 0));
     Work &wk = sc->wk;
     const size_t NS = (size_t)W * pl.D * pl.T, NI = (size_t)W * pl.P;
     Ctx c{pl, W, coupled, st, NS, NI, nblk_for(NS / W), nblk_for(NI / W), wk};
@@ -591,6 +609,8 @@ static int solve_l2(Plan &pl, const float *b_in, float *rec, int W, int num_iter
             rc = MSOT_ECUDA;
         }
     } while (0);
+    cudaEventRecord(sc->ev_out, st);
+    cudaStreamWaitEvent(user, sc->ev_out, 0);
     return rc;
 }
 
