@@ -109,10 +109,14 @@ __global__ void k_permute(const float *__restrict__ in, float *__restrict__ out,
 // U + f V + e1 s[b-F] + e2 s[b+F+1].
 // ---------------------------------------------------------------------------
 // CTA = (tile of TB = 256 - 2F - 2 output samples, detector, WT instances).
-// Phase 0 copies the CTA's contiguous range of (tau, pixel) entries to shared
-// memory (in chunks of FWD_CHUNK); phase 1: one bucket per thread reduces the
-// four moments of its pixels, issuing FWD_UNR independent pixel gathers at a
-// time; phase 2: each output sample applies the (2F+2)-tap filter.
+// The CTA's contiguous range of (tau, pixel) entries (sorted by bucket) is
+// copied to shared memory in chunks of FWD_CHUNK and split into equal runs,
+// one per thread, so every thread does the same work whatever the bucket
+// sizes.  A thread accumulates the four moments of its current bucket in
+// registers, issuing FWD_UNR independent pixel gathers at a time, and adds
+// them to the shared-memory moments when its run changes bucket (the only
+// shared-memory atomics).  Then each output sample applies the
+// (2F+2)-tap filter over the bucket moments.
 constexpr int FWD_CHUNK = 2048;
 constexpr int FWD_UNR = 4;
 
@@ -133,27 +137,38 @@ __global__ void __launch_bounds__(256) k_das_fwd3(const int32_t *__restrict__ of
     const int b_lo = t0 - F - 1;
     const int32_t *o = off + (size_t)d * (T + 1);
     const int2 *e = ent + (size_t)d * P;
-    const int b = b_lo + (int)threadIdx.x;
-    const bool valid = b >= 0 && b < T;
-    const int j0 = valid ? __ldg(o + b) : 0, j1 = valid ? __ldg(o + b + 1) : 0;
     const int J0 = __ldg(o + max(b_lo, 0)), J1 = __ldg(o + min(b_lo + NB, T));
     const int mask = (1 << fb) - 1;
     const float step = __int_as_float((127 - fb) << 23);  // 2^-fb
-    float m0[WT], m1[WT], m2[WT], m3[WT];
 #pragma unroll
-    for (int i = 0; i < WT; ++i) m0[i] = m1[i] = m2[i] = m3[i] = 0.f;
+    for (int c = 0; c < 4 * WT; ++c) mom[c * NB + threadIdx.x] = 0.f;
+    float m0[WT], m1[WT], m2[WT], m3[WT];
+    int cur = -1;
+    auto flush = [&]() {
+        if (cur >= 0) {
+#pragma unroll
+            for (int i = 0; i < WT; ++i) {
+                atomicAdd(&mom[(0 * WT + i) * NB + cur], m0[i]);
+                atomicAdd(&mom[(1 * WT + i) * NB + cur], m1[i]);
+                atomicAdd(&mom[(2 * WT + i) * NB + cur], m2[i]);
+                atomicAdd(&mom[(3 * WT + i) * NB + cur], m3[i]);
+            }
+        }
+    };
     for (int c0 = J0; c0 < J1; c0 += FWD_CHUNK) {
         const int c1 = min(J1, c0 + FWD_CHUNK);
-        if (c0 > J0) __syncthreads();  // previous chunk fully consumed
+        __syncthreads();  // moments zeroed / previous chunk consumed
         for (int j = c0 + (int)threadIdx.x; j < c1; j += NB) es[j - c0] = __ldg(e + j);
         __syncthreads();
-        const int a0 = max(j0, c0), a1 = min(j1, c1);
-        for (int j = a0; j < a1; j += FWD_UNR) {
+        const int per = (c1 - c0 + NB - 1) / NB;
+        const int r0 = c0 + (int)threadIdx.x * per, r1 = min(c1, r0 + per);
+        cur = -1;
+        for (int j = r0; j < r1; j += FWD_UNR) {
             int2 q[FWD_UNR];
             float xv[FWD_UNR][WT];
 #pragma unroll
             for (int u = 0; u < FWD_UNR; ++u) {
-                q[u] = j + u < a1 ? es[j + u - c0] : make_int2(0, -1);
+                q[u] = j + u < r1 ? es[j + u - c0] : make_int2(0, -1);
                 if (q[u].y >= 0) {
                     const float *xp = xpm + (size_t)q[u].y * W + w0;
                     if constexpr (WT % 4 == 0) {
@@ -166,13 +181,18 @@ __global__ void __launch_bounds__(256) k_das_fwd3(const int32_t *__restrict__ of
 #pragma unroll
                         for (int i = 0; i < WT; ++i) xv[u][i] = __ldg(xp + i);
                     }
-                } else {
-#pragma unroll
-                    for (int i = 0; i < WT; ++i) xv[u][i] = 0.f;
                 }
             }
 #pragma unroll
             for (int u = 0; u < FWD_UNR; ++u) {
+                if (q[u].y < 0) break;
+                const int bl = (q[u].x >> fb) - b_lo;
+                if (bl != cur) {
+                    flush();
+                    cur = bl;
+#pragma unroll
+                    for (int i = 0; i < WT; ++i) m0[i] = m1[i] = m2[i] = m3[i] = 0.f;
+                }
                 const float f = (float)(q[u].x & mask) * step;
                 const float e1 = fmaxf(0.f, fmaf(-f, inv_r, ce1));
                 const float e2 = fmaxf(0.f, fmaf(f, inv_r, -ce2));
@@ -185,13 +205,7 @@ __global__ void __launch_bounds__(256) k_das_fwd3(const int32_t *__restrict__ of
                 }
             }
         }
-    }
-#pragma unroll
-    for (int i = 0; i < WT; ++i) {
-        mom[(0 * WT + i) * NB + threadIdx.x] = m0[i];
-        mom[(1 * WT + i) * NB + threadIdx.x] = m1[i];
-        mom[(2 * WT + i) * NB + threadIdx.x] = m2[i];
-        mom[(3 * WT + i) * NB + threadIdx.x] = m3[i];
+        flush();
     }
     __syncthreads();
     const int ti = threadIdx.x;
