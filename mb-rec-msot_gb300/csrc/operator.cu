@@ -109,16 +109,10 @@ __global__ void k_permute(const float *__restrict__ in, float *__restrict__ out,
 // U + f V + e1 s[b-F] + e2 s[b+F+1].
 // ---------------------------------------------------------------------------
 // CTA = (tile of TB = 256 - 2F - 2 output samples, detector, WT instances).
-// The CTA's contiguous range of (tau, pixel) entries (sorted by bucket) is
-// copied to shared memory in chunks of FWD_CHUNK and split into equal runs,
-// one per thread, so every thread does the same work whatever the bucket
-// sizes.  A thread accumulates the four moments of its current bucket in
-// registers, issuing FWD_UNR independent pixel gathers at a time, and adds
-// them to the shared-memory moments when its run changes bucket (the only
-// shared-memory atomics).  Then each output sample applies the
-// (2F+2)-tap filter over the bucket moments.
-constexpr int FWD_CHUNK = 2048;
-constexpr int FWD_UNR = 4;
+// Phase 1: one bucket per thread reduces the four moments of its pixels,
+// loading FWD_UNR (entry, pixel) pairs at a time; phase 2: each output sample
+// applies the (2F+2)-tap filter over the bucket moments.
+constexpr int FWD_UNR = 2;
 
 template <int WT, int F>
 __global__ void __launch_bounds__(256) k_das_fwd3(const int32_t *__restrict__ off,
@@ -129,48 +123,30 @@ __global__ void __launch_bounds__(256) k_das_fwd3(const int32_t *__restrict__ of
                                                   float ce2, float scale) {
     constexpr int NB = 256;
     constexpr int TB = NB - 2 * F - 2;
-    extern __shared__ float smf[];
-    float *mom = smf;                                            // [4][WT][NB]
-    int2 *es = reinterpret_cast<int2 *>(smf + 4 * WT * NB);     // [FWD_CHUNK]
+    __shared__ float mom[4 * WT * NB];  // [4][WT][NB], bucket fastest
     const int d = blockIdx.y, w0 = blockIdx.z * WT;
     const int t0 = blockIdx.x * TB;
     const int b_lo = t0 - F - 1;
-    const int32_t *o = off + (size_t)d * (T + 1);
-    const int2 *e = ent + (size_t)d * P;
-    const int J0 = __ldg(o + max(b_lo, 0)), J1 = __ldg(o + min(b_lo + NB, T));
-    const int mask = (1 << fb) - 1;
-    const float step = __int_as_float((127 - fb) << 23);  // 2^-fb
+    {
+        float m0[WT], m1[WT], m2[WT], m3[WT];
 #pragma unroll
-    for (int c = 0; c < 4 * WT; ++c) mom[c * NB + threadIdx.x] = 0.f;
-    float m0[WT], m1[WT], m2[WT], m3[WT];
-    int cur = -1;
-    auto flush = [&]() {
-        if (cur >= 0) {
+        for (int i = 0; i < WT; ++i) m0[i] = m1[i] = m2[i] = m3[i] = 0.f;
+        const int b = b_lo + (int)threadIdx.x;
+        if (b >= 0 && b < T) {
+            const int32_t *o = off + (size_t)d * (T + 1);
+            const int j0 = __ldg(o + b), j1 = __ldg(o + b + 1);
+            const int2 *e = ent + (size_t)d * P;
+            const int mask = (1 << fb) - 1;
+            const float step = __int_as_float((127 - fb) << 23);  // 2^-fb
+            for (int j = j0; j < j1; j += FWD_UNR) {
+                int2 q[FWD_UNR];
+                float xv[FWD_UNR][WT];
 #pragma unroll
-            for (int i = 0; i < WT; ++i) {
-                atomicAdd(&mom[(0 * WT + i) * NB + cur], m0[i]);
-                atomicAdd(&mom[(1 * WT + i) * NB + cur], m1[i]);
-                atomicAdd(&mom[(2 * WT + i) * NB + cur], m2[i]);
-                atomicAdd(&mom[(3 * WT + i) * NB + cur], m3[i]);
-            }
-        }
-    };
-    for (int c0 = J0; c0 < J1; c0 += FWD_CHUNK) {
-        const int c1 = min(J1, c0 + FWD_CHUNK);
-        __syncthreads();  // moments zeroed / previous chunk consumed
-        for (int j = c0 + (int)threadIdx.x; j < c1; j += NB) es[j - c0] = __ldg(e + j);
-        __syncthreads();
-        const int per = (c1 - c0 + NB - 1) / NB;
-        const int r0 = c0 + (int)threadIdx.x * per, r1 = min(c1, r0 + per);
-        cur = -1;
-        for (int j = r0; j < r1; j += FWD_UNR) {
-            int2 q[FWD_UNR];
-            float xv[FWD_UNR][WT];
+                for (int u = 0; u < FWD_UNR; ++u)
+                    q[u] = j + u < j1 ? __ldg(e + j + u) : make_int2(0, -1);
 #pragma unroll
-            for (int u = 0; u < FWD_UNR; ++u) {
-                q[u] = j + u < r1 ? es[j + u - c0] : make_int2(0, -1);
-                if (q[u].y >= 0) {
-                    const float *xp = xpm + (size_t)q[u].y * W + w0;
+                for (int u = 0; u < FWD_UNR; ++u) {
+                    const float *xp = xpm + (size_t)max(q[u].y, 0) * W + w0;
                     if constexpr (WT % 4 == 0) {
 #pragma unroll
                         for (int i = 0; i < WT; i += 4) {
@@ -182,30 +158,29 @@ __global__ void __launch_bounds__(256) k_das_fwd3(const int32_t *__restrict__ of
                         for (int i = 0; i < WT; ++i) xv[u][i] = __ldg(xp + i);
                     }
                 }
-            }
 #pragma unroll
-            for (int u = 0; u < FWD_UNR; ++u) {
-                if (q[u].y < 0) break;
-                const int bl = (q[u].x >> fb) - b_lo;
-                if (bl != cur) {
-                    flush();
-                    cur = bl;
+                for (int u = 0; u < FWD_UNR; ++u) {
+                    if (q[u].y < 0) break;
+                    const float f = (float)(q[u].x & mask) * step;
+                    const float e1 = fmaxf(0.f, fmaf(-f, inv_r, ce1));
+                    const float e2 = fmaxf(0.f, fmaf(f, inv_r, -ce2));
 #pragma unroll
-                    for (int i = 0; i < WT; ++i) m0[i] = m1[i] = m2[i] = m3[i] = 0.f;
-                }
-                const float f = (float)(q[u].x & mask) * step;
-                const float e1 = fmaxf(0.f, fmaf(-f, inv_r, ce1));
-                const float e2 = fmaxf(0.f, fmaf(f, inv_r, -ce2));
-#pragma unroll
-                for (int i = 0; i < WT; ++i) {
-                    m0[i] += xv[u][i];
-                    m1[i] = fmaf(f, xv[u][i], m1[i]);
-                    m2[i] = fmaf(e1, xv[u][i], m2[i]);
-                    m3[i] = fmaf(e2, xv[u][i], m3[i]);
+                    for (int i = 0; i < WT; ++i) {
+                        m0[i] += xv[u][i];
+                        m1[i] = fmaf(f, xv[u][i], m1[i]);
+                        m2[i] = fmaf(e1, xv[u][i], m2[i]);
+                        m3[i] = fmaf(e2, xv[u][i], m3[i]);
+                    }
                 }
             }
         }
-        flush();
+#pragma unroll
+        for (int i = 0; i < WT; ++i) {
+            mom[(0 * WT + i) * NB + threadIdx.x] = m0[i];
+            mom[(1 * WT + i) * NB + threadIdx.x] = m1[i];
+            mom[(2 * WT + i) * NB + threadIdx.x] = m2[i];
+            mom[(3 * WT + i) * NB + threadIdx.x] = m3[i];
+        }
     }
     __syncthreads();
     const int ti = threadIdx.x;
@@ -787,11 +762,8 @@ template <int WT, int F>
 static int das_fwd_launch(const Plan &pl, const float *xpm, float *raw, int W, float scale,
                           cudaStream_t st) {
     constexpr int NB = 256, TB = NB - 2 * F - 2;
-    const size_t smem = (size_t)4 * WT * NB * sizeof(float) + FWD_CHUNK * sizeof(int2);
-    int rc;
-    if ((rc = set_smem(k_das_fwd3<WT, F>, smem)) != MSOT_OK) return rc;
     dim3 grid(div_up(pl.T, TB), pl.D, W / WT);
-    KLAUNCH(k_das_fwd3<WT, F><<<grid, NB, smem, st>>>(pl.fwd_off, pl.fwd_ent, xpm, raw, pl.P,
+    KLAUNCH(k_das_fwd3<WT, F><<<grid, NB, 0, st>>>(pl.fwd_off, pl.fwd_ent, xpm, raw, pl.P,
                                                       pl.D, pl.T, W, pl.frac_bits, pl.inv_r,
                                                       pl.ce1, pl.ce2, scale));
     MSOT_LAUNCH_CHECK();
