@@ -70,3 +70,19 @@ def test_library_reports_errors_without_a_device():
     h = ctypes.c_void_p()
     rc = L.msot_plan_create(None, ctypes.byref(h))
     assert rc == -1 and b"plan" in L.msot_last_error()
+
+
+@pytest.mark.parametrize("name", ["forwardDelayAndSumMex", "transposeDelayAndSumMex",
+                                  "forwardMex", "transposeMex"])
+def test_mex_gateways_compile_against_the_mex_api(name, tmp_path):
+    """The MATLAB gateways of the C ABI compile against the MEX API (the
+    project's stand-in header here, MATLAB's mex.h on a MATLAB host)."""
+    import shutil
+    import subprocess
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    src = os.path.join(ROOT, "mb-rec-msot_gb300", "mex", name + ".cpp")
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I",
+                        os.path.join(ROOT, "oracle", "mex_shim"), "-I",
+                        os.path.join(ROOT, "include"), src], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
