@@ -92,6 +92,21 @@ int msot_interp_forward(msot_plan_t plan, const float *d_coeffs, float *d_raw, i
 int msot_interp_transpose(msot_plan_t plan, const float *d_raw, float *d_coeffs, int batch,
                           void *stream);
 
+/* Allocation-free form of msot_interp_transpose for plans without SIR; no
+ * counterpart in the reference.  It is for callers that are not allowed to
+ * allocate device memory, e.g. a host application whose device memory is
+ * owned by another allocator or that runs under a fixed memory budget.  Its
+ * partial sums live in a 16 MiB array inside the library (held on every
+ * device that loads the library until the process exits) instead of the
+ * plan's scratch, so the call performs no cudaMalloc / cudaFree.  Limit:
+ * batch * nx * nz <= 4 Mi (4194304) elements, else MSOT_ERANGE.  The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress)
+ * with that device current; make that first call before any stream capture.
+ * All calls share the one array: calls that overlap on the GPU (other streams
+ * or threads) race and must be serialised by the caller. */
+int msot_interp_transpose_noalloc(msot_plan_t plan, const float *d_raw, float *d_coeffs,
+                                  int batch, void *stream);
+
 /* Estimate sigma_max of the unnormalised operator by power iteration on the
  * GPU (replaces the svds call, MSOTmodel.m:277-278); FP64 norms. */
 int msot_estimate_norm(msot_plan_t plan, int iters, uint64_t seed, double *sigma_max,

@@ -19,6 +19,7 @@
 // floor((tau_fx + r_fx)/2^fb)] and the weight is 1 - |t - tau| / r, computed
 // from the exact integer difference (t << fb) - tau_fx.
 #include <algorithm>
+#include <mutex>
 
 #include "common.cuh"
 
@@ -1018,6 +1019,95 @@ int apply_transpose(const Plan &pl, const float *sino, float *img, int W, cudaSt
 
 }  // namespace msot
 
+namespace msot {
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the DAS adjoint.
+//
+// The adjoint keeps one partial image per detector group in scratch memory.
+// msot_interp_transpose takes that scratch from the plan; this variant takes
+// it from a fixed array that is part of the library image instead, so a call
+// allocates no device memory at all.  The array is NOALLOC_PART_FLOATS floats
+// (16 MiB) on every device that loads the library, for the lifetime of the
+// process.  Host code cannot pass the array's name to a kernel (on the host
+// it is only a stand-in symbol), so its device address is looked up once per
+// device with cudaGetSymbolAddress, on the first call made with that device
+// current.
+// ---------------------------------------------------------------------------
+constexpr size_t NOALLOC_PART_FLOATS = (size_t)4 << 20;
+static __device__ __align__(256) float g_noalloc_part[NOALLOC_PART_FLOATS];
+
+static int noalloc_part_address(float **out) {
+    constexpr int kMaxDev = 64;
+    static float *addr[kMaxDev] = {};
+    static std::mutex mu;
+    int dev = 0;
+    MSOT_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDev) {
+        set_error("noalloc: device index %d not supported", dev);
+        return MSOT_EINVAL;
+    }
+    std::lock_guard<std::mutex> g(mu);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_part);
+        if (e != cudaSuccess || !p) {
+            set_error("noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+            return MSOT_ECUDA;
+        }
+        addr[dev] = static_cast<float *>(p);
+    }
+    *out = addr[dev];
+    return MSOT_OK;
+}
+
+template <int WT, int F>
+static int das_adj_launch_fixed(const Plan &pl, const float *raw, float *x, int W,
+                                cudaStream_t st, float *part) {
+    const int SL = div_up(pl.blk_span_max, ADJ_BPT) * ADJ_BPT + 2 * F + 2;
+    const size_t smem = (size_t)((WT * SL + 3) & ~3) * sizeof(float) +
+                        (size_t)WT * pl.blk_span_max * sizeof(float4);
+    int rc;
+    if ((rc = set_smem(k_das_adj4<WT, F>, smem)) != MSOT_OK) return rc;
+    const size_t stride = (size_t)W * pl.P;
+    const int base = pl.n_blk * (W / WT);
+    int groups = std::max(1, std::min(pl.D, div_up(2 * 152, base)));
+    groups = std::min<size_t>(groups, NOALLOC_PART_FLOATS / stride);
+    const int dpg = div_up(pl.D, groups);
+    groups = div_up(pl.D, dpg);
+    dim3 grid(pl.n_blk, W / WT, groups);
+    // every (group, instance, pixel) element of the array is written by
+    // k_das_adj4 before k_sum_parts reads it: nothing needs clearing
+    KLAUNCH(k_das_adj4<WT, F><<<grid, BLK_THREADS, smem, st>>>(
+        pl.blk_tau, pl.blk_span, raw, part, pl.nx, pl.nz, pl.n_blk_x, pl.D, pl.T,
+        pl.frac_bits, pl.inv_r, pl.ce1, pl.ce2, pl.blk_span_max, dpg, stride));
+    MSOT_LAUNCH_CHECK();
+    KLAUNCH(k_sum_parts<<<(unsigned)std::min<size_t>(4096, div_up((int)stride, 256)), 256, 0,
+                          st>>>(part, x, stride, groups, stride, 1.f));
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
+}
+
+template <int WT>
+static int das_adj_fixed_f(const Plan &pl, const float *raw, float *x, int W, cudaStream_t st,
+                           float *part) {
+    switch (pl.F) {
+        case 0: return das_adj_launch_fixed<WT, 0>(pl, raw, x, W, st, part);
+        case 1: return das_adj_launch_fixed<WT, 1>(pl, raw, x, W, st, part);
+        case 2: return das_adj_launch_fixed<WT, 2>(pl, raw, x, W, st, part);
+        case 3: return das_adj_launch_fixed<WT, 3>(pl, raw, x, W, st, part);
+        case 4: return das_adj_launch_fixed<WT, 4>(pl, raw, x, W, st, part);
+        case 5: return das_adj_launch_fixed<WT, 5>(pl, raw, x, W, st, part);
+        case 6: return das_adj_launch_fixed<WT, 6>(pl, raw, x, W, st, part);
+        case 7: return das_adj_launch_fixed<WT, 7>(pl, raw, x, W, st, part);
+        case 8: return das_adj_launch_fixed<WT, 8>(pl, raw, x, W, st, part);
+        default:
+            set_error("DAS adjoint: interpolation radius %g above 9 samples is not supported",
+                      pl.radius);
+            return MSOT_EINVAL;
+    }
+}
+}  // namespace msot
+
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
@@ -1068,6 +1158,33 @@ int msot_interp_transpose(msot_plan_t plan, const float *d_raw, float *d_coeffs,
     int rc = check_batch(plan, batch, d_raw, d_coeffs);
     if (rc) return rc;
     return interp_adjoint(plan->p, d_raw, d_coeffs, batch, 1.f, (cudaStream_t)stream);
+}
+
+int msot_interp_transpose_noalloc(msot_plan_t plan, const float *d_raw, float *d_coeffs,
+                                  int batch, void *stream) {
+    if (!plan || !d_raw || !d_coeffs || batch <= 0) {
+        set_error("interp_transpose_noalloc: null plan/pointer or non-positive batch");
+        return MSOT_EINVAL;
+    }
+    const Plan &pl = plan->p;
+    if (pl.S) {
+        set_error("interp_transpose_noalloc: plans with a spatial impulse response are not "
+                  "supported");
+        return MSOT_EINVAL;
+    }
+    if ((size_t)batch * pl.P > NOALLOC_PART_FLOATS) {
+        set_error("interp_transpose_noalloc: batch x pixels = %zu exceeds the fixed scratch of "
+                  "%zu floats",
+                  (size_t)batch * pl.P, NOALLOC_PART_FLOATS);
+        return MSOT_ERANGE;
+    }
+    float *part = nullptr;
+    int rc = noalloc_part_address(&part);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int wt = pick_wt(batch, 1, 2);
+    if (wt == 2) return das_adj_fixed_f<2>(pl, d_raw, d_coeffs, batch, st, part);
+    return das_adj_fixed_f<1>(pl, d_raw, d_coeffs, batch, st, part);
 }
 
 }  // extern "C"
