@@ -132,6 +132,27 @@ int msot_rec_nn_with_L1_eye_reg(msot_plan_t plan, const float *d_b, float *d_rec
                                 double *err_img, double *err_reg, void *stream);
 
 /* ------------------------------------------------------------------------ */
+/* Analytic reconstructors.  d_sig: [W][D][T] device FP32 (MATLAB T x D x W);
+ * x (nx) and z (nz): host FP64 pixel coordinate vectors (the meshgrid of
+ * Discretization.m:34 -- fov_x varies along columns, fov_z along rows);
+ * outputs [W][nx][nz] device FP32.  An index outside the sinogram returns
+ * MSOT_ERANGE (the reference errors).  Synchronous. */
+
+/* dmas_cf.m:19-107: DMAS-CF, DMAS, coherence factor and DAS images. */
+int msot_dmas_cf(const float *d_sig, int W, int D, int T, const double *x, int nx,
+                 const double *z, int nz, double c, double fs, double n_crop, double coverage_deg,
+                 double radius, float *d_dmas_cf, float *d_dmas, float *d_cf, float *d_das,
+                 void *stream);
+
+/* backproject_waveeq.m:1-50: psf host FP64 m x n (column-major, m along T);
+ * d_K device FP32 K_n x K_n column-major (bp_kernel.m of the full acquisition
+ * times; the samples n_crop+1 .. n_crop+T are used). */
+int msot_backproject_waveeq(const float *d_sig, int W, int D, int T, const double *x, int nx,
+                            const double *z, int nz, double c, double fs, double n_crop,
+                            double coverage_deg, double radius, const double *psf, int psf_m,
+                            int psf_n, const float *d_K, int K_n, float *d_out, void *stream);
+
+/* ------------------------------------------------------------------------ */
 /* Instrumentation (no counterpart in the reference, whose only timing is
  * tic/toc, e.g. rec_nn_with_L2_reg.m:44-49). */
 

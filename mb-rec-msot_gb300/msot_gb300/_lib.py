@@ -68,6 +68,13 @@ SIGNATURES = {
                                           C.c_int, _dp, _dp, _vp]),
     "msot_rec_nn_with_L1_eye_reg": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_double, _vp,
                                               C.c_int, _dp, _dp, _vp]),
+    "msot_dmas_cf": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _dp, C.c_int, _dp, C.c_int,
+                               C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                               _vp, _vp, _vp, _vp, _vp]),
+    "msot_backproject_waveeq": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _dp, C.c_int, _dp,
+                                          C.c_int, C.c_double, C.c_double, C.c_double,
+                                          C.c_double, C.c_double, _dp, C.c_int, C.c_int, _vp,
+                                          C.c_int, _vp, _vp]),
     "msot_launch_count": (C.c_longlong, []),
     "msot_profile_enable": (C.c_int, [C.c_int]),
     "msot_profile_kernel_name": (C.c_char_p, [C.c_int]),

@@ -154,3 +154,17 @@ def test_sb_itv2_reduces_tv():
     g += 0.1 * rng.standard_normal((n, n))
     u = S.sb_itv2(g, 0.05, B, Bt, BtB).reshape(n, n, order="F")
     assert S.itv(u) < S.itv(g)
+
+
+def test_bp_kernel_is_antisymmetric_and_dmas_identity():
+    from oracle import backprojection as B
+    t = np.arange(1, 41) / 4e7
+    K = B.bp_kernel(t)
+    assert np.allclose(K, -K.T, atol=1e-12 * np.abs(K).max())
+    rng = np.random.default_rng(9)
+    sig = rng.standard_normal((1, 16, 400))
+    x = np.linspace(-0.002, 0.002, 6)
+    z = np.linspace(-0.002, 0.002, 5)
+    dmcf, dm, cf, das = B.dmas_cf(sig, x, z, 1500.0, 4e7, 0.0, 135.0, 0.008)
+    assert np.allclose(dmcf, dm * cf)
+    assert (cf >= 0).all() and (cf <= 1.0 + 1e-9).all()
