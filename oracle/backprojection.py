@@ -84,8 +84,6 @@ def convn_same_td(sig_wdt, psf):
     dimensions of each wavelength; sig is (W, D, T), psf is MATLAB m x n
     (m along T, n along D)."""
     psf = np.atleast_2d(np.asarray(psf, dtype=np.float64))
-    if psf.shape[0] == 1 and psf.ndim == 2 and psf.size > 1:
-        pass
     m, n = psf.shape
     W, D, T = sig_wdt.shape
     out = np.zeros_like(sig_wdt, dtype=np.float64)
@@ -120,7 +118,7 @@ def backproject_waveeq(sig_wdt, x, z, c, fs, n_crop, coverage, R, psf, K):
     W, D, T = sig.shape
     dt = 1.0 / fs
     ang = transducer_angles(D, coverage)
-    acq_samples = np.arange(1, T + 1) + n_crop
+    acq_samples = np.arange(1, T + 1) + int(round(n_crop))
     acq = acq_samples * dt
     s = cumtrapz_cols(acq, sig / c) / acq
     s = convn_same_td(s, psf) / np.asarray(psf, dtype=np.float64).sum()
