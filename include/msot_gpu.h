@@ -131,6 +131,23 @@ int msot_rec_nn_with_L1_eye_reg(msot_plan_t plan, const float *d_b, float *d_rec
                                 int num_iter, double reg, const float *d_x0, int coupled,
                                 double *err_img, double *err_reg, void *stream);
 
+/* rec_nn_with_TV_reg.m:1 (nnls_sparsa_based_reg_matrix_less.m:31-85; prox
+ * SB_ITV2.m:20-40, TV term ITV.m:5-6).  Square grids only (MSOT_EINVAL
+ * otherwise, as rec_nn_with_TV_reg.m:23-25 errors).  sparsa_iter is SpaRSA's
+ * MaxiterA (2 in the reference, nnls_sparsa_based_reg_matrix_less.m:64);
+ * err_reg receives ITV of each reconstruction. */
+int msot_rec_nn_with_TV_reg(msot_plan_t plan, const float *d_b, float *d_rec, int batch,
+                            int num_iter, double reg, int sparsa_iter, const float *d_x0,
+                            int coupled, double *err_img, double *err_reg, void *stream);
+
+/* SB_ITV2.m:1-40: u = argmin 1/2 ||u - g||^2 + mu ITV(u) for `batch` n x n
+ * images (device FP32, [batch][n][n] column-major per image).  Synchronous. */
+int msot_sb_itv2(const float *d_g, float *d_u, int batch, int n, double mu, void *stream);
+
+/* ITV.m:1-6: isotropic TV of `batch` n x n device images -> host itv[batch].
+ * Synchronous. */
+int msot_itv(const float *d_x, double *itv, int batch, int n, void *stream);
+
 /* ------------------------------------------------------------------------ */
 /* Analytic reconstructors.  d_sig: [W][D][T] device FP32 (MATLAB T x D x W);
  * x (nx) and z (nz): host FP64 pixel coordinate vectors (the meshgrid of

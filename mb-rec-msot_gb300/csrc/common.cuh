@@ -101,7 +101,7 @@ enum KernelId {
     KID_CONV = 3,
     KID_VECTOR = 4,
     KID_PERMUTE = 5,
-    KID_TOEPLITZ = 6,
+    KID_TV_PROX = 6,
     KID_COUNT = 7
 };
 

@@ -13,7 +13,7 @@ namespace msot {
 std::atomic<long long> g_launch_count{0};
 
 static const char *kNames[KID_COUNT] = {"prefilter", "interp_forward", "interp_adjoint",
-                                        "ir_conv", "solver_vector", "permute", "toeplitz_mma"};
+                                        "ir_conv", "solver_vector", "permute", "tv_prox"};
 
 struct EventPair {
     cudaEvent_t a, b;

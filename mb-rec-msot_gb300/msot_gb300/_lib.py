@@ -68,6 +68,10 @@ SIGNATURES = {
                                           C.c_int, _dp, _dp, _vp]),
     "msot_rec_nn_with_L1_eye_reg": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_double, _vp,
                                               C.c_int, _dp, _dp, _vp]),
+    "msot_rec_nn_with_TV_reg": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_double, C.c_int,
+                                          _vp, C.c_int, _dp, _dp, _vp]),
+    "msot_sb_itv2": (C.c_int, [_vp, _vp, C.c_int, C.c_int, C.c_double, _vp]),
+    "msot_itv": (C.c_int, [_vp, _dp, C.c_int, C.c_int, _vp]),
     "msot_dmas_cf": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _dp, C.c_int, _dp, C.c_int,
                                C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                _vp, _vp, _vp, _vp, _vp]),

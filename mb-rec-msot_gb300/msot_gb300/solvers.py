@@ -82,3 +82,52 @@ def rec_nn_with_L1_eye_reg(model: MSOTmodel, data_filt, num_iter: int, regParam:
     if coupled:
         e1, e2 = np.array([e1.sum()]), np.array([e2.sum()])
     return rec, e1, e2, np.zeros(0), t
+
+
+def rec_nn_with_TV_reg(model: MSOTmodel, data_filt, num_iter: int, regParam: float, *,
+                       sparsa_iter: int = 2, x0=None, coupled: bool = False, stream=None):
+    """rec_nn_with_TV_reg.m:1 (square grids only).  Returns (rec_img,
+    lCurveErrImg, lCurveErrReg, err, t); lCurveErrReg is ITV of each
+    reconstruction.  sparsa_iter is SpaRSA's MaxiterA (the reference passes
+    2, nnls_sparsa_based_reg_matrix_less.m:64)."""
+    b, W, x0p, rec = _prep(model, data_filt, x0)
+    e1 = np.zeros(W)
+    e2 = np.zeros(W)
+    t0 = time.perf_counter()
+    _lib.check(_lib.load().msot_rec_nn_with_TV_reg(
+        model.plan, C.c_void_p(b.data_ptr()), C.c_void_p(rec.data_ptr()), W, int(num_iter),
+        float(regParam), int(sparsa_iter), C.c_void_p(x0p.data_ptr()) if x0p is not None else None,
+        1 if coupled else 0, e1.ctypes.data_as(C.POINTER(C.c_double)),
+        e2.ctypes.data_as(C.POINTER(C.c_double)), _stream_ptr(stream)))
+    t = time.perf_counter() - t0
+    if coupled:
+        e1, e2 = np.array([e1.sum()]), np.array([e2.sum()])
+    return rec, e1, e2, np.zeros(0), t
+
+
+def SB_ITV2(g, mu: float, *, stream=None):
+    """SB_ITV2.m:1 on a batch of square images g [W, n, n] (or one [n, n])."""
+    t = torch.as_tensor(g)
+    if not t.is_cuda:
+        t = t.cuda()
+    squeeze = t.dim() == 2
+    t = t.to(torch.float32).reshape(-1, t.shape[-2], t.shape[-1]).contiguous()
+    if t.shape[-1] != t.shape[-2]:
+        raise ValueError("SB_ITV2 needs square images")
+    u = torch.empty_like(t)
+    _lib.check(_lib.load().msot_sb_itv2(C.c_void_p(t.data_ptr()), C.c_void_p(u.data_ptr()),
+                                        t.shape[0], t.shape[-1], float(mu), _stream_ptr(stream)))
+    return u[0] if squeeze else u
+
+
+def ITV(x, *, stream=None):
+    """ITV.m:1 for a batch of square images x [W, n, n]; returns [W] numpy."""
+    t = torch.as_tensor(x)
+    if not t.is_cuda:
+        t = t.cuda()
+    t = t.to(torch.float32).reshape(-1, t.shape[-2], t.shape[-1]).contiguous()
+    out = np.zeros(t.shape[0])
+    _lib.check(_lib.load().msot_itv(C.c_void_p(t.data_ptr()),
+                                    out.ctypes.data_as(C.POINTER(C.c_double)), t.shape[0],
+                                    t.shape[-1], _stream_ptr(stream)))
+    return out

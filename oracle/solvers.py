@@ -279,8 +279,9 @@ def sparsa(y, A, At, tau, psi, phi, x0, maxiter, tol=1e-8, alpha_min=1e-30, alph
     return x
 
 
-def rec_nn_with_TV_reg(fwd, adj, b, nx, nz, n_wl, num_iter, reg):
-    """rec_nn_with_TV_reg.m:137-170 + nnls_sparsa_based_reg_matrix_less.m."""
+def rec_nn_with_TV_reg(fwd, adj, b, nx, nz, n_wl, num_iter, reg, sparsa_iter=2):
+    """rec_nn_with_TV_reg.m:20-54 + nnls_sparsa_based_reg_matrix_less.m:31-85
+    (SpaRSA's MaxiterA = sparsa_iter, 2 in the reference, :64)."""
     if nx != nz:
         raise ValueError("This TV implementation works only with square images!")
     B, Bt, BtB = diff_oper(nx)
@@ -310,7 +311,7 @@ def rec_nn_with_TV_reg(fwd, adj, b, nx, nz, n_wl, num_iter, reg):
 
     for _ in range(num_iter):
         rhs = np.concatenate([sl * b, sb * (w + v)])
-        u = sparsa(rhs, Aaug, Aaug_t, reg, Psi, Phi, w, 2)
+        u = sparsa(rhs, Aaug, Aaug_t, reg, Psi, Phi, w, sparsa_iter)
         w = np.maximum(u - v, 0.0)
         v = v + w - u
     err_img = float(np.linalg.norm(fwd(w) - b) ** 2)
