@@ -18,8 +18,9 @@
  *     transfers themselves.
  *   - A plan is immutable after creation and may be used from several host
  *     threads on different streams, except for the functions documented as
- *     using the plan's scratch (msot_forward/transpose with a NULL workspace
- *     and the solvers), which must not overlap on the GPU for one plan.
+ *     using the plan's scratch (msot_forward, msot_transpose,
+ *     msot_interp_transpose and the solvers), which must not overlap on the
+ *     GPU for one plan.
  */
 #ifndef MSOT_GPU_H
 #define MSOT_GPU_H
@@ -173,6 +174,12 @@ int msot_backproject_waveeq(const float *d_sig, int W, int D, int T, const doubl
 /* Instrumentation (no counterpart in the reference, whose only timing is
  * tic/toc, e.g. rec_nn_with_L2_reg.m:44-49). */
 
+/* SB_ITV2 kernel choice: 0 (default) = the shared-memory cluster kernel
+ * wherever the image fits, 1 = always the global-memory kernel. */
+int msot_tv_prox_path(int path);
+/* Split-Bregman sweeps and CGS steps summed over all images of all cluster-
+ * kernel SB_ITV2 launches since the last call (then reset); syncs the device. */
+int msot_tv_prox_stats(long long *sweeps, long long *cg_steps);
 /* Number of kernels the library has launched since it was loaded. */
 long long msot_launch_count(void);
 /* on != 0: record a CUDA event pair around every launch of the hot kernel

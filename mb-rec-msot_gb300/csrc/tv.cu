@@ -28,7 +28,10 @@
 // synchronisation.  coupled = 1 makes the batch one SpaRSA problem (the
 // reference's multi-wavelength call: one alpha and one objective over all
 // wavelengths); coupled = 0 runs W independent reconstructions.
+#include <cooperative_groups.h>
+
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <vector>
 
@@ -53,19 +56,20 @@ struct TvVecs {
     float *u, *up, *rhs, *b1, *b2, *d1, *d2, *x, *r, *rt, *uc, *p, *q, *vh, *uh, *xmin;
 };
 
-// sum over the block; every thread gets the result
-__device__ double tv_block_sum(double v, double *sh) {
+// sum over the block (float within warps, double across warps); every
+// thread gets the result
+__device__ double tv_block_sum(float v, double *sh) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     __syncthreads();  // sh may still be read from the previous call
-    if (lane == 0) sh[wid] = v;
+    if (lane == 0) sh[wid] = (double)v;
     __syncthreads();
     if (wid == 0) {
-        v = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+        double d = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) sh[32] = v;
+        for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xffffffffu, d, o);
+        if (lane == 0) sh[32] = d;
     }
     __syncthreads();
     return sh[32];
@@ -74,8 +78,16 @@ __device__ double tv_block_sum(double v, double *sh) {
 __device__ double tv_dot(const float *a, const float *b, int P, double *sh) {
     float acc = 0.f;
     for (int i = threadIdx.x; i < P; i += blockDim.x) acc = fmaf(a[i], b[i], acc);
-    return tv_block_sum((double)acc, sh);
+    return tv_block_sum(acc, sh);
 }
+
+// broadcast flags of the thread-0 scalar logic (FP64 on GB300 is far too
+// slow to replicate divisions and square roots across all threads)
+enum : int { TVB_BREAK = 1, TVB_CONVERGED = 2, TVB_IMPROVED = 4, TVB_RUN = 8 };
+struct TvBcast {
+    float beta, alpha;
+    int flag;
+};
 
 // out = (I + B'B) in
 __device__ void tv_apply_M(const float *in, float *out, int N) {
@@ -95,24 +107,28 @@ __device__ void tv_apply_M(const float *in, float *out, int N) {
 // u = cgs(I + B'B, rhs, tol, TV_CG_MAX) from x0 = 0 (Sonneveld's CGS with the
 // recursively updated residual; the smallest-residual iterate when it does
 // not converge, as MATLAB's cgs returns)
-__device__ void tv_cgs(const TvVecs &V, int N, float tol, double *sh) {
+__device__ void tv_cgs(const TvVecs &V, int N, double tol, double *sh, TvBcast &bc) {
     const int P = N * N;
-    const double n2b = sqrt(tv_dot(V.rhs, V.rhs, P, sh));
+    const double n2b2 = tv_dot(V.rhs, V.rhs, P, sh);
+    double n2b = 0.0, rho = 0.0, rho1 = 1.0, normrmin = 0.0;  // thread 0 only
     for (int i = threadIdx.x; i < P; i += blockDim.x) {
         V.x[i] = 0.f;
         V.xmin[i] = 0.f;
         V.r[i] = V.rhs[i];
         V.rt[i] = V.rhs[i];
     }
+    if (threadIdx.x == 0) {
+        n2b = sqrt(n2b2);
+        rho = n2b2;  // rt' r of the first step (rt = r = rhs)
+        normrmin = n2b;
+        bc.flag = n2b > 0.0 ? TVB_RUN : 0;
+        bc.beta = 0.f;
+    }
     __syncthreads();
     bool converged = false;
-    if (n2b > 0.0) {
-        double normrmin = n2b, rho = 1.0;
+    if (bc.flag & TVB_RUN) {
         for (int it = 0; it < TV_CG_MAX; ++it) {
-            const double rho1 = rho;
-            rho = tv_dot(V.rt, V.r, P, sh);
-            if (rho == 0.0 || !isfinite(rho)) break;
-            const float beta = it ? (float)(rho / rho1) : 0.f;
+            const float beta = bc.beta;
             for (int i = threadIdx.x; i < P; i += blockDim.x) {
                 if (it == 0) {
                     V.uc[i] = V.r[i];
@@ -126,8 +142,17 @@ __device__ void tv_cgs(const TvVecs &V, int N, float tol, double *sh) {
             __syncthreads();
             tv_apply_M(V.p, V.vh, N);
             const double rtvh = tv_dot(V.rt, V.vh, P, sh);
-            if (rtvh == 0.0 || !isfinite(rtvh)) break;
-            const float alpha = (float)(rho / rtvh);
+            if (threadIdx.x == 0) {
+                if (rtvh == 0.0 || !isfinite(rtvh)) {
+                    bc.flag = TVB_BREAK;
+                } else {
+                    bc.flag = 0;
+                    bc.alpha = (float)(rho / rtvh);
+                }
+            }
+            __syncthreads();
+            if (bc.flag & TVB_BREAK) break;
+            const float alpha = bc.alpha;
             for (int i = threadIdx.x; i < P; i += blockDim.x) {
                 const float qq = fmaf(-alpha, V.vh[i], V.uc[i]);
                 V.q[i] = qq;
@@ -137,19 +162,43 @@ __device__ void tv_cgs(const TvVecs &V, int N, float tol, double *sh) {
             }
             __syncthreads();
             tv_apply_M(V.uh, V.vh, N);  // vh is free again: holds M uh
-            for (int i = threadIdx.x; i < P; i += blockDim.x)
-                V.r[i] = fmaf(-alpha, V.vh[i], V.r[i]);
+            float a_rr = 0.f;
+            for (int i = threadIdx.x; i < P; i += blockDim.x) {
+                const float rv = fmaf(-alpha, V.vh[i], V.r[i]);
+                V.r[i] = rv;
+                a_rr = fmaf(rv, rv, a_rr);
+            }
+            const double rr = tv_block_sum(a_rr, sh);
+            const double rtr = tv_dot(V.rt, V.r, P, sh);
+            if (threadIdx.x == 0) {
+                const double normr = sqrt(rr);
+                int f = 0;
+                if (normr <= tol * n2b) {
+                    f = TVB_CONVERGED;
+                } else {
+                    if (normr < normrmin) {
+                        normrmin = normr;
+                        f |= TVB_IMPROVED;
+                    }
+                    rho1 = rho;
+                    rho = rtr;  // rt' r of the next step
+                    if (rho == 0.0 || !isfinite(rho))
+                        f |= TVB_BREAK;
+                    else
+                        bc.beta = (float)(rho / rho1);
+                }
+                bc.flag = f;
+            }
             __syncthreads();
-            const double normr = sqrt(tv_dot(V.r, V.r, P, sh));
-            if (normr <= (double)tol * n2b) {
+            const int f = bc.flag;
+            if (f & TVB_CONVERGED) {
                 converged = true;
                 break;
             }
-            if (normr < normrmin) {
-                normrmin = normr;
+            if (f & TVB_IMPROVED) {
                 for (int i = threadIdx.x; i < P; i += blockDim.x) V.xmin[i] = V.x[i];
-                __syncthreads();
             }
+            if (f & TVB_BREAK) break;
         }
     }
     const float *src = converged ? V.x : V.xmin;
@@ -163,6 +212,7 @@ __global__ void __launch_bounds__(TV_THREADS)
     k_tv_prox(const float *__restrict__ g_all, const TvState *__restrict__ st, double mu_const,
               int coupled, float *__restrict__ out_all, float *__restrict__ work, int N) {
     __shared__ double sh[33];
+    __shared__ TvBcast bc;
     const int w = blockIdx.x, gw = coupled ? 0 : w;
     if (st && st[gw].done) return;
     const int P = N * N;
@@ -190,7 +240,7 @@ __global__ void __launch_bounds__(TV_THREADS)
             V.rhs[i] = g[i] - ((c1 - c1n) + (c2 - c2n));
         }
         __syncthreads();
-        tv_cgs(V, N, 1e-5f, sh);
+        tv_cgs(V, N, 1e-5, sh, bc);
         // Bub = B u + b ; d = shrink(Bub, mu) ; b = Bub - d
         float dif = 0.f, nrm = 0.f;
         for (int i = threadIdx.x; i < P; i += blockDim.x) {
@@ -208,13 +258,368 @@ __global__ void __launch_bounds__(TV_THREADS)
             dif = fmaf(e, e, dif);
             nrm = fmaf(c, c, nrm);
         }
-        const double d2 = tv_block_sum((double)dif, sh);
-        const double n2 = tv_block_sum((double)nrm, sh);
-        if (!(n2 > 0.0) || sqrt(d2 / n2) <= 1e-3) break;
+        const double d2 = tv_block_sum(dif, sh);
+        const double n2 = tv_block_sum(nrm, sh);
+        if (threadIdx.x == 0) bc.flag = (!(n2 > 0.0) || sqrt(d2 / n2) <= 1e-3) ? TVB_BREAK : 0;
+        __syncthreads();
+        if (bc.flag & TVB_BREAK) break;
     }
     float *o = out_all + (size_t)w * P;
     for (int i = threadIdx.x; i < P; i += blockDim.x) o[i] = V.u[i];
 }
+
+// ---------------------------------------------------------------------------
+// Cluster-resident prox: one thread-block cluster of C CTAs per image, CTA
+// `rank` owning the column slab ix in [rank*nloc, rank*nloc + nl).  All
+// eleven work vectors of the split-Bregman + CGS iteration live in shared
+// memory (same layout in every CTA); the stencil's x-neighbours in the
+// adjacent slabs are read through distributed shared memory.  Cluster-wide
+// sums: every CTA adds the C per-CTA partials in rank order, so all CTAs
+// see bitwise-identical scalars and take identical branches.
+//
+// The Bregman pair (b, d) is carried as Bub = B u + b only: with
+// f = max(|Bub| - mu, 0) / |Bub| (0 where |Bub| = 0), d = f Bub,
+// b = Bub - d and b - d = b - f Bub, so both are recomputed per pixel.
+// ---------------------------------------------------------------------------
+// iteration statistics of all prox launches (SB sweeps, CGS steps), read and
+// reset by msot_tv_prox_stats
+__device__ unsigned long long g_tv_stats[2];
+
+constexpr int TVC_THREADS = 512;
+constexpr int TVC_MAXC = 16;  // largest cluster
+// u, x, bub1, bub2, r, rt, p (two buffers), q, uc, uh, vh, xmin
+constexpr int TVC_NV = 13;
+enum TvcVec { V_U = 0, V_X, V_B1, V_B2, V_R, V_RT, V_P0, V_P1, V_Q, V_UC, V_UH, V_VH, V_XMIN };
+
+// Thread mapping inside a slab: thread t owns row iz = t % N of the columns
+// lc = t / N, t / N + G, ... (G = TVC_THREADS / N column groups; N <= 512).
+struct TvcCtx {
+    float *sm;        // this CTA's vectors
+    const float *sl;  // left neighbour's vectors (rank - 1), or null
+    const float *sr;  // right neighbour's vectors (rank + 1), or null
+    int N, nloc, nl, ix0, iz, G, lc0;
+    bool zlo, zhi;
+};
+
+// the Bregman quantities b = Bub - d and b - d of one pixel from its Bub pair
+__device__ __forceinline__ void tvc_bd(float a1, float a2, float mu, float &b1, float &b2,
+                                       float &c1, float &c2) {
+    const float s = sqrtf(fmaf(a1, a1, a2 * a2));
+    const float f = s > 0.f ? fmaxf(s - mu, 0.f) / s : 0.f;
+    const float d1 = f * a1, d2 = f * a2;
+    b1 = a1 - d1;
+    b2 = a2 - d2;
+    c1 = b1 - d1;
+    c2 = b2 - d2;
+}
+
+// value of vector o at the left / right x-neighbour of (lc, iz), element l
+__device__ __forceinline__ float tvc_left(const TvcCtx &c, int o, int lc, int l) {
+    return lc == 0 ? c.sl[o + (c.nloc - 1) * c.N + c.iz] : c.sm[o + l - c.N];
+}
+__device__ __forceinline__ float tvc_right(const TvcCtx &c, int o, int lc, int l) {
+    return lc == c.nl - 1 ? c.sr[o + c.iz] : c.sm[o + l + c.N];
+}
+
+// (I + B'B) of vector oi at (lc, iz) (same stencil as tv_apply_M).  The
+// x-neighbours in the adjacent slabs are not read from oi there: halo(base,
+// k) recomputes them from that CTA's vectors (base = its shared memory, k =
+// the element), with the same float operations the owner used.
+template <class Halo>
+__device__ __forceinline__ float tvc_M(const TvcCtx &c, int oi, int lc, int l, Halo halo) {
+    const float *in = c.sm + oi;
+    const int ix = c.ix0 + lc;
+    const float v = in[l];
+    const float g1 = c.zlo ? v - in[l - 1] : 0.f;
+    const float g1n = c.zhi ? in[l + 1] - v : 0.f;
+    float g2 = 0.f, g2n = 0.f;
+    if (ix >= 1) g2 = v - (lc == 0 ? halo(c.sl, (c.nloc - 1) * c.N + c.iz) : in[l - c.N]);
+    if (ix + 1 < c.N) g2n = (lc == c.nl - 1 ? halo(c.sr, c.iz) : in[l + c.N]) - v;
+    return v + (g1 - g1n) + (g2 - g2n);
+}
+
+// Cluster-wide sums of two per-thread values, valid in thread 0 of every
+// CTA.  Each CTA pushes its two block sums into slot [par][rank] of every
+// CTA of the cluster (remote stores, then the barrier), and thread 0 adds
+// the C slots in rank order: identical results in all CTAs.  The scalar
+// logic that follows runs on thread 0 only and is broadcast through shared
+// memory: FP64 on GB300 is far too slow to replicate divisions and square
+// roots across all threads.
+__device__ __forceinline__ void tvc_reduce(float a, float b, double &A, double &B, float *wsum,
+                                           double *red, int &par, int C, int rank) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        wsum[wid] = a;
+        wsum[32 + wid] = b;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        constexpr int NW = TVC_THREADS / 32;
+        double da = lane < NW ? (double)wsum[lane] : 0.0;
+        double db = lane < NW ? (double)wsum[32 + lane] : 0.0;
+#pragma unroll
+        for (int o = NW / 2; o > 0; o >>= 1) {
+            da += __shfl_down_sync(0xffffffffu, da, o);
+            db += __shfl_down_sync(0xffffffffu, db, o);
+        }
+        da = __shfl_sync(0xffffffffu, da, 0);
+        db = __shfl_sync(0xffffffffu, db, 0);
+        if (lane < C) {
+            double *dst = cl.map_shared_rank(red, lane) + (par * TVC_MAXC + rank) * 2;
+            dst[0] = da;
+            dst[1] = db;
+        }
+    }
+    cl.sync();
+    if (threadIdx.x == 0) {
+        const double *src = red + par * TVC_MAXC * 2;
+        A = 0.0;
+        B = 0.0;
+        for (int r = 0; r < C; ++r) {
+            A += src[2 * r];
+            B += src[2 * r + 1];
+        }
+    }
+    par ^= 1;
+}
+
+// loop over this thread's elements (lc, l) of the slab
+#define TVC_FOR(c) for (int lc = (c).lc0, l = lc * (c).N + (c).iz; lc < (c).nl; lc += (c).G, l += (c).G * (c).N)
+
+// CGS step structure (per step two cluster barriers, both inside the sums):
+//   uc = r + beta q ; p_new = uc + beta (q + beta p_old)     (local)
+//   __syncthreads ; vh = M p_new, halo p_new from the neighbour's r, q, p_old
+//   sum rt'vh -> alpha
+//   q = uc - alpha vh ; uh = uc + q ; x += alpha uh         (local)
+//   __syncthreads ; r -= alpha M uh, halo uh from the neighbour's uc, vh
+//   sum r'r, rt'r -> convergence, beta
+// p alternates between two buffers so that a neighbour can still read p_old
+// while this CTA writes p_new; every vector read remotely in a phase was
+// written before the barrier that opened the phase.
+__global__ void __launch_bounds__(TVC_THREADS, 2)
+    k_tv_prox_cl(const float *__restrict__ g_all, const TvState *__restrict__ st, double mu_const,
+                 int coupled, float *__restrict__ out_all, int N, int C, int nloc) {
+    namespace cg = cooperative_groups;
+    extern __shared__ float4 tvc_smem[];
+    __shared__ float wsum[64];
+    __shared__ double red[2 * TVC_MAXC * 2];
+    __shared__ TvBcast bc;
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    const int w = blockIdx.x / C, gw = coupled ? 0 : w;
+    if (st && st[gw].done) return;  // uniform over the cluster
+    TvcCtx c;
+    c.sm = reinterpret_cast<float *>(tvc_smem);
+    c.N = N;
+    c.nloc = nloc;
+    c.ix0 = rank * nloc;
+    c.nl = max(0, min(nloc, N - c.ix0));
+    c.G = TVC_THREADS / N;
+    c.iz = threadIdx.x % N;
+    c.lc0 = (int)threadIdx.x / N;
+    if (c.lc0 >= c.G) c.lc0 = c.nl;  // idle thread: empty loops
+    c.zlo = c.iz >= 1;
+    c.zhi = c.iz + 1 < N;
+    c.sl = rank > 0 ? cl.map_shared_rank(c.sm, rank - 1) : nullptr;
+    c.sr = rank + 1 < C ? cl.map_shared_rank(c.sm, rank + 1) : nullptr;
+    const float mu = (float)(st ? st[gw].mu : mu_const);
+    const float *g = g_all + (size_t)w * N * N + (size_t)c.ix0 * N;
+    const int V = nloc * N;
+    float *S = c.sm;
+    int ou = V_U * V, ox = V_X * V;  // swapped after every sweep
+    const int ob1 = V_B1 * V, ob2 = V_B2 * V, orr = V_R * V, ort = V_RT * V, oq = V_Q * V,
+              ouc = V_UC * V, ouh = V_UH * V, ovh = V_VH * V, oxm = V_XMIN * V;
+    int op = V_P0 * V, opo = V_P1 * V;  // p_new, p_old
+    int par = 0, n_sweeps = 0, n_cg = 0;
+    double A = 0.0, B = 0.0;                                  // thread 0 only
+    double n2b = 0.0, rho = 0.0, rho1 = 1.0, normrmin = 0.0;  // thread 0 only
+    TVC_FOR(c) {
+        S[ou + l] = g[l];
+        S[ob1 + l] = 0.f;
+        S[ob2 + l] = 0.f;
+    }
+    cl.sync();
+    for (int it = 0; it < TV_SB_MAX; ++it) {
+        ++n_sweeps;
+        // rhs = g - B'(b - d); r = rt = rhs; x = xmin = 0
+        float n2 = 0.f;
+        TVC_FOR(c) {
+            const int ix = c.ix0 + lc;
+            float b1, b2, c1, c2, t1, t2, e1, e2;
+            tvc_bd(S[ob1 + l], S[ob2 + l], mu, b1, b2, c1, c2);
+            float acc = 0.f;
+            if (c.zlo) acc += c1;
+            if (c.zhi) {
+                tvc_bd(S[ob1 + l + 1], S[ob2 + l + 1], mu, t1, t2, e1, e2);
+                acc -= e1;
+            }
+            float acc2 = 0.f;
+            if (ix >= 1) acc2 += c2;
+            if (ix + 1 < N) {
+                tvc_bd(tvc_right(c, ob1, lc, l), tvc_right(c, ob2, lc, l), mu, t1, t2, e1, e2);
+                acc2 -= e2;
+            }
+            const float rhs = g[l] - (acc + acc2);
+            S[orr + l] = rhs;
+            S[ort + l] = rhs;
+            S[ox + l] = 0.f;
+            S[oxm + l] = 0.f;
+            n2 = fmaf(rhs, rhs, n2);
+        }
+        tvc_reduce(n2, 0.f, A, B, wsum, red, par, C, rank);
+        if (threadIdx.x == 0) {
+            n2b = sqrt(A);
+            rho = A;  // rt' r of the first step (rt = r = rhs)
+            rho1 = 1.0;
+            normrmin = n2b;
+            bc.flag = n2b > 0.0 ? TVB_RUN : 0;
+            bc.beta = 0.f;
+        }
+        __syncthreads();
+        bool converged = false;
+        if (bc.flag & TVB_RUN) {
+            for (int cit = 0; cit < TV_CG_MAX; ++cit) {
+                ++n_cg;
+                const float beta = bc.beta;
+                {
+                    const int t = op;
+                    op = opo;
+                    opo = t;
+                }
+                if (cit == 0) {
+                    TVC_FOR(c) {
+                        const float rv = S[orr + l];
+                        S[ouc + l] = rv;
+                        S[op + l] = rv;
+                    }
+                } else {
+                    TVC_FOR(c) {
+                        const float qv = S[oq + l];
+                        const float uv = fmaf(beta, qv, S[orr + l]);
+                        S[ouc + l] = uv;
+                        S[op + l] = fmaf(beta, fmaf(beta, S[opo + l], qv), uv);
+                    }
+                }
+                __syncthreads();  // p_new complete in this slab
+                const bool first = cit == 0;
+                const int opo_ = opo;
+                auto halo_p = [=](const float *b, int k) {
+                    const float rv = b[orr + k];
+                    if (first) return rv;
+                    const float qv = b[oq + k];
+                    const float uv = fmaf(beta, qv, rv);
+                    return fmaf(beta, fmaf(beta, b[opo_ + k], qv), uv);
+                };
+                float a_rtvh = 0.f;
+                TVC_FOR(c) {
+                    const float vhv = tvc_M(c, op, lc, l, halo_p);
+                    S[ovh + l] = vhv;
+                    a_rtvh = fmaf(S[ort + l], vhv, a_rtvh);
+                }
+                tvc_reduce(a_rtvh, 0.f, A, B, wsum, red, par, C, rank);
+                if (threadIdx.x == 0) {
+                    if (A == 0.0 || !isfinite(A)) {
+                        bc.flag = TVB_BREAK;
+                    } else {
+                        bc.flag = 0;
+                        bc.alpha = (float)(rho / A);
+                    }
+                }
+                __syncthreads();
+                if (bc.flag & TVB_BREAK) break;
+                const float alpha = bc.alpha;
+                TVC_FOR(c) {
+                    const float uv = S[ouc + l];
+                    const float qq = fmaf(-alpha, S[ovh + l], uv);
+                    S[oq + l] = qq;
+                    const float uh = uv + qq;
+                    S[ouh + l] = uh;
+                    S[ox + l] = fmaf(alpha, uh, S[ox + l]);
+                }
+                __syncthreads();  // uh complete in this slab
+                auto halo_uh = [=](const float *b, int k) {
+                    const float uv = b[ouc + k];
+                    return uv + fmaf(-alpha, b[ovh + k], uv);
+                };
+                float a_rr = 0.f, a_rtr = 0.f;
+                TVC_FOR(c) {
+                    const float rv = fmaf(-alpha, tvc_M(c, ouh, lc, l, halo_uh), S[orr + l]);
+                    S[orr + l] = rv;
+                    a_rr = fmaf(rv, rv, a_rr);
+                    a_rtr = fmaf(S[ort + l], rv, a_rtr);
+                }
+                tvc_reduce(a_rr, a_rtr, A, B, wsum, red, par, C, rank);
+                if (threadIdx.x == 0) {
+                    const double normr = sqrt(A);
+                    int f = 0;
+                    if (normr <= 1e-5 * n2b) {
+                        f = TVB_CONVERGED;
+                    } else {
+                        if (normr < normrmin) {
+                            normrmin = normr;
+                            f |= TVB_IMPROVED;
+                        }
+                        rho1 = rho;
+                        rho = B;  // rt' r of the next step
+                        if (rho == 0.0 || !isfinite(rho))
+                            f |= TVB_BREAK;
+                        else
+                            bc.beta = (float)(rho / rho1);
+                    }
+                    bc.flag = f;
+                }
+                __syncthreads();
+                const int f = bc.flag;
+                if (f & TVB_CONVERGED) {
+                    converged = true;
+                    break;
+                }
+                if (f & TVB_IMPROVED) {
+                    TVC_FOR(c) S[oxm + l] = S[ox + l];
+                }
+                if (f & TVB_BREAK) break;
+            }
+        }
+        if (!converged) {
+            TVC_FOR(c) S[ox + l] = S[oxm + l];
+        }
+        cl.sync();  // new u (in x) complete in every slab
+        // Bub = B u + b ; change of u
+        float dif = 0.f, nrm = 0.f;
+        TVC_FOR(c) {
+            float b1, b2, c1, c2;
+            tvc_bd(S[ob1 + l], S[ob2 + l], mu, b1, b2, c1, c2);
+            const float v = S[ox + l];
+            S[ob1 + l] = (c.zlo ? v - S[ox + l - 1] : 0.f) + b1;
+            S[ob2 + l] = (c.ix0 + lc >= 1 ? v - tvc_left(c, ox, lc, l) : 0.f) + b2;
+            const float e = S[ou + l] - v;
+            dif = fmaf(e, e, dif);
+            nrm = fmaf(v, v, nrm);
+        }
+        tvc_reduce(dif, nrm, A, B, wsum, red, par, C, rank);
+        if (threadIdx.x == 0) bc.flag = (!(B > 0.0) || sqrt(A / B) <= 1e-3) ? TVB_BREAK : 0;
+        __syncthreads();
+        const int t = ou;
+        ou = ox;
+        ox = t;
+        if (bc.flag & TVB_BREAK) break;
+    }
+    float *o = out_all + (size_t)w * N * N + (size_t)c.ix0 * N;
+    TVC_FOR(c) o[l] = S[ou + l];
+    if (rank == 0 && threadIdx.x == 0) {
+        atomicAdd(&g_tv_stats[0], (unsigned long long)n_sweeps);
+        atomicAdd(&g_tv_stats[1], (unsigned long long)n_cg);
+    }
+    cl.sync();  // no CTA leaves while a neighbour may still read its shared memory
+}
+#undef TVC_FOR
 
 // isotropic TV term of pixel i of the N x N image x
 __device__ __forceinline__ float itv_term(const float *x, int i, int N) {
@@ -235,7 +640,7 @@ __device__ __forceinline__ float itv_term(const float *x, int i, int N) {
 enum TvSum { TS_RS = 0, TS_RI, TS_PHI, TS_DX, TS_AS, TS_N };
 
 
-__device__ __forceinline__ void tv_store(double v, double *part, int q, int W, double *sh) {
+__device__ __forceinline__ void tv_store(float v, double *part, int q, int W, double *sh) {
     const double s = tv_block_sum(v, sh);
     if (threadIdx.x == 0) part[((size_t)q * W + blockIdx.y) * gridDim.x + blockIdx.x] = s;
 }
@@ -438,6 +843,95 @@ struct DevBufs {
 
 int blocks_per_instance(int W) { return std::max(1, std::min(64, (4 * 152 + W - 1) / W)); }
 
+// 0: cluster path where it fits, 1: force the global-memory kernel
+std::atomic<int> g_prox_path{0};
+
+// cluster geometry of the shared-memory-resident prox for an N x N image:
+// the smallest cluster whose slab fits two CTAs per SM (portable sizes up to
+// 8), else one CTA per SM (up to 16); none if the image does not fit.
+struct TvcGeom {
+    int C = 0, nloc = 0;
+    size_t smem = 0;
+};
+
+TvcGeom tvc_geometry(int N) {
+    TvcGeom g;
+    if (N > TVC_THREADS) return g;
+    const size_t two_per_sm = 113 * 1024, one_per_sm = 225 * 1024;
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int C = 1; C <= (pass ? 16 : 8); C *= 2) {
+            const int nloc = (N + C - 1) / C;
+            const size_t bytes = (size_t)TVC_NV * nloc * N * sizeof(float);
+            if (bytes <= (pass ? one_per_sm : two_per_sm)) {
+                g.C = C;
+                g.nloc = nloc;
+                g.smem = bytes;
+                return g;
+            }
+        }
+    }
+    return g;
+}
+
+cudaError_t tvc_launch(const TvcGeom &gm, const float *z, const TvState *sv, double mu,
+                       int coupled, float *out, int W, int N, cudaStream_t st, bool &fits) {
+    auto kern = k_tv_prox_cl;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)gm.smem);
+    if (e != cudaSuccess) return e;
+    if (gm.C > 8) {
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) return e;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(W * gm.C));
+    cfg.blockDim = dim3(TVC_THREADS);
+    cfg.dynamicSmemBytes = gm.smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)gm.C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    e = cudaOccupancyMaxActiveClusters(&clusters, kern, &cfg);
+    if (e != cudaSuccess || clusters < 1) {
+        (void)cudaGetLastError();
+        fits = false;
+        return cudaSuccess;
+    }
+    fits = true;
+    ++g_launch_count;
+    return cudaLaunchKernelEx(&cfg, kern, z, sv, mu, coupled, out, N, gm.C, gm.nloc);
+}
+
+// SB_ITV2 of W images: the cluster kernel where it fits, else the
+// global-memory kernel on `work` (TV_NVEC vectors per image)
+
+int tv_prox(const float *z, const TvState *sv, double mu, int coupled, float *out, float *work,
+            int W, int N, cudaStream_t st) {
+    TimedScope ts(KID_TV_PROX, st);
+    const TvcGeom gm = tvc_geometry(N);
+    if (g_prox_path.load() == 0 && gm.C) {
+        bool fits = false;
+        const cudaError_t e = tvc_launch(gm, z, sv, mu, coupled, out, W, N, st, fits);
+        if (e != cudaSuccess) {
+            set_error("tv prox (cluster %d): %s", gm.C, cudaGetErrorString(e));
+            return MSOT_ECUDA;
+        }
+        if (fits) return MSOT_OK;
+    }
+    if (!work) {
+        set_error("tv prox: no workspace for the global-memory path");
+        return MSOT_EINVAL;
+    }
+    KLAUNCH(k_tv_prox<<<W, TV_THREADS, 0, st>>>(z, sv, mu, coupled, out, work, N));
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
+}
+
 // per-instance sums of (a - b)^2 or ITV(a), copied to the host
 int tv_sums(const float *a, const float *b, size_t n, int itv_n, int W, double *part,
             double *dout, std::vector<double> &h, cudaStream_t st) {
@@ -463,14 +957,33 @@ int msot_sb_itv2(const float *d_g, float *d_u, int batch, int n, double mu, void
     cudaStream_t st = (cudaStream_t)stream;
     DevBufs b;
     const size_t P = (size_t)n * n;
-    float *work = b.get<float>((size_t)batch * TV_NVEC * P);
+    float *work = b.get<float>((size_t)batch * TV_NVEC * P);  // global-memory path only
     if (!b.ok) {
         set_error("sb_itv2: device allocation failed");
         return MSOT_ENOMEM;
     }
-    KLAUNCH(k_tv_prox<<<batch, TV_THREADS, 0, st>>>(d_g, nullptr, mu, 1, d_u, work, n));
-    MSOT_LAUNCH_CHECK();
+    int rc = tv_prox(d_g, nullptr, mu, 1, d_u, work, batch, n, st);
+    if (rc) return rc;
     MSOT_CUDA_TRY(cudaStreamSynchronize(st));
+    return MSOT_OK;
+}
+
+int msot_tv_prox_stats(long long *sweeps, long long *cg_steps) {
+    unsigned long long h[2] = {0, 0}, z[2] = {0, 0};
+    MSOT_CUDA_TRY(cudaDeviceSynchronize());
+    MSOT_CUDA_TRY(cudaMemcpyFromSymbol(h, g_tv_stats, sizeof(h)));
+    MSOT_CUDA_TRY(cudaMemcpyToSymbol(g_tv_stats, z, sizeof(z)));
+    if (sweeps) *sweeps = (long long)h[0];
+    if (cg_steps) *cg_steps = (long long)h[1];
+    return MSOT_OK;
+}
+
+int msot_tv_prox_path(int path) {
+    if (path < 0 || path > 1) {
+        set_error("tv_prox_path: 0 (automatic) or 1 (global-memory kernel)");
+        return MSOT_EINVAL;
+    }
+    g_prox_path.store(path);
     return MSOT_OK;
 }
 
@@ -548,11 +1061,7 @@ int msot_rec_nn_with_TV_reg(msot_plan_t plan, const float *d_b, float *d_rec, in
         for (int k = 0; k < sparsa_iter; ++k) {
             TV_CK(apply_transpose(pl, rs, atr, W, st));
             KLAUNCH(k_tv_z<<<grid, TV_RED, 0, st>>>(x, atr, ri, sv, coupled, z, P, sl, sb));
-            {
-                TimedScope ts(KID_TV_PROX, st);
-                KLAUNCH(k_tv_prox<<<W, TV_THREADS, 0, st>>>(z, sv, 0.0, coupled, xn, work, N));
-            }
-            MSOT_LAUNCH_CHECK();
+            TV_CK(tv_prox(z, sv, 0.0, coupled, xn, work, W, N, st));
             KLAUNCH(k_tv_step<<<grid, TV_RED, 0, st>>>(x, xn, ri, dx, sv, coupled, N, sb, W, part));
             MSOT_LAUNCH_CHECK();
             TV_CK(apply_forward(pl, dx, As, W, st));

@@ -28,17 +28,41 @@ def _noisy_blocks(n, W, seed):
     return out
 
 
-@pytest.mark.parametrize("n,mu", [(32, 0.05), (64, 0.1), (50, 0.02)])
+# sizes cover the shared-memory cluster kernel with 1, 2, 4 (ragged last
+# slab), 8 and 16 CTAs per image
+@pytest.mark.parametrize("n,mu", [(32, 0.05), (64, 0.1), (50, 0.02), (90, 0.05), (128, 0.05),
+                                  (200, 0.03)])
 def test_sb_itv2_matches_oracle(cuda, n, mu):
     import torch
     from msot_gb300 import SB_ITV2
-    g = _noisy_blocks(n, 3, 100 + n)
+    W = 3 if n <= 128 else 1
+    g = _noisy_blocks(n, W, 100 + n)
     u = SB_ITV2(torch.tensor(g, dtype=torch.float32), mu).cpu().numpy()
     B, Bt, BtB = S.diff_oper(n)
-    for w in range(3):
+    for w in range(W):
         # images are [nx][nz] (p = ix*nz + iz): the oracle's column-major n x n view
         ref = S.sb_itv2(g[w].T, mu, B, Bt, BtB).reshape(n, n, order="F").T
         assert rel(u[w], ref) <= 1e-3
+
+
+@pytest.mark.parametrize("n", [48, 128])
+def test_sb_itv2_global_memory_kernel(cuda, n):
+    # the fallback for images too large for shared memory, forced at small sizes
+    import torch
+    from msot_gb300 import SB_ITV2, _lib
+    L = _lib.load()
+    g = _noisy_blocks(n, 2, 300 + n)
+    _lib.check(L.msot_tv_prox_path(1))
+    try:
+        u_glob = SB_ITV2(torch.tensor(g, dtype=torch.float32), 0.05).cpu().numpy()
+    finally:
+        _lib.check(L.msot_tv_prox_path(0))
+    u_cl = SB_ITV2(torch.tensor(g, dtype=torch.float32), 0.05).cpu().numpy()
+    B, Bt, BtB = S.diff_oper(n)
+    for w in range(2):
+        ref = S.sb_itv2(g[w].T, 0.05, B, Bt, BtB).reshape(n, n, order="F").T
+        assert rel(u_glob[w], ref) <= 1e-3
+        assert rel(u_cl[w], u_glob[w]) <= 1e-3
 
 
 def test_sb_itv2_zero_mu(cuda):
