@@ -176,6 +176,14 @@ def oracle_solve(model, b_np, threads):
     return rec.reshape(g.nx, g.nz), time.perf_counter() - t0
 
 
+# DRAM bytes (read + write) per launch of each family's kernel at batch 64,
+# from one ncu --set full capture of `bench.py --op --batch 64`
+NCU_TRAFFIC_B64 = {"interp_forward": 49.811712e6 + 85.703936e6,
+                   "interp_adjoint": 77.512192e6 + 3.013888e6,
+                   "ir_conv": 133.145344e6 + 84.419328e6,
+                   "prefilter": 4.203008e6}
+
+
 def algorithmic_bytes(kid_name, batch):
     P, D, T = N_GRID * N_GRID, N_DET, N_T
     if kid_name in ("interp_forward", "interp_adjoint"):
@@ -296,7 +304,8 @@ def run_ours(args, rank, world):
         alg = algorithmic_bytes(name, B)
         ach = alg / avg_s / 1e9 if alg else None
         roof = {"bound": "hbm", "kernel": name, "achieved": ach, "peak": peak, "unit": "GB/s",
-                "frac": ach / peak if ach else None, "traffic": None,
+                "frac": ach / peak if ach else None,
+                "traffic": NCU_TRAFFIC_B64.get(name) if B == 64 else None,
                 "peak_source": f"{peak_kind} hbm_gbs (copy)",
                 "avg_launch_us": avg_s * 1e6, "bytes_per_launch": alg,
                 "families_ms_per_solve": {k: round(v["ms"], 3) for k, v in fam.items()}}
