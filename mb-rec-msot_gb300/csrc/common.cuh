@@ -160,6 +160,25 @@ int interp_forward(const Plan &pl, const float *x_pi, float *raw, int W, float s
 int interp_adjoint(const Plan &pl, const float *raw, float *x, int W, float scale,
                    cudaStream_t st);
 int apply_forward(const Plan &pl, const float *img, float *sino, int W, cudaStream_t st);
+
+// Per-group scalars of the Krylov solvers (one group = one instance, or the
+// whole batch when coupled).
+struct Scal {
+    double alpha, beta, c, s, phibar, normr, normrmin, normb;
+    double rho, thet, phi, gamma;  // gamma = alpha / beta_prev
+    double rho_cg, rho1_cg, alpha_cg;
+    int done, improved, pad0, pad1;
+};
+
+// Forward operator with the LSQR sinogram update fused into the EIR
+// convolution's epilogue (y = A img never stored):
+//   mode 0: u = sl*b - sl*y ; mode 1: u = sl*y - gamma*u (u kept where done)
+// and per-block partial sums of u^2 in part[w * nparts + slot].  Returns 1
+// (nothing launched) when the plan's convolution path cannot fuse it.
+int apply_forward_update(const Plan &pl, const float *img, float *u, const float *b, int W,
+                         int mode, float sl, const Scal *sc, int coupled, double *part,
+                         int *nparts, cudaStream_t st);
+bool forward_update_fusable(const Plan &pl, int W);
 void solver_cache_free(Plan &pl);  // solver.cu
 bool profiling_enabled();          // timing.cu
 int apply_transpose(const Plan &pl, const float *sino, float *img, int W, cudaStream_t st);

@@ -75,6 +75,110 @@ __global__ void k_prefilter(const float *__restrict__ in, float *__restrict__ ou
         out[(size_t)w * P + j] = acc * scale;
 }
 
+// ---------------------------------------------------------------------------
+// Both prefilter axes in one pass through shared memory.  CTA = (tile of TX
+// columns ix, instance w); it stages the columns ix0 - KM .. ix0 + TX + KM - 1
+// (circular) of the image, filters every staged column along z into a second
+// buffer, then filters along x into the TX output columns.  Each thread
+// slides a register window over 8 consecutive outputs, so a tap costs one
+// FMA and (8 + 2 KM) / 8 / (2 KM + 1) shared loads.  Taps are zero-padded to
+// the compile-time half width KM >= K.  out_mode 0 = [W][P], 2 = [P][W].
+// ---------------------------------------------------------------------------
+constexpr int PF_TX = 32, PF_R = 8, PF_THREADS = 256;
+
+__device__ __forceinline__ int wrap_mod(int a, int n) {
+    a %= n;
+    return a < 0 ? a + n : a;
+}
+
+template <int KM>
+__global__ void __launch_bounds__(PF_THREADS) k_prefilter2d(
+    const float *__restrict__ in, float *__restrict__ out, const float *__restrict__ taps_x,
+    const float *__restrict__ taps_z, int Kx, int Kz, int nx, int nz, int W, int transpose,
+    int out_mode) {
+    constexpr int NC = PF_TX + 2 * KM;  // staged columns
+    constexpr int NTAP = 2 * KM + 1;
+    constexpr int NW = PF_THREADS / 32;
+    extern __shared__ float pf_smem[];
+    const int ld = nz | 1;         // odd column stride: lanes over columns hit distinct banks
+    float *A = pf_smem;            // [NC][ld] staged input
+    float *B = A + NC * ld;        // [NC][ld] z-filtered
+    float *hz = B + NC * ld;       // [NTAP] tap for offset k at hz[k + KM]
+    float *hx = hz + NTAP;
+    const int w = blockIdx.y, ix0 = blockIdx.x * PF_TX;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const float *src = in + (size_t)w * nx * nz;
+    for (int k = threadIdx.x; k < NTAP; k += PF_THREADS) {
+        const int o = k - KM;
+        hz[k] = (o >= -Kz && o <= Kz) ? taps_z[transpose ? Kz - o : Kz + o] : 0.f;
+        hx[k] = (o >= -Kx && o <= Kx) ? taps_x[transpose ? Kx - o : Kx + o] : 0.f;
+    }
+    // stage: one warp per column, lanes along z
+    for (int c = warp; c < NC; c += NW) {
+        const float *scol = src + (size_t)wrap_mod(ix0 - KM + c, nx) * nz;
+        float *dcol = A + c * ld;
+        for (int z = lane; z < nz; z += 32) dcol[z] = __ldg(scol + z);
+    }
+    __syncthreads();
+    // z pass, lanes over columns: B[c][z] = sum_k hz[k] A[c][z - k (circular)]
+    const int nzc = (nz + PF_R - 1) / PF_R;
+    constexpr int NCG = (NC + 31) / 32;
+    for (int it = warp; it < NCG * nzc; it += NW) {
+        const int cg = it / nzc, z0 = (it - cg * nzc) * PF_R;
+        const int c = cg * 32 + lane;
+        if (c < NC) {
+            const float *col = A + c * ld;
+            float win[PF_R + 2 * KM];
+#pragma unroll
+            for (int i = 0; i < PF_R + 2 * KM; ++i) {
+                int z = z0 - KM + i;
+                z = (z >= 0 && z < nz) ? z : wrap_mod(z, nz);
+                win[i] = col[z];
+            }
+            float acc[PF_R];
+#pragma unroll
+            for (int j = 0; j < PF_R; ++j) acc[j] = 0.f;
+#pragma unroll
+            for (int k = -KM; k <= KM; ++k) {
+                const float h = hz[k + KM];
+#pragma unroll
+                for (int j = 0; j < PF_R; ++j) acc[j] = fmaf(h, win[j - k + KM], acc[j]);
+            }
+#pragma unroll
+            for (int j = 0; j < PF_R; ++j)
+                if (z0 + j < nz) B[c * ld + z0 + j] = acc[j];
+        }
+    }
+    __syncthreads();
+    // x pass, lanes along z: out[ix0 + c][z] = sum_k hx[k] B[c + KM - k][z]
+    constexpr int NXC = PF_TX / PF_R;
+    for (int it = threadIdx.x; it < NXC * nz; it += PF_THREADS) {
+        const int cc = it / nz, z = it - cc * nz, c0 = cc * PF_R;
+        float win[PF_R + 2 * KM];
+#pragma unroll
+        for (int i = 0; i < PF_R + 2 * KM; ++i) win[i] = B[(c0 + i) * ld + z];
+        float acc[PF_R];
+#pragma unroll
+        for (int j = 0; j < PF_R; ++j) acc[j] = 0.f;
+#pragma unroll
+        for (int k = -KM; k <= KM; ++k) {
+            const float h = hx[k + KM];
+#pragma unroll
+            for (int j = 0; j < PF_R; ++j) acc[j] = fmaf(h, win[j - k + KM], acc[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < PF_R; ++j) {
+            const int ix = ix0 + c0 + j;
+            if (ix >= nx) break;
+            const size_t p = (size_t)ix * nz + z;
+            if (out_mode == 2)
+                out[p * W + w] = acc[j];
+            else
+                out[(size_t)w * nx * nz + p] = acc[j];
+        }
+    }
+}
+
 // [W][P] -> pixel-major [P][W]
 __global__ void k_to_pixmajor(const float *__restrict__ in, float *__restrict__ out, int P,
                               int W) {
@@ -587,15 +691,26 @@ __device__ __forceinline__ void fft32(float2 (&v)[32]) {
     for (int i = 0; i < 32; ++i) v[i] = t[i];
 }
 
+// Epilogue of the convolution for the LSQR sinogram update (EPI 1: u =
+// sl*b - sl*y, EPI 2: u = sl*y - gamma*u) with per-CTA partial sums of u^2.
+struct ConvEpi {
+    const float *b;
+    const Scal *sc;
+    float sl;
+    int coupled, D, nparts;
+    double *part;
+};
+
 // 1024-point overlap-save convolution by the four-step FFT 1024 = 32 x 32:
 // one warp per transform (two real columns), 32-point FFTs in registers and
 // two warp-local transposes through padded shared memory per direction.
-template <int FPC>
+// EPI != 0 requires every CTA's columns to lie in one instance.
+template <int FPC, int EPI = 0>
 __global__ void __launch_bounds__(32 * FPC) k_conv_fft1k(const float *__restrict__ in,
                                                          float *__restrict__ out,
                                                          const float2 *__restrict__ tw,
                                                          const float2 *__restrict__ H, int C,
-                                                         int T, int L) {
+                                                         int T, int L, ConvEpi epi = {}) {
     __shared__ float2 S[FPC][32][33];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int pair = blockIdx.y * FPC + warp;
@@ -641,13 +756,71 @@ __global__ void __launch_bounds__(32 * FPC) k_conv_fft1k(const float *__restrict
     for (int k1 = 0; k1 < 32; ++k1) v[k1] = Sw[lane][k1];
     fft32<1>(v);  // over k1, this lane is n1': v[n2'] = y[n1' + 32 n2']
     float *y1 = out + (size_t)c1 * T, *y2 = out + (size_t)c2 * T;
+    if constexpr (EPI == 0) {
 #pragma unroll
-    for (int n2 = 0; n2 < 32; ++n2) {
-        const int n = lane + 32 * n2;
-        const int t = t0 + n - (L - 1);
-        if (n >= L - 1 && t < T) {
-            y1[t] = v[n2].x;
-            if (has2) y2[t] = v[n2].y;
+        for (int n2 = 0; n2 < 32; ++n2) {
+            const int n = lane + 32 * n2;
+            const int t = t0 + n - (L - 1);
+            if (n >= L - 1 && t < T) {
+                y1[t] = v[n2].x;
+                if (has2) y2[t] = v[n2].y;
+            }
+        }
+    } else {
+        const int w = c1 / epi.D;
+        const Scal &q = epi.sc[epi.coupled ? 0 : w];
+        const float g = (float)q.gamma, sl = epi.sl;
+        const bool done = EPI == 2 && q.done;
+        const float *b1 = epi.b + (size_t)c1 * T, *b2 = epi.b + (size_t)c2 * T;
+        float acc = 0.f;
+        // chunks of 8 outputs: all loads of a chunk are issued before its
+        // stores (the stores could alias the loads of later iterations)
+        constexpr int CH = 8;
+#pragma unroll
+        for (int c0 = 0; c0 < 32; c0 += CH) {
+            float l1[CH], l2[CH];
+#pragma unroll
+            for (int j = 0; j < CH; ++j) {
+                const int n = lane + 32 * (c0 + j);
+                const int t = t0 + n - (L - 1);
+                const bool ok = n >= L - 1 && t < T;
+                const float *s1 = EPI == 1 ? b1 : y1, *s2 = EPI == 1 ? b2 : y2;
+                l1[j] = ok ? s1[t] : 0.f;
+                l2[j] = (ok && has2) ? s2[t] : 0.f;
+            }
+#pragma unroll
+            for (int j = 0; j < CH; ++j) {
+                const int n2 = c0 + j;
+                const int n = lane + 32 * n2;
+                const int t = t0 + n - (L - 1);
+                if (n >= L - 1 && t < T) {
+                    float a, bb;
+                    if (EPI == 1) {
+                        a = fmaf(sl, l1[j], -sl * v[n2].x);
+                        bb = has2 ? fmaf(sl, l2[j], -sl * v[n2].y) : 0.f;
+                    } else {
+                        a = done ? l1[j] : fmaf(sl, v[n2].x, -g * l1[j]);
+                        bb = done ? l2[j] : fmaf(sl, v[n2].y, -g * l2[j]);
+                    }
+                    y1[t] = a;
+                    if (has2) y2[t] = bb;
+                    acc = fmaf(a, a, acc);
+                    acc = fmaf(bb, bb, acc);
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        __shared__ float wacc[FPC];
+        if (lane == 0) wacc[warp] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double sum = 0.0;
+#pragma unroll
+            for (int k = 0; k < FPC; ++k) sum += (double)wacc[k];
+            const int per_inst = epi.D / (2 * FPC);  // CTAs (along y) per instance
+            const int slot = (blockIdx.y - w * per_inst) * gridDim.x + blockIdx.x;
+            epi.part[(size_t)w * epi.nparts + slot] = sum;
         }
     }
 }
@@ -732,6 +905,33 @@ int launch_prefilter(const Plan &pl, const float *in, float *out, int W, bool tr
         in, out, taps, K, pl.nx, pl.nz, W, along_x, transpose, scale, pl.perm, out_mode));
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
+}
+
+// both axes in one launch where the staged tile fits shared memory; returns
+// 1 (nothing launched) when the caller must use the per-axis kernels
+template <int KM>
+static int prefilter2d_km(const Plan &pl, const float *in, float *out, int W, bool transpose,
+                          int out_mode, cudaStream_t st) {
+    constexpr int NC = PF_TX + 2 * KM;
+    const size_t smem = (size_t)(2 * NC * (pl.nz | 1) + 2 * (2 * KM + 1)) * sizeof(float);
+    if (smem > 200 * 1024) return 1;
+    MSOT_CUDA_TRY(cudaFuncSetAttribute(k_prefilter2d<KM>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const dim3 grid((unsigned)((pl.nx + PF_TX - 1) / PF_TX), (unsigned)W);
+    KLAUNCH(k_prefilter2d<KM><<<grid, PF_THREADS, smem, st>>>(
+        in, out, pl.pre_x, pl.pre_z, pl.Kx, pl.Kz, pl.nx, pl.nz, W, transpose ? 1 : 0, out_mode));
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
+}
+
+int launch_prefilter2d(const Plan &pl, const float *in, float *out, int W, bool transpose,
+                       int out_mode, cudaStream_t st) {
+    if (pl.Kx < 0 || pl.Kz < 0 || (out_mode != 0 && out_mode != 2)) return 1;
+    TimedScope ts_(KID_PREFILTER, st);
+    const int K = std::max(pl.Kx, pl.Kz);
+    if (K <= 8) return prefilter2d_km<8>(pl, in, out, W, transpose, out_mode, st);
+    if (K <= 16) return prefilter2d_km<16>(pl, in, out, W, transpose, out_mode, st);
+    return 1;
 }
 
 int launch_permute(const Plan &pl, const float *in, float *out, int W, cudaStream_t st) {
@@ -919,6 +1119,8 @@ int launch_sir_adjoint(const Plan &pl, const float *raw, float *x, int W, float 
     return sir_adj_nt<1>(pl, raw, x, scale, grid, st);
 }
 
+constexpr int CONV_FPC = 4;
+
 int launch_conv(const Plan &pl, const float *in, float *out, int W, bool transpose,
                 cudaStream_t st) {
     TimedScope ts_(KID_CONV, st);
@@ -930,7 +1132,7 @@ int launch_conv(const Plan &pl, const float *in, float *out, int W, bool transpo
         const size_t smem = 2 * (size_t)N * sizeof(float2);
         int rc;
         if (pl.fft_log4n == 5) {
-            constexpr int FPC = 4;
+            constexpr int FPC = CONV_FPC;
             dim3 g1(div_up(pl.T, V), div_up(div_up(C, 2), FPC));
             KLAUNCH(k_conv_fft1k<FPC><<<g1, 32 * FPC, 0, st>>>(in, out, pl.fft_tw, H, C, pl.T,
                                                                pl.L));
@@ -955,6 +1157,13 @@ int launch_conv(const Plan &pl, const float *in, float *out, int W, bool transpo
     return MSOT_OK;
 }
 
+bool forward_update_fusable(const Plan &pl, int W) {
+    if (pl.L <= 0 || pl.fft_log4n != 5 || pl.D % (2 * CONV_FPC) != 0) return false;
+    const int V = 1024 - pl.L + 1;
+    const int nparts = (pl.D / (2 * CONV_FPC)) * div_up(pl.T, V);
+    return nparts <= 256 && W >= 1;
+}
+
 // ---------------------------------------------------------------------------
 // chains
 // ---------------------------------------------------------------------------
@@ -970,11 +1179,19 @@ int interp_adjoint(const Plan &pl, const float *raw, float *x, int W, float scal
                 : launch_das_adjoint(pl, raw, x, W, scale, st);
 }
 
+static int forward_to_raw(const Plan &pl, const float *img, int W, cudaStream_t st);
+
 int apply_forward(const Plan &pl, const float *img, float *sino, int W, cudaStream_t st) {
     int rc;
+    if (pl.L > 0) {
+        if ((rc = forward_to_raw(pl, img, W, st))) return rc;
+        return launch_conv(pl, pl.scr_sino, sino, W, false, st);
+    }
     float *xpi = pl.scr_img1;
     const int mode = pl.S ? 1 : 2;  // scatter order (SIR) or pixel-major (bucket moments)
-    if (pl.Kz >= 0 && pl.Kx >= 0) {
+    if ((rc = launch_prefilter2d(pl, img, xpi, W, false, mode, st)) <= 0) {
+        if (rc) return rc;
+    } else if (pl.Kz >= 0 && pl.Kx >= 0) {
         if ((rc = launch_prefilter(pl, img, pl.scr_img0, W, false, false, 1.f, 0, st)))
             return rc;
         if ((rc = launch_prefilter(pl, pl.scr_img0, xpi, W, false, true, 1.f, mode, st)))
@@ -988,11 +1205,60 @@ int apply_forward(const Plan &pl, const float *img, float *sino, int W, cudaStre
     } else {
         if ((rc = launch_to_pixmajor(pl, img, xpi, W, st))) return rc;
     }
-    if (pl.L > 0) {
-        if ((rc = interp_forward(pl, xpi, pl.scr_sino, W, 1.f, st))) return rc;
-        return launch_conv(pl, pl.scr_sino, sino, W, false, st);
-    }
     return interp_forward(pl, xpi, sino, W, pl.scale, st);
+}
+
+// prefilter + interpolation into the plan's sinogram scratch (the
+// convolution's input); shared by apply_forward and apply_forward_update
+static int forward_to_raw(const Plan &pl, const float *img, int W, cudaStream_t st) {
+    int rc;
+    float *xpi = pl.scr_img1;
+    const int mode = pl.S ? 1 : 2;
+    if ((rc = launch_prefilter2d(pl, img, xpi, W, false, mode, st)) <= 0) {
+        if (rc) return rc;
+    } else if (pl.Kz >= 0 && pl.Kx >= 0) {
+        if ((rc = launch_prefilter(pl, img, pl.scr_img0, W, false, false, 1.f, 0, st)))
+            return rc;
+        if ((rc = launch_prefilter(pl, pl.scr_img0, xpi, W, false, true, 1.f, mode, st)))
+            return rc;
+    } else if (pl.Kz >= 0) {
+        if ((rc = launch_prefilter(pl, img, xpi, W, false, false, 1.f, mode, st))) return rc;
+    } else if (pl.Kx >= 0) {
+        if ((rc = launch_prefilter(pl, img, xpi, W, false, true, 1.f, mode, st))) return rc;
+    } else if (pl.S) {
+        if ((rc = launch_permute(pl, img, xpi, W, st))) return rc;
+    } else {
+        if ((rc = launch_to_pixmajor(pl, img, xpi, W, st))) return rc;
+    }
+    return interp_forward(pl, xpi, pl.scr_sino, W, 1.f, st);
+}
+
+int apply_forward_update(const Plan &pl, const float *img, float *u, const float *b, int W,
+                         int mode, float sl, const Scal *sc, int coupled, double *part,
+                         int *nparts, cudaStream_t st) {
+    if (!forward_update_fusable(pl, W)) return 1;
+    int rc;
+    if ((rc = forward_to_raw(pl, img, W, st))) return rc;
+    TimedScope ts_(KID_CONV, st);
+    const int C = W * pl.D, V = 1024 - pl.L + 1;
+    const dim3 g1(div_up(pl.T, V), div_up(div_up(C, 2), CONV_FPC));
+    ConvEpi e;
+    e.b = b;
+    e.sc = sc;
+    e.sl = sl;
+    e.coupled = coupled;
+    e.D = pl.D;
+    e.nparts = (pl.D / (2 * CONV_FPC)) * (int)g1.x;
+    e.part = part;
+    *nparts = e.nparts;
+    if (mode == 0)
+        KLAUNCH(k_conv_fft1k<CONV_FPC, 1><<<g1, 32 * CONV_FPC, 0, st>>>(
+            pl.scr_sino, u, pl.fft_tw, pl.fft_hf, C, pl.T, pl.L, e));
+    else
+        KLAUNCH(k_conv_fft1k<CONV_FPC, 2><<<g1, 32 * CONV_FPC, 0, st>>>(
+            pl.scr_sino, u, pl.fft_tw, pl.fft_hf, C, pl.T, pl.L, e));
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
 }
 
 int apply_transpose(const Plan &pl, const float *sino, float *img, int W, cudaStream_t st) {
@@ -1007,6 +1273,7 @@ int apply_transpose(const Plan &pl, const float *sino, float *img, int W, cudaSt
     const bool pre = pl.Kx >= 0 || pl.Kz >= 0;
     float *x = pre ? pl.scr_img0 : img;
     if ((rc = interp_adjoint(pl, src, x, W, scale, st))) return rc;
+    if ((rc = launch_prefilter2d(pl, pl.scr_img0, img, W, true, 0, st)) <= 0) return rc;
     if (pl.Kx >= 0 && pl.Kz >= 0) {
         if ((rc = launch_prefilter(pl, pl.scr_img0, pl.scr_img1, W, true, true, 1.f, 0, st)))
             return rc;

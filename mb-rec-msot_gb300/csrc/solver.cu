@@ -24,13 +24,6 @@ namespace msot {
 
 constexpr int RED_THREADS = 256;
 
-struct Scal {
-    double alpha, beta, c, s, phibar, normr, normrmin, normb;
-    double rho, thet, phi, gamma;  // gamma = alpha / beta_prev
-    double rho_cg, rho1_cg, alpha_cg;
-    int done, improved, pad0, pad1;
-};
-
 __device__ __forceinline__ double block_sum(double v) {
     __shared__ double sh[RED_THREADS / 32];
     __syncthreads();  // sh may still be read by a previous call
@@ -168,33 +161,42 @@ __global__ void k_l2_v_img(const float *__restrict__ atu, const float *__restric
     STORE_PARTIAL((double)acc, part);
 }
 
-__device__ double sum_parts(const double *part, int nblk, int w) {
-    double s = 0.0;
-    for (int b = 0; b < nblk; ++b) s += part[(size_t)w * nblk + b];
-    return s;
-}
-
+// Sum of the partials of group g, computed by the whole warp (lane-strided,
+// then a butterfly): every lane returns the same value.  The scalar kernels
+// below give each warp a group and let lane 0 run the scalar logic; a
+// thread-serial FP64 sum over hundreds of partials is slow on GB300.
 __device__ double group_sum(const double *p1, int n1, const double *p2, int n2, int g,
                             int W, int coupled) {
+    const int lane = threadIdx.x & 31;
     double s = 0.0;
     const int w0 = coupled ? 0 : g, w1 = coupled ? W : g + 1;
     for (int w = w0; w < w1; ++w) {
-        if (p1) s += sum_parts(p1, n1, w);
-        if (p2) s += sum_parts(p2, n2, w);
+        if (p1)
+            for (int b = lane; b < n1; b += 32) s += p1[(size_t)w * n1 + b];
+        if (p2)
+            for (int b = lane; b < n2; b += 32) s += p2[(size_t)w * n2 + b];
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     return s;
 }
+
+#define FOR_GROUP_WARP(G)                                                                  \
+    for (int g = (int)(threadIdx.x >> 5); g < (G); g += (int)(blockDim.x >> 5))
+#define LANE0_ONLY                                                                         \
+    if ((threadIdx.x & 31) != 0) continue
 
 // stage 0: beta after init; stage 1: alpha (init or step); stage 2: LSQR step scalars
 __global__ void k_l2_scalar(Scal *sc, int stage, const double *p1, int n1, const double *p2,
                             int n2, const double *p3, int n3, const double *normb2_sino,
                             double sl, double sb, int W, int coupled, double tol) {
     const int G = coupled ? 1 : W;
-    for (int g = threadIdx.x; g < G; g += blockDim.x) {
+    FOR_GROUP_WARP(G) {
         Scal &q = sc[g];
         if (stage == 0) {
             const double b2 = group_sum(p1, n1, p2, n2, g, W, coupled);
             const double wv2 = group_sum(p3, n3, nullptr, 0, g, W, coupled);
+            LANE0_ONLY;
             q.normb = sqrt(sl * sl * normb2_sino[g] + sb * sb * wv2);
             q.beta = sqrt(b2);
             q.normr = q.beta;
@@ -206,12 +208,14 @@ __global__ void k_l2_scalar(Scal *sc, int stage, const double *p1, int n1, const
             q.improved = 0;
         } else if (stage == 1) {
             const double a2 = group_sum(p1, n1, nullptr, 0, g, W, coupled);
+            LANE0_ONLY;
             if (!q.done) {
                 q.alpha = sqrt(a2);
                 if (!(q.alpha > 0.0) || !isfinite(q.alpha)) q.done = 1;
             }
         } else {
             const double b2 = group_sum(p1, n1, p2, n2, g, W, coupled);
+            LANE0_ONLY;
             q.improved = 0;
             if (q.done) continue;
             const double beta = sqrt(b2);
@@ -305,8 +309,10 @@ __global__ void k_fill(float *__restrict__ b, float v, size_t n) {
 
 __global__ void k_group_sums(const double *part, int nblk, int W, int coupled, double *out) {
     const int G = coupled ? 1 : W;
-    for (int g = threadIdx.x; g < G; g += blockDim.x)
-        out[g] = group_sum(part, nblk, nullptr, 0, g, W, coupled);
+    FOR_GROUP_WARP(G) {
+        const double v = group_sum(part, nblk, nullptr, 0, g, W, coupled);
+        if ((threadIdx.x & 31) == 0) out[g] = v;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -381,7 +387,7 @@ static int group_sumsq(const Ctx &c, const float *x, const float *y, size_t N, i
                        std::vector<double> &out) {
     KLAUNCH(k_sumsq<<<dim3(nb, c.W), RED_THREADS, 0, c.st>>>(x, y, N / c.W, c.P(3)));
     MSOT_LAUNCH_CHECK();
-    KLAUNCH(k_group_sums<<<1, 256, 0, c.st>>>(c.P(3), nb, c.W, c.coupled, c.wk.gsum));
+    KLAUNCH(k_group_sums<<<1, 1024, 0, c.st>>>(c.P(3), nb, c.W, c.coupled, c.wk.gsum));
     MSOT_LAUNCH_CHECK();
     const int G = c.coupled ? 1 : c.W;
     out.resize(G);
@@ -403,30 +409,46 @@ static int l2_outer(const Ctx &c, const float *b, float *wv, float *vm, double s
     const dim3 gs(c.nbs, c.W), gi(c.nbi, c.W);
     const int G = c.coupled ? 1 : c.W;
     cudaStream_t st = c.st;
+    // The sinogram part of u is updated inside the forward operator's
+    // convolution where the plan allows it (no A v round trip through HBM);
+    // nps = partial sums per instance that the update leaves in P(0).
+    const bool fuse = forward_update_fusable(c.pl, c.W);
+    int nps = c.nbs;
     // init: u = b_aug - A_aug w
-    TRY(apply_forward(c.pl, wv, tmp_s, c.W, st));
-    KLAUNCH(k_sino_update<<<gs, RED_THREADS, 0, st>>>(tmp_s, b, us, ns, 0, sl, k.sc, c.coupled, c.P(0)));
+    if (fuse) {
+        TRY(apply_forward_update(c.pl, wv, us, b, c.W, 0, (float)sl, k.sc, c.coupled, c.P(0),
+                                 &nps, st));
+    } else {
+        TRY(apply_forward(c.pl, wv, tmp_s, c.W, st));
+        KLAUNCH(k_sino_update<<<gs, RED_THREADS, 0, st>>>(tmp_s, b, us, ns, 0, sl, k.sc,
+                                                          c.coupled, c.P(0)));
+    }
     KLAUNCH(k_l2_init_img<<<gi, RED_THREADS, 0, st>>>(wv, vm, ur, ub, ni, sl, sr, sb, has_reg, c.P(1),
                                               c.P(2)));
-    KLAUNCH(k_l2_scalar<<<1, 256, 0, st>>>(k.sc, 0, c.P(0), c.nbs, c.P(1), c.nbi, c.P(2), c.nbi, normb2,
+    KLAUNCH(k_l2_scalar<<<1, 1024, 0, st>>>(k.sc, 0, c.P(0), nps, c.P(1), c.nbi, c.P(2), c.nbi, normb2,
                                    sl, sb, c.W, c.coupled, 1e-8));
     MSOT_LAUNCH_CHECK();
     // v = A_aug^T u / beta
     TRY(apply_transpose(c.pl, us, tmp_i, c.W, st));
     KLAUNCH(k_l2_v_img<<<gi, RED_THREADS, 0, st>>>(tmp_i, ur, ub, v, ni, sl, sr, sb, has_reg, 1, k.sc,
                                            c.coupled, c.P(1)));
-    KLAUNCH(k_l2_scalar<<<1, 256, 0, st>>>(k.sc, 1, c.P(1), c.nbi, nullptr, 0, nullptr, 0, nullptr, sl,
+    KLAUNCH(k_l2_scalar<<<1, 1024, 0, st>>>(k.sc, 1, c.P(1), c.nbi, nullptr, 0, nullptr, 0, nullptr, sl,
                                    sb, c.W, c.coupled, 1e-8));
     KLAUNCH(k_l2_scale_v<<<gi, RED_THREADS, 0, st>>>(v, d, x, xmin, wv, ni, 1, k.sc, c.coupled));
     MSOT_LAUNCH_CHECK();
     for (int it = 0; it < 2; ++it) {
         KLAUNCH(k_l2_gamma<<<1, 256, 0, st>>>(k.sc, G));
-        TRY(apply_forward(c.pl, v, tmp_s, c.W, st));
-        KLAUNCH(k_sino_update<<<gs, RED_THREADS, 0, st>>>(tmp_s, nullptr, us, ns, 1, sl, k.sc,
-                                                  c.coupled, c.P(0)));
+        if (fuse) {
+            TRY(apply_forward_update(c.pl, v, us, nullptr, c.W, 1, (float)sl, k.sc, c.coupled,
+                                     c.P(0), &nps, st));
+        } else {
+            TRY(apply_forward(c.pl, v, tmp_s, c.W, st));
+            KLAUNCH(k_sino_update<<<gs, RED_THREADS, 0, st>>>(tmp_s, nullptr, us, ns, 1, sl, k.sc,
+                                                              c.coupled, c.P(0)));
+        }
         KLAUNCH(k_l2_u_img<<<gi, RED_THREADS, 0, st>>>(v, ur, ub, ni, sl, sr, sb, has_reg, k.sc,
                                                c.coupled, c.P(1)));
-        KLAUNCH(k_l2_scalar<<<1, 256, 0, st>>>(k.sc, 2, c.P(0), c.nbs, c.P(1), c.nbi, nullptr, 0,
+        KLAUNCH(k_l2_scalar<<<1, 1024, 0, st>>>(k.sc, 2, c.P(0), nps, c.P(1), c.nbi, nullptr, 0,
                                        nullptr, sl, sb, c.W, c.coupled, 1e-8));
         KLAUNCH(k_l2_dx<<<gi, RED_THREADS, 0, st>>>(v, d, x, xmin, ni, k.sc, c.coupled));
         KLAUNCH(k_l2_mark_converged<<<1, 256, 0, st>>>(k.sc, G));
@@ -435,7 +457,7 @@ static int l2_outer(const Ctx &c, const float *b, float *wv, float *vm, double s
         TRY(apply_transpose(c.pl, us, tmp_i, c.W, st));
         KLAUNCH(k_l2_v_img<<<gi, RED_THREADS, 0, st>>>(tmp_i, ur, ub, v, ni, sl, sr, sb, has_reg, 0,
                                                k.sc, c.coupled, c.P(1)));
-        KLAUNCH(k_l2_scalar<<<1, 256, 0, st>>>(k.sc, 1, c.P(1), c.nbi, nullptr, 0, nullptr, 0, nullptr,
+        KLAUNCH(k_l2_scalar<<<1, 1024, 0, st>>>(k.sc, 1, c.P(1), c.nbi, nullptr, 0, nullptr, 0, nullptr,
                                        sl, sb, c.W, c.coupled, 1e-8));
         KLAUNCH(k_l2_scale_v<<<gi, RED_THREADS, 0, st>>>(v, d, x, xmin, wv, ni, 0, k.sc, c.coupled));
         MSOT_LAUNCH_CHECK();
@@ -532,7 +554,7 @@ static int solve_l2(Plan &pl, const float *b_in, float *rec, int W, int num_iter
         KLAUNCH(k_fill<<<256, 256, 0, st>>>(vm, 0.f, NI));
         // ||b||^2 per group enters ||b_aug|| of lsqr's tolerance test
         KLAUNCH(k_sumsq<<<dim3(c.nbs, W), RED_THREADS, 0, st>>>(b, nullptr, NS / W, c.P(3)));
-        KLAUNCH(k_group_sums<<<1, 256, 0, st>>>(c.P(3), c.nbs, W, coupled, wk.gsum));
+        KLAUNCH(k_group_sums<<<1, 1024, 0, st>>>(c.P(3), c.nbs, W, coupled, wk.gsum));
         if (cudaGetLastError() != cudaSuccess) {
             set_error("solver: launch failed");
             rc = MSOT_ECUDA;
@@ -649,9 +671,10 @@ __global__ void k_l1_rhs(const float *u, const float *bp, const float *atb, floa
 __global__ void k_cgs_scalar(Scal *sc, int stage, const double *p, int nb, int W, int coupled,
                              double tol) {
     const int G = coupled ? 1 : W;
-    for (int g = threadIdx.x; g < G; g += blockDim.x) {
+    FOR_GROUP_WARP(G) {
         Scal &q = sc[g];
         const double v = group_sum(p, nb, nullptr, 0, g, W, coupled);
+        LANE0_ONLY;
         if (stage == 0) {
             q.normb = sqrt(v);
             q.normr = q.normb;
@@ -818,19 +841,19 @@ static int solve_l1(const Plan &pl, const float *b, float *rec, int W, int num_i
         for (int it = 0; it < num_iter && rc == MSOT_OK; ++it) {
             KLAUNCH(k_l1_rhs<<<gi, RED_THREADS, 0, st>>>(u, bp, atb, dv, rhs, x, r, rt, xmin, ni, lam, eta,
                                                  c.P(0)));
-            KLAUNCH(k_cgs_scalar<<<1, 256, 0, st>>>(wk.sc, 0, c.P(0), c.nbi, W, coupled, 1e-8));
+            KLAUNCH(k_cgs_scalar<<<1, 1024, 0, st>>>(wk.sc, 0, c.P(0), c.nbi, W, coupled, 1e-8));
             for (int ci = 0; ci < 2 && rc == MSOT_OK; ++ci) {
                 KLAUNCH(k_dot<<<gi, RED_THREADS, 0, st>>>(rt, r, ni, c.P(0)));
-                KLAUNCH(k_cgs_scalar<<<1, 256, 0, st>>>(wk.sc, 1, c.P(0), c.nbi, W, coupled, 1e-8));
+                KLAUNCH(k_cgs_scalar<<<1, 1024, 0, st>>>(wk.sc, 1, c.P(0), c.nbi, W, coupled, 1e-8));
                 KLAUNCH(k_cgs_dir<<<gi, RED_THREADS, 0, st>>>(r, q, uc, p, ni, ci == 0, wk.sc, coupled));
                 if ((rc = normal_op(c, p, atmp))) break;
                 KLAUNCH(k_cgs_op<<<gi, RED_THREADS, 0, st>>>(atmp, p, vh, rt, ni, lam, c.P(0)));
-                KLAUNCH(k_cgs_scalar<<<1, 256, 0, st>>>(wk.sc, 2, c.P(0), c.nbi, W, coupled, 1e-8));
+                KLAUNCH(k_cgs_scalar<<<1, 1024, 0, st>>>(wk.sc, 2, c.P(0), c.nbi, W, coupled, 1e-8));
                 KLAUNCH(k_cgs_upd<<<gi, RED_THREADS, 0, st>>>(uc, vh, q, uh, x, ni, wk.sc, coupled));
                 if ((rc = normal_op(c, uh, atmp))) break;
                 KLAUNCH(k_cgs_res<<<gi, RED_THREADS, 0, st>>>(atmp, uh, r, ni, lam, wk.sc, coupled,
                                                       c.P(0)));
-                KLAUNCH(k_cgs_scalar<<<1, 256, 0, st>>>(wk.sc, 3, c.P(0), c.nbi, W, coupled, 1e-8));
+                KLAUNCH(k_cgs_scalar<<<1, 1024, 0, st>>>(wk.sc, 3, c.P(0), c.nbi, W, coupled, 1e-8));
                 KLAUNCH(k_cgs_keep<<<gi, RED_THREADS, 0, st>>>(x, xmin, ni, wk.sc, coupled));
                 KLAUNCH(k_cgs_mark<<<1, 256, 0, st>>>(wk.sc, G));
             }
