@@ -108,6 +108,16 @@ int msot_interp_transpose(msot_plan_t plan, const float *d_raw, float *d_coeffs,
 int msot_interp_transpose_noalloc(msot_plan_t plan, const float *d_raw, float *d_coeffs,
                                   int batch, void *stream);
 
+/* Travel-time table of a single speed of sound on the GPU (FP64):
+ * MSOTmodel.m:350-382 with calculate_travel_time's straight rays and the arc
+ * detector positions of Probe.m:112-116.  x (nx) and z (nz) are the pixel
+ * coordinate vectors (Discretization.m:34); travel receives host
+ * [n_det][nx*nz] = |x_p - x_d| / c * fs - delay - n_crop, the layout
+ * msot_plan_desc.travel takes.  Synchronous. */
+int msot_travel_times(int n_det, double radius, double coverage_deg, const double *x, int nx,
+                      const double *z, int nz, double c, double fs, double delay, double n_crop,
+                      double *travel);
+
 /* Estimate sigma_max of the unnormalised operator by power iteration on the
  * GPU (replaces the svds call, MSOTmodel.m:277-278); FP64 norms. */
 int msot_estimate_norm(msot_plan_t plan, int iters, uint64_t seed, double *sigma_max,

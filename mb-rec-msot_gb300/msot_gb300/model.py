@@ -179,6 +179,21 @@ class _Funcs:
         self.applyTranspose = model.transpose
 
 
+def travel_times(probe: Probe, disc: Discretization, c: float, n_crop: int = 0) -> np.ndarray:
+    """[n_det][nx*nz] FP64 fractional sample indices |x_p - x_d| / c * fs -
+    delay - n_crop (MSOTmodel.m:350-382, single speed of sound), computed by
+    msot_travel_times on the GPU."""
+    out = np.empty((probe.n_det, disc.nx * disc.nz), dtype=np.float64)
+    x = np.ascontiguousarray(disc.x, dtype=np.float64)
+    z = np.ascontiguousarray(disc.z, dtype=np.float64)
+    P = C.POINTER(C.c_double)
+    _lib.check(_lib.load().msot_travel_times(
+        int(probe.n_det), float(probe.radius), float(probe.angular_coverage),
+        x.ctypes.data_as(P), x.size, z.ctypes.data_as(P), z.size, float(c), float(probe.fs),
+        float(probe.delay), float(n_crop), out.ctypes.data_as(P)))
+    return out
+
+
 class MSOTmodel:
     """MSOTmodel(probe, discretization, speed_of_sound, include_sir,
     use_single_speed_of_sound, num_cropped_samples_at_sinogram_start,
@@ -204,11 +219,9 @@ class MSOTmodel:
         self.n_t = int(probe.n_samples - self.n_crop)
         self.max_batch = int(max_batch)
         disc = discretization
-        # travel-time indices (MSOTmodel.m:380-381; straight rays, refraction.m:327)
-        xd, zd = probe.detector_positions()
-        xp, zp = disc.pixel_coordinates()
-        dist = np.hypot(xd[:, None] - xp[None, :], zd[:, None] - zp[None, :])
-        self.travel = np.ascontiguousarray(dist / self.c * probe.fs - probe.delay - self.n_crop)
+        # travel-time indices (MSOTmodel.m:380-381; straight rays, refraction.m:327),
+        # computed on the GPU in FP64
+        self.travel = travel_times(probe, disc, self.c, self.n_crop)
         # interpolation radius (MSOTmodel.m:36-38)
         self.radius = float(disc.dz / (self.c / probe.fs))
         self.ir = np.ascontiguousarray(

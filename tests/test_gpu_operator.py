@@ -165,3 +165,14 @@ def test_norm_estimate_matches_oracle(cuda):
     s_gpu = pm.estimate_sigma_max(200)
     s_ref = M.estimate_sigma_max(om.forward, om.transpose, (1, 64, 64), iters=200)
     assert abs(s_gpu - s_ref) / s_ref < 1e-4
+
+
+def test_travel_times_on_gpu_match_oracle(cuda):
+    # MSOTmodel.m:350-382 (single speed of sound) in FP64 on the GPU
+    from msot_gb300 import Discretization, Probe
+    from msot_gb300.model import travel_times
+    for n, crop in ((128, 0), (57, 3)):
+        tau = travel_times(Probe(), Discretization([-0.0127, 0.0127], n), 1500.0, crop)
+        ref = M.travel_time_indices(M.config1_probe(), M.config_grid(n), 1500.0, crop)
+        assert tau.shape == ref.shape
+        assert np.max(np.abs(tau - ref)) <= 1e-12 * np.max(np.abs(ref))
