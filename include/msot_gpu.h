@@ -118,6 +118,44 @@ int msot_travel_times(int n_det, double radius, double coverage_deg, const doubl
                       const double *z, int nz, double c, double fs, double delay, double n_crop,
                       double *travel);
 
+/* Spatial pixel model response (SPMR) tables for include_sir plans, the
+ * role of calculate_polarSPMR.m:21-184 + MSOTmodel.m:463-480 (2-D, single
+ * speed of sound).  The reference obtains the element's spatial impulse
+ * response from Field II (not available); here it is the Rayleigh integral
+ * over sub_x x sub_y point sources on the element.  The rest follows the
+ * reference: N-shape pixel response and order-8 Butterworth low pass at fs/2
+ * at 5 GHz, DAC-rate sampling around the travel time, 1e-4 zeroing,
+ * start/end samples, common crop, and the pixel -> column index of
+ * MSOTmodel.m:472-477.  Outputs match msot_plan_desc's sir / sir_start_end /
+ * sir_idx. */
+typedef struct msot_spmr_spec {
+    int n_det;                  /* arc array (Probe.m:112-116) */
+    double radius, coverage_deg;
+    const double *x;            /* host pixel coordinate vectors, nx and nz entries */
+    int nx;
+    const double *z;
+    int nz;
+    double c, fs;               /* speed of sound [m/s], DAC sampling rate [Hz] */
+    double pixel_sigma;         /* Gaussian pixel model sigma [m] (Discretization.m:43) */
+    double elem_width, elem_height;  /* element size [m] (pitch - separation, height) */
+    double elem_elev_radius;    /* elevation focus radius [m]; 0 = flat element */
+    int sub_x, sub_y;           /* point sources along the width / the height */
+    int half_window;            /* DAC samples each side of the travel time (45 in the reference) */
+} msot_spmr_spec;
+typedef struct msot_spmr_info {
+    double d_min, d_step, a_step_deg;  /* polar grid (MSOTmodel.m:600-613) */
+    int n_dist, n_angle;
+    int n_sir, sir_len;         /* table columns (n_dist * n_angle) and cropped length */
+} msot_spmr_info;
+/* Sizes and grid of the tables (computes them once). */
+int msot_spmr_query(const msot_spmr_spec *spec, msot_spmr_info *info);
+/* sir: host [n_sir][sir_len]; start_end: host [n_sir][2] (1-based inclusive);
+ * sir_idx: host [n_det][nx*nz] (1-based column).  MSOT_ERANGE when a column's
+ * response reaches the edge of the half_window (widen it) or a pixel maps
+ * outside the table. */
+int msot_spmr_tables(const msot_spmr_spec *spec, double *sir, int32_t *start_end,
+                     int32_t *sir_idx);
+
 /* Estimate sigma_max of the unnormalised operator by power iteration on the
  * GPU (replaces the svds call, MSOTmodel.m:277-278); FP64 norms. */
 int msot_estimate_norm(msot_plan_t plan, int iters, uint64_t seed, double *sigma_max,

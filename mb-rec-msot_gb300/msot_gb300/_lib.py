@@ -51,6 +51,24 @@ _vp = C.c_void_p
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
 
+
+class SpmrSpec(C.Structure):
+    _fields_ = [
+        ("n_det", C.c_int), ("radius", C.c_double), ("coverage_deg", C.c_double),
+        ("x", _dp), ("nx", C.c_int), ("z", _dp), ("nz", C.c_int),
+        ("c", C.c_double), ("fs", C.c_double), ("pixel_sigma", C.c_double),
+        ("elem_width", C.c_double), ("elem_height", C.c_double),
+        ("elem_elev_radius", C.c_double), ("sub_x", C.c_int), ("sub_y", C.c_int),
+        ("half_window", C.c_int),
+    ]
+
+
+class SpmrInfo(C.Structure):
+    _fields_ = [
+        ("d_min", C.c_double), ("d_step", C.c_double), ("a_step_deg", C.c_double),
+        ("n_dist", C.c_int), ("n_angle", C.c_int), ("n_sir", C.c_int), ("sir_len", C.c_int),
+    ]
+
 # name: (restype, argtypes)
 SIGNATURES = {
     "msot_last_error": (C.c_char_p, []),
@@ -77,6 +95,8 @@ SIGNATURES = {
     "msot_travel_times": (C.c_int, [C.c_int, C.c_double, C.c_double, _dp, C.c_int, _dp,
                                     C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                     _dp]),
+    "msot_spmr_query": (C.c_int, [C.POINTER(SpmrSpec), C.POINTER(SpmrInfo)]),
+    "msot_spmr_tables": (C.c_int, [C.POINTER(SpmrSpec), _dp, _ip, _ip]),
     "msot_dmas_cf": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _dp, C.c_int, _dp, C.c_int,
                                C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                _vp, _vp, _vp, _vp, _vp]),

