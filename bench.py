@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--no-oracle", action="store_true", help="skip the FP64 oracle solve")
     ap.add_argument("--op", action="store_true",
                     help="time the operator alone: one step = A then A^T on the batch")
+    ap.add_argument("--sweep", action="store_true",
+                    help="SIR operator sweep (128^2, 256^2, 400^2; generated 8x8-sub-element "
+                         "SPMR tables): one JSON line per grid")
     return ap.parse_args()
 
 
@@ -383,6 +386,92 @@ def run_reference(args, rank):
     }
 
 
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12  # FMA pipe, nominal max clock
+
+
+def run_sweep(args):
+    """Operator throughput sweep of the SIR model: A and A^T, FP32, on random
+    non-negative images U[0, 1], grids 128^2 / 256^2 / 400^2 over the fixed
+    25.4 mm FOV, 256 elements x 2030 samples, SPMR tables from 8 x 8
+    point sources on a 0.25 mm x 10 mm flat element.  Times the interpolation
+    kernels (the forwardMex / transposeMex equivalents) and the full operator
+    with CUDA events, a 512 MB L2 flush between timed launches; reports the
+    adjoint test, GB/s against the HBM peak and the FP32 rate."""
+    import ctypes as C
+    import torch
+    from msot_gb300 import Discretization, MSOTmodel, Probe, _lib
+    from msot_gb300.sir import spmr_tables
+    from msot_gb300.synthetic import gauss_pulse_eir
+    L = _lib.load()
+    W = args.batch if args.batch != 64 else 8
+    peak, peak_kind = peaks()
+    flush = torch.empty(512 * 1024 * 1024 // 4, device="cuda")
+    out = []
+    for n in (128, 256, 400):
+        probe = Probe(n_det=N_DET, radius=0.040, angular_coverage=135.0, fs=4e7, n_samples=N_T,
+                      delay=0.0, eir=gauss_pulse_eir(), eir_length=257)
+        disc = Discretization([-0.0127, 0.0127], n)
+        t0 = time.perf_counter()
+        sir, se, idx, meta = spmr_tables(probe, disc, 1500.0, element=(0.25e-3, 10e-3, 0.0),
+                                         sub=(8, 8))
+        t_tab = time.perf_counter() - t0
+        model = MSOTmodel(probe, disc, 1500.0, True, True, 0, 1e5, 12e6, 1.0,
+                          sir_tables=(sir, se, idx), max_batch=W)
+        gen = torch.Generator(device="cuda").manual_seed(n)
+        x = torch.rand((W, n, n), device="cuda", generator=gen)
+        ys = torch.randn((W, N_DET, N_T), device="cuda", generator=gen)
+        raw = torch.empty((W, N_DET, N_T), device="cuda")
+        xr = torch.empty((W, n, n), device="cuda")
+
+        def interp_f():
+            _lib.check(L.msot_interp_forward(model.plan, C.c_void_p(x.data_ptr()),
+                                             C.c_void_p(raw.data_ptr()), W, None))
+
+        def interp_t():
+            _lib.check(L.msot_interp_transpose(model.plan, C.c_void_p(ys.data_ptr()),
+                                               C.c_void_p(xr.data_ptr()), W, None))
+
+        res = {}
+        for name, fn in (("interp_forward", interp_f), ("interp_transpose", interp_t),
+                         ("A", lambda: model.forward(x)), ("AT", lambda: model.transpose(ys))):
+            for _ in range(args.warmup):
+                fn()
+            ms = []
+            for _ in range(args.steps):
+                flush.zero_()
+                a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record()
+                fn()
+                z.record()
+                torch.cuda.synchronize()
+                ms.append(a.elapsed_time(z))
+            res[name] = float(np.median(ms))
+        y = model.forward(x)
+        xa = model.transpose(ys)
+        yd, sd = y.double(), ys.double()
+        adj = abs(float((yd * sd).sum()) - float((x.double() * xa.double()).sum())) / (
+            float(yd.norm()) * float(sd.norm()))
+        P, NS, S = n * n, sir.shape[0], sir.shape[1]
+        s_mean = float(np.mean((se[:, 1] - se[:, 0] + 1)[idx.ravel() - 1]))
+        n_taps = 2.0 * model.radius
+        alg_bytes = 4 * P * N_DET * 2 + 4 * S * NS + 4 * P * W + 4 * N_T * N_DET * W
+        flops = 2.0 * P * N_DET * W * s_mean * n_taps
+        line = {"sweep": "sir_operator", "grid": [n, n], "n_det": N_DET, "n_t": N_T,
+                "batch": W, "spmr": {"n_sir": NS, "sir_len": S, "mean_support": s_mean,
+                                      "build_s": t_tab},
+                "ms": res, "adjoint_test": adj}
+        for k in ("interp_forward", "interp_transpose"):
+            sec = res[k] / 1e3
+            line[k] = {"gbs": alg_bytes / sec / 1e9, "hbm_frac": alg_bytes / sec / 1e9 / peak,
+                       "tflops": flops / sec / 1e12,
+                       "fp32_frac_nominal": flops / sec / 1e12 / FP32_NOMINAL_TFLOPS}
+        line["peak_source"] = f"{peak_kind} hbm_gbs (copy); FP32 nominal {FP32_NOMINAL_TFLOPS:.1f} TF/s"
+        out.append(line)
+        print(json.dumps(line), flush=True)
+        del model
+    return None
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -393,6 +482,10 @@ def main():
         import torch
         torch.cuda.set_device(0)
         out = run_operator(args)
+    elif args.sweep:
+        import torch
+        torch.cuda.set_device(0)
+        out = run_sweep(args)
     else:
         if world > 1:
             import torch
