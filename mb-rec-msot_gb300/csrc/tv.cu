@@ -343,10 +343,11 @@ __device__ __forceinline__ float tvc_M(const TvcCtx &c, int oi, int lc, int l, H
 // CTA of the cluster (remote stores, then the barrier), and thread 0 adds
 // the C slots in rank order: identical results in all CTAs.  The scalar
 // logic that follows runs on thread 0 only and is broadcast through shared
-// memory: FP64 on GB300 is far too slow to replicate divisions and square
-// roots across all threads.
-__device__ __forceinline__ void tvc_reduce(float a, float b, double &A, double &B, float *wsum,
-                                           double *red, int &par, int C, int rank) {
+// memory.  The sums and scalars are FP32 like the vectors: thread 0's scalar
+// work lies on every CGS step's critical path, and FP64 latency on GB300 is
+// long.
+__device__ __forceinline__ void tvc_reduce(float a, float b, float &A, float &B, float *wsum,
+                                           float *red, int &par, int C, int rank) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
 #pragma unroll
@@ -362,8 +363,8 @@ __device__ __forceinline__ void tvc_reduce(float a, float b, double &A, double &
     __syncthreads();
     if (wid == 0) {
         constexpr int NW = TVC_THREADS / 32;
-        double da = lane < NW ? (double)wsum[lane] : 0.0;
-        double db = lane < NW ? (double)wsum[32 + lane] : 0.0;
+        float da = lane < NW ? wsum[lane] : 0.f;
+        float db = lane < NW ? wsum[32 + lane] : 0.f;
 #pragma unroll
         for (int o = NW / 2; o > 0; o >>= 1) {
             da += __shfl_down_sync(0xffffffffu, da, o);
@@ -372,16 +373,16 @@ __device__ __forceinline__ void tvc_reduce(float a, float b, double &A, double &
         da = __shfl_sync(0xffffffffu, da, 0);
         db = __shfl_sync(0xffffffffu, db, 0);
         if (lane < C) {
-            double *dst = cl.map_shared_rank(red, lane) + (par * TVC_MAXC + rank) * 2;
+            float *dst = cl.map_shared_rank(red, lane) + (par * TVC_MAXC + rank) * 2;
             dst[0] = da;
             dst[1] = db;
         }
     }
     cl.sync();
     if (threadIdx.x == 0) {
-        const double *src = red + par * TVC_MAXC * 2;
-        A = 0.0;
-        B = 0.0;
+        const float *src = red + par * TVC_MAXC * 2;
+        A = 0.f;
+        B = 0.f;
         for (int r = 0; r < C; ++r) {
             A += src[2 * r];
             B += src[2 * r + 1];
@@ -409,7 +410,7 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
     namespace cg = cooperative_groups;
     extern __shared__ float4 tvc_smem[];
     __shared__ float wsum[64];
-    __shared__ double red[2 * TVC_MAXC * 2];
+    __shared__ float red[2 * TVC_MAXC * 2];
     __shared__ TvBcast bc;
     cg::cluster_group cl = cg::this_cluster();
     const int rank = (int)cl.block_rank();
@@ -438,8 +439,8 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
               ouc = V_UC * V, ouh = V_UH * V, ovh = V_VH * V, oxm = V_XMIN * V;
     int op = V_P0 * V, opo = V_P1 * V;  // p_new, p_old
     int par = 0, n_sweeps = 0, n_cg = 0;
-    double A = 0.0, B = 0.0;                                  // thread 0 only
-    double n2b = 0.0, rho = 0.0, rho1 = 1.0, normrmin = 0.0;  // thread 0 only
+    float A = 0.f, B = 0.f;                                  // thread 0 only
+    float n2b = 0.f, rho = 0.f, rho1 = 1.f, normrmin = 0.f;  // thread 0 only
     TVC_FOR(c) {
         S[ou + l] = g[l];
         S[ob1 + l] = 0.f;
@@ -475,11 +476,11 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
         }
         tvc_reduce(n2, 0.f, A, B, wsum, red, par, C, rank);
         if (threadIdx.x == 0) {
-            n2b = sqrt(A);
+            n2b = sqrtf(A);
             rho = A;  // rt' r of the first step (rt = r = rhs)
-            rho1 = 1.0;
+            rho1 = 1.f;
             normrmin = n2b;
-            bc.flag = n2b > 0.0 ? TVB_RUN : 0;
+            bc.flag = n2b > 0.f ? TVB_RUN : 0;
             bc.beta = 0.f;
         }
         __syncthreads();
@@ -525,11 +526,11 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
                 }
                 tvc_reduce(a_rtvh, 0.f, A, B, wsum, red, par, C, rank);
                 if (threadIdx.x == 0) {
-                    if (A == 0.0 || !isfinite(A)) {
+                    if (A == 0.f || !isfinite(A)) {
                         bc.flag = TVB_BREAK;
                     } else {
                         bc.flag = 0;
-                        bc.alpha = (float)(rho / A);
+                        bc.alpha = rho / A;
                     }
                 }
                 __syncthreads();
@@ -557,9 +558,9 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
                 }
                 tvc_reduce(a_rr, a_rtr, A, B, wsum, red, par, C, rank);
                 if (threadIdx.x == 0) {
-                    const double normr = sqrt(A);
+                    const float normr = sqrtf(A);
                     int f = 0;
-                    if (normr <= 1e-5 * n2b) {
+                    if (normr <= 1e-5f * n2b) {
                         f = TVB_CONVERGED;
                     } else {
                         if (normr < normrmin) {
@@ -568,10 +569,10 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
                         }
                         rho1 = rho;
                         rho = B;  // rt' r of the next step
-                        if (rho == 0.0 || !isfinite(rho))
+                        if (rho == 0.f || !isfinite(rho))
                             f |= TVB_BREAK;
                         else
-                            bc.beta = (float)(rho / rho1);
+                            bc.beta = rho / rho1;
                     }
                     bc.flag = f;
                 }
@@ -604,7 +605,7 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
             nrm = fmaf(v, v, nrm);
         }
         tvc_reduce(dif, nrm, A, B, wsum, red, par, C, rank);
-        if (threadIdx.x == 0) bc.flag = (!(B > 0.0) || sqrt(A / B) <= 1e-3) ? TVB_BREAK : 0;
+        if (threadIdx.x == 0) bc.flag = (!(B > 0.f) || sqrtf(A / B) <= 1e-3f) ? TVB_BREAK : 0;
         __syncthreads();
         const int t = ou;
         ou = ox;
@@ -620,6 +621,334 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
     cl.sync();  // no CTA leaves while a neighbour may still read its shared memory
 }
 #undef TVC_FOR
+
+// ---------------------------------------------------------------------------
+// The same cluster prox with 4 consecutive z-pixels per thread (N % 4 == 0):
+// 128-bit shared-memory accesses; thread t owns group jz = t % (N/4) (pixels
+// 4 jz .. 4 jz + 3) of the columns lc = t / (N/4), ... + G.  Arithmetic is
+// the scalar kernel's, per component.
+// ---------------------------------------------------------------------------
+struct F4 {
+    float v[4];
+};
+__device__ __forceinline__ F4 ld4(const float *p) {
+    const float4 a = *reinterpret_cast<const float4 *>(p);
+    return F4{{a.x, a.y, a.z, a.w}};
+}
+__device__ __forceinline__ void st4(float *p, const F4 &a) {
+    *reinterpret_cast<float4 *>(p) = make_float4(a.v[0], a.v[1], a.v[2], a.v[3]);
+}
+
+struct Tvc4Ctx {
+    float *sm;
+    const float *sl, *sr;
+    int N, nloc, nl, ix0, iz0, G, lc0;
+};
+
+// (I + B'B) in of the 4 pixels at (lc, iz0 .. iz0 + 3), element l = lc N + iz0
+template <class Halo>
+__device__ __forceinline__ F4 tvc4_M(const Tvc4Ctx &c, int oi, int lc, int l, Halo halo) {
+    const float *in = c.sm + oi;
+    const int ix = c.ix0 + lc;
+    const F4 v = ld4(in + l);
+    float a[6];
+    a[0] = c.iz0 >= 1 ? in[l - 1] : 0.f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a[k + 1] = v.v[k];
+    a[5] = c.iz0 + 4 < c.N ? in[l + 4] : 0.f;
+    F4 L{}, R{};
+    if (ix >= 1) L = lc == 0 ? halo(c.sl, (c.nloc - 1) * c.N + c.iz0) : ld4(in + l - c.N);
+    if (ix + 1 < c.N) R = lc == c.nl - 1 ? halo(c.sr, c.iz0) : ld4(in + l + c.N);
+    F4 o;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int iz = c.iz0 + k;
+        const float x = a[k + 1];
+        const float g1 = iz >= 1 ? x - a[k] : 0.f;
+        const float g1n = iz + 1 < c.N ? a[k + 2] - x : 0.f;
+        const float g2 = ix >= 1 ? x - L.v[k] : 0.f;
+        const float g2n = ix + 1 < c.N ? R.v[k] - x : 0.f;
+        o.v[k] = x + (g1 - g1n) + (g2 - g2n);
+    }
+    return o;
+}
+
+#define TVC4_FOR(c) for (int lc = (c).lc0, l = lc * (c).N + (c).iz0; lc < (c).nl; lc += (c).G, l += (c).G * (c).N)
+
+__global__ void __launch_bounds__(TVC_THREADS, 2)
+    k_tv_prox_cl4(const float *__restrict__ g_all, const TvState *__restrict__ st,
+                  double mu_const, int coupled, float *__restrict__ out_all, int N, int C,
+                  int nloc) {
+    namespace cg = cooperative_groups;
+    extern __shared__ float4 tvc_smem[];
+    __shared__ float wsum[64];
+    __shared__ float red[2 * TVC_MAXC * 2];
+    __shared__ TvBcast bc;
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    const int w = blockIdx.x / C, gw = coupled ? 0 : w;
+    if (st && st[gw].done) return;  // uniform over the cluster
+    Tvc4Ctx c;
+    c.sm = reinterpret_cast<float *>(tvc_smem);
+    c.N = N;
+    c.nloc = nloc;
+    c.ix0 = rank * nloc;
+    c.nl = max(0, min(nloc, N - c.ix0));
+    const int NG = N / 4;
+    c.G = TVC_THREADS / NG;
+    c.iz0 = 4 * ((int)threadIdx.x % NG);
+    c.lc0 = (int)threadIdx.x / NG;
+    if (c.lc0 >= c.G) c.lc0 = c.nl;  // idle thread
+    c.sl = rank > 0 ? cl.map_shared_rank(c.sm, rank - 1) : nullptr;
+    c.sr = rank + 1 < C ? cl.map_shared_rank(c.sm, rank + 1) : nullptr;
+    const float mu = (float)(st ? st[gw].mu : mu_const);
+    const float *g = g_all + (size_t)w * N * N + (size_t)c.ix0 * N;
+    const int V = nloc * N;
+    float *S = c.sm;
+    int ou = V_U * V, ox = V_X * V;
+    const int ob1 = V_B1 * V, ob2 = V_B2 * V, orr = V_R * V, ort = V_RT * V, oq = V_Q * V,
+              ouc = V_UC * V, ouh = V_UH * V, ovh = V_VH * V, oxm = V_XMIN * V;
+    int op = V_P0 * V, opo = V_P1 * V;
+    int par = 0, n_sweeps = 0, n_cg = 0;
+    float A = 0.f, B = 0.f;
+    float n2b = 0.f, rho = 0.f, rho1 = 1.f, normrmin = 0.f;
+    const F4 zero4{{0.f, 0.f, 0.f, 0.f}};
+    TVC4_FOR(c) {
+        st4(S + ou + l, ld4(g + l));
+        st4(S + ob1 + l, zero4);
+        st4(S + ob2 + l, zero4);
+    }
+    cl.sync();
+    for (int it = 0; it < TV_SB_MAX; ++it) {
+        ++n_sweeps;
+        float n2 = 0.f;
+        TVC4_FOR(c) {
+            const int ix = c.ix0 + lc;
+            const F4 B1 = ld4(S + ob1 + l), B2 = ld4(S + ob2 + l), G4 = ld4(g + l);
+            float c1[5], c2[4];
+            for (int k = 0; k < 4; ++k) {
+                float b1, b2;
+                tvc_bd(B1.v[k], B2.v[k], mu, b1, b2, c1[k], c2[k]);
+            }
+            if (c.iz0 + 4 < N) {
+                float b1, b2, e2;
+                tvc_bd(S[ob1 + l + 4], S[ob2 + l + 4], mu, b1, b2, c1[4], e2);
+            } else {
+                c1[4] = 0.f;
+            }
+            float e2r[4] = {0.f, 0.f, 0.f, 0.f};
+            if (ix + 1 < N) {
+                const F4 R1 = lc == c.nl - 1 ? ld4(c.sr + ob1 + c.iz0) : ld4(S + ob1 + l + N);
+                const F4 R2 = lc == c.nl - 1 ? ld4(c.sr + ob2 + c.iz0) : ld4(S + ob2 + l + N);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    float b1, b2, e1;
+                    tvc_bd(R1.v[k], R2.v[k], mu, b1, b2, e1, e2r[k]);
+                }
+            }
+            F4 rh;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int iz = c.iz0 + k;
+                float acc = 0.f;
+                if (iz >= 1) acc += c1[k];
+                if (iz + 1 < N) acc -= c1[k + 1];
+                float acc2 = 0.f;
+                if (ix >= 1) acc2 += c2[k];
+                if (ix + 1 < N) acc2 -= e2r[k];
+                rh.v[k] = G4.v[k] - (acc + acc2);
+                n2 = fmaf(rh.v[k], rh.v[k], n2);
+            }
+            st4(S + orr + l, rh);
+            st4(S + ort + l, rh);
+            st4(S + ox + l, zero4);
+            st4(S + oxm + l, zero4);
+        }
+        tvc_reduce(n2, 0.f, A, B, wsum, red, par, C, rank);
+        if (threadIdx.x == 0) {
+            n2b = sqrtf(A);
+            rho = A;
+            rho1 = 1.f;
+            normrmin = n2b;
+            bc.flag = n2b > 0.f ? TVB_RUN : 0;
+            bc.beta = 0.f;
+        }
+        __syncthreads();
+        bool converged = false;
+        if (bc.flag & TVB_RUN) {
+            for (int cit = 0; cit < TV_CG_MAX; ++cit) {
+                ++n_cg;
+                const float beta = bc.beta;
+                {
+                    const int t = op;
+                    op = opo;
+                    opo = t;
+                }
+                TVC4_FOR(c) {
+                    const F4 rv = ld4(S + orr + l);
+                    if (cit == 0) {
+                        st4(S + ouc + l, rv);
+                        st4(S + op + l, rv);
+                    } else {
+                        const F4 qv = ld4(S + oq + l), pv = ld4(S + opo + l);
+                        F4 uv, pn;
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) {
+                            uv.v[k] = fmaf(beta, qv.v[k], rv.v[k]);
+                            pn.v[k] = fmaf(beta, fmaf(beta, pv.v[k], qv.v[k]), uv.v[k]);
+                        }
+                        st4(S + ouc + l, uv);
+                        st4(S + op + l, pn);
+                    }
+                }
+                __syncthreads();
+                const bool first = cit == 0;
+                const int opo_ = opo;
+                auto halo_p = [=](const float *b, int k) {
+                    const F4 rv = ld4(b + orr + k);
+                    if (first) return rv;
+                    const F4 qv = ld4(b + oq + k), pv = ld4(b + opo_ + k);
+                    F4 o;
+#pragma unroll
+                    for (int m = 0; m < 4; ++m) {
+                        const float uv = fmaf(beta, qv.v[m], rv.v[m]);
+                        o.v[m] = fmaf(beta, fmaf(beta, pv.v[m], qv.v[m]), uv);
+                    }
+                    return o;
+                };
+                float a_rtvh = 0.f;
+                TVC4_FOR(c) {
+                    const F4 vh = tvc4_M(c, op, lc, l, halo_p);
+                    st4(S + ovh + l, vh);
+                    const F4 rt = ld4(S + ort + l);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) a_rtvh = fmaf(rt.v[k], vh.v[k], a_rtvh);
+                }
+                tvc_reduce(a_rtvh, 0.f, A, B, wsum, red, par, C, rank);
+                if (threadIdx.x == 0) {
+                    if (A == 0.f || !isfinite(A)) {
+                        bc.flag = TVB_BREAK;
+                    } else {
+                        bc.flag = 0;
+                        bc.alpha = rho / A;
+                    }
+                }
+                __syncthreads();
+                if (bc.flag & TVB_BREAK) break;
+                const float alpha = bc.alpha;
+                TVC4_FOR(c) {
+                    const F4 uv = ld4(S + ouc + l), vh = ld4(S + ovh + l), xv = ld4(S + ox + l);
+                    F4 q, uh, xn;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        q.v[k] = fmaf(-alpha, vh.v[k], uv.v[k]);
+                        uh.v[k] = uv.v[k] + q.v[k];
+                        xn.v[k] = fmaf(alpha, uh.v[k], xv.v[k]);
+                    }
+                    st4(S + oq + l, q);
+                    st4(S + ouh + l, uh);
+                    st4(S + ox + l, xn);
+                }
+                __syncthreads();
+                auto halo_uh = [=](const float *b, int k) {
+                    const F4 uv = ld4(b + ouc + k), vh = ld4(b + ovh + k);
+                    F4 o;
+#pragma unroll
+                    for (int m = 0; m < 4; ++m) o.v[m] = uv.v[m] + fmaf(-alpha, vh.v[m], uv.v[m]);
+                    return o;
+                };
+                float a_rr = 0.f, a_rtr = 0.f;
+                TVC4_FOR(c) {
+                    const F4 mv = tvc4_M(c, ouh, lc, l, halo_uh);
+                    const F4 rv = ld4(S + orr + l), rt = ld4(S + ort + l);
+                    F4 rn;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        rn.v[k] = fmaf(-alpha, mv.v[k], rv.v[k]);
+                        a_rr = fmaf(rn.v[k], rn.v[k], a_rr);
+                        a_rtr = fmaf(rt.v[k], rn.v[k], a_rtr);
+                    }
+                    st4(S + orr + l, rn);
+                }
+                tvc_reduce(a_rr, a_rtr, A, B, wsum, red, par, C, rank);
+                if (threadIdx.x == 0) {
+                    const float normr = sqrtf(A);
+                    int f = 0;
+                    if (normr <= 1e-5f * n2b) {
+                        f = TVB_CONVERGED;
+                    } else {
+                        if (normr < normrmin) {
+                            normrmin = normr;
+                            f |= TVB_IMPROVED;
+                        }
+                        rho1 = rho;
+                        rho = B;
+                        if (rho == 0.f || !isfinite(rho))
+                            f |= TVB_BREAK;
+                        else
+                            bc.beta = rho / rho1;
+                    }
+                    bc.flag = f;
+                }
+                __syncthreads();
+                const int f = bc.flag;
+                if (f & TVB_CONVERGED) {
+                    converged = true;
+                    break;
+                }
+                if (f & TVB_IMPROVED) {
+                    TVC4_FOR(c) st4(S + oxm + l, ld4(S + ox + l));
+                }
+                if (f & TVB_BREAK) break;
+            }
+        }
+        if (!converged) {
+            TVC4_FOR(c) st4(S + ox + l, ld4(S + oxm + l));
+        }
+        cl.sync();
+        float dif = 0.f, nrm = 0.f;
+        TVC4_FOR(c) {
+            const int ix = c.ix0 + lc;
+            const F4 B1 = ld4(S + ob1 + l), B2 = ld4(S + ob2 + l), X = ld4(S + ox + l),
+                     U = ld4(S + ou + l);
+            float xa[5];
+            xa[0] = c.iz0 >= 1 ? S[ox + l - 1] : 0.f;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) xa[k + 1] = X.v[k];
+            F4 Lx{};
+            if (ix >= 1) Lx = lc == 0 ? ld4(c.sl + ox + (c.nloc - 1) * N + c.iz0) : ld4(S + ox + l - N);
+            F4 n1, n2v;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                float b1, b2, cc1, cc2;
+                tvc_bd(B1.v[k], B2.v[k], mu, b1, b2, cc1, cc2);
+                const float v = X.v[k];
+                n1.v[k] = (c.iz0 + k >= 1 ? v - xa[k] : 0.f) + b1;
+                n2v.v[k] = (ix >= 1 ? v - Lx.v[k] : 0.f) + b2;
+                const float e = U.v[k] - v;
+                dif = fmaf(e, e, dif);
+                nrm = fmaf(v, v, nrm);
+            }
+            st4(S + ob1 + l, n1);
+            st4(S + ob2 + l, n2v);
+        }
+        tvc_reduce(dif, nrm, A, B, wsum, red, par, C, rank);
+        if (threadIdx.x == 0) bc.flag = (!(B > 0.f) || sqrtf(A / B) <= 1e-3f) ? TVB_BREAK : 0;
+        __syncthreads();
+        const int t = ou;
+        ou = ox;
+        ox = t;
+        if (bc.flag & TVB_BREAK) break;
+    }
+    float *o = out_all + (size_t)w * N * N + (size_t)c.ix0 * N;
+    TVC4_FOR(c) st4(o + l, ld4(S + ou + l));
+    if (rank == 0 && threadIdx.x == 0) {
+        atomicAdd(&g_tv_stats[0], (unsigned long long)n_sweeps);
+        atomicAdd(&g_tv_stats[1], (unsigned long long)n_cg);
+    }
+    cl.sync();
+}
+#undef TVC4_FOR
 
 // isotropic TV term of pixel i of the N x N image x
 __device__ __forceinline__ float itv_term(const float *x, int i, int N) {
@@ -875,7 +1204,8 @@ TvcGeom tvc_geometry(int N) {
 
 cudaError_t tvc_launch(const TvcGeom &gm, const float *z, const TvState *sv, double mu,
                        int coupled, float *out, int W, int N, cudaStream_t st, bool &fits) {
-    auto kern = k_tv_prox_cl;
+    // 4 z-pixels per thread where N allows (16-byte aligned groups)
+    auto kern = (N % 4 == 0 && N / 4 <= TVC_THREADS) ? k_tv_prox_cl4 : k_tv_prox_cl;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)gm.smem);
     if (e != cudaSuccess) return e;
