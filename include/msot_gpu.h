@@ -222,6 +222,11 @@ int msot_backproject_waveeq(const float *d_sig, int W, int D, int T, const doubl
 /* Instrumentation (no counterpart in the reference, whose only timing is
  * tic/toc, e.g. rec_nn_with_L2_reg.m:44-49). */
 
+/* Kernel tuning knob (no reference counterpart; results change only in
+ * float summation order):
+ *   "tv_prox_cluster"  CTAs per image of the shared-memory SB_ITV2 kernel
+ *                      (1, 2, 4, 8, 16; 0 = automatic). */
+int msot_tune_set(const char *key, int value);
 /* SB_ITV2 kernel choice: 0 (default) = the shared-memory cluster kernel
  * wherever the image fits, 1 = always the global-memory kernel. */
 int msot_tv_prox_path(int path);

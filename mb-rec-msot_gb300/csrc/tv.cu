@@ -33,6 +33,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "common.cuh"
@@ -338,14 +339,14 @@ __device__ __forceinline__ float tvc_M(const TvcCtx &c, int oi, int lc, int l, H
     return v + (g1 - g1n) + (g2 - g2n);
 }
 
-// Cluster-wide sums of two per-thread values, valid in thread 0 of every
-// CTA.  Each CTA pushes its two block sums into slot [par][rank] of every
-// CTA of the cluster (remote stores, then the barrier), and thread 0 adds
-// the C slots in rank order: identical results in all CTAs.  The scalar
-// logic that follows runs on thread 0 only and is broadcast through shared
-// memory.  The sums and scalars are FP32 like the vectors: thread 0's scalar
-// work lies on every CGS step's critical path, and FP64 latency on GB300 is
-// long.
+// Cluster-wide sums of two per-thread values, returned to every thread.
+// Each CTA pushes its two block sums into slot [par][rank] of every CTA of
+// the cluster (remote stores, then the barrier), and every thread adds the C
+// slots of its own CTA in rank order: bitwise-identical results in all
+// threads of all CTAs, so every thread evaluates the scalar recurrences
+// itself and all take the same branches (no broadcast barrier).  Sums and
+// scalars are FP32 like the vectors: they lie on every CGS step's critical
+// path, and FP64 latency on GB300 is long.
 __device__ __forceinline__ void tvc_reduce(float a, float b, float &A, float &B, float *wsum,
                                            float *red, int &par, int C, int rank) {
     namespace cg = cooperative_groups;
@@ -379,14 +380,12 @@ __device__ __forceinline__ void tvc_reduce(float a, float b, float &A, float &B,
         }
     }
     cl.sync();
-    if (threadIdx.x == 0) {
-        const float *src = red + par * TVC_MAXC * 2;
-        A = 0.f;
-        B = 0.f;
-        for (int r = 0; r < C; ++r) {
-            A += src[2 * r];
-            B += src[2 * r + 1];
-        }
+    const float *src = red + par * TVC_MAXC * 2;
+    A = 0.f;
+    B = 0.f;
+    for (int r = 0; r < C; ++r) {
+        A += src[2 * r];
+        B += src[2 * r + 1];
     }
     par ^= 1;
 }
@@ -411,7 +410,6 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
     extern __shared__ float4 tvc_smem[];
     __shared__ float wsum[64];
     __shared__ float red[2 * TVC_MAXC * 2];
-    __shared__ TvBcast bc;
     cg::cluster_group cl = cg::this_cluster();
     const int rank = (int)cl.block_rank();
     const int w = blockIdx.x / C, gw = coupled ? 0 : w;
@@ -439,8 +437,8 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
               ouc = V_UC * V, ouh = V_UH * V, ovh = V_VH * V, oxm = V_XMIN * V;
     int op = V_P0 * V, opo = V_P1 * V;  // p_new, p_old
     int par = 0, n_sweeps = 0, n_cg = 0;
-    float A = 0.f, B = 0.f;                                  // thread 0 only
-    float n2b = 0.f, rho = 0.f, rho1 = 1.f, normrmin = 0.f;  // thread 0 only
+    float A = 0.f, B = 0.f;
+    float n2b = 0.f, rho = 0.f, rho1 = 1.f, normrmin = 0.f;
     TVC_FOR(c) {
         S[ou + l] = g[l];
         S[ob1 + l] = 0.f;
@@ -475,20 +473,16 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
             n2 = fmaf(rhs, rhs, n2);
         }
         tvc_reduce(n2, 0.f, A, B, wsum, red, par, C, rank);
-        if (threadIdx.x == 0) {
-            n2b = sqrtf(A);
-            rho = A;  // rt' r of the first step (rt = r = rhs)
-            rho1 = 1.f;
-            normrmin = n2b;
-            bc.flag = n2b > 0.f ? TVB_RUN : 0;
-            bc.beta = 0.f;
-        }
-        __syncthreads();
+        n2b = sqrtf(A);
+        rho = A;  // rt' r of the first step (rt = r = rhs)
+        rho1 = 1.f;
+        normrmin = n2b;
+        float beta_next = 0.f;
         bool converged = false;
-        if (bc.flag & TVB_RUN) {
+        if (n2b > 0.f) {
             for (int cit = 0; cit < TV_CG_MAX; ++cit) {
                 ++n_cg;
-                const float beta = bc.beta;
+                const float beta = beta_next;
                 {
                     const int t = op;
                     op = opo;
@@ -525,17 +519,8 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
                     a_rtvh = fmaf(S[ort + l], vhv, a_rtvh);
                 }
                 tvc_reduce(a_rtvh, 0.f, A, B, wsum, red, par, C, rank);
-                if (threadIdx.x == 0) {
-                    if (A == 0.f || !isfinite(A)) {
-                        bc.flag = TVB_BREAK;
-                    } else {
-                        bc.flag = 0;
-                        bc.alpha = rho / A;
-                    }
-                }
-                __syncthreads();
-                if (bc.flag & TVB_BREAK) break;
-                const float alpha = bc.alpha;
+                if (A == 0.f || !isfinite(A)) break;
+                const float alpha = rho / A;
                 TVC_FOR(c) {
                     const float uv = S[ouc + l];
                     const float qq = fmaf(-alpha, S[ovh + l], uv);
@@ -557,9 +542,9 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
                     a_rtr = fmaf(S[ort + l], rv, a_rtr);
                 }
                 tvc_reduce(a_rr, a_rtr, A, B, wsum, red, par, C, rank);
-                if (threadIdx.x == 0) {
+                int f = 0;
+                {
                     const float normr = sqrtf(A);
-                    int f = 0;
                     if (normr <= 1e-5f * n2b) {
                         f = TVB_CONVERGED;
                     } else {
@@ -572,12 +557,9 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
                         if (rho == 0.f || !isfinite(rho))
                             f |= TVB_BREAK;
                         else
-                            bc.beta = rho / rho1;
+                            beta_next = rho / rho1;
                     }
-                    bc.flag = f;
                 }
-                __syncthreads();
-                const int f = bc.flag;
                 if (f & TVB_CONVERGED) {
                     converged = true;
                     break;
@@ -605,12 +587,11 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
             nrm = fmaf(v, v, nrm);
         }
         tvc_reduce(dif, nrm, A, B, wsum, red, par, C, rank);
-        if (threadIdx.x == 0) bc.flag = (!(B > 0.f) || sqrtf(A / B) <= 1e-3f) ? TVB_BREAK : 0;
-        __syncthreads();
+        const bool stop = !(B > 0.f) || sqrtf(A / B) <= 1e-3f;
         const int t = ou;
         ou = ox;
         ox = t;
-        if (bc.flag & TVB_BREAK) break;
+        if (stop) break;
     }
     float *o = out_all + (size_t)w * N * N + (size_t)c.ix0 * N;
     TVC_FOR(c) o[l] = S[ou + l];
@@ -683,7 +664,6 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
     extern __shared__ float4 tvc_smem[];
     __shared__ float wsum[64];
     __shared__ float red[2 * TVC_MAXC * 2];
-    __shared__ TvBcast bc;
     cg::cluster_group cl = cg::this_cluster();
     const int rank = (int)cl.block_rank();
     const int w = blockIdx.x / C, gw = coupled ? 0 : w;
@@ -765,20 +745,16 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
             st4(S + oxm + l, zero4);
         }
         tvc_reduce(n2, 0.f, A, B, wsum, red, par, C, rank);
-        if (threadIdx.x == 0) {
-            n2b = sqrtf(A);
-            rho = A;
-            rho1 = 1.f;
-            normrmin = n2b;
-            bc.flag = n2b > 0.f ? TVB_RUN : 0;
-            bc.beta = 0.f;
-        }
-        __syncthreads();
+        n2b = sqrtf(A);
+        rho = A;
+        rho1 = 1.f;
+        normrmin = n2b;
+        float beta_next = 0.f;
         bool converged = false;
-        if (bc.flag & TVB_RUN) {
+        if (n2b > 0.f) {
             for (int cit = 0; cit < TV_CG_MAX; ++cit) {
                 ++n_cg;
-                const float beta = bc.beta;
+                const float beta = beta_next;
                 {
                     const int t = op;
                     op = opo;
@@ -825,17 +801,8 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
                     for (int k = 0; k < 4; ++k) a_rtvh = fmaf(rt.v[k], vh.v[k], a_rtvh);
                 }
                 tvc_reduce(a_rtvh, 0.f, A, B, wsum, red, par, C, rank);
-                if (threadIdx.x == 0) {
-                    if (A == 0.f || !isfinite(A)) {
-                        bc.flag = TVB_BREAK;
-                    } else {
-                        bc.flag = 0;
-                        bc.alpha = rho / A;
-                    }
-                }
-                __syncthreads();
-                if (bc.flag & TVB_BREAK) break;
-                const float alpha = bc.alpha;
+                if (A == 0.f || !isfinite(A)) break;
+                const float alpha = rho / A;
                 TVC4_FOR(c) {
                     const F4 uv = ld4(S + ouc + l), vh = ld4(S + ovh + l), xv = ld4(S + ox + l);
                     F4 q, uh, xn;
@@ -871,9 +838,9 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
                     st4(S + orr + l, rn);
                 }
                 tvc_reduce(a_rr, a_rtr, A, B, wsum, red, par, C, rank);
-                if (threadIdx.x == 0) {
+                int f = 0;
+                {
                     const float normr = sqrtf(A);
-                    int f = 0;
                     if (normr <= 1e-5f * n2b) {
                         f = TVB_CONVERGED;
                     } else {
@@ -882,16 +849,13 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
                             f |= TVB_IMPROVED;
                         }
                         rho1 = rho;
-                        rho = B;
+                        rho = B;  // rt' r of the next step
                         if (rho == 0.f || !isfinite(rho))
                             f |= TVB_BREAK;
                         else
-                            bc.beta = rho / rho1;
+                            beta_next = rho / rho1;
                     }
-                    bc.flag = f;
                 }
-                __syncthreads();
-                const int f = bc.flag;
                 if (f & TVB_CONVERGED) {
                     converged = true;
                     break;
@@ -933,12 +897,11 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
             st4(S + ob2 + l, n2v);
         }
         tvc_reduce(dif, nrm, A, B, wsum, red, par, C, rank);
-        if (threadIdx.x == 0) bc.flag = (!(B > 0.f) || sqrtf(A / B) <= 1e-3f) ? TVB_BREAK : 0;
-        __syncthreads();
+        const bool stop = !(B > 0.f) || sqrtf(A / B) <= 1e-3f;
         const int t = ou;
         ou = ox;
         ox = t;
-        if (bc.flag & TVB_BREAK) break;
+        if (stop) break;
     }
     float *o = out_all + (size_t)w * N * N + (size_t)c.ix0 * N;
     TVC4_FOR(c) st4(o + l, ld4(S + ou + l));
@@ -1183,9 +1146,21 @@ struct TvcGeom {
     size_t smem = 0;
 };
 
+std::atomic<int> g_tv_cluster{0};  // forced cluster size (msot_tune_set), 0 = automatic
+
 TvcGeom tvc_geometry(int N) {
     TvcGeom g;
     if (N > TVC_THREADS) return g;
+    if (const int Cf = g_tv_cluster.load()) {
+        const int nloc = (N + Cf - 1) / Cf;
+        const size_t bytes = (size_t)TVC_NV * nloc * N * sizeof(float);
+        if (bytes <= 225 * 1024) {
+            g.C = Cf;
+            g.nloc = nloc;
+            g.smem = bytes;
+        }
+        return g;
+    }
     const size_t two_per_sm = 113 * 1024, one_per_sm = 225 * 1024;
     for (int pass = 0; pass < 2; ++pass) {
         for (int C = 1; C <= (pass ? 16 : 8); C *= 2) {
@@ -1306,6 +1281,16 @@ int msot_tv_prox_stats(long long *sweeps, long long *cg_steps) {
     if (sweeps) *sweeps = (long long)h[0];
     if (cg_steps) *cg_steps = (long long)h[1];
     return MSOT_OK;
+}
+
+int msot_tune_set(const char *key, int value) {
+    if (key && std::strcmp(key, "tv_prox_cluster") == 0 &&
+        (value == 0 || value == 1 || value == 2 || value == 4 || value == 8 || value == 16)) {
+        g_tv_cluster.store(value);
+        return MSOT_OK;
+    }
+    set_error("tune_set: unknown key or value out of range");
+    return MSOT_EINVAL;
 }
 
 int msot_tv_prox_path(int path) {

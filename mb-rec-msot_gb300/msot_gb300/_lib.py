@@ -91,6 +91,7 @@ SIGNATURES = {
     "msot_sb_itv2": (C.c_int, [_vp, _vp, C.c_int, C.c_int, C.c_double, _vp]),
     "msot_itv": (C.c_int, [_vp, _dp, C.c_int, C.c_int, _vp]),
     "msot_tv_prox_path": (C.c_int, [C.c_int]),
+    "msot_tune_set": (C.c_int, [C.c_char_p, C.c_int]),
     "msot_tv_prox_stats": (C.c_int, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "msot_travel_times": (C.c_int, [C.c_int, C.c_double, C.c_double, _dp, C.c_int, _dp,
                                     C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
