@@ -626,6 +626,18 @@ struct Tvc4Ctx {
     int N, nloc, nl, ix0, iz0, G, lc0;
 };
 
+// a neighbour slab's float4: shared memory of the neighbour CTA, or (GM)
+// global memory written by another SM, read past L1
+template <bool GM>
+__device__ __forceinline__ F4 ld4n(const float *p) {
+    if constexpr (GM) {
+        const float4 a = __ldcg(reinterpret_cast<const float4 *>(p));
+        return F4{{a.x, a.y, a.z, a.w}};
+    } else {
+        return ld4(p);
+    }
+}
+
 // (I + B'B) in of the 4 pixels at (lc, iz0 .. iz0 + 3), element l = lc N + iz0
 template <class Halo>
 __device__ __forceinline__ F4 tvc4_M(const Tvc4Ctx &c, int oi, int lc, int l, Halo halo) {
@@ -656,10 +668,11 @@ __device__ __forceinline__ F4 tvc4_M(const Tvc4Ctx &c, int oi, int lc, int l, Ha
 
 #define TVC4_FOR(c) for (int lc = (c).lc0, l = lc * (c).N + (c).iz0; lc < (c).nl; lc += (c).G, l += (c).G * (c).N)
 
+template <bool GM>
 __global__ void __launch_bounds__(TVC_THREADS, 2)
     k_tv_prox_cl4(const float *__restrict__ g_all, const TvState *__restrict__ st,
                   double mu_const, int coupled, float *__restrict__ out_all, int N, int C,
-                  int nloc) {
+                  int nloc, float *__restrict__ gwork) {
     namespace cg = cooperative_groups;
     extern __shared__ float4 tvc_smem[];
     __shared__ float wsum[64];
@@ -669,7 +682,6 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
     const int w = blockIdx.x / C, gw = coupled ? 0 : w;
     if (st && st[gw].done) return;  // uniform over the cluster
     Tvc4Ctx c;
-    c.sm = reinterpret_cast<float *>(tvc_smem);
     c.N = N;
     c.nloc = nloc;
     c.ix0 = rank * nloc;
@@ -679,8 +691,17 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
     c.iz0 = 4 * ((int)threadIdx.x % NG);
     c.lc0 = (int)threadIdx.x / NG;
     if (c.lc0 >= c.G) c.lc0 = c.nl;  // idle thread
-    c.sl = rank > 0 ? cl.map_shared_rank(c.sm, rank - 1) : nullptr;
-    c.sr = rank + 1 < C ? cl.map_shared_rank(c.sm, rank + 1) : nullptr;
+    if constexpr (GM) {
+        // slabs of the cluster's CTAs are consecutive in the workspace
+        const size_t slab = (size_t)TVC_NV * nloc * N;
+        c.sm = gwork + ((size_t)w * C + rank) * slab;
+        c.sl = rank > 0 ? c.sm - slab : nullptr;
+        c.sr = rank + 1 < C ? c.sm + slab : nullptr;
+    } else {
+        c.sm = reinterpret_cast<float *>(tvc_smem);
+        c.sl = rank > 0 ? cl.map_shared_rank(c.sm, rank - 1) : nullptr;
+        c.sr = rank + 1 < C ? cl.map_shared_rank(c.sm, rank + 1) : nullptr;
+    }
     const float mu = (float)(st ? st[gw].mu : mu_const);
     const float *g = g_all + (size_t)w * N * N + (size_t)c.ix0 * N;
     const int V = nloc * N;
@@ -718,8 +739,8 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
             }
             float e2r[4] = {0.f, 0.f, 0.f, 0.f};
             if (ix + 1 < N) {
-                const F4 R1 = lc == c.nl - 1 ? ld4(c.sr + ob1 + c.iz0) : ld4(S + ob1 + l + N);
-                const F4 R2 = lc == c.nl - 1 ? ld4(c.sr + ob2 + c.iz0) : ld4(S + ob2 + l + N);
+                const F4 R1 = lc == c.nl - 1 ? ld4n<GM>(c.sr + ob1 + c.iz0) : ld4(S + ob1 + l + N);
+                const F4 R2 = lc == c.nl - 1 ? ld4n<GM>(c.sr + ob2 + c.iz0) : ld4(S + ob2 + l + N);
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     float b1, b2, e1;
@@ -781,9 +802,9 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
                 const bool first = cit == 0;
                 const int opo_ = opo;
                 auto halo_p = [=](const float *b, int k) {
-                    const F4 rv = ld4(b + orr + k);
+                    const F4 rv = ld4n<GM>(b + orr + k);
                     if (first) return rv;
-                    const F4 qv = ld4(b + oq + k), pv = ld4(b + opo_ + k);
+                    const F4 qv = ld4n<GM>(b + oq + k), pv = ld4n<GM>(b + opo_ + k);
                     F4 o;
 #pragma unroll
                     for (int m = 0; m < 4; ++m) {
@@ -818,7 +839,7 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
                 }
                 __syncthreads();
                 auto halo_uh = [=](const float *b, int k) {
-                    const F4 uv = ld4(b + ouc + k), vh = ld4(b + ovh + k);
+                    const F4 uv = ld4n<GM>(b + ouc + k), vh = ld4n<GM>(b + ovh + k);
                     F4 o;
 #pragma unroll
                     for (int m = 0; m < 4; ++m) o.v[m] = uv.v[m] + fmaf(-alpha, vh.v[m], uv.v[m]);
@@ -880,7 +901,8 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
 #pragma unroll
             for (int k = 0; k < 4; ++k) xa[k + 1] = X.v[k];
             F4 Lx{};
-            if (ix >= 1) Lx = lc == 0 ? ld4(c.sl + ox + (c.nloc - 1) * N + c.iz0) : ld4(S + ox + l - N);
+            if (ix >= 1)
+                Lx = lc == 0 ? ld4n<GM>(c.sl + ox + (c.nloc - 1) * N + c.iz0) : ld4(S + ox + l - N);
             F4 n1, n2v;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
@@ -1177,10 +1199,9 @@ TvcGeom tvc_geometry(int N) {
     return g;
 }
 
-cudaError_t tvc_launch(const TvcGeom &gm, const float *z, const TvState *sv, double mu,
-                       int coupled, float *out, int W, int N, cudaStream_t st, bool &fits) {
-    // 4 z-pixels per thread where N allows (16-byte aligned groups)
-    auto kern = (N % 4 == 0 && N / 4 <= TVC_THREADS) ? k_tv_prox_cl4 : k_tv_prox_cl;
+template <class K>
+static cudaError_t tvc_config(K kern, const TvcGeom &gm, int W, cudaStream_t st,
+                              cudaLaunchConfig_t &cfg, cudaLaunchAttribute *at, bool &fits) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)gm.smem);
     if (e != cudaSuccess) return e;
@@ -1188,12 +1209,11 @@ cudaError_t tvc_launch(const TvcGeom &gm, const float *z, const TvState *sv, dou
         e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         if (e != cudaSuccess) return e;
     }
-    cudaLaunchConfig_t cfg = {};
+    cfg = cudaLaunchConfig_t{};
     cfg.gridDim = dim3((unsigned)(W * gm.C));
     cfg.blockDim = dim3(TVC_THREADS);
     cfg.dynamicSmemBytes = gm.smem;
     cfg.stream = st;
-    cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
     at[0].val.clusterDim.x = (unsigned)gm.C;
     at[0].val.clusterDim.y = 1;
@@ -1208,8 +1228,61 @@ cudaError_t tvc_launch(const TvcGeom &gm, const float *z, const TvState *sv, dou
         return cudaSuccess;
     }
     fits = true;
+    return cudaSuccess;
+}
+
+cudaError_t tvc_launch(const TvcGeom &gm, const float *z, const TvState *sv, double mu,
+                       int coupled, float *out, int W, int N, cudaStream_t st, bool &fits) {
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute at[1];
+    // 4 z-pixels per thread where N allows (16-byte aligned groups)
+    if (N % 4 == 0 && N / 4 <= TVC_THREADS) {
+        cudaError_t e = tvc_config(k_tv_prox_cl4<false>, gm, W, st, cfg, at, fits);
+        if (e != cudaSuccess || !fits) return e;
+        ++g_launch_count;
+        return cudaLaunchKernelEx(&cfg, k_tv_prox_cl4<false>, z, sv, mu, coupled, out, N, gm.C,
+                                  gm.nloc, (float *)nullptr);
+    }
+    cudaError_t e = tvc_config(k_tv_prox_cl, gm, W, st, cfg, at, fits);
+    if (e != cudaSuccess || !fits) return e;
     ++g_launch_count;
-    return cudaLaunchKernelEx(&cfg, kern, z, sv, mu, coupled, out, N, gm.C, gm.nloc);
+    return cudaLaunchKernelEx(&cfg, k_tv_prox_cl, z, sv, mu, coupled, out, N, gm.C, gm.nloc);
+}
+
+// cluster of 16 CTAs per image with the work vectors in `work` (L2-resident)
+// for images too large for shared memory (N % 4 == 0); false if it cannot
+// run here
+cudaError_t tvc_launch_gm(const float *z, const TvState *sv, double mu, int coupled, float *out,
+                          float *work, int W, int N, cudaStream_t st, bool &ran) {
+    ran = false;
+    const int C = 16, nloc = (N + C - 1) / C;
+    // the slabs must fit the workspace of TV_NVEC vectors per image
+    if (N % 4 != 0 || N / 4 > TVC_THREADS || (size_t)C * TVC_NV * nloc > (size_t)TV_NVEC * N)
+        return cudaSuccess;
+    auto kern = k_tv_prox_cl4<true>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(W * C));
+    cfg.blockDim = dim3(TVC_THREADS);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    e = cudaOccupancyMaxActiveClusters(&clusters, kern, &cfg);
+    if (e != cudaSuccess || clusters < 1) {
+        (void)cudaGetLastError();
+        return cudaSuccess;
+    }
+    ran = true;
+    ++g_launch_count;
+    return cudaLaunchKernelEx(&cfg, kern, z, sv, mu, coupled, out, N, C, nloc, work);
 }
 
 // SB_ITV2 of W images: the cluster kernel where it fits, else the
@@ -1231,6 +1304,15 @@ int tv_prox(const float *z, const TvState *sv, double mu, int coupled, float *ou
     if (!work) {
         set_error("tv prox: no workspace for the global-memory path");
         return MSOT_EINVAL;
+    }
+    if (g_prox_path.load() == 0) {
+        bool ran = false;
+        const cudaError_t e = tvc_launch_gm(z, sv, mu, coupled, out, work, W, N, st, ran);
+        if (e != cudaSuccess) {
+            set_error("tv prox (cluster, global vectors): %s", cudaGetErrorString(e));
+            return MSOT_ECUDA;
+        }
+        if (ran) return MSOT_OK;
     }
     KLAUNCH(k_tv_prox<<<W, TV_THREADS, 0, st>>>(z, sv, mu, coupled, out, work, N));
     MSOT_LAUNCH_CHECK();

@@ -28,10 +28,11 @@ def _noisy_blocks(n, W, seed):
     return out
 
 
-# sizes cover the shared-memory cluster kernel with 1, 2, 4 (ragged last
-# slab), 8 and 16 CTAs per image
+# sizes cover the shared-memory cluster kernels (1 or 4 z-pixels per
+# thread) with 1, 2, 4 (ragged last slab), 8 and 16 CTAs per image, and the
+# 16-CTA cluster with its vectors in global memory (300)
 @pytest.mark.parametrize("n,mu", [(32, 0.05), (64, 0.1), (50, 0.02), (90, 0.05), (128, 0.05),
-                                  (200, 0.03)])
+                                  (200, 0.03), (300, 0.05)])
 def test_sb_itv2_matches_oracle(cuda, n, mu):
     import torch
     from msot_gb300 import SB_ITV2
