@@ -175,6 +175,16 @@ int msot_rec_nn_with_L2_reg(msot_plan_t plan, const float *d_b, float *d_rec, in
                             int num_iter, double lambdaL2, const float *d_x0, int coupled,
                             double *err_img, double *err_reg, void *stream);
 
+/* Warm start of both splitting variables of nnls_L2_less (no reference
+ * counterpart: the reference starts w and v from zero, nnls_L2_less.m:94-95).
+ * d_w0 seeds the image w, d_v0 the multiplier v; at the method's fixed point
+ * v = (A'(A w - b) + lambdaL2 w) / beta on the zero set of w and 0 elsewhere
+ * (beta = 1e-3), which is what a consistent warm start supplies. */
+int msot_rec_nn_with_L2_reg_warm(msot_plan_t plan, const float *d_b, float *d_rec, int batch,
+                                 int num_iter, double lambdaL2, const float *d_w0,
+                                 const float *d_v0, int coupled, double *err_img,
+                                 double *err_reg, void *stream);
+
 /* rec_nn_with_L1_eye_reg.m:1 */
 int msot_rec_nn_with_L1_eye_reg(msot_plan_t plan, const float *d_b, float *d_rec, int batch,
                                 int num_iter, double reg, const float *d_x0, int coupled,

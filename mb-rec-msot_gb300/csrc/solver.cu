@@ -529,8 +529,8 @@ static long count_kernel_nodes(cudaGraph_t g) {
 }
 
 static int solve_l2(Plan &pl, const float *b_in, float *rec, int W, int num_iter,
-                    double lambdaL2, const float *x0, int coupled, double *err_img,
-                    double *err_reg, cudaStream_t user) {
+                    double lambdaL2, const float *x0, const float *v0, int coupled,
+                    double *err_img, double *err_reg, cudaStream_t user) {
     int rc;
     SolverCache *sc = cache_for(pl, W, rc);
     if (rc) return rc;
@@ -551,7 +551,10 @@ static int solve_l2(Plan &pl, const float *b_in, float *rec, int W, int num_iter
             KLAUNCH(k_copy<<<256, 256, 0, st>>>(x0, wv, NI));
         else
             KLAUNCH(k_fill<<<256, 256, 0, st>>>(wv, 0.f, NI));
-        KLAUNCH(k_fill<<<256, 256, 0, st>>>(vm, 0.f, NI));
+        if (v0)
+            KLAUNCH(k_copy<<<256, 256, 0, st>>>(v0, vm, NI));
+        else
+            KLAUNCH(k_fill<<<256, 256, 0, st>>>(vm, 0.f, NI));
         // ||b||^2 per group enters ||b_aug|| of lsqr's tolerance test
         KLAUNCH(k_sumsq<<<dim3(c.nbs, W), RED_THREADS, 0, st>>>(b, nullptr, NS / W, c.P(3)));
         KLAUNCH(k_group_sums<<<1, 1024, 0, st>>>(c.P(3), c.nbs, W, coupled, wk.gsum));
@@ -967,8 +970,24 @@ extern "C" int msot_rec_nn_with_L2_reg(msot_plan_t plan, const float *d_b, float
         set_error("batch %d exceeds the plan's max_batch %d", batch, plan->p.max_batch);
         return MSOT_EINVAL;
     }
-    return solve_l2(plan->p, d_b, d_rec, batch, num_iter, lambdaL2, d_x0, coupled ? 1 : 0,
-                    err_img, err_reg, (cudaStream_t)stream);
+    return solve_l2(plan->p, d_b, d_rec, batch, num_iter, lambdaL2, d_x0, nullptr,
+                    coupled ? 1 : 0, err_img, err_reg, (cudaStream_t)stream);
+}
+
+extern "C" int msot_rec_nn_with_L2_reg_warm(msot_plan_t plan, const float *d_b, float *d_rec,
+                                            int batch, int num_iter, double lambdaL2,
+                                            const float *d_w0, const float *d_v0, int coupled,
+                                            double *err_img, double *err_reg, void *stream) {
+    if (!plan || !d_b || !d_rec || batch <= 0 || num_iter < 0 || !d_w0 || !d_v0) {
+        set_error("rec_nn_with_L2_reg_warm: bad arguments");
+        return MSOT_EINVAL;
+    }
+    if (batch > plan->p.max_batch) {
+        set_error("batch %d exceeds the plan's max_batch %d", batch, plan->p.max_batch);
+        return MSOT_EINVAL;
+    }
+    return solve_l2(plan->p, d_b, d_rec, batch, num_iter, lambdaL2, d_w0, d_v0,
+                    coupled ? 1 : 0, err_img, err_reg, (cudaStream_t)stream);
 }
 
 extern "C" int msot_rec_nn_with_L1_eye_reg(msot_plan_t plan, const float *d_b, float *d_rec,

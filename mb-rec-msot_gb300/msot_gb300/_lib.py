@@ -84,6 +84,8 @@ SIGNATURES = {
     "msot_estimate_norm": (C.c_int, [_vp, C.c_int, C.c_uint64, _dp, _vp]),
     "msot_rec_nn_with_L2_reg": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_double, _vp,
                                           C.c_int, _dp, _dp, _vp]),
+    "msot_rec_nn_with_L2_reg_warm": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_double,
+                                               _vp, _vp, C.c_int, _dp, _dp, _vp]),
     "msot_rec_nn_with_L1_eye_reg": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_double, _vp,
                                               C.c_int, _dp, _dp, _vp]),
     "msot_rec_nn_with_TV_reg": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_double, C.c_int,

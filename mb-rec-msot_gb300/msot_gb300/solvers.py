@@ -37,9 +37,26 @@ def _prep(model: MSOTmodel, data_filt, x0):
     return b, W, x0p, rec
 
 
+def kkt_multiplier(model: MSOTmodel, data_filt, w0, lambdaL2: float = 0.0, beta: float = 1e-3):
+    """The splitting multiplier v consistent with an image w0 (nnls_L2_less's
+    fixed point): v = (A'(A w0 - b) + lambdaL2 w0) / beta where w0 <= 0
+    (clipped at 0), 0 elsewhere.  Costs one A and one A'."""
+    b = torch.as_tensor(data_filt)
+    if not b.is_cuda:
+        b = b.cuda()
+    b = b.to(torch.float32).reshape(-1, *model.sinogram_shape)
+    w = torch.as_tensor(w0).to(device=b.device, dtype=torch.float32).clamp_min(0)
+    w = w.reshape(b.shape[0], *model.image_shape).contiguous()
+    g = model.transpose(model.forward(w) - b)
+    if lambdaL2 and lambdaL2 > 0:
+        g = g + lambdaL2 * w
+    v = torch.where(w > 0, torch.zeros_like(g), (g / beta).clamp_min(0))
+    return w, v.contiguous()
+
+
 def rec_nn_with_L2_reg(model: MSOTmodel, data_filt, num_iter_nn_outer: int, lambdaL2: float = 0.0,
                        RegL2="identity", RegL2T="identity", lambdaL2_2=None, RegL2_2=None,
-                       RegL2T_2=None, *, x0=None, coupled: bool = False, stream=None):
+                       RegL2T_2=None, *, x0=None, v0=None, coupled: bool = False, stream=None):
     """rec_nn_with_L2_reg.m:1.  Returns (rec_img, lCurveErrImg, lCurveErrReg,
     lCurveErrReg_2, err, t) like the reference; lCurveErr* are per-instance
     numpy arrays (one value when coupled), err is empty (the reference only
@@ -53,12 +70,24 @@ def rec_nn_with_L2_reg(model: MSOTmodel, data_filt, num_iter_nn_outer: int, lamb
     e1 = np.zeros(W)
     e2 = np.zeros(W)
     t0 = time.perf_counter()
-    _lib.check(_lib.load().msot_rec_nn_with_L2_reg(
-        model.plan, C.c_void_p(b.data_ptr()), C.c_void_p(rec.data_ptr()), W,
-        int(num_iter_nn_outer), float(lambdaL2 or 0.0),
-        C.c_void_p(x0p.data_ptr()) if x0p is not None else None, 1 if coupled else 0,
-        e1.ctypes.data_as(C.POINTER(C.c_double)), e2.ctypes.data_as(C.POINTER(C.c_double)),
-        _stream_ptr(stream)))
+    if v0 is not None:
+        if x0p is None:
+            raise ValueError("v0 needs x0")
+        v0p = torch.as_tensor(v0).to(device=b.device, dtype=torch.float32)
+        v0p = v0p.reshape(W, *model.image_shape).contiguous()
+        _lib.check(_lib.load().msot_rec_nn_with_L2_reg_warm(
+            model.plan, C.c_void_p(b.data_ptr()), C.c_void_p(rec.data_ptr()), W,
+            int(num_iter_nn_outer), float(lambdaL2 or 0.0), C.c_void_p(x0p.data_ptr()),
+            C.c_void_p(v0p.data_ptr()), 1 if coupled else 0,
+            e1.ctypes.data_as(C.POINTER(C.c_double)), e2.ctypes.data_as(C.POINTER(C.c_double)),
+            _stream_ptr(stream)))
+    else:
+        _lib.check(_lib.load().msot_rec_nn_with_L2_reg(
+            model.plan, C.c_void_p(b.data_ptr()), C.c_void_p(rec.data_ptr()), W,
+            int(num_iter_nn_outer), float(lambdaL2 or 0.0),
+            C.c_void_p(x0p.data_ptr()) if x0p is not None else None, 1 if coupled else 0,
+            e1.ctypes.data_as(C.POINTER(C.c_double)), e2.ctypes.data_as(C.POINTER(C.c_double)),
+            _stream_ptr(stream)))
     t = time.perf_counter() - t0
     if coupled:
         e1, e2 = np.array([e1.sum()]), np.array([e2.sum()])

@@ -86,3 +86,22 @@ def test_l1_nnls_matches_fp64_oracle(norm_pair):
         ref, ref_img, ref_reg = S.rec_nn_with_L1_eye_reg(fwd, adj, b[w].ravel(), 15, 1e-3)
         assert rel(rec[w], ref) <= 1e-3
         assert abs(e_img[w] - ref_img) / ref_img < 1e-3
+
+
+def test_l2_warm_start_with_consistent_multiplier(norm_pair):
+    # Seeding w alone restarts the splitting multiplier v at zero and the
+    # iterates leave even an exact solution; seeding v from the fixed-point
+    # relation (kkt_multiplier) keeps them there.
+    import torch
+    from msot_gb300 import rec_nn_with_L2_reg
+    from msot_gb300.solvers import kkt_multiplier
+    pm, om = norm_pair
+    _, b = _data(om, 64, 2, 25)
+    bt = torch.tensor(b, dtype=torch.float32)
+    ref = rec_nn_with_L2_reg(pm, bt, 300, 1e-2)[0]
+    w0, v0 = kkt_multiplier(pm, bt, ref, 1e-2)
+    warm = rec_nn_with_L2_reg(pm, bt, 5, 1e-2, x0=w0, v0=v0)[0].cpu().numpy()
+    w_only = rec_nn_with_L2_reg(pm, bt, 5, 1e-2, x0=w0)[0].cpu().numpy()
+    r = ref.cpu().numpy()
+    assert rel(warm, r) < 1e-2
+    assert rel(warm, r) < 0.5 * rel(w_only, r)
