@@ -229,6 +229,33 @@ int msot_backproject_waveeq(const float *d_sig, int W, int D, int T, const doubl
                             int psf_n, const float *d_K, int K_n, float *d_out, void *stream);
 
 /* ------------------------------------------------------------------------ */
+/* Learned warm start (no counterpart in the reference): a U-Net that maps an
+ * image (e.g. the adjoint of the data) to an NNLS start.  levels, base
+ * channels c0 (c_l = c0 2^l), square side divisible by 2^(levels-1);
+ * encoder conv3x3+ReLU x2 and 2x2 average pooling, decoder nearest
+ * upsampling + concat + conv3x3+ReLU x2, output conv1x1.  Weights FP32
+ * (Adam) used as BF16 in the convolutions, FP32 accumulation; activations
+ * [n][1][side][side] FP32 on the device.  Parameter layout: per conv (encoder
+ * a, b for level 0..L-1, decoder c, d for level L-2..0, output) the weights
+ * [Co][Ci][k][k] then the biases [Co]. */
+typedef struct msot_unet *msot_unet_t;
+int msot_unet_create(int levels, int base_channels, int side, int max_batch, uint64_t seed,
+                     msot_unet_t *net);
+int msot_unet_destroy(msot_unet_t net);
+int msot_unet_param_count(msot_unet_t net, size_t *n);
+int msot_unet_get_params(msot_unet_t net, float *host_params);
+int msot_unet_set_params(msot_unet_t net, const float *host_params);
+int msot_unet_forward(msot_unet_t net, const float *d_in, float *d_out, int n, void *stream);
+/* Forward + backward of the mean squared error against d_target; the
+ * gradients stay in the net for msot_unet_adam_step and are copied to
+ * host_grad when it is not NULL.  Synchronous. */
+int msot_unet_gradients(msot_unet_t net, const float *d_in, const float *d_target, int n,
+                        double *loss, float *host_grad, void *stream);
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on the last gradients;
+ * step counts from 1 for the bias correction. */
+int msot_unet_adam_step(msot_unet_t net, double lr, int step, void *stream);
+
+/* ------------------------------------------------------------------------ */
 /* Instrumentation (no counterpart in the reference, whose only timing is
  * tic/toc, e.g. rec_nn_with_L2_reg.m:44-49). */
 

@@ -1,0 +1,679 @@
+// unet.cu -- the learned warm start: a U-Net on the project's own kernels.
+//
+// No counterpart in the reference.  Architecture (levels L, base channels
+// c0, channels c_l = c0 2^l, square images of side S divisible by 2^(L-1)):
+//   encoder l = 0..L-1:  conv3x3 + ReLU, conv3x3 + ReLU (-> e_l), 2x2 average
+//                        pool (l < L-1)
+//   decoder l = L-2..0:  nearest 2x upsampling of d_{l+1} (d_{L-1} = e_{L-1}),
+//                        concat [up, e_l], conv3x3 + ReLU, conv3x3 + ReLU (-> d_l)
+//   output:              conv1x1 c0 -> 1
+// Activations NCHW FP32; weights kept in FP32 (Adam) and used as BF16 in the
+// forward and data-gradient convolutions, FP32 accumulation everywhere.
+// Parameter layout (flat): per conv in the order enc (a, b) l = 0..L-1, dec
+// (c, d) l = L-2..0, output: weight [Co][Ci][k][k], then bias [Co].
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstdint>
+#include <random>
+#include <vector>
+
+#include "common.cuh"
+
+namespace msot {
+
+constexpr int CT = 16;   // spatial tile
+constexpr int COT = 8;   // output channels per CTA
+constexpr int CIT = 8;   // input channels per shared-memory stage
+
+// 3x3 "same" convolution, out[n][o][y][x] = bias[o] + sum_i sum_k w(o, i, k)
+// in[n][i][y + ky - 1][x + kx - 1]; TRANS reads the data-gradient weights
+// w(o, i, k) = W[i][o][8 - k] of a layer W[Co'][Ci'][9] (Ci' = Co here).
+template <bool TRANS>
+__global__ void __launch_bounds__(256) k_conv3(const float *__restrict__ in, int Ci,
+                                               const __nv_bfloat16 *__restrict__ w,
+                                               const float *__restrict__ bias,
+                                               float *__restrict__ out, int Co, int H, int Wd,
+                                               int relu, int tiles_x) {
+    __shared__ float s_in[CIT][CT + 2][CT + 3];
+    __shared__ float s_w[COT][CIT][9];
+    const int tile = blockIdx.x, ty0 = (tile / tiles_x) * CT, tx0 = (tile % tiles_x) * CT;
+    const int co0 = blockIdx.y * COT, n = blockIdx.z;
+    const int tx = threadIdx.x % CT, ty = threadIdx.x / CT;
+    const float *inn = in + (size_t)n * Ci * H * Wd;
+    float acc[COT];
+#pragma unroll
+    for (int c = 0; c < COT; ++c) acc[c] = 0.f;
+    for (int ci0 = 0; ci0 < Ci; ci0 += CIT) {
+        for (int i = threadIdx.x; i < CIT * (CT + 2) * (CT + 2); i += 256) {
+            const int c = i / ((CT + 2) * (CT + 2)), r = i % ((CT + 2) * (CT + 2));
+            const int yy = r / (CT + 2), xx = r % (CT + 2);
+            const int y = ty0 + yy - 1, x = tx0 + xx - 1;
+            float v = 0.f;
+            if (ci0 + c < Ci && y >= 0 && y < H && x >= 0 && x < Wd)
+                v = inn[((size_t)(ci0 + c) * H + y) * Wd + x];
+            s_in[c][yy][xx] = v;
+        }
+        for (int i = threadIdx.x; i < COT * CIT * 9; i += 256) {
+            const int o = i / (CIT * 9), r = i % (CIT * 9), c = r / 9, k = r % 9;
+            float v = 0.f;
+            if (co0 + o < Co && ci0 + c < Ci) {
+                const size_t idx = TRANS ? ((size_t)(ci0 + c) * Co + (co0 + o)) * 9 + (8 - k)
+                                         : ((size_t)(co0 + o) * Ci + (ci0 + c)) * 9 + k;
+                v = __bfloat162float(w[idx]);
+            }
+            s_w[o][c][k] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < CIT; ++c)
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                const float v = s_in[c][ty + k / 3][tx + k % 3];
+#pragma unroll
+                for (int o = 0; o < COT; ++o) acc[o] = fmaf(s_w[o][c][k], v, acc[o]);
+            }
+        __syncthreads();
+    }
+    const int y = ty0 + ty, x = tx0 + tx;
+    if (y >= H || x >= Wd) return;
+#pragma unroll
+    for (int o = 0; o < COT; ++o) {
+        if (co0 + o >= Co) break;
+        float v = acc[o] + (bias ? bias[co0 + o] : 0.f);
+        if (relu) v = fmaxf(v, 0.f);
+        out[(((size_t)n * Co + co0 + o) * H + y) * Wd + x] = v;
+    }
+}
+
+// dW[o][i][k] += sum over (n, y, x) of dy[n][o][y][x] x[n][i][y + ky - 1][x + kx - 1]
+// CTA = (8 output channels, 8 input channels, split of the (n, tile) range)
+__global__ void __launch_bounds__(256) k_conv3_dw(const float *__restrict__ x, int Ci,
+                                                  const float *__restrict__ dy, int Co,
+                                                  float *__restrict__ dw, int H, int Wd, int N,
+                                                  int tiles_x, int tiles_img, int splits) {
+    __shared__ float s_x[CIT][CT + 2][CT + 3];
+    __shared__ float s_dy[COT][CT][CT + 1];
+    const int co0 = blockIdx.x * COT, ci0 = blockIdx.y * CIT;
+    constexpr int NOUT = COT * CIT * 9;  // 576
+    float acc[3] = {0.f, 0.f, 0.f};
+    int oo[3], ii[3], kk[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        const int t = threadIdx.x + j * 256;
+        oo[j] = t / (CIT * 9);
+        ii[j] = (t / 9) % CIT;
+        kk[j] = t % 9;
+    }
+    const int total = N * tiles_img;
+    for (int tt = blockIdx.z; tt < total; tt += splits) {
+        const int n = tt / tiles_img, tile = tt % tiles_img;
+        const int ty0 = (tile / tiles_x) * CT, tx0 = (tile % tiles_x) * CT;
+        __syncthreads();
+        for (int i = threadIdx.x; i < CIT * (CT + 2) * (CT + 2); i += 256) {
+            const int c = i / ((CT + 2) * (CT + 2)), r = i % ((CT + 2) * (CT + 2));
+            const int yy = r / (CT + 2), xx = r % (CT + 2);
+            const int y = ty0 + yy - 1, xq = tx0 + xx - 1;
+            float v = 0.f;
+            if (ci0 + c < Ci && y >= 0 && y < H && xq >= 0 && xq < Wd)
+                v = x[(((size_t)n * Ci + ci0 + c) * H + y) * Wd + xq];
+            s_x[c][yy][xx] = v;
+        }
+        for (int i = threadIdx.x; i < COT * CT * CT; i += 256) {
+            const int o = i / (CT * CT), r = i % (CT * CT), yy = r / CT, xx = r % CT;
+            const int y = ty0 + yy, xq = tx0 + xx;
+            float v = 0.f;
+            if (co0 + o < Co && y < H && xq < Wd)
+                v = dy[(((size_t)n * Co + co0 + o) * H + y) * Wd + xq];
+            s_dy[o][yy][xx] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            if (threadIdx.x + j * 256 >= NOUT) break;
+            const int o = oo[j], c = ii[j], ky = kk[j] / 3, kx = kk[j] % 3;
+            float a = acc[j];
+            for (int yy = 0; yy < CT; ++yy)
+#pragma unroll
+                for (int xx = 0; xx < CT; ++xx)
+                    a = fmaf(s_dy[o][yy][xx], s_x[c][yy + ky][xx + kx], a);
+            acc[j] = a;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        if (threadIdx.x + j * 256 >= NOUT) break;
+        const int o = co0 + oo[j], c = ci0 + ii[j];
+        if (o < Co && c < Ci) atomicAdd(&dw[((size_t)o * Ci + c) * 9 + kk[j]], acc[j]);
+    }
+}
+
+// db[o] += sum over (n, p) dy[n][o][p]; one CTA per (o, n)
+__global__ void k_bias_grad(const float *__restrict__ dy, int Co, int HW, float *db) {
+    __shared__ float sh[32];
+    const int o = blockIdx.x, n = blockIdx.y;
+    const float *p = dy + ((size_t)n * Co + o) * HW;
+    float a = 0.f;
+    for (int i = threadIdx.x; i < HW; i += blockDim.x) a += p[i];
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) a += __shfl_down_sync(0xffffffffu, a, s);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = a;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        a = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.f;
+#pragma unroll
+        for (int s = 16; s > 0; s >>= 1) a += __shfl_down_sync(0xffffffffu, a, s);
+        if (threadIdx.x == 0) atomicAdd(&db[o], a);
+    }
+}
+
+// dy_pre = dy_post * (y_post > 0)
+__global__ void k_relu_bwd(const float *__restrict__ y, const float *__restrict__ dy,
+                           float *__restrict__ out, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        out[i] = y[i] > 0.f ? dy[i] : 0.f;
+}
+
+// 2x2 average pool of [NC][H][W] -> [NC][H/2][W/2], and its adjoint
+__global__ void k_pool(const float *__restrict__ in, float *__restrict__ out, int NC, int H,
+                       int Wd) {
+    const int h = H / 2, w = Wd / 2;
+    const size_t n = (size_t)NC * h * w;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const size_t c = i / ((size_t)h * w);
+        const int r = (int)(i % ((size_t)h * w)), y = r / w, x = r % w;
+        const float *p = in + (c * H + 2 * y) * Wd + 2 * x;
+        out[i] = 0.25f * (p[0] + p[1] + p[Wd] + p[Wd + 1]);
+    }
+}
+__global__ void k_pool_bwd(const float *__restrict__ dout, float *__restrict__ din, int NC,
+                           int H, int Wd, int accumulate) {
+    const size_t n = (size_t)NC * H * Wd;
+    const int w = Wd / 2, h = H / 2;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const size_t c = i / ((size_t)H * Wd);
+        const int r = (int)(i % ((size_t)H * Wd)), y = r / Wd, x = r % Wd;
+        const float g = 0.25f * dout[(c * h + y / 2) * w + x / 2];
+        din[i] = accumulate ? din[i] + g : g;
+    }
+}
+// nearest 2x upsampling of [N][C][h][w] into channels [0, C) of [N][Ctot][2h][2w]
+__global__ void k_up_into(const float *__restrict__ in, float *__restrict__ out, int N, int C,
+                          int Ctot, int h, int w) {
+    const int H = 2 * h, Wd = 2 * w;
+    const size_t n = (size_t)N * C * H * Wd;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const size_t nc = i / ((size_t)H * Wd);
+        const int r = (int)(i % ((size_t)H * Wd)), y = r / Wd, x = r % Wd;
+        const int b = (int)(nc / C), c = (int)(nc % C);
+        out[(((size_t)b * Ctot + c) * H + y) * Wd + x] = in[(nc * h + y / 2) * w + x / 2];
+    }
+}
+// adjoint: dsmall[n][c][y][x] = sum of the 2x2 block of channel c of dbig [N][Ctot][2h][2w]
+__global__ void k_up_bwd(const float *__restrict__ dbig, float *__restrict__ dsmall, int N,
+                         int C, int Ctot, int h, int w) {
+    const size_t n = (size_t)N * C * h * w;
+    const int Wd = 2 * w, H = 2 * h;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const size_t nc = i / ((size_t)h * w);
+        const int r = (int)(i % ((size_t)h * w)), y = r / w, x = r % w;
+        const int b = (int)(nc / C), c = (int)(nc % C);
+        const float *p = dbig + (((size_t)b * Ctot + c) * H + 2 * y) * Wd + 2 * x;
+        dsmall[i] = p[0] + p[1] + p[Wd] + p[Wd + 1];
+    }
+}
+// copy [N][C][HW] into channels [c0, c0 + C) of [N][Ctot][HW] (or back, adding when acc)
+__global__ void k_chan_copy(const float *__restrict__ src, int Cs, int cs0, float *__restrict__ dst,
+                            int Cd, int cd0, int N, int C, int HW, int acc) {
+    const size_t n = (size_t)N * C * HW;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int p = (int)(i % HW);
+        const size_t nc = i / HW;
+        const int b = (int)(nc / C), c = (int)(nc % C);
+        const float v = src[((size_t)b * Cs + cs0 + c) * HW + p];
+        float &d = dst[((size_t)b * Cd + cd0 + c) * HW + p];
+        d = acc ? d + v : v;
+    }
+}
+// 1x1 output conv c0 -> 1 and its gradients
+__global__ void k_conv1(const float *__restrict__ in, int C, const float *__restrict__ w,
+                        const float *__restrict__ b, float *__restrict__ out, int N, int HW) {
+    const size_t n = (size_t)N * HW;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int bi = (int)(i / HW), p = (int)(i % HW);
+        float a = b[0];
+        for (int c = 0; c < C; ++c) a = fmaf(w[c], in[((size_t)bi * C + c) * HW + p], a);
+        out[i] = a;
+    }
+}
+__global__ void k_conv1_bwd_data(const float *__restrict__ dout, const float *__restrict__ w,
+                                 float *__restrict__ din, int C, int N, int HW) {
+    const size_t n = (size_t)N * C * HW;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int p = (int)(i % HW);
+        const size_t nc = i / HW;
+        const int bi = (int)(nc / C), c = (int)(nc % C);
+        din[i] = w[c] * dout[(size_t)bi * HW + p];
+    }
+}
+// dw[c] += sum dout * in[c]; one CTA per (c, n)
+__global__ void k_conv1_dw(const float *__restrict__ dout, const float *__restrict__ in,
+                           float *dw, int C, int HW) {
+    __shared__ float sh[32];
+    const int c = blockIdx.x, n = blockIdx.y;
+    const float *a = dout + (size_t)n * HW, *x = in + ((size_t)n * C + c) * HW;
+    float s = 0.f;
+    for (int i = threadIdx.x; i < HW; i += blockDim.x) s = fmaf(a[i], x[i], s);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) atomicAdd(&dw[c], s);
+    }
+}
+// loss = mean (out - t)^2 (partial sums in FP64 per CTA), dout = 2 (out - t) / n
+__global__ void k_mse(const float *__restrict__ out, const float *__restrict__ t,
+                      float *__restrict__ dout, size_t n, double *loss) {
+    __shared__ double sh[32];
+    double s = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const float d = out[i] - t[i];
+        s += (double)d * d;
+        dout[i] = 2.f * d / (float)n;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) atomicAdd(loss, s / (double)n);
+    }
+}
+// Adam (Kingma & Ba) with bias correction; refreshes the BF16 copy
+__global__ void k_adam(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
+                       float *__restrict__ v, __nv_bfloat16 *__restrict__ pb, size_t n, float lr,
+                       float b1, float b2, float eps, float c1, float c2) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        const float pi = p[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+        p[i] = pi;
+        pb[i] = __float2bfloat16_rn(pi);
+    }
+}
+__global__ void k_to_bf16(const float *__restrict__ p, __nv_bfloat16 *__restrict__ pb, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        pb[i] = __float2bfloat16_rn(p[i]);
+}
+
+}  // namespace msot
+
+using namespace msot;
+
+struct ConvL {
+    int Ci, Co, S;        // channels and spatial side
+    size_t w_off, b_off;  // in the flat parameter array
+};
+
+struct msot_unet {
+    int L = 0, c0 = 0, S = 0, max_n = 0;
+    std::vector<int> ch, side;
+    std::vector<ConvL> enc_a, enc_b, dec_c, dec_d;
+    size_t out_w = 0, out_b = 0, n_par = 0;
+    float *par = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;
+    __nv_bfloat16 *parb = nullptr;
+    // forward activations (post-ReLU) per level
+    std::vector<float *> ea, e, pool, cat, da, d;
+    // gradient buffers per level: Ga (concat-sized), Gb, Gc, Gd, Gs (c_l channels)
+    std::vector<float *> Ga, Gb, Gc, Gd, Gs;
+    float *outb = nullptr, *dout = nullptr;
+    double *loss = nullptr;
+    std::vector<void *> all;
+    ~msot_unet() {
+        for (void *q : all) cudaFree(q);
+    }
+};
+
+namespace {
+
+inline unsigned nblk(size_t n) { return (unsigned)std::min<size_t>((n + 255) / 256, 65535); }
+
+template <class T>
+T *dalloc(msot_unet *u, size_t n) {
+    void *p = nullptr;
+    if (cudaMalloc(&p, (n ? n : 1) * sizeof(T)) != cudaSuccess) return nullptr;
+    u->all.push_back(p);
+    return static_cast<T *>(p);
+}
+
+int conv_fwd(msot_unet *u, const ConvL &c, const float *in, float *out, int N, cudaStream_t st) {
+    const int tx = (c.S + CT - 1) / CT;
+    dim3 grid(tx * tx, (c.Co + COT - 1) / COT, N);
+    KLAUNCH(k_conv3<false><<<grid, 256, 0, st>>>(in, c.Ci, u->parb + c.w_off, u->par + c.b_off,
+                                                 out, c.Co, c.S, c.S, 1, tx));
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
+}
+
+// conv c with input x and ReLU output y; dy_post = d loss / d y.  Adds dW, db;
+// writes dy_pre (scratch) and dx (if non-null).  No two pointers alias.
+int conv_bwd(msot_unet *u, const ConvL &c, const float *x, const float *y, const float *dy_post,
+             float *dy_pre, float *dx, int N, cudaStream_t st) {
+    const size_t ny = (size_t)N * c.Co * c.S * c.S;
+    KLAUNCH(k_relu_bwd<<<nblk(ny), 256, 0, st>>>(y, dy_post, dy_pre, ny));
+    const int tx = (c.S + CT - 1) / CT, tiles = tx * tx;
+    const int cog = (c.Co + COT - 1) / COT, cig = (c.Ci + CIT - 1) / CIT;
+    const int splits = std::max(1, std::min(N * tiles, (4 * 152 + cog * cig - 1) / (cog * cig)));
+    KLAUNCH(k_conv3_dw<<<dim3(cog, cig, splits), 256, 0, st>>>(
+        x, c.Ci, dy_pre, c.Co, u->grad + c.w_off, c.S, c.S, N, tx, tiles, splits));
+    KLAUNCH(k_bias_grad<<<dim3(c.Co, N), 256, 0, st>>>(dy_pre, c.Co, c.S * c.S,
+                                                        u->grad + c.b_off));
+    if (dx) {
+        dim3 grid(tiles, (c.Ci + COT - 1) / COT, N);
+        KLAUNCH(k_conv3<true><<<grid, 256, 0, st>>>(dy_pre, c.Co, u->parb + c.w_off, nullptr, dx,
+                                                    c.Ci, c.S, c.S, 0, tx));
+    }
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
+}
+
+int forward(msot_unet *u, const float *in, int N, cudaStream_t st) {
+    int rc;
+    const int L = u->L;
+    const float *x = in;
+    for (int l = 0; l < L; ++l) {
+        if ((rc = conv_fwd(u, u->enc_a[l], x, u->ea[l], N, st))) return rc;
+        if ((rc = conv_fwd(u, u->enc_b[l], u->ea[l], u->e[l], N, st))) return rc;
+        if (l + 1 < L) {
+            const int S = u->side[l];
+            const size_t n = (size_t)N * u->ch[l] * (S / 2) * (S / 2);
+            KLAUNCH(k_pool<<<nblk(n), 256, 0, st>>>(u->e[l], u->pool[l], N * u->ch[l], S, S));
+            x = u->pool[l];
+        }
+    }
+    const float *dn = u->e[L - 1];
+    for (int l = L - 2; l >= 0; --l) {
+        const int S = u->side[l], Cu = u->ch[l + 1], Ce = u->ch[l], Ct = Cu + Ce;
+        KLAUNCH(k_up_into<<<nblk((size_t)N * Cu * S * S), 256, 0, st>>>(dn, u->cat[l], N, Cu, Ct,
+                                                                         S / 2, S / 2));
+        KLAUNCH(k_chan_copy<<<nblk((size_t)N * Ce * S * S), 256, 0, st>>>(
+            u->e[l], Ce, 0, u->cat[l], Ct, Cu, N, Ce, S * S, 0));
+        if ((rc = conv_fwd(u, u->dec_c[l], u->cat[l], u->da[l], N, st))) return rc;
+        if ((rc = conv_fwd(u, u->dec_d[l], u->da[l], u->d[l], N, st))) return rc;
+        dn = u->d[l];
+    }
+    const int HW = u->S * u->S;
+    KLAUNCH(k_conv1<<<nblk((size_t)N * HW), 256, 0, st>>>(dn, u->c0, u->par + u->out_w,
+                                                          u->par + u->out_b, u->outb, N, HW));
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
+}
+
+// gradients of mean (out - target)^2 after forward(); loss in u->loss
+int backward(msot_unet *u, const float *in, const float *target, int N, cudaStream_t st) {
+    int rc;
+    const int HW = u->S * u->S, L = u->L;
+    MSOT_CUDA_TRY(cudaMemsetAsync(u->grad, 0, u->n_par * sizeof(float), st));
+    MSOT_CUDA_TRY(cudaMemsetAsync(u->loss, 0, sizeof(double), st));
+    KLAUNCH(k_mse<<<nblk((size_t)N * HW), 256, 0, st>>>(u->outb, target, u->dout,
+                                                       (size_t)N * HW, u->loss));
+    const float *top = L >= 2 ? u->d[0] : u->e[0];
+    KLAUNCH(k_conv1_dw<<<dim3(u->c0, N), 256, 0, st>>>(u->dout, top, u->grad + u->out_w, u->c0,
+                                                       HW));
+    KLAUNCH(k_bias_grad<<<dim3(1, N), 256, 0, st>>>(u->dout, 1, HW, u->grad + u->out_b));
+    KLAUNCH(k_conv1_bwd_data<<<nblk((size_t)N * u->c0 * HW), 256, 0, st>>>(
+        u->dout, u->par + u->out_w, u->Gb[0], u->c0, N, HW));
+    MSOT_LAUNCH_CHECK();
+    // decoder, shallow to deep: Gb[l] = d loss / d d_l on entry
+    for (int l = 0; l + 1 < L; ++l) {
+        const int S = u->side[l], Cu = u->ch[l + 1], Ce = u->ch[l], Ct = Cu + Ce;
+        if ((rc = conv_bwd(u, u->dec_d[l], u->da[l], u->d[l], u->Gb[l], u->Gc[l], u->Gd[l], N,
+                           st)))
+            return rc;
+        if ((rc = conv_bwd(u, u->dec_c[l], u->cat[l], u->da[l], u->Gd[l], u->Gc[l], u->Ga[l], N,
+                           st)))
+            return rc;
+        KLAUNCH(k_chan_copy<<<nblk((size_t)N * Ce * S * S), 256, 0, st>>>(
+            u->Ga[l], Ct, Cu, u->Gs[l], Ce, 0, N, Ce, S * S, 0));
+        const int h = S / 2;
+        KLAUNCH(k_up_bwd<<<nblk((size_t)N * Cu * h * h), 256, 0, st>>>(u->Ga[l], u->Gb[l + 1], N,
+                                                                        Cu, Ct, h, h));
+        MSOT_LAUNCH_CHECK();
+    }
+    // encoder, deep to shallow: Gb[l] = d loss / d e_l from above
+    for (int l = L - 1; l >= 0; --l) {
+        const int S = u->side[l];
+        if (l + 1 < L) {
+            const size_t n = (size_t)N * u->ch[l] * S * S;
+            KLAUNCH(k_chan_copy<<<nblk(n), 256, 0, st>>>(u->Gs[l], u->ch[l], 0, u->Gb[l],
+                                                         u->ch[l], 0, N, u->ch[l], S * S, 1));
+        }
+        if ((rc = conv_bwd(u, u->enc_b[l], u->ea[l], u->e[l], u->Gb[l], u->Gc[l], u->Gd[l], N,
+                           st)))
+            return rc;
+        const float *xin = l == 0 ? in : u->pool[l - 1];
+        if ((rc = conv_bwd(u, u->enc_a[l], xin, u->ea[l], u->Gd[l], u->Gc[l],
+                           l > 0 ? u->Ga[l] : nullptr, N, st)))
+            return rc;
+        if (l > 0) {
+            const int Sp = u->side[l - 1];
+            const size_t n = (size_t)N * u->ch[l - 1] * Sp * Sp;
+            KLAUNCH(k_pool_bwd<<<nblk(n), 256, 0, st>>>(u->Ga[l], u->Gb[l - 1], N * u->ch[l - 1],
+                                                        Sp, Sp, 0));
+            MSOT_LAUNCH_CHECK();
+        }
+    }
+    return MSOT_OK;
+}
+
+int check_net(msot_unet_t u, int N, const void *a, const void *b) {
+    if (!u || N <= 0 || N > u->max_n || !a || !b) {
+        set_error("unet: bad arguments (batch %d, max %d)", N, u ? u->max_n : 0);
+        return MSOT_EINVAL;
+    }
+    return MSOT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int msot_unet_create(int levels, int base_channels, int side, int max_batch, uint64_t seed,
+                     msot_unet_t *out) {
+    if (!out || levels < 1 || levels > 6 || base_channels < 1 || base_channels > 256 ||
+        max_batch < 1 || side < 1 || side % (1 << (levels - 1)) != 0) {
+        set_error("unet_create: bad arguments (side must be divisible by 2^(levels-1))");
+        return MSOT_EINVAL;
+    }
+    auto *u = new msot_unet();
+    u->L = levels;
+    u->c0 = base_channels;
+    u->S = side;
+    u->max_n = max_batch;
+    size_t off = 0;
+    auto add = [&](std::vector<ConvL> &vec, int Ci, int Co, int S) {
+        ConvL c{Ci, Co, S, off, off + (size_t)Co * Ci * 9};
+        off = c.b_off + Co;
+        vec.push_back(c);
+    };
+    for (int l = 0; l < levels; ++l) {
+        u->ch.push_back(base_channels << l);
+        u->side.push_back(side >> l);
+    }
+    u->dec_c.resize(levels);
+    u->dec_d.resize(levels);
+    for (int l = 0; l < levels; ++l) {
+        add(u->enc_a, l == 0 ? 1 : u->ch[l - 1], u->ch[l], u->side[l]);
+        add(u->enc_b, u->ch[l], u->ch[l], u->side[l]);
+    }
+    for (int l = levels - 2; l >= 0; --l) {
+        std::vector<ConvL> tmp;
+        add(tmp, u->ch[l + 1] + u->ch[l], u->ch[l], u->side[l]);
+        add(tmp, u->ch[l], u->ch[l], u->side[l]);
+        u->dec_c[l] = tmp[0];
+        u->dec_d[l] = tmp[1];
+    }
+    u->out_w = off;
+    u->out_b = off + base_channels;
+    u->n_par = u->out_b + 1;
+    // He-normal weights (fan-in), zero biases
+    std::vector<float> h(u->n_par, 0.f);
+    std::mt19937_64 rng(seed);
+    std::normal_distribution<float> nd(0.f, 1.f);
+    auto init = [&](const ConvL &c) {
+        const float sd = std::sqrt(2.f / (float)(c.Ci * 9));
+        for (size_t i = 0; i < (size_t)c.Co * c.Ci * 9; ++i) h[c.w_off + i] = sd * nd(rng);
+    };
+    for (auto &c : u->enc_a) init(c);
+    for (auto &c : u->enc_b) init(c);
+    for (int l = 0; l + 1 < levels; ++l) {
+        init(u->dec_c[l]);
+        init(u->dec_d[l]);
+    }
+    for (int c = 0; c < base_channels; ++c) h[u->out_w + c] = std::sqrt(1.f / base_channels) * nd(rng);
+    bool ok = true;
+    auto F = [&](size_t n) {
+        float *p = dalloc<float>(u, n);
+        ok = ok && p;
+        return p;
+    };
+    u->par = F(u->n_par);
+    u->grad = F(u->n_par);
+    u->m = F(u->n_par);
+    u->v = F(u->n_par);
+    u->parb = dalloc<__nv_bfloat16>(u, u->n_par);
+    ok = ok && u->parb;
+    const size_t N = max_batch;
+    for (int l = 0; l < levels; ++l) {
+        const size_t S2 = (size_t)u->side[l] * u->side[l], c = u->ch[l];
+        const size_t ct = l + 1 < levels ? (size_t)u->ch[l + 1] + c : c;
+        u->ea.push_back(F(N * c * S2));
+        u->e.push_back(F(N * c * S2));
+        u->pool.push_back(l + 1 < levels ? F(N * c * S2 / 4) : nullptr);
+        u->cat.push_back(l + 1 < levels ? F(N * ct * S2) : nullptr);
+        u->da.push_back(l + 1 < levels ? F(N * c * S2) : nullptr);
+        u->d.push_back(l + 1 < levels ? F(N * c * S2) : nullptr);
+        u->Ga.push_back(F(N * ct * S2));
+        u->Gb.push_back(F(N * c * S2));
+        u->Gc.push_back(F(N * c * S2));
+        u->Gd.push_back(F(N * c * S2));
+        u->Gs.push_back(F(N * c * S2));
+    }
+    u->outb = F(N * side * side);
+    u->dout = F(N * side * side);
+    u->loss = dalloc<double>(u, 1);
+    ok = ok && u->loss;
+    if (!ok) {
+        delete u;
+        set_error("unet_create: device allocation failed");
+        return MSOT_ENOMEM;
+    }
+    cudaError_t e = cudaMemcpy(u->par, h.data(), sizeof(float) * u->n_par, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(u->m, 0, sizeof(float) * u->n_par);
+    if (e == cudaSuccess) e = cudaMemset(u->v, 0, sizeof(float) * u->n_par);
+    if (e != cudaSuccess) {
+        delete u;
+        set_error("unet_create: %s", cudaGetErrorString(e));
+        return MSOT_ECUDA;
+    }
+    KLAUNCH(k_to_bf16<<<nblk(u->n_par), 256>>>(u->par, u->parb, u->n_par));
+    *out = u;
+    return MSOT_OK;
+}
+
+int msot_unet_destroy(msot_unet_t u) {
+    delete u;
+    return MSOT_OK;
+}
+
+int msot_unet_param_count(msot_unet_t u, size_t *n) {
+    if (!u || !n) {
+        set_error("unet_param_count: null argument");
+        return MSOT_EINVAL;
+    }
+    *n = u->n_par;
+    return MSOT_OK;
+}
+
+int msot_unet_get_params(msot_unet_t u, float *host) {
+    if (!u || !host) {
+        set_error("unet_get_params: null argument");
+        return MSOT_EINVAL;
+    }
+    MSOT_CUDA_TRY(cudaMemcpy(host, u->par, sizeof(float) * u->n_par, cudaMemcpyDeviceToHost));
+    return MSOT_OK;
+}
+
+int msot_unet_set_params(msot_unet_t u, const float *host) {
+    if (!u || !host) {
+        set_error("unet_set_params: null argument");
+        return MSOT_EINVAL;
+    }
+    MSOT_CUDA_TRY(cudaMemcpy(u->par, host, sizeof(float) * u->n_par, cudaMemcpyHostToDevice));
+    KLAUNCH(k_to_bf16<<<nblk(u->n_par), 256>>>(u->par, u->parb, u->n_par));
+    MSOT_LAUNCH_CHECK();
+    MSOT_CUDA_TRY(cudaDeviceSynchronize());
+    return MSOT_OK;
+}
+
+int msot_unet_forward(msot_unet_t u, const float *d_in, float *d_out, int n, void *stream) {
+    int rc = check_net(u, n, d_in, d_out);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    if ((rc = forward(u, d_in, n, st))) return rc;
+    MSOT_CUDA_TRY(cudaMemcpyAsync(d_out, u->outb, sizeof(float) * n * u->S * u->S,
+                                  cudaMemcpyDeviceToDevice, st));
+    return MSOT_OK;
+}
+
+int msot_unet_gradients(msot_unet_t u, const float *d_in, const float *d_target, int n,
+                        double *loss, float *host_grad, void *stream) {
+    int rc = check_net(u, n, d_in, d_target);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    if ((rc = forward(u, d_in, n, st))) return rc;
+    if ((rc = backward(u, d_in, d_target, n, st))) return rc;
+    if (loss)
+        MSOT_CUDA_TRY(cudaMemcpyAsync(loss, u->loss, sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (host_grad)
+        MSOT_CUDA_TRY(cudaMemcpyAsync(host_grad, u->grad, sizeof(float) * u->n_par,
+                                      cudaMemcpyDeviceToHost, st));
+    MSOT_CUDA_TRY(cudaStreamSynchronize(st));
+    return MSOT_OK;
+}
+
+int msot_unet_adam_step(msot_unet_t u, double lr, int step, void *stream) {
+    if (!u || step < 1 || !(lr > 0)) {
+        set_error("unet_adam_step: bad arguments");
+        return MSOT_EINVAL;
+    }
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - std::pow(b1, (float)step), c2 = 1.f - std::pow(b2, (float)step);
+    KLAUNCH(k_adam<<<nblk(u->n_par), 256, 0, (cudaStream_t)stream>>>(
+        u->par, u->grad, u->m, u->v, u->parb, u->n_par, (float)lr, b1, b2, 1e-8f, c1, c2));
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
+}
+
+}  // extern "C"

@@ -100,6 +100,15 @@ SIGNATURES = {
                                     _dp]),
     "msot_spmr_query": (C.c_int, [C.POINTER(SpmrSpec), C.POINTER(SpmrInfo)]),
     "msot_spmr_tables": (C.c_int, [C.POINTER(SpmrSpec), _dp, _ip, _ip]),
+    "msot_unet_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64,
+                                   C.POINTER(C.c_void_p)]),
+    "msot_unet_destroy": (C.c_int, [_vp]),
+    "msot_unet_param_count": (C.c_int, [_vp, C.POINTER(C.c_size_t)]),
+    "msot_unet_get_params": (C.c_int, [_vp, C.POINTER(C.c_float)]),
+    "msot_unet_set_params": (C.c_int, [_vp, C.POINTER(C.c_float)]),
+    "msot_unet_forward": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp]),
+    "msot_unet_gradients": (C.c_int, [_vp, _vp, _vp, C.c_int, _dp, C.POINTER(C.c_float), _vp]),
+    "msot_unet_adam_step": (C.c_int, [_vp, C.c_double, C.c_int, _vp]),
     "msot_dmas_cf": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _dp, C.c_int, _dp, C.c_int,
                                C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                _vp, _vp, _vp, _vp, _vp]),

@@ -1,0 +1,87 @@
+"""The warm-start U-Net's CUDA kernels against a PyTorch CPU fp32 reference
+of the same network (BF16-rounded convolution weights, as the GPU uses)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _ref_forward(torch, params, x, L, c0, leaves):
+    """Same network on the CPU; the 3x3 weights are rounded to BF16 as the
+    GPU uses them and become float leaves (the gradient of a dtype cast would
+    itself be rounded).  ``leaves`` receives the leaves in parameter order."""
+    F = torch.nn.functional
+    off = [0]
+
+    def take(co, ci, k, round_bf16=True):
+        n = co * ci * k * k
+        w = params[off[0]:off[0] + n].view(co, ci, k, k)
+        off[0] += n
+        b = params[off[0]:off[0] + co]
+        off[0] += co
+        if round_bf16:
+            w = w.to(torch.bfloat16).float()
+        w = w.detach().clone().requires_grad_()
+        b = b.detach().clone().requires_grad_()
+        leaves.extend([w, b])
+        return w, b
+
+    ch = [c0 << l for l in range(L)]
+    enc = [(take(ch[l], 1 if l == 0 else ch[l - 1], 3), take(ch[l], ch[l], 3)) for l in range(L)]
+    dec = {}
+    for l in range(L - 2, -1, -1):
+        dec[l] = (take(ch[l], ch[l + 1] + ch[l], 3), take(ch[l], ch[l], 3))
+    wo, bo = take(1, c0, 1, round_bf16=False)
+    es = []
+    h = x
+    for l in range(L):
+        (wa, ba), (wb, bb) = enc[l]
+        a = F.relu(F.conv2d(h, wa, ba, padding=1))
+        e = F.relu(F.conv2d(a, wb, bb, padding=1))
+        es.append(e)
+        if l < L - 1:
+            h = F.avg_pool2d(e, 2)
+    d = es[L - 1]
+    for l in range(L - 2, -1, -1):
+        u = F.interpolate(d, scale_factor=2, mode="nearest")
+        (wc, bc), (wd, bd) = dec[l]
+        da = F.relu(F.conv2d(torch.cat([u, es[l]], 1), wc, bc, padding=1))
+        d = F.relu(F.conv2d(da, wd, bd, padding=1))
+    return F.conv2d(d, wo, bo)
+
+
+@pytest.mark.parametrize("L,c0,side,n", [(3, 4, 32, 2), (4, 8, 32, 3), (1, 8, 16, 2)])
+def test_unet_forward_and_gradients_match_torch_reference(cuda, L, c0, side, n):
+    import torch
+    from msot_gb300.warmstart import UNet
+    net = UNet(levels=L, base_channels=c0, side=side, max_batch=4, seed=7)
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal((n, 1, side, side)).astype(np.float32)
+    t = rng.standard_normal((n, 1, side, side)).astype(np.float32)
+    p = torch.tensor(net.get_params())
+    leaves = []
+    out_ref = _ref_forward(torch, p, torch.tensor(x), L, c0, leaves)
+    out = net.forward(x).cpu()
+    assert float((out - out_ref.detach()).norm() / out_ref.detach().norm()) < 1e-4
+    loss_ref = ((out_ref - torch.tensor(t)) ** 2).mean()
+    loss_ref.backward()
+    # _ref_forward takes the blocks in the parameter layout's order
+    g_ref = torch.cat([v.grad.reshape(-1) for v in leaves]).numpy()
+    loss, g = net.gradients(x, t)
+    assert abs(loss - float(loss_ref)) / float(loss_ref) < 1e-4
+    assert np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref) < 1e-4
+
+
+def test_unet_training_reduces_loss(cuda):
+    # learn a fixed smoothing of the input: the loss must drop by 10x
+    import torch
+    from msot_gb300.warmstart import UNet
+    net = UNet(levels=3, base_channels=8, side=32, max_batch=8, seed=3)
+    rng = np.random.default_rng(2)
+    x = torch.tensor(rng.standard_normal((8, 1, 32, 32)).astype(np.float32), device="cuda")
+    k = torch.ones(1, 1, 3, 3, device="cuda") / 9.0
+    t = torch.nn.functional.conv2d(x, k, padding=1)
+    first = net.train_step(x, t, lr=3e-3)
+    for _ in range(300):
+        last = net.train_step(x, t, lr=3e-3)
+    assert last < 0.1 * first
