@@ -2,6 +2,15 @@
 reference): a U-Net on the project's CUDA kernels (msot_unet_*), trained on
 pairs the plain GPU solver generates, whose prediction seeds both splitting
 variables of rec_nn_with_L2_reg (image w and multiplier v, kkt_multiplier).
+
+The network input f is either the backprojection A'b of a sinogram b
+(input_iters = 0) or the plain solver's iterate after input_iters
+iterations.  Input f / s, output x / (kappa s), with s = rms(f) per instance
+and kappa = median rms(x) / rms(f) over the training pairs, so one network
+serves any data scale; with ``residual`` (an iterate as input, kappa = 1)
+the network predicts the correction x / s - f / s.  The plain solver stays
+the fallback: an instance whose prediction has a larger objective
+|A x0 - b|^2 + lambda |x0|^2 than the zero start (|b|^2) is started from zero.
 """
 from __future__ import annotations
 
@@ -12,6 +21,7 @@ import torch
 
 from . import _lib
 from .model import _stream_ptr
+from .solvers import rec_nn_with_L2_reg
 
 
 class UNet:
@@ -82,3 +92,119 @@ class UNet:
         _lib.check(_lib.load().msot_unet_adam_step(self._h, float(lr), self.step_count,
                                                    _stream_ptr(stream)))
         return loss.value
+
+
+class LearnedWarmStart:
+    """Warm start of rec_nn_with_L2_reg(model, b, iters, lambdaL2) from a
+    U-Net prediction (see the module docstring)."""
+
+    def __init__(self, model, lambdaL2: float = 0.0, net: UNet | None = None, levels=4,
+                 base_channels=32, max_batch=16, seed=0, beta=1e-3, input_iters=0,
+                 residual=None):
+        nx, nz = model.image_shape
+        if nx != nz:
+            raise ValueError("the warm-start network needs a square grid")
+        self.model, self.lam, self.beta = model, float(lambdaL2 or 0.0), beta
+        self.net = net or UNet(levels, base_channels, nx, max_batch, seed)
+        self.input_iters = int(input_iters)
+        self.residual = bool(self.input_iters > 0 if residual is None else residual)
+        if self.residual and self.input_iters <= 0:
+            raise ValueError("the residual form needs an iterate as input (input_iters > 0)")
+        self.kappa = 1.0 if self.residual else None
+
+    def _chunks(self, W):
+        m = self.model.max_batch
+        return [(i, min(W, i + m)) for i in range(0, W, m)]
+
+    def _sino(self, b):
+        b = torch.as_tensor(b)
+        if not b.is_cuda:
+            b = b.cuda()
+        return b.to(torch.float32).reshape(-1, *self.model.sinogram_shape).contiguous()
+
+    def features(self, b):
+        """(f / s as (W, 1, n, n), s (W,)); f = A'b or the plain iterate."""
+        b = self._sino(b)
+        if self.input_iters > 0:
+            f = torch.cat([rec_nn_with_L2_reg(self.model, b[i:j], self.input_iters, self.lam)[0]
+                           for i, j in self._chunks(b.shape[0])])
+        else:
+            f = torch.cat([self.model.transpose(b[i:j]) for i, j in self._chunks(b.shape[0])])
+        s = f.flatten(1).pow(2).mean(1).sqrt().clamp_min(1e-30)
+        return (f / s.view(-1, 1, 1)).unsqueeze(1).contiguous(), s
+
+    def make_pairs(self, images, iters=200, noise=0.01, seed=0):
+        """Training pairs from phantoms (W, nx, nz): sinograms A x + noise
+        (``noise`` x rms of A x, Gaussian), the plain solver's ``iters``
+        iteration reconstruction as the target.  Returns (inputs, targets,
+        sinograms); sets kappa on the first call."""
+        images = torch.as_tensor(images).cuda().to(torch.float32)
+        gen = torch.Generator(device="cuda")
+        gen.manual_seed(int(seed))
+        bs, recs = [], []
+        for i, j in self._chunks(images.shape[0]):
+            y = self.model.forward(images[i:j].contiguous())
+            r = y.flatten(1).pow(2).mean(1).sqrt().view(-1, 1, 1)
+            y = y + noise * r * torch.randn(y.shape, generator=gen, device="cuda")
+            bs.append(y)
+            recs.append(rec_nn_with_L2_reg(self.model, y, iters, self.lam)[0])
+        b, rec = torch.cat(bs), torch.cat(recs)
+        f, s = self.features(b)
+        if self.kappa is None:
+            ratio = rec.flatten(1).pow(2).mean(1).sqrt() / s
+            self.kappa = float(ratio.median())
+        t = (rec / (self.kappa * s.view(-1, 1, 1))).unsqueeze(1)
+        if self.residual:
+            t = t - f
+        return f, t.contiguous(), b
+
+    def fit(self, inputs, targets, steps, batch=16, lr=1e-3, lr_final=1e-5, seed=0):
+        """Adam on random minibatches with a cosine learning-rate decay;
+        returns the per-step losses."""
+        batch = min(batch, self.net.max_batch)
+        g = torch.Generator(device="cuda")
+        g.manual_seed(int(seed))
+        W = inputs.shape[0]
+        losses = []
+        for k in range(steps):
+            idx = torch.randint(0, W, (batch,), generator=g, device="cuda")
+            a = lr_final + 0.5 * (lr - lr_final) * (1 + np.cos(np.pi * k / max(1, steps)))
+            losses.append(self.net.train_step(inputs[idx], targets[idx], lr=a))
+        return losses
+
+    def predict(self, b):
+        """x0 = kappa s relu(net(A'b / s)), (W, nx, nz)."""
+        if self.kappa is None:
+            raise RuntimeError("kappa unset: make_pairs (or set kappa) before predicting")
+        f, s = self.features(b)
+        out = self.net.forward(f)
+        if self.residual:
+            out = out + f
+        return (out.squeeze(1).clamp_min(0) * (self.kappa * s.view(-1, 1, 1))).contiguous()
+
+    def start(self, b, x0=None):
+        """(w0, v0, fallback mask): the prediction, its consistent multiplier
+        and which instances were put back to the zero start."""
+        b = self._sino(b)
+        w = self.predict(b) if x0 is None else torch.as_tensor(x0).cuda().to(torch.float32)
+        v = torch.empty_like(w)
+        fell = torch.zeros(b.shape[0], dtype=torch.bool, device="cuda")
+        for i, j in self._chunks(b.shape[0]):
+            r = self.model.forward(w[i:j].contiguous()) - b[i:j]
+            obj = r.flatten(1).pow(2).sum(1) + self.lam * w[i:j].flatten(1).pow(2).sum(1)
+            fell[i:j] = obj >= b[i:j].flatten(1).pow(2).sum(1)
+            g = self.model.transpose(r.contiguous())
+            if self.lam > 0:
+                g = g + self.lam * w[i:j]
+            v[i:j] = torch.where(w[i:j] > 0, torch.zeros_like(g), (g / self.beta).clamp_min(0))
+        keep = (~fell).view(-1, 1, 1).to(torch.float32)
+        return (w * keep).contiguous(), (v * keep).contiguous(), fell
+
+    def solve(self, b, iters, x0=None):
+        """rec_nn_with_L2_reg from the learned start; returns (rec, fallback
+        mask)."""
+        b = self._sino(b)
+        w, v, fell = self.start(b, x0)
+        recs = [rec_nn_with_L2_reg(self.model, b[i:j], iters, self.lam, x0=w[i:j],
+                                   v0=v[i:j])[0] for i, j in self._chunks(b.shape[0])]
+        return torch.cat(recs), fell

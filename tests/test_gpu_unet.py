@@ -85,3 +85,63 @@ def test_unet_training_reduces_loss(cuda):
     for _ in range(300):
         last = net.train_step(x, t, lr=3e-3)
     assert last < 0.1 * first
+
+
+def _ws_model(n, max_batch):
+    from msot_gb300 import Discretization, MSOTmodel, Probe
+    from msot_gb300.synthetic import gauss_pulse_eir
+    h = 0.2e-3 * (n - 1) / 2
+    probe = Probe(n_det=256, radius=0.040, angular_coverage=135.0, fs=4e7, n_samples=2030,
+                  delay=0.0, eir=gauss_pulse_eir(), eir_length=257)
+    return MSOTmodel(probe, Discretization([-h, h], n), 1500.0, False, True, 0, 1e5, 12e6, None,
+                     max_batch=max_batch)
+
+
+def test_learned_warm_start_gain(cuda):
+    # trained on pairs of the plain solver (10-iteration iterate -> 200-iteration
+    # solution), the network's start must beat the iterate it was given and,
+    # 10 iterations on, the plain solve of the same total iteration count,
+    # measured against a 1500-iteration solve
+    import torch
+    from msot_gb300 import rec_nn_with_L2_reg
+    from msot_gb300.synthetic import phantom_batch
+    from msot_gb300.warmstart import LearnedWarmStart
+    lam = 1e-2
+    model = _ws_model(64, 64)
+    ws = LearnedWarmStart(model, lam, levels=4, base_channels=32, max_batch=16, input_iters=10)
+    f, t, b = ws.make_pairs(phantom_batch(model.Discretization, 2048 + 32, seed=1), 200, seed=2)
+    ws.fit(f[:2048], t[:2048], 2500, batch=16, lr=2e-3)
+    bt = b[2048:]
+    xs = rec_nn_with_L2_reg(model, bt, 1500, lam)[0]
+    err = lambda x: float((x - xs).norm() / xs.norm())
+    w0, _, fell = ws.start(bt)
+    assert not bool(fell.any())
+    e_in = err(rec_nn_with_L2_reg(model, bt, 10, lam)[0])
+    e_pred = err(w0)
+    e_warm = err(ws.solve(bt, 10)[0])
+    e_plain = err(rec_nn_with_L2_reg(model, bt, 20, lam)[0])
+    assert e_pred < 0.75 * e_in, (e_pred, e_in)
+    assert e_warm < 0.85 * e_plain, (e_warm, e_plain)
+
+
+def test_learned_warm_start_falls_back_to_zero_start(cuda):
+    # a start worse than zero (objective above |b|^2) is replaced by the zero
+    # start: the solve then equals the plain one
+    import torch
+    from msot_gb300 import rec_nn_with_L2_reg
+    from msot_gb300.synthetic import phantom_batch
+    from msot_gb300.warmstart import LearnedWarmStart
+    model = _ws_model(32, 4)
+    ws = LearnedWarmStart(model, 1e-2, levels=3, base_channels=8, max_batch=4)
+    x = phantom_batch(model.Discretization, 2, seed=5)
+    b = model.forward(x)
+    bad = 100.0 * x.max() * torch.rand((2, 32, 32), device="cuda")
+    # a regularised solution (the phantom itself can score above the zero
+    # start once lambda |x|^2 is counted)
+    good = rec_nn_with_L2_reg(model, b, 50, 1e-2)[0]
+    w, v, fell = ws.start(b, torch.stack([bad[0], good[1]]))
+    assert fell.tolist() == [True, False]
+    assert float(w[0].abs().max()) == 0.0 and float(v[0].abs().max()) == 0.0
+    rec, fell = ws.solve(b, 5, torch.stack([bad[0], good[1]]))
+    plain = rec_nn_with_L2_reg(model, b, 5, 1e-2)[0]
+    assert float((rec[0] - plain[0]).norm() / plain[0].norm()) < 1e-5
