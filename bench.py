@@ -68,6 +68,10 @@ def parse():
     ap.add_argument("--ws-train-steps", type=int, default=3000)
     ap.add_argument("--ws-frames", type=int, default=256)
     ap.add_argument("--ws-input-iters", type=int, default=10)
+    ap.add_argument("--unet", action="store_true",
+                    help="warm-start U-Net alone (4 levels, 32 base channels, batch 16): "
+                         "training steps and forward passes: one JSON line")
+    ap.add_argument("--unet-side", type=int, default=128)
     return ap.parse_args()
 
 
@@ -675,6 +679,60 @@ def run_warmstart(args):
     }
 
 
+def unet_flops(L, c0, side):
+    """Multiply-adds x 2 of one forward pass of the U-Net on one image."""
+    ch = [c0 << l for l in range(L)]
+    macs = 0
+    for l in range(L):
+        px = (side >> l) ** 2
+        macs += px * 9 * ((1 if l == 0 else ch[l - 1]) * ch[l] + ch[l] * ch[l])
+        if l + 1 < L:
+            macs += px * 9 * ((ch[l + 1] + ch[l]) * ch[l] + ch[l] * ch[l])
+    macs += side * side * c0
+    return 2 * macs
+
+
+def run_unet(args):
+    """U-Net training step (forward + backward + Adam) and forward pass at
+    batch 16 through the C-ABI, CUDA events; FLOPs of the 3x3/1x1
+    convolutions (a training step counts 3x the forward)."""
+    import torch
+    from msot_gb300 import _lib
+    from msot_gb300.warmstart import UNet
+    S, B = args.unet_side, 16
+    net = UNet(4, 32, S, B, seed=0)
+    g = torch.Generator(device="cuda").manual_seed(0)
+    x = torch.randn((B, 1, S, S), device="cuda", generator=g)
+    t = torch.randn((B, 1, S, S), device="cuda", generator=g)
+    L = _lib.load()
+    for _ in range(args.warmup):
+        net.train_step(x, t, 1e-4)
+    net.check()
+    n0 = L.msot_launch_count()
+    train_ms = _event_ms(lambda: [net.train_step(x, t, 1e-4) for _ in range(args.steps)])[1]
+    launches = (L.msot_launch_count() - n0) // max(1, args.steps)
+    fwd_ms = _event_ms(lambda: [net.forward(x) for _ in range(args.steps)])[1]
+    net.check()
+    train_ms /= args.steps
+    fwd_ms /= args.steps
+    fl = unet_flops(4, 32, S) * B
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            bf16 = float(json.load(f)["bf16_tflops"])
+    except Exception:
+        bf16 = None
+    return {"metric": "U-Net training images/s", "value": B / (train_ms / 1e3), "unit": "images/s",
+            "ms_per_step": train_ms, "forward_ms": fwd_ms, "forward_images_per_s": B / (fwd_ms / 1e3),
+            "train_tflops": 3 * fl / (train_ms * 1e9), "forward_tflops": fl / (fwd_ms * 1e9),
+            "peak_bf16_tflops_measured": bf16,
+            "peak_tf32_tflops_est": bf16 / 2 if bf16 else None,
+            "gpu_launches_per_step": launches,
+            "higher_is_better": True, "steps": args.steps, "warmup": args.warmup,
+            "dtype": "TF32 tensor-core convolutions (BF16 weights), FP32 accumulate",
+            "data": "synthetic Gaussian images",
+            "config": {"workload": f"U-Net 4 levels, 32 base channels, {S}x{S}, batch {B}"}}
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -697,6 +755,10 @@ def main():
         import torch
         torch.cuda.set_device(0)
         out = run_warmstart(args)
+    elif args.unet:
+        import torch
+        torch.cuda.set_device(0)
+        out = run_unet(args)
     else:
         if world > 1:
             import torch

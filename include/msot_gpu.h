@@ -235,7 +235,9 @@ int msot_backproject_waveeq(const float *d_sig, int W, int D, int T, const doubl
  * encoder conv3x3+ReLU x2 and 2x2 average pooling, decoder nearest
  * upsampling + concat + conv3x3+ReLU x2, output conv1x1.  Weights FP32
  * (Adam) used as BF16 in the convolutions, FP32 accumulation; activations
- * [n][1][side][side] FP32 on the device.  Parameter layout: per conv (encoder
+ * [n][1][side][side] FP32 on the device.  3x3 convolutions with >= 8 input
+ * and a multiple of 32 output channels (forward and data gradient) run on
+ * the tensor cores (tcgen05, TF32-rounded activations).  Parameter layout: per conv (encoder
  * a, b for level 0..L-1, decoder c, d for level L-2..0, output) the weights
  * [Co][Ci][k][k] then the biases [Co]. */
 typedef struct msot_unet *msot_unet_t;
@@ -254,6 +256,9 @@ int msot_unet_gradients(msot_unet_t net, const float *d_in, const float *d_targe
 /* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on the last gradients;
  * step counts from 1 for the bias correction. */
 int msot_unet_adam_step(msot_unet_t net, double lr, int step, void *stream);
+/* Synchronises the device and reports (then clears) a tensor-core
+ * convolution whose bounded wait for its MMAs ran out (MSOT_ECUDA). */
+int msot_unet_check(msot_unet_t net);
 
 /* ------------------------------------------------------------------------ */
 /* Instrumentation (no counterpart in the reference, whose only timing is
@@ -262,7 +267,10 @@ int msot_unet_adam_step(msot_unet_t net, double lr, int step, void *stream);
 /* Kernel tuning knob (no reference counterpart; results change only in
  * float summation order):
  *   "tv_prox_cluster"  CTAs per image of the shared-memory SB_ITV2 kernel
- *                      (1, 2, 4, 8, 16; 0 = automatic). */
+ *                      (1, 2, 4, 8, 16; 0 = automatic).
+ *   "unet_tensor_cores" 1 (default) = U-Net 3x3 convolutions on the tensor
+ *                      cores where the shape allows, 0 = CUDA cores only
+ *                      (FP32 activations, no TF32 rounding). */
 int msot_tune_set(const char *key, int value);
 /* SB_ITV2 kernel choice: 0 (default) = the shared-memory cluster kernel
  * wherever the image fits, 1 = always the global-memory kernel. */

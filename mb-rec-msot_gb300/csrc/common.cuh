@@ -89,6 +89,9 @@ struct Plan {
 
 const char *set_error(const char *fmt, ...);
 
+// tensor-core convolutions of the warm-start U-Net on (1) or off (0); unet.cu
+extern std::atomic<int> g_unet_tc;
+
 // launch counter (every kernel launch of the library goes through KLAUNCH)
 extern std::atomic<long long> g_launch_count;
 #define KLAUNCH(...) (++::msot::g_launch_count, __VA_ARGS__)

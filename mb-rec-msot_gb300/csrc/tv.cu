@@ -1366,6 +1366,10 @@ int msot_tv_prox_stats(long long *sweeps, long long *cg_steps) {
 }
 
 int msot_tune_set(const char *key, int value) {
+    if (key && std::strcmp(key, "unet_tensor_cores") == 0 && (value == 0 || value == 1)) {
+        msot::g_unet_tc.store(value);
+        return MSOT_OK;
+    }
     if (key && std::strcmp(key, "tv_prox_cluster") == 0 &&
         (value == 0 || value == 1 || value == 2 || value == 4 || value == 8 || value == 16)) {
         g_tv_cluster.store(value);

@@ -13,6 +13,7 @@
 // (c, d) l = L-2..0, output: weight [Co][Ci][k][k], then bias [Co].
 #include <cuda_bf16.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <random>
@@ -84,6 +85,372 @@ __global__ void __launch_bounds__(256) k_conv3(const float *__restrict__ in, int
         if (relu) v = fmaxf(v, 0.f);
         out[(((size_t)n * Co + co0 + o) * H + y) * Wd + x] = v;
     }
+}
+
+// ---------------------------------------------------------------------------
+// Tensor-core 3x3 convolution (tcgen05.mma kind::tf32, accumulator in TMEM).
+//
+// Implicit GEMM per CTA: D[m][o] (m = pixel of an 8 x 16 tile, o = NT output
+// channels) += sum over taps k and input channels i of A_k[m][i] B_k[i][o],
+// A_k the input shifted by tap k, B_k[i][o] = w(o, i, k).  Input channels
+// go through shared memory TC_CK at a time; each MMA consumes K = 8 channels.
+// Both operands are K-major in the canonical no-swizzle layout: core
+// matrices of 8 rows x 16 bytes (4 channels), 128 contiguous bytes; LBO =
+// distance of the core matrices adjacent in K, SBO = in M (or N).
+//   A: three copies kx = 0..2 of the 10 x 16 halo window starting at column
+//      kx (core matrix (halo row, 8-column group)), so tap (ky, kx) is copy
+//      kx from halo row ky: rows of D map to pixel (m / 16, m % 16).
+//   B: [tap][channel group][o / 8][o % 8][channel % 4].
+// Activations are rounded to TF32 (cvt.rna) when staged; BF16 weights are
+// exact in TF32.  Every wait is bounded: on a timeout the CTA sets *err,
+// skips its stores and still frees its TMEM.
+// ---------------------------------------------------------------------------
+constexpr int TC_TY = 8, TC_TX = 16;              // pixel tile (M = 128)
+constexpr int TC_CK = 32;                         // input channels per stage
+constexpr int TC_HY = TC_TY + 2, TC_HX = TC_TX + 2;
+constexpr int TC_LBO_A = TC_HY * 2 * 128;         // 2560 B: next 4 channels
+constexpr int TC_ACOPY = (TC_CK / 4) * TC_LBO_A;  // 20480 B per kx copy
+constexpr int TC_THREADS = 256;
+
+__host__ __device__ constexpr size_t tc_smem_bytes(int NT) {
+    return 3 * (size_t)TC_ACOPY + 9 * (size_t)NT * 128;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ uint64_t tc_mdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    // start (16 B units) | LBO << 16 | SBO << 32 | descriptor version 1 at bit
+    // 46; base offset 0, no swizzle
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// instruction descriptor: D F32 (bits 4-5 = 1), A and B TF32 (bits 7-9,
+// 10-12 = 2), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+__host__ __device__ constexpr uint32_t tc_idesc_tf32(int M, int N) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(M >> 4) << 24);
+}
+__device__ __forceinline__ float tc_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+__device__ __forceinline__ bool tc_mbar_test(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.b32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait for phase `parity` of the barrier (about a second)
+__device__ __forceinline__ bool tc_mbar_wait(uint32_t bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!tc_mbar_test(bar, parity))
+        if (clock64() - t0 > 2000000000ll) return false;
+    return true;
+}
+
+__device__ int g_unet_tc_err = 0;  // set by a tensor-core CTA whose wait timed out
+std::atomic<int> g_unet_tc{1};     // tensor-core convolutions on (msot_tune_set)
+
+template <bool TRANS, int NT>
+__global__ void __launch_bounds__(TC_THREADS) k_conv3_tc(const float *__restrict__ in, int Ci,
+                                                         const __nv_bfloat16 *__restrict__ w,
+                                                         const float *__restrict__ bias,
+                                                         float *__restrict__ out, int Co, int H,
+                                                         int Wd, int relu, int tiles_x) {
+    static_assert(NT == 32 || NT == 64, "N tile");
+    extern __shared__ __align__(1024) uint8_t tc_smem[];
+    float *sA = reinterpret_cast<float *>(tc_smem);
+    float *sB = reinterpret_cast<float *>(tc_smem + 3 * TC_ACOPY);
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    const int ty0 = (blockIdx.x / tiles_x) * TC_TY, tx0 = (blockIdx.x % tiles_x) * TC_TX;
+    const int co0 = blockIdx.y * NT, n = blockIdx.z;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t bar = smem_u32(&mbar);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&tmem_slot)),
+                     "r"((uint32_t)NT));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (threadIdx.x == 32) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tm = tmem_slot;
+    const float *inn = in + (size_t)n * Ci * H * Wd;
+    const int nstage = (Ci + TC_CK - 1) / TC_CK;
+    bool ok = true;
+    int issued = 0;  // stages whose MMAs were committed
+    for (int s = 0; s < nstage; ++s) {
+        const int ci0 = s * TC_CK;
+        if (s > 0) {  // the previous stage's MMAs must be done with shared memory
+            const bool mine = tc_mbar_wait(bar, (uint32_t)(s - 1) & 1u);
+            ok = !__syncthreads_or(!mine);
+            if (!ok) break;
+        }
+        for (int i = threadIdx.x; i < TC_CK * TC_HY * TC_HX; i += TC_THREADS) {
+            const int c = i / (TC_HY * TC_HX), r = i % (TC_HY * TC_HX);
+            const int hy = r / TC_HX, hx = r % TC_HX;
+            const int y = ty0 + hy - 1, x = tx0 + hx - 1;
+            float v = 0.f;
+            if (ci0 + c < Ci && y >= 0 && y < H && x >= 0 && x < Wd)
+                v = inn[((size_t)(ci0 + c) * H + y) * Wd + x];
+            v = tc_tf32(v);
+            float *dst = sA + (c >> 2) * (TC_LBO_A / 4) + hy * 64 + (c & 3);
+#pragma unroll
+            for (int kx = 0; kx < 3; ++kx) {
+                const int xx = hx - kx;
+                if (xx >= 0 && xx < TC_TX)
+                    dst[kx * (TC_ACOPY / 4) + (xx >> 3) * 32 + (xx & 7) * 4] = v;
+            }
+        }
+        for (int i = threadIdx.x; i < NT * TC_CK * 9; i += TC_THREADS) {
+            const int o = i / (TC_CK * 9), r = i % (TC_CK * 9), c = r / 9, k = r % 9;
+            float v = 0.f;
+            if (co0 + o < Co && ci0 + c < Ci) {
+                const size_t idx = TRANS ? ((size_t)(ci0 + c) * Co + (co0 + o)) * 9 + (8 - k)
+                                         : ((size_t)(co0 + o) * Ci + (ci0 + c)) * 9 + k;
+                v = __bfloat162float(w[idx]);
+            }
+            sB[k * NT * 32 + (c >> 2) * NT * 4 + (o >> 3) * 32 + (o & 7) * 4 + (c & 3)] = v;
+        }
+        // generic-proxy stores -> visible to the tensor core (async proxy)
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+            constexpr uint32_t idesc = tc_idesc_tf32(128, NT);
+#pragma unroll 1
+            for (int k = 0; k < 9; ++k) {
+                const int ky = k / 3, kx = k % 3;
+#pragma unroll
+                for (int q = 0; q < TC_CK / 8; ++q) {
+                    const uint64_t da = tc_mdesc(
+                        a0 + kx * TC_ACOPY + ky * 256 + q * 2 * TC_LBO_A, TC_LBO_A, 128);
+                    const uint64_t db =
+                        tc_mdesc(b0 + k * NT * 128 + q * 2 * (NT * 16), NT * 16, 128);
+                    const uint32_t acc = (s | k | q) != 0;
+                    asm volatile(
+                        "{\n\t.reg .pred p;\n\t"
+                        "setp.ne.b32 p, %4, 0;\n\t"
+                        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tm),
+                        "l"(da), "l"(db), "r"(idesc), "r"(acc));
+                }
+            }
+            asm volatile(
+                "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                    bar)
+                : "memory");
+        }
+        issued = s + 1;
+    }
+    if (ok) {
+        const bool mine = tc_mbar_wait(bar, (uint32_t)(nstage - 1) & 1u);
+        ok = !__syncthreads_or(!mine);
+    }
+    if (!ok) {
+        if (threadIdx.x == 0) atomicExch(&g_unet_tc_err, 1);
+        // give the MMAs in flight a second bounded chance before the TMEM is freed
+        if (issued > 0) tc_mbar_wait(bar, (uint32_t)(issued - 1) & 1u);
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (= pixels), columns
+    // (w / 4) NT / 2 .. + NT / 2 (= output channels)
+    const int m = (warp & 3) * 32 + lane;
+    const int y = ty0 + m / TC_TX, x = tx0 + m % TC_TX;
+    const bool inside = ok && y < H && x < Wd;
+#pragma unroll
+    for (int j0 = (warp >> 2) * (NT / 2); j0 < (warp >> 2) * (NT / 2) + NT / 2; j0 += 16) {
+        uint32_t r[16];
+        const uint32_t ta = tm + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)j0;
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, "
+            "%10, %11, %12, %13, %14, %15}, [%16];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+              "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+              "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(ta));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (inside) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int o = co0 + j0 + j;
+                if (o < Co) {
+                    float v = __uint_as_float(r[j]) + (bias ? bias[o] : 0.f);
+                    if (relu) v = fmaxf(v, 0.f);
+                    out[(((size_t)n * Co + o) * H + y) * Wd + x] = v;
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm),
+                     "r"((uint32_t)NT));
+}
+
+// Tensor-core weight gradient: dW[o][i][k] += sum over pixels p of
+// dy[o][p] x[i][p + off_k].  Per CTA: M = 128 output channels (rows beyond
+// Co are never read back), N = 32 input channels, all 9 taps accumulated in
+// TMEM (columns k * 32 + i); K = the pixels of the (image, 8 x 16 tile)
+// stages this CTA takes (split over blockIdx.z), 8 per MMA.
+//   A (dy):  [o / 8][pixel / 4][o % 8][pixel % 4], pixel = r * 16 + x.
+//   B (x):   three copies kx of the halo window starting at column kx,
+//            [i / 8][halo row][x / 4][i % 8][x % 4].
+// Then each CTA adds its 128 x 288 partial sums to dW with float atomics.
+constexpr int DW_LBO = 128;                      // K-adjacent core matrices
+constexpr int DW_SBO_A = 32 * 128;               // next 8 output channels
+constexpr int DW_SBO_B = TC_HY * 4 * 128;        // next 8 input channels (5120 B)
+constexpr int DW_ABYTES = 16 * DW_SBO_A;         // 65536
+constexpr int DW_BCOPY = 4 * DW_SBO_B;           // 20480 per kx copy
+constexpr size_t DW_SMEM = (size_t)DW_ABYTES + 3 * DW_BCOPY;
+
+__global__ void __launch_bounds__(TC_THREADS) k_conv3_dw_tc(const float *__restrict__ x, int Ci,
+                                                            const float *__restrict__ dy, int Co,
+                                                            float *__restrict__ dw, int H, int Wd,
+                                                            int N, int tiles_x, int tiles_img,
+                                                            int splits) {
+    extern __shared__ __align__(1024) uint8_t tc_smem[];
+    float *sA = reinterpret_cast<float *>(tc_smem);
+    float *sB = reinterpret_cast<float *>(tc_smem + DW_ABYTES);
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    const int co0 = blockIdx.x * 128, ci0 = blockIdx.y * 32;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t bar = smem_u32(&mbar);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&tmem_slot)),
+                     "r"(512u));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (threadIdx.x == 32) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tm = tmem_slot;
+    const int rows = min(128, Co - co0);
+    bool ok = true;
+    int issued = 0;
+    const int total = N * tiles_img;
+    for (int tt = blockIdx.z; tt < total; tt += splits) {
+        const int n = tt / tiles_img, tile = tt % tiles_img;
+        const int ty0 = (tile / tiles_x) * TC_TY, tx0 = (tile % tiles_x) * TC_TX;
+        if (issued > 0) {
+            const bool mine = tc_mbar_wait(bar, (uint32_t)(issued - 1) & 1u);
+            ok = !__syncthreads_or(!mine);
+            if (!ok) break;
+        }
+        const float *dyn = dy + ((size_t)n * Co + co0) * H * Wd;
+        for (int i = threadIdx.x; i < rows * 128; i += TC_THREADS) {
+            const int o = i >> 7, pix = i & 127, r = pix >> 4, xx = pix & 15;
+            const int y = ty0 + r, xq = tx0 + xx;
+            const float v = (y < H && xq < Wd) ? dyn[((size_t)o * H + y) * Wd + xq] : 0.f;
+            sA[(o >> 3) * (DW_SBO_A / 4) + (r * 4 + (xx >> 2)) * 32 + (o & 7) * 4 + (xx & 3)] =
+                tc_tf32(v);
+        }
+        const float *xn = x + ((size_t)n * Ci + ci0) * H * Wd;
+        for (int i = threadIdx.x; i < 32 * TC_HY * TC_HX; i += TC_THREADS) {
+            const int c = i / (TC_HY * TC_HX), r = i % (TC_HY * TC_HX);
+            const int hy = r / TC_HX, hx = r % TC_HX;
+            const int y = ty0 + hy - 1, xq = tx0 + hx - 1;
+            float v = 0.f;
+            if (ci0 + c < Ci && y >= 0 && y < H && xq >= 0 && xq < Wd)
+                v = xn[((size_t)c * H + y) * Wd + xq];
+            v = tc_tf32(v);
+            float *dst = sB + (c >> 3) * (DW_SBO_B / 4) + hy * 128 + (c & 7) * 4;
+#pragma unroll
+            for (int kx = 0; kx < 3; ++kx) {
+                const int xx = hx - kx;
+                if (xx >= 0 && xx < TC_TX) dst[kx * (DW_BCOPY / 4) + (xx >> 2) * 32 + (xx & 3)] = v;
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+            constexpr uint32_t idesc = tc_idesc_tf32(128, 32);
+#pragma unroll 1
+            for (int k = 0; k < 9; ++k) {
+                const int ky = k / 3, kx = k % 3;
+#pragma unroll 4
+                for (int j = 0; j < 16; ++j) {
+                    const uint64_t da = tc_mdesc(a0 + j * 256, DW_LBO, DW_SBO_A);
+                    const uint64_t db = tc_mdesc(
+                        b0 + kx * DW_BCOPY + (((j >> 1) + ky) * 4 + (j & 1) * 2) * 128, DW_LBO,
+                        DW_SBO_B);
+                    const uint32_t acc = (issued | j) != 0;
+                    asm volatile(
+                        "{\n\t.reg .pred p;\n\t"
+                        "setp.ne.b32 p, %4, 0;\n\t"
+                        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(
+                            tm + (uint32_t)(k * 32)),
+                        "l"(da), "l"(db), "r"(idesc), "r"(acc));
+                }
+            }
+            asm volatile(
+                "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                    bar)
+                : "memory");
+        }
+        ++issued;
+    }
+    if (ok && issued > 0) {
+        const bool mine = tc_mbar_wait(bar, (uint32_t)(issued - 1) & 1u);
+        ok = !__syncthreads_or(!mine);
+    }
+    if (!ok) {
+        if (threadIdx.x == 0) atomicExch(&g_unet_tc_err, 1);
+        if (issued > 0) tc_mbar_wait(bar, (uint32_t)(issued - 1) & 1u);
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // epilogue: warp w reads lanes 32 (w % 4) + lane (= output channel) of the
+    // taps k = w / 4, w / 4 + 2, ... (32 columns each)
+    const int o = co0 + (warp & 3) * 32 + lane;
+    const bool live = ok && issued > 0 && (warp & 3) * 32 + lane < rows;
+    for (int k = warp >> 2; k < 9; k += 2) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            uint32_t r[16];
+            const uint32_t ta = tm + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(k * 32 + h * 16);
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, "
+                "%10, %11, %12, %13, %14, %15}, [%16];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                  "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+                  "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                : "r"(ta));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (live) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int c = ci0 + h * 16 + j;
+                    if (c < Ci) atomicAdd(&dw[((size_t)o * Ci + c) * 9 + k], __uint_as_float(r[j]));
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(512u));
 }
 
 // dW[o][i][k] += sum over (n, y, x) of dy[n][o][y][x] x[n][i][y + ky - 1][x + kx - 1]
@@ -367,13 +734,38 @@ T *dalloc(msot_unet *u, size_t n) {
     return static_cast<T *>(p);
 }
 
-int conv_fwd(msot_unet *u, const ConvL &c, const float *in, float *out, int N, cudaStream_t st) {
-    const int tx = (c.S + CT - 1) / CT;
-    dim3 grid(tx * tx, (c.Co + COT - 1) / COT, N);
-    KLAUNCH(k_conv3<false><<<grid, 256, 0, st>>>(in, c.Ci, u->parb + c.w_off, u->par + c.b_off,
-                                                 out, c.Co, c.S, c.S, 1, tx));
+template <bool TRANS, int NT>
+int conv3_tc(const float *in, int Ci, const __nv_bfloat16 *w, const float *bias, float *out,
+             int Co, int S, int N, int relu, cudaStream_t st) {
+    const size_t smem = tc_smem_bytes(NT);
+    MSOT_CUDA_TRY(cudaFuncSetAttribute(k_conv3_tc<TRANS, NT>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int tx = (S + TC_TX - 1) / TC_TX, ty = (S + TC_TY - 1) / TC_TY;
+    dim3 grid(tx * ty, Co / NT, N);
+    KLAUNCH(k_conv3_tc<TRANS, NT><<<grid, TC_THREADS, smem, st>>>(in, Ci, w, bias, out, Co, S, S,
+                                                                 relu, tx));
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
+}
+
+// 3x3 "same" convolution of [N][Ci][S][S] into [N][Co][S][S]: tensor cores
+// when Ci >= 8 and Co is a multiple of 32 (every layer but the network's
+// first), else the CUDA-core kernel
+template <bool TRANS>
+int conv3(const float *in, int Ci, const __nv_bfloat16 *w, const float *bias, float *out, int Co,
+          int S, int N, int relu, cudaStream_t st) {
+    if (g_unet_tc.load() && Ci >= 8 && Co % 32 == 0)
+        return Co % 64 == 0 ? conv3_tc<TRANS, 64>(in, Ci, w, bias, out, Co, S, N, relu, st)
+                            : conv3_tc<TRANS, 32>(in, Ci, w, bias, out, Co, S, N, relu, st);
+    const int tx = (S + CT - 1) / CT;
+    dim3 grid(tx * tx, (Co + COT - 1) / COT, N);
+    KLAUNCH(k_conv3<TRANS><<<grid, 256, 0, st>>>(in, Ci, w, bias, out, Co, S, S, relu, tx));
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
+}
+
+int conv_fwd(msot_unet *u, const ConvL &c, const float *in, float *out, int N, cudaStream_t st) {
+    return conv3<false>(in, c.Ci, u->parb + c.w_off, u->par + c.b_off, out, c.Co, c.S, N, 1, st);
 }
 
 // conv c with input x and ReLU output y; dy_post = d loss / d y.  Adds dW, db;
@@ -382,19 +774,27 @@ int conv_bwd(msot_unet *u, const ConvL &c, const float *x, const float *y, const
              float *dy_pre, float *dx, int N, cudaStream_t st) {
     const size_t ny = (size_t)N * c.Co * c.S * c.S;
     KLAUNCH(k_relu_bwd<<<nblk(ny), 256, 0, st>>>(y, dy_post, dy_pre, ny));
-    const int tx = (c.S + CT - 1) / CT, tiles = tx * tx;
-    const int cog = (c.Co + COT - 1) / COT, cig = (c.Ci + CIT - 1) / CIT;
-    const int splits = std::max(1, std::min(N * tiles, (4 * 152 + cog * cig - 1) / (cog * cig)));
-    KLAUNCH(k_conv3_dw<<<dim3(cog, cig, splits), 256, 0, st>>>(
-        x, c.Ci, dy_pre, c.Co, u->grad + c.w_off, c.S, c.S, N, tx, tiles, splits));
+    if (g_unet_tc.load() && c.Ci >= 8) {
+        const int tx = (c.S + TC_TX - 1) / TC_TX, ty = (c.S + TC_TY - 1) / TC_TY;
+        const int tiles = tx * ty, cog = (c.Co + 127) / 128, cig = (c.Ci + 31) / 32;
+        const int splits = std::max(1, std::min(N * tiles, 148 / (cog * cig)));
+        MSOT_CUDA_TRY(cudaFuncSetAttribute(k_conv3_dw_tc,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)DW_SMEM));
+        KLAUNCH(k_conv3_dw_tc<<<dim3(cog, cig, splits), TC_THREADS, DW_SMEM, st>>>(
+            x, c.Ci, dy_pre, c.Co, u->grad + c.w_off, c.S, c.S, N, tx, tiles, splits));
+    } else {
+        const int tx = (c.S + CT - 1) / CT, tiles = tx * tx;
+        const int cog = (c.Co + COT - 1) / COT, cig = (c.Ci + CIT - 1) / CIT;
+        const int splits =
+            std::max(1, std::min(N * tiles, (4 * 152 + cog * cig - 1) / (cog * cig)));
+        KLAUNCH(k_conv3_dw<<<dim3(cog, cig, splits), 256, 0, st>>>(
+            x, c.Ci, dy_pre, c.Co, u->grad + c.w_off, c.S, c.S, N, tx, tiles, splits));
+    }
     KLAUNCH(k_bias_grad<<<dim3(c.Co, N), 256, 0, st>>>(dy_pre, c.Co, c.S * c.S,
                                                         u->grad + c.b_off));
-    if (dx) {
-        dim3 grid(tiles, (c.Ci + COT - 1) / COT, N);
-        KLAUNCH(k_conv3<true><<<grid, 256, 0, st>>>(dy_pre, c.Co, u->parb + c.w_off, nullptr, dx,
-                                                    c.Ci, c.S, c.S, 0, tx));
-    }
     MSOT_LAUNCH_CHECK();
+    if (dx) return conv3<true>(dy_pre, c.Co, u->parb + c.w_off, nullptr, dx, c.Ci, c.S, N, 0, st);
     return MSOT_OK;
 }
 
@@ -660,6 +1060,23 @@ int msot_unet_gradients(msot_unet_t u, const float *d_in, const float *d_target,
         MSOT_CUDA_TRY(cudaMemcpyAsync(host_grad, u->grad, sizeof(float) * u->n_par,
                                       cudaMemcpyDeviceToHost, st));
     MSOT_CUDA_TRY(cudaStreamSynchronize(st));
+    return MSOT_OK;
+}
+
+int msot_unet_check(msot_unet_t u) {
+    if (!u) {
+        set_error("unet_check: null net");
+        return MSOT_EINVAL;
+    }
+    MSOT_CUDA_TRY(cudaDeviceSynchronize());
+    int flag = 0;
+    MSOT_CUDA_TRY(cudaMemcpyFromSymbol(&flag, g_unet_tc_err, sizeof(int)));
+    if (flag) {
+        const int zero = 0;
+        MSOT_CUDA_TRY(cudaMemcpyToSymbol(g_unet_tc_err, &zero, sizeof(int)));
+        set_error("unet: a tensor-core convolution timed out waiting for its MMAs");
+        return MSOT_ECUDA;
+    }
     return MSOT_OK;
 }
 

@@ -43,6 +43,10 @@ class UNet:
             _lib.load().msot_unet_destroy(self._h)
             self._h = None
 
+    def check(self):
+        """Synchronise and raise if a tensor-core convolution timed out."""
+        _lib.check(_lib.load().msot_unet_check(self._h))
+
     def get_params(self) -> np.ndarray:
         p = np.empty(self.n_params, dtype=np.float32)
         _lib.check(_lib.load().msot_unet_get_params(self._h, p.ctypes.data_as(
