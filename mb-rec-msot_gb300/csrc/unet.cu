@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(256) k_conv3(const float *__restrict__ in, int
 // ---------------------------------------------------------------------------
 constexpr int TC_TY = 8, TC_TX = 16;              // pixel tile (M = 128)
 constexpr int TC_CK = 32;                         // input channels per stage
-constexpr int TC_HY = TC_TY + 2, TC_HX = TC_TX + 2;
+constexpr int TC_HY = TC_TY + 2;                  // halo rows
 constexpr int TC_LBO_A = TC_HY * 2 * 128;         // 2560 B: next 4 channels
 constexpr int TC_ACOPY = (TC_CK / 4) * TC_LBO_A;  // 20480 B per kx copy
 constexpr int TC_THREADS = 256;
@@ -158,22 +158,87 @@ __device__ __forceinline__ bool tc_mbar_wait(uint32_t bar, uint32_t parity) {
 __device__ int g_unet_tc_err = 0;  // set by a tensor-core CTA whose wait timed out
 std::atomic<int> g_unet_tc{1};     // tensor-core convolutions on (msot_tune_set)
 
-template <bool TRANS, int NT>
+__device__ __forceinline__ void tc_bulk_load(uint32_t dst, const void *src, uint32_t bytes,
+                                             uint32_t bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            dst),
+        "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}
+
+// Input channels ci0 .. ci0 + 31 of the tile's halo window, staged in two
+// steps so that the loads of one stage are all in flight together (and can
+// overlap the previous stage's MMAs): tc_load_input fills registers, task t
+// (< 1440) = 4 channels of halo pixel (row hy, column hx), hx fastest, and
+// tc_store_input writes them as one 16-byte vector into each kx copy that
+// holds the pixel.  Eight consecutive lanes write eight consecutive pixels
+// (the eight 16-byte rows of a core matrix): no bank conflicts.
+constexpr int TC_HX = TC_TX + 2;
+constexpr int TC_NT_IN = (TC_CK / 4) * TC_HY * TC_HX;  // 1440 tasks
+constexpr int TC_IN_PER = (TC_NT_IN + TC_THREADS - 1) / TC_THREADS;
+struct TcIn {
+    float4 q[TC_IN_PER];
+};
+__device__ __forceinline__ void tc_load_input(TcIn &R, const float *inn, int Ci, int ci0, int H,
+                                              int Wd, int ty0, int tx0, bool) {
+    const size_t plane = (size_t)H * Wd;
+#pragma unroll
+    for (int u = 0; u < TC_IN_PER; ++u) {
+        const int t = threadIdx.x + u * TC_THREADS;
+        const int hx = t % TC_HX, hy = (t / TC_HX) % TC_HY, cq = t / (TC_HX * TC_HY);
+        const int y = ty0 + hy - 1, x = tx0 + hx - 1, c = ci0 + 4 * cq;
+        float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (t < TC_NT_IN && y >= 0 && y < H && x >= 0 && x < Wd) {
+            const float *p0 = inn + (size_t)c * plane + (size_t)y * Wd + x;
+            q.x = c < Ci ? p0[0] : 0.f;
+            q.y = c + 1 < Ci ? p0[plane] : 0.f;
+            q.z = c + 2 < Ci ? p0[2 * plane] : 0.f;
+            q.w = c + 3 < Ci ? p0[3 * plane] : 0.f;
+        }
+        R.q[u] = q;
+    }
+}
+__device__ __forceinline__ void tc_store_input(const TcIn &R, float *sA) {
+#pragma unroll
+    for (int u = 0; u < TC_IN_PER; ++u) {
+        const int t = threadIdx.x + u * TC_THREADS;
+        if (t >= TC_NT_IN) break;
+        const int hx = t % TC_HX, hy = (t / TC_HX) % TC_HY, cq = t / (TC_HX * TC_HY);
+        const float4 v = make_float4(tc_tf32(R.q[u].x), tc_tf32(R.q[u].y), tc_tf32(R.q[u].z),
+                                     tc_tf32(R.q[u].w));
+        float *base = sA + cq * (TC_LBO_A / 4) + hy * 64;
+#pragma unroll
+        for (int kx = 0; kx < 3; ++kx) {
+            const int xx = hx - kx;
+            if (xx >= 0 && xx < TC_TX)
+                *reinterpret_cast<float4 *>(base + kx * (TC_ACOPY / 4) + (xx >> 3) * 32 +
+                                            (xx & 7) * 4) = v;
+        }
+    }
+}
+
+// wpk: the layer's weights packed per (output tile, channel stage) in the
+// shared-memory B layout (NT * 288 floats each, TF32-exact), see
+// k_pack_weights; bias may be null (data gradient)
+template <int NT>
 __global__ void __launch_bounds__(TC_THREADS) k_conv3_tc(const float *__restrict__ in, int Ci,
-                                                         const __nv_bfloat16 *__restrict__ w,
+                                                         const float *__restrict__ wpk,
                                                          const float *__restrict__ bias,
                                                          float *__restrict__ out, int Co, int H,
-                                                         int Wd, int relu, int tiles_x) {
+                                                         int Wd, int relu, int tiles_x, int vec) {
     static_assert(NT == 32 || NT == 64, "N tile");
     extern __shared__ __align__(1024) uint8_t tc_smem[];
     float *sA = reinterpret_cast<float *>(tc_smem);
     float *sB = reinterpret_cast<float *>(tc_smem + 3 * TC_ACOPY);
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar[2];  // [0] MMAs done, [1] weights landed
     __shared__ uint32_t tmem_slot;
     const int ty0 = (blockIdx.x / tiles_x) * TC_TY, tx0 = (blockIdx.x % tiles_x) * TC_TX;
     const int co0 = blockIdx.y * NT, n = blockIdx.z;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t bar = smem_u32(&mbar);
+    const uint32_t bar = smem_u32(&mbar[0]), bar_w = smem_u32(&mbar[1]);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32(&tmem_slot)),
@@ -182,6 +247,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3_tc(const float *__restrict
     }
     if (threadIdx.x == 32) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_w));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -190,45 +256,25 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3_tc(const float *__restrict
     const uint32_t tm = tmem_slot;
     const float *inn = in + (size_t)n * Ci * H * Wd;
     const int nstage = (Ci + TC_CK - 1) / TC_CK;
+    const float *wt = wpk + (size_t)blockIdx.y * nstage * (NT * 288);
+    constexpr uint32_t WBYTES = NT * 288 * 4;
     bool ok = true;
-    int issued = 0;  // stages whose MMAs were committed
+    int issued = 0;
+    TcIn R;
+    tc_load_input(R, inn, Ci, 0, H, Wd, ty0, tx0, vec != 0);
     for (int s = 0; s < nstage; ++s) {
-        const int ci0 = s * TC_CK;
         if (s > 0) {  // the previous stage's MMAs must be done with shared memory
             const bool mine = tc_mbar_wait(bar, (uint32_t)(s - 1) & 1u);
             ok = !__syncthreads_or(!mine);
             if (!ok) break;
         }
-        for (int i = threadIdx.x; i < TC_CK * TC_HY * TC_HX; i += TC_THREADS) {
-            const int c = i / (TC_HY * TC_HX), r = i % (TC_HY * TC_HX);
-            const int hy = r / TC_HX, hx = r % TC_HX;
-            const int y = ty0 + hy - 1, x = tx0 + hx - 1;
-            float v = 0.f;
-            if (ci0 + c < Ci && y >= 0 && y < H && x >= 0 && x < Wd)
-                v = inn[((size_t)(ci0 + c) * H + y) * Wd + x];
-            v = tc_tf32(v);
-            float *dst = sA + (c >> 2) * (TC_LBO_A / 4) + hy * 64 + (c & 3);
-#pragma unroll
-            for (int kx = 0; kx < 3; ++kx) {
-                const int xx = hx - kx;
-                if (xx >= 0 && xx < TC_TX)
-                    dst[kx * (TC_ACOPY / 4) + (xx >> 3) * 32 + (xx & 7) * 4] = v;
-            }
-        }
-        for (int i = threadIdx.x; i < NT * TC_CK * 9; i += TC_THREADS) {
-            const int o = i / (TC_CK * 9), r = i % (TC_CK * 9), c = r / 9, k = r % 9;
-            float v = 0.f;
-            if (co0 + o < Co && ci0 + c < Ci) {
-                const size_t idx = TRANS ? ((size_t)(ci0 + c) * Co + (co0 + o)) * 9 + (8 - k)
-                                         : ((size_t)(co0 + o) * Ci + (ci0 + c)) * 9 + k;
-                v = __bfloat162float(w[idx]);
-            }
-            sB[k * NT * 32 + (c >> 2) * NT * 4 + (o >> 3) * 32 + (o & 7) * 4 + (c & 3)] = v;
-        }
+        if (threadIdx.x == 0) tc_bulk_load(smem_u32(sB), wt + (size_t)s * NT * 288, WBYTES, bar_w);
+        tc_store_input(R, sA);
         // generic-proxy stores -> visible to the tensor core (async proxy)
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (threadIdx.x == 0) {
+            if (!tc_mbar_wait(bar_w, (uint32_t)s & 1u)) atomicExch(&g_unet_tc_err, 1);
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
             constexpr uint32_t idesc = tc_idesc_tf32(128, NT);
@@ -255,6 +301,8 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3_tc(const float *__restrict
                 : "memory");
         }
         issued = s + 1;
+        // the next stage's loads overlap this stage's MMAs
+        if (s + 1 < nstage) tc_load_input(R, inn, Ci, (s + 1) * TC_CK, H, Wd, ty0, tx0, vec != 0);
     }
     if (ok) {
         const bool mine = tc_mbar_wait(bar, (uint32_t)(nstage - 1) & 1u);
@@ -262,8 +310,10 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3_tc(const float *__restrict
     }
     if (!ok) {
         if (threadIdx.x == 0) atomicExch(&g_unet_tc_err, 1);
-        // give the MMAs in flight a second bounded chance before the TMEM is freed
+        // give the MMAs and the weight copy in flight a second bounded chance
+        // before the TMEM and the shared memory are released
         if (issued > 0) tc_mbar_wait(bar, (uint32_t)(issued - 1) & 1u);
+        if (threadIdx.x == 0 && issued < nstage) tc_mbar_wait(bar_w, (uint32_t)issued & 1u);
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (= pixels), columns
@@ -302,6 +352,45 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3_tc(const float *__restrict
                      "r"((uint32_t)NT));
 }
 
+// Packs the BF16 weights of every tensor-core convolution into the
+// shared-memory B layout of k_conv3_tc: for entry e (one layer, forward or
+// data gradient) and element j of [Co / NT][stage][tap k][channel group]
+// [o / 8][o % 8][c % 4]: w(o, c, k) = W[o][c][k] (forward) or W[c][o][8 - k]
+// (data gradient: o runs over the layer's inputs, c over its outputs), 0
+// outside the channel ranges.
+struct PackEntry {
+    size_t dst;        // offset in the packed buffer
+    size_t src;        // weight offset in the BF16 parameter array
+    int Ci, Co;        // channels of the convolution as launched
+    int Wci, Wco;      // dimensions of the stored weights W[Wco][Wci][9]
+    int NT, nstage, trans;
+    size_t count;      // Co / NT * nstage * NT * 288
+};
+__global__ void k_pack_weights(const __nv_bfloat16 *__restrict__ wb, float *__restrict__ wpk,
+                               const PackEntry *__restrict__ ent, int n_ent, size_t total) {
+    for (size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x; g < total;
+         g += (size_t)gridDim.x * blockDim.x) {
+        int e = 0;
+        while (e + 1 < n_ent && g >= ent[e + 1].dst) ++e;
+        const PackEntry E = ent[e];
+        const size_t j = g - E.dst;
+        const int per = E.NT * 288;
+        const int blk = (int)(j / per), r = (int)(j % per);
+        const int cot = blk / E.nstage, stg = blk % E.nstage;
+        const int k = r / (E.NT * 32), r2 = r % (E.NT * 32);
+        const int cg = r2 / (E.NT * 4), r3 = r2 % (E.NT * 4);
+        const int o = cot * E.NT + (r3 / 32) * 8 + (r3 % 32) / 4;
+        const int c = stg * TC_CK + cg * 4 + r3 % 4;
+        float v = 0.f;
+        if (o < E.Co && c < E.Ci) {
+            const size_t idx = E.trans ? ((size_t)c * E.Wci + o) * 9 + (8 - k)
+                                       : ((size_t)o * E.Wci + c) * 9 + k;
+            v = __bfloat162float(wb[E.src + idx]);
+        }
+        wpk[g] = v;
+    }
+}
+
 // Tensor-core weight gradient: dW[o][i][k] += sum over pixels p of
 // dy[o][p] x[i][p + off_k].  Per CTA: M = 128 output channels (rows beyond
 // Co are never read back), N = 32 input channels, all 9 taps accumulated in
@@ -318,11 +407,87 @@ constexpr int DW_ABYTES = 16 * DW_SBO_A;         // 65536
 constexpr int DW_BCOPY = 4 * DW_SBO_B;           // 20480 per kx copy
 constexpr size_t DW_SMEM = (size_t)DW_ABYTES + 3 * DW_BCOPY;
 
+// One stage of k_conv3_dw_tc in registers.  Lane mappings put the 8 rows
+// of a core matrix (output / input channel mod 8) on 8 consecutive lanes, so
+// every 16-byte shared store of an 8-lane phase fills one 128-byte core
+// matrix (no bank conflicts), and each channel row's 16 pixels are 64
+// contiguous bytes of 4 lanes' float4 loads.
+//   a[u]: task t = tid + 256 u < 256 ceil(rows / 8): o = 8 (t >> 8) + (t & 7)
+//         (zero for o >= rows), pixel quad (t >> 3) & 3 of tile row (t >> 5) & 7.
+//   b[u]: task t < 1280: channel 8 (t / 320) + (t & 7), quad (t >> 3) & 3 of
+//         halo row (t >> 5) % 10; l[u] / r[u] the pixels left of and right of
+//         the quad, so the shifted copies 0 and 2 are vectors too.
+struct DwIn {
+    float4 a[16];
+    float4 b[5];
+    float l[5], r[5];
+};
+__device__ __forceinline__ float4 dw_row4(const float *row, int x0, int Wd, bool vec) {
+    if (vec && x0 + 3 < Wd) return *reinterpret_cast<const float4 *>(row + x0);
+    return make_float4(x0 < Wd ? row[x0] : 0.f, x0 + 1 < Wd ? row[x0 + 1] : 0.f,
+                       x0 + 2 < Wd ? row[x0 + 2] : 0.f, x0 + 3 < Wd ? row[x0 + 3] : 0.f);
+}
+__device__ __forceinline__ void dw_load(DwIn &R, const float *x, int Ci, int ci0, const float *dy,
+                                        int Co, int co0, int rows, int H, int Wd, int n, int tile,
+                                        int tiles_x, bool vec) {
+    const int ty0 = (tile / tiles_x) * TC_TY, tx0 = (tile % tiles_x) * TC_TX;
+    const float *dyn = dy + ((size_t)n * Co + co0) * H * Wd;
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+        const int t = threadIdx.x + u * TC_THREADS;
+        const int o = 8 * (t >> 8) + (t & 7), xq = (t >> 3) & 3, r = (t >> 5) & 7;
+        const int y = ty0 + r;
+        R.a[u] = (t < ((rows + 7) >> 3) * 256 && o < rows && y < H)
+                     ? dw_row4(dyn + ((size_t)o * H + y) * Wd, tx0 + 4 * xq, Wd, vec)
+                     : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    const float *xn = x + ((size_t)n * Ci + ci0) * H * Wd;
+#pragma unroll
+    for (int u = 0; u < 5; ++u) {
+        const int t = threadIdx.x + u * TC_THREADS;
+        const int c = 8 * (t / 320) + (t & 7), xq = (t >> 3) & 3, hy = (t >> 5) % TC_HY;
+        const int y = ty0 + hy - 1, x0 = tx0 + 4 * xq;
+        const bool live = t < 32 * TC_HY * 4 && ci0 + c < Ci && y >= 0 && y < H;
+        const float *row = xn + ((size_t)c * H + y) * Wd;
+        R.b[u] = live ? dw_row4(row, x0, Wd, vec) : make_float4(0.f, 0.f, 0.f, 0.f);
+        R.l[u] = live && x0 >= 1 && x0 - 1 < Wd ? row[x0 - 1] : 0.f;
+        R.r[u] = live && x0 + 4 < Wd ? row[x0 + 4] : 0.f;
+    }
+}
+// layouts: see k_conv3_dw_tc; copy kx, column xx holds input column
+// tx0 + xx + kx - 1, so for quad g copy 1 is the loaded float4, copy 0 is
+// (left, x, y, z) and copy 2 is (y, z, w, right)
+__device__ __forceinline__ void dw_store(const DwIn &R, float *sA, float *sB, int rows) {
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+        const int t = threadIdx.x + u * TC_THREADS;
+        if (t >= ((rows + 7) >> 3) * 256) break;
+        const int o = 8 * (t >> 8) + (t & 7), xq = (t >> 3) & 3, r = (t >> 5) & 7;
+        const float4 v = R.a[u];
+        *reinterpret_cast<float4 *>(sA + (o >> 3) * (DW_SBO_A / 4) + (r * 4 + xq) * 32 +
+                                    (o & 7) * 4) =
+            make_float4(tc_tf32(v.x), tc_tf32(v.y), tc_tf32(v.z), tc_tf32(v.w));
+    }
+#pragma unroll
+    for (int u = 0; u < 5; ++u) {
+        const int t = threadIdx.x + u * TC_THREADS;
+        if (t >= 32 * TC_HY * 4) break;
+        const int c = 8 * (t / 320) + (t & 7), xq = (t >> 3) & 3, hy = (t >> 5) % TC_HY;
+        const float4 v = R.b[u];
+        const float e0 = tc_tf32(v.x), e1 = tc_tf32(v.y), e2 = tc_tf32(v.z), e3 = tc_tf32(v.w);
+        float *dst = sB + (c >> 3) * (DW_SBO_B / 4) + hy * 128 + xq * 32 + (c & 7) * 4;
+        *reinterpret_cast<float4 *>(dst) = make_float4(tc_tf32(R.l[u]), e0, e1, e2);
+        *reinterpret_cast<float4 *>(dst + DW_BCOPY / 4) = make_float4(e0, e1, e2, e3);
+        *reinterpret_cast<float4 *>(dst + 2 * (DW_BCOPY / 4)) =
+            make_float4(e1, e2, e3, tc_tf32(R.r[u]));
+    }
+}
+
 __global__ void __launch_bounds__(TC_THREADS) k_conv3_dw_tc(const float *__restrict__ x, int Ci,
                                                             const float *__restrict__ dy, int Co,
                                                             float *__restrict__ dw, int H, int Wd,
                                                             int N, int tiles_x, int tiles_img,
-                                                            int splits) {
+                                                            int splits, int vec) {
     extern __shared__ __align__(1024) uint8_t tc_smem[];
     float *sA = reinterpret_cast<float *>(tc_smem);
     float *sB = reinterpret_cast<float *>(tc_smem + DW_ABYTES);
@@ -349,38 +514,17 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3_dw_tc(const float *__restr
     bool ok = true;
     int issued = 0;
     const int total = N * tiles_img;
+    DwIn R;
+    if ((int)blockIdx.z < total)
+        dw_load(R, x, Ci, ci0, dy, Co, co0, rows, H, Wd, blockIdx.z / tiles_img,
+                blockIdx.z % tiles_img, tiles_x, vec != 0);
     for (int tt = blockIdx.z; tt < total; tt += splits) {
-        const int n = tt / tiles_img, tile = tt % tiles_img;
-        const int ty0 = (tile / tiles_x) * TC_TY, tx0 = (tile % tiles_x) * TC_TX;
         if (issued > 0) {
             const bool mine = tc_mbar_wait(bar, (uint32_t)(issued - 1) & 1u);
             ok = !__syncthreads_or(!mine);
             if (!ok) break;
         }
-        const float *dyn = dy + ((size_t)n * Co + co0) * H * Wd;
-        for (int i = threadIdx.x; i < rows * 128; i += TC_THREADS) {
-            const int o = i >> 7, pix = i & 127, r = pix >> 4, xx = pix & 15;
-            const int y = ty0 + r, xq = tx0 + xx;
-            const float v = (y < H && xq < Wd) ? dyn[((size_t)o * H + y) * Wd + xq] : 0.f;
-            sA[(o >> 3) * (DW_SBO_A / 4) + (r * 4 + (xx >> 2)) * 32 + (o & 7) * 4 + (xx & 3)] =
-                tc_tf32(v);
-        }
-        const float *xn = x + ((size_t)n * Ci + ci0) * H * Wd;
-        for (int i = threadIdx.x; i < 32 * TC_HY * TC_HX; i += TC_THREADS) {
-            const int c = i / (TC_HY * TC_HX), r = i % (TC_HY * TC_HX);
-            const int hy = r / TC_HX, hx = r % TC_HX;
-            const int y = ty0 + hy - 1, xq = tx0 + hx - 1;
-            float v = 0.f;
-            if (ci0 + c < Ci && y >= 0 && y < H && xq >= 0 && xq < Wd)
-                v = xn[((size_t)c * H + y) * Wd + xq];
-            v = tc_tf32(v);
-            float *dst = sB + (c >> 3) * (DW_SBO_B / 4) + hy * 128 + (c & 7) * 4;
-#pragma unroll
-            for (int kx = 0; kx < 3; ++kx) {
-                const int xx = hx - kx;
-                if (xx >= 0 && xx < TC_TX) dst[kx * (DW_BCOPY / 4) + (xx >> 2) * 32 + (xx & 3)] = v;
-            }
-        }
+        dw_store(R, sA, sB, rows);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -411,6 +555,11 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3_dw_tc(const float *__restr
                 : "memory");
         }
         ++issued;
+        // the next stage's loads overlap this stage's MMAs
+        const int nt = tt + splits;
+        if (nt < total)
+            dw_load(R, x, Ci, ci0, dy, Co, co0, rows, H, Wd, nt / tiles_img, nt % tiles_img,
+                    tiles_x, vec != 0);
     }
     if (ok && issued > 0) {
         const bool mine = tc_mbar_wait(bar, (uint32_t)(issued - 1) & 1u);
@@ -698,9 +847,12 @@ __global__ void k_to_bf16(const float *__restrict__ p, __nv_bfloat16 *__restrict
 
 using namespace msot;
 
+constexpr size_t NO_PACK = ~(size_t)0;
+
 struct ConvL {
     int Ci, Co, S;        // channels and spatial side
     size_t w_off, b_off;  // in the flat parameter array
+    size_t pk_fwd = NO_PACK, pk_bwd = NO_PACK;  // packed tensor-core weights (k_pack_weights)
 };
 
 struct msot_unet {
@@ -710,6 +862,10 @@ struct msot_unet {
     size_t out_w = 0, out_b = 0, n_par = 0;
     float *par = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;
     __nv_bfloat16 *parb = nullptr;
+    float *wpk = nullptr;  // tensor-core weights in the shared-memory operand layout
+    PackEntry *pk_ent = nullptr;
+    int n_pk = 0;
+    size_t pk_total = 0;
     // forward activations (post-ReLU) per level
     std::vector<float *> ea, e, pool, cat, da, d;
     // gradient buffers per level: Ga (concat-sized), Gb, Gc, Gd, Gs (c_l channels)
@@ -734,29 +890,34 @@ T *dalloc(msot_unet *u, size_t n) {
     return static_cast<T *>(p);
 }
 
-template <bool TRANS, int NT>
-int conv3_tc(const float *in, int Ci, const __nv_bfloat16 *w, const float *bias, float *out,
-             int Co, int S, int N, int relu, cudaStream_t st) {
+inline bool tc_shape(int Ci, int Co) { return Ci >= 8 && Co % 32 == 0; }
+inline int tc_nt(int Co) { return Co % 64 == 0 ? 64 : 32; }
+
+template <int NT>
+int conv3_tc(const float *in, int Ci, const float *wpk, const float *bias, float *out, int Co,
+             int S, int N, int relu, cudaStream_t st) {
     const size_t smem = tc_smem_bytes(NT);
-    MSOT_CUDA_TRY(cudaFuncSetAttribute(k_conv3_tc<TRANS, NT>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MSOT_CUDA_TRY(cudaFuncSetAttribute(k_conv3_tc<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
     const int tx = (S + TC_TX - 1) / TC_TX, ty = (S + TC_TY - 1) / TC_TY;
+    const int vec = (S % 4 == 0) && ((uintptr_t)in % 16 == 0);
     dim3 grid(tx * ty, Co / NT, N);
-    KLAUNCH(k_conv3_tc<TRANS, NT><<<grid, TC_THREADS, smem, st>>>(in, Ci, w, bias, out, Co, S, S,
-                                                                 relu, tx));
+    KLAUNCH(k_conv3_tc<NT><<<grid, TC_THREADS, smem, st>>>(in, Ci, wpk, bias, out, Co, S, S, relu,
+                                                          tx, vec));
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
 }
 
-// 3x3 "same" convolution of [N][Ci][S][S] into [N][Co][S][S]: tensor cores
-// when Ci >= 8 and Co is a multiple of 32 (every layer but the network's
-// first), else the CUDA-core kernel
+// 3x3 "same" convolution of [N][Ci][S][S] into [N][Co][S][S]: on the tensor
+// cores when the layer's weights were packed for this direction (Ci >= 8,
+// Co a multiple of 32: every layer but the network's first), else the
+// CUDA-core kernel on the BF16 weights
 template <bool TRANS>
-int conv3(const float *in, int Ci, const __nv_bfloat16 *w, const float *bias, float *out, int Co,
-          int S, int N, int relu, cudaStream_t st) {
-    if (g_unet_tc.load() && Ci >= 8 && Co % 32 == 0)
-        return Co % 64 == 0 ? conv3_tc<TRANS, 64>(in, Ci, w, bias, out, Co, S, N, relu, st)
-                            : conv3_tc<TRANS, 32>(in, Ci, w, bias, out, Co, S, N, relu, st);
+int conv3(const float *in, int Ci, const __nv_bfloat16 *w, const float *wpk, const float *bias,
+          float *out, int Co, int S, int N, int relu, cudaStream_t st) {
+    if (g_unet_tc.load() && wpk)
+        return tc_nt(Co) == 64 ? conv3_tc<64>(in, Ci, wpk, bias, out, Co, S, N, relu, st)
+                               : conv3_tc<32>(in, Ci, wpk, bias, out, Co, S, N, relu, st);
     const int tx = (S + CT - 1) / CT;
     dim3 grid(tx * tx, (Co + COT - 1) / COT, N);
     KLAUNCH(k_conv3<TRANS><<<grid, 256, 0, st>>>(in, Ci, w, bias, out, Co, S, S, relu, tx));
@@ -765,7 +926,17 @@ int conv3(const float *in, int Ci, const __nv_bfloat16 *w, const float *bias, fl
 }
 
 int conv_fwd(msot_unet *u, const ConvL &c, const float *in, float *out, int N, cudaStream_t st) {
-    return conv3<false>(in, c.Ci, u->parb + c.w_off, u->par + c.b_off, out, c.Co, c.S, N, 1, st);
+    return conv3<false>(in, c.Ci, u->parb + c.w_off,
+                        c.pk_fwd == NO_PACK ? nullptr : u->wpk + c.pk_fwd, u->par + c.b_off, out,
+                        c.Co, c.S, N, 1, st);
+}
+
+int pack_weights(msot_unet *u, cudaStream_t st) {
+    if (!u->pk_total) return MSOT_OK;
+    KLAUNCH(k_pack_weights<<<nblk(u->pk_total), 256, 0, st>>>(u->parb, u->wpk, u->pk_ent,
+                                                              u->n_pk, u->pk_total));
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
 }
 
 // conv c with input x and ReLU output y; dy_post = d loss / d y.  Adds dW, db;
@@ -781,8 +952,9 @@ int conv_bwd(msot_unet *u, const ConvL &c, const float *x, const float *y, const
         MSOT_CUDA_TRY(cudaFuncSetAttribute(k_conv3_dw_tc,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)DW_SMEM));
+        const int vec = (c.S % 4 == 0) && ((uintptr_t)x % 16 == 0) && ((uintptr_t)dy_pre % 16 == 0);
         KLAUNCH(k_conv3_dw_tc<<<dim3(cog, cig, splits), TC_THREADS, DW_SMEM, st>>>(
-            x, c.Ci, dy_pre, c.Co, u->grad + c.w_off, c.S, c.S, N, tx, tiles, splits));
+            x, c.Ci, dy_pre, c.Co, u->grad + c.w_off, c.S, c.S, N, tx, tiles, splits, vec));
     } else {
         const int tx = (c.S + CT - 1) / CT, tiles = tx * tx;
         const int cog = (c.Co + COT - 1) / COT, cig = (c.Ci + CIT - 1) / CIT;
@@ -794,7 +966,10 @@ int conv_bwd(msot_unet *u, const ConvL &c, const float *x, const float *y, const
     KLAUNCH(k_bias_grad<<<dim3(c.Co, N), 256, 0, st>>>(dy_pre, c.Co, c.S * c.S,
                                                         u->grad + c.b_off));
     MSOT_LAUNCH_CHECK();
-    if (dx) return conv3<true>(dy_pre, c.Co, u->parb + c.w_off, nullptr, dx, c.Ci, c.S, N, 0, st);
+    if (dx)
+        return conv3<true>(dy_pre, c.Co, u->parb + c.w_off,
+                           c.pk_bwd == NO_PACK ? nullptr : u->wpk + c.pk_bwd, nullptr, dx, c.Ci,
+                           c.S, N, 0, st);
     return MSOT_OK;
 }
 
@@ -937,6 +1112,33 @@ int msot_unet_create(int levels, int base_channels, int side, int max_batch, uin
     u->out_w = off;
     u->out_b = off + base_channels;
     u->n_par = u->out_b + 1;
+    // tensor-core packing of every eligible layer and direction
+    std::vector<PackEntry> ents;
+    auto pack = [&](ConvL &c) {
+        if (tc_shape(c.Ci, c.Co)) {
+            PackEntry e{u->pk_total, c.w_off, c.Ci, c.Co, c.Ci, c.Co, tc_nt(c.Co),
+                        (c.Ci + TC_CK - 1) / TC_CK, 0, 0};
+            e.count = (size_t)(c.Co / e.NT) * e.nstage * e.NT * 288;
+            c.pk_fwd = u->pk_total;
+            u->pk_total += e.count;
+            ents.push_back(e);
+        }
+        if (tc_shape(c.Co, c.Ci)) {
+            PackEntry e{u->pk_total, c.w_off, c.Co, c.Ci, c.Ci, c.Co, tc_nt(c.Ci),
+                        (c.Co + TC_CK - 1) / TC_CK, 1, 0};
+            e.count = (size_t)(c.Ci / e.NT) * e.nstage * e.NT * 288;
+            c.pk_bwd = u->pk_total;
+            u->pk_total += e.count;
+            ents.push_back(e);
+        }
+    };
+    for (auto &c : u->enc_a) pack(c);
+    for (auto &c : u->enc_b) pack(c);
+    for (int l = 0; l + 1 < levels; ++l) {
+        pack(u->dec_c[l]);
+        pack(u->dec_d[l]);
+    }
+    u->n_pk = (int)ents.size();
     // He-normal weights (fan-in), zero biases
     std::vector<float> h(u->n_par, 0.f);
     std::mt19937_64 rng(seed);
@@ -964,6 +1166,11 @@ int msot_unet_create(int levels, int base_channels, int side, int max_batch, uin
     u->v = F(u->n_par);
     u->parb = dalloc<__nv_bfloat16>(u, u->n_par);
     ok = ok && u->parb;
+    if (u->pk_total) {
+        u->wpk = F(u->pk_total);
+        u->pk_ent = dalloc<PackEntry>(u, ents.size());
+        ok = ok && u->pk_ent;
+    }
     const size_t N = max_batch;
     for (int l = 0; l < levels; ++l) {
         const size_t S2 = (size_t)u->side[l] * u->side[l], c = u->ch[l];
@@ -990,6 +1197,9 @@ int msot_unet_create(int levels, int base_channels, int side, int max_batch, uin
         return MSOT_ENOMEM;
     }
     cudaError_t e = cudaMemcpy(u->par, h.data(), sizeof(float) * u->n_par, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && u->n_pk)
+        e = cudaMemcpy(u->pk_ent, ents.data(), sizeof(PackEntry) * ents.size(),
+                       cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(u->m, 0, sizeof(float) * u->n_par);
     if (e == cudaSuccess) e = cudaMemset(u->v, 0, sizeof(float) * u->n_par);
     if (e != cudaSuccess) {
@@ -998,6 +1208,10 @@ int msot_unet_create(int levels, int base_channels, int side, int max_batch, uin
         return MSOT_ECUDA;
     }
     KLAUNCH(k_to_bf16<<<nblk(u->n_par), 256>>>(u->par, u->parb, u->n_par));
+    if (int rc = pack_weights(u, 0)) {
+        delete u;
+        return rc;
+    }
     *out = u;
     return MSOT_OK;
 }
@@ -1033,6 +1247,7 @@ int msot_unet_set_params(msot_unet_t u, const float *host) {
     MSOT_CUDA_TRY(cudaMemcpy(u->par, host, sizeof(float) * u->n_par, cudaMemcpyHostToDevice));
     KLAUNCH(k_to_bf16<<<nblk(u->n_par), 256>>>(u->par, u->parb, u->n_par));
     MSOT_LAUNCH_CHECK();
+    if (int rc = pack_weights(u, 0)) return rc;
     MSOT_CUDA_TRY(cudaDeviceSynchronize());
     return MSOT_OK;
 }
@@ -1090,7 +1305,7 @@ int msot_unet_adam_step(msot_unet_t u, double lr, int step, void *stream) {
     KLAUNCH(k_adam<<<nblk(u->n_par), 256, 0, (cudaStream_t)stream>>>(
         u->par, u->grad, u->m, u->v, u->parb, u->n_par, (float)lr, b1, b2, 1e-8f, c1, c2));
     MSOT_LAUNCH_CHECK();
-    return MSOT_OK;
+    return pack_weights(u, (cudaStream_t)stream);
 }
 
 }  // extern "C"
