@@ -273,6 +273,9 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3_tc(const float *__restrict
         // generic-proxy stores -> visible to the tensor core (async proxy)
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
+        // the next stage's loads go out first (warp 0 included) and overlap
+        // this stage's MMAs
+        if (s + 1 < nstage) tc_load_input(R, inn, Ci, (s + 1) * TC_CK, H, Wd, ty0, tx0, vec != 0);
         if (threadIdx.x == 0) {
             if (!tc_mbar_wait(bar_w, (uint32_t)s & 1u)) atomicExch(&g_unet_tc_err, 1);
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -301,8 +304,6 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3_tc(const float *__restrict
                 : "memory");
         }
         issued = s + 1;
-        // the next stage's loads overlap this stage's MMAs
-        if (s + 1 < nstage) tc_load_input(R, inn, Ci, (s + 1) * TC_CK, H, Wd, ty0, tx0, vec != 0);
     }
     if (ok) {
         const bool mine = tc_mbar_wait(bar, (uint32_t)(nstage - 1) & 1u);
@@ -527,6 +528,12 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3_dw_tc(const float *__restr
         dw_store(R, sA, sB, rows);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
+        // the next stage's loads go out first (warp 0 included) and overlap
+        // this stage's MMAs
+        const int nt = tt + splits;
+        if (nt < total)
+            dw_load(R, x, Ci, ci0, dy, Co, co0, rows, H, Wd, nt / tiles_img, nt % tiles_img,
+                    tiles_x, vec != 0);
         if (threadIdx.x == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
@@ -555,11 +562,6 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3_dw_tc(const float *__restr
                 : "memory");
         }
         ++issued;
-        // the next stage's loads overlap this stage's MMAs
-        const int nt = tt + splits;
-        if (nt < total)
-            dw_load(R, x, Ci, ci0, dy, Co, co0, rows, H, Wd, nt / tiles_img, nt % tiles_img,
-                    tiles_x, vec != 0);
     }
     if (ok && issued > 0) {
         const bool mine = tc_mbar_wait(bar, (uint32_t)(issued - 1) & 1u);
