@@ -632,6 +632,7 @@ def run_warmstart(args):
     x200, plain_ms = _event_ms(lambda: solve(200))
     target = err(x200)
     # warm: input iterations + network + consistent multiplier, then k iterations
+    ws.start(bt[:64])  # warm-up (graph capture of the input iterations)
     (w0, v0, fell), start_ms = _event_ms(lambda: ws.start(bt))
     net_ms = _event_ms(lambda: ws.net.forward(ws.features(bt)[0]))[1]
     rec_nn_with_L2_reg(model, bt[:64], 1, LAMBDA, x0=w0[:64], v0=v0[:64])  # warm-up
