@@ -72,6 +72,14 @@ def parse():
                     help="warm-start U-Net alone (4 levels, 32 base channels, batch 16): "
                          "training steps and forward passes: one JSON line")
     ap.add_argument("--unet-side", type=int, default=128)
+    ap.add_argument("--l1", action="store_true",
+                    help="batched L1-NNLS (rec_nn_with_L1_eye_reg) at 400x400 px, 512-element "
+                         "arc over 270 deg, 4096 samples, 64 instances: one JSON line")
+    ap.add_argument("--l1-grid", type=int, default=400)
+    ap.add_argument("--l1-iters", type=int, default=50)
+    ap.add_argument("--l1-check-iters", type=int, default=0,
+                    help="iterations of the instance-0 solve compared with the FP64 oracle "
+                         "(0: the same as --l1-iters)")
     return ap.parse_args()
 
 
@@ -510,6 +518,80 @@ def oracle_tv_solve(model, b_np, n_iter, reg, threads):
     return rec.reshape(g.nx, g.nz), time.perf_counter() - t0
 
 
+def oracle_l1_solve(model, b_np, n_iter, reg, threads):
+    """FP64 oracle L1 solve of one instance with the same model parameters."""
+    from oracle import model as M
+    from oracle import native
+    from oracle import solvers as S
+    native.port().set_threads(threads)
+    g = model.Discretization
+    p = model.Probe
+    op = M.ArcProbe(n_det=p.n_det, radius=p.radius, coverage_deg=p.angular_coverage, fs=p.fs,
+                    n_samples=p.n_samples, delay=p.delay, eir=p.eir, eir_length=p.eir_length)
+    om = M.Model(op, M.Grid(g.nx, g.nz, g.fov), c=model.c, fmin=model.fmin, fmax=model.fmax,
+                 norm=model.norm)
+    fwd = lambda v: om.forward(v.reshape(1, g.nx, g.nz)).ravel()
+    adj = lambda y: om.transpose(y.reshape(1, p.n_det, -1)).ravel()
+    t0 = time.perf_counter()
+    rec = S.rec_nn_with_L1_eye_reg(fwd, adj, b_np.astype(np.float64).ravel(), n_iter, reg)[0]
+    return rec.reshape(g.nx, g.nz), time.perf_counter() - t0
+
+
+def run_l1(args):
+    """Batched L1-regularised NNLS (rec_nn_with_L1_eye_reg): 64 instances of
+    400 x 400 px (25.4 mm FOV), 512-element arc of radius 40 mm over 270 deg,
+    4096 samples at 40 MHz, seeded disk + vessel phantoms with 1 % noise,
+    regParam 1e-3, l1_iters outer iterations.  FP32 storage and arithmetic
+    with FP64 inner products, norms and stopping tests.  Accuracy: instance 0
+    solved with l1_check_iters (default l1_iters) iterations on the GPU and by
+    the FP64 oracle on all host cores, which is also the CPU baseline."""
+    import torch
+    from msot_gb300 import Discretization, MSOTmodel, Probe, rec_nn_with_L1_eye_reg
+    from msot_gb300 import _lib
+    from msot_gb300.synthetic import gauss_pulse_eir, phantom_batch
+    n, B, D, T, reg = args.l1_grid, 64, 512, 4096, 1e-3
+    probe = Probe(n_det=D, radius=0.040, angular_coverage=270.0, fs=4e7, n_samples=T,
+                  delay=0.0, eir=gauss_pulse_eir(), eir_length=257)
+    disc = Discretization([-0.0127, 0.0127], n)
+    model = MSOTmodel(probe, disc, 1500.0, False, True, 0, 1e5, 12e6, None, max_batch=B)
+    x = phantom_batch(disc, B, seed=404)
+    y = model.forward(x)
+    amp = y.abs().amax(dim=(1, 2), keepdim=True)
+    gen = torch.Generator(device="cuda").manual_seed(405)
+    b = (y + 0.01 * amp * torch.randn(y.shape, device="cuda", generator=gen)).contiguous()
+    L = _lib.load()
+    for _ in range(max(1, args.warmup)):
+        rec_nn_with_L1_eye_reg(model, b, args.l1_iters, reg)
+    n0 = L.msot_launch_count()
+    ms = []
+    for _ in range(args.steps):
+        ms.append(_event_ms(lambda: rec_nn_with_L1_eye_reg(model, b, args.l1_iters, reg))[1])
+    launches = (L.msot_launch_count() - n0) // max(1, args.steps)
+    ms_step = float(np.mean(ms))
+    acc = None
+    if not args.no_oracle:
+        k = args.l1_check_iters or args.l1_iters
+        g0 = rec_nn_with_L1_eye_reg(model, b[:1], k, reg)[0][0].cpu().numpy().astype(np.float64)
+        ref, t_cpu = oracle_l1_solve(model, b[0].cpu().numpy(), k, reg, os.cpu_count() or 1)
+        acc = {"instance": 0, "iterations": k,
+               "rel_error_vs_fp64": float(np.linalg.norm(g0 - ref) / np.linalg.norm(ref)),
+               "cpu_fp64_s": t_cpu, "cores": os.cpu_count()}
+    cpu = None
+    if acc and acc["iterations"] == args.l1_iters:
+        cpu = {"value": 1.0 / acc["cpu_fp64_s"], "unit": "recons/s", "cores": os.cpu_count(),
+               "kind": "port", "sample": "instance 0, FP64 oracle solve"}
+    return {"mode": "l1_nnls", "metric": "L1-NNLS recons/s", "value": B / (ms_step / 1e3),
+            "cpu_baseline": cpu,
+            "unit": "recons/s", "ms_per_step": ms_step, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "gpu_launches_per_step": launches,
+            "accuracy": acc, "dtype": "f32 (FP64 inner products / norms / stopping tests)",
+            "data": "synthetic seeded disk+vessel phantoms, 1% noise",
+            "config": {"workload": f"rec_nn_with_L1_eye_reg, {n}x{n} px @25.4 mm FOV, 512-el "
+                                   f"arc R=40 mm 270 deg, 4096 samples @40 MHz, EIR 257 taps, "
+                                   f"regParam={reg}, {args.l1_iters} outer iterations",
+                       "batch": B, "grid": [n, n], "n_det": D, "n_t": T}}
+
+
 def run_tv(args):
     """Batched multispectral TV-regularised NNLS (rec_nn_with_TV_reg): 28
     wavelengths x 16 frames = 448 sinograms of 256 x 2030; each instance's
@@ -760,6 +842,10 @@ def main():
         import torch
         torch.cuda.set_device(0)
         out = run_unet(args)
+    elif args.l1:
+        import torch
+        torch.cuda.set_device(0)
+        out = run_l1(args)
     else:
         if world > 1:
             import torch

@@ -105,3 +105,25 @@ def test_l2_warm_start_with_consistent_multiplier(norm_pair):
     r = ref.cpu().numpy()
     assert rel(warm, r) < 1e-2
     assert rel(warm, r) < 0.5 * rel(w_only, r)
+
+
+def test_l1_nnls_512_elements_270deg_4096_samples(cuda):
+    # the mixed-geometry L1 configuration (512-element arc over 270 degrees,
+    # 4096 samples at 40 MHz, 25.4 mm FOV) on an 80 x 80 grid the oracle
+    # solves in seconds; the full 400 x 400, 64-instance case is measured by
+    # bench.py --l1 against the same oracle
+    import torch
+    from msot_gb300 import rec_nn_with_L1_eye_reg
+    kw = dict(n=80, n_det=512, n_samples=4096, radius=0.040, coverage=270.0, fov_half=0.0127,
+              max_batch=2)
+    pm, _ = make_pair(norm=1.0, **kw)
+    pm, om = make_pair(norm=pm.estimate_sigma_max(100), **kw)
+    _, b = _data(om, 80, 2, 26)
+    rec = rec_nn_with_L1_eye_reg(pm, torch.tensor(b, dtype=torch.float32), 20, 1e-3)[0]
+    rec = rec.cpu().numpy()
+    fwd = lambda v: om.forward(v.reshape(1, 80, 80)).ravel()
+    adj = lambda y: om.transpose(y.reshape(1, 512, -1)).ravel()
+    for w in range(2):
+        ref = S.rec_nn_with_L1_eye_reg(fwd, adj, b[w].ravel(), 20, 1e-3)[0]
+        assert rec[w].min() >= 0
+        assert rel(rec[w], ref) <= 1e-3
