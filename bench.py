@@ -72,6 +72,9 @@ def parse():
                     help="warm-start U-Net alone (4 levels, 32 base channels, batch 16): "
                          "training steps and forward passes: one JSON line")
     ap.add_argument("--unet-side", type=int, default=128)
+    ap.add_argument("--prep", action="store_true",
+                    help="raw-sinogram pre-processing (crop 3, Butterworth window, zero-phase "
+                         "filter) of 64 x 256 x 2033 samples: one JSON line")
     ap.add_argument("--l1", action="store_true",
                     help="batched L1-NNLS (rec_nn_with_L1_eye_reg) at 400x400 px, 512-element "
                          "arc over 270 deg, 4096 samples, 64 instances: one JSON line")
@@ -592,6 +595,34 @@ def run_l1(args):
                        "batch": B, "grid": [n, n], "n_det": D, "n_t": T}}
 
 
+def run_prep(args):
+    """Pre-processing of a batch of raw sinograms (64 instances x 256
+    detectors x 2033 samples, crop 3 -> 2030): window (order-2 band-pass
+    [300, T - 200]) and zero-phase filter (0.1-12 MHz at 40 MHz), CUDA
+    events; the filter is the T x T circulant GEMM (2 T^2 flops per column)."""
+    import torch
+    from msot_gb300 import _lib
+    from msot_gb300.preprocess import Preprocessor
+    W, D, T_raw, n_crop = 64, N_DET, N_T + 3, 3
+    T = T_raw - n_crop
+    g = torch.Generator(device="cuda").manual_seed(7)
+    x = torch.randn((W, D, T_raw), device="cuda", generator=g)
+    out = torch.empty((W, D, T), device="cuda")
+    prep = Preprocessor(T_raw, n_crop, (2, 300.0, T - 200.0), 4e7, 1e5, 12e6, max_cols=W * D)
+    for _ in range(args.warmup):
+        prep(x, out)
+    L = _lib.load()
+    n0 = L.msot_launch_count()
+    ms = _event_ms(lambda: [prep(x, out) for _ in range(args.steps)])[1] / args.steps
+    flops = 2.0 * T * T * W * D
+    return {"mode": "preprocess", "metric": "sinograms pre-processed / s",
+            "value": W / (ms / 1e3), "unit": "sinograms/s", "ms_per_step": ms,
+            "gemm_tflops": flops / (ms * 1e9), "steps": args.steps, "warmup": args.warmup,
+            "gpu_launches_per_step": (L.msot_launch_count() - n0) // args.steps,
+            "dtype": "f32", "data": "synthetic Gaussian noise",
+            "config": {"workload": f"crop {n_crop}, window, zero-phase filter; {W} x {D} x {T_raw}"}}
+
+
 def run_tv(args):
     """Batched multispectral TV-regularised NNLS (rec_nn_with_TV_reg): 28
     wavelengths x 16 frames = 448 sinograms of 256 x 2030; each instance's
@@ -846,6 +877,10 @@ def main():
         import torch
         torch.cuda.set_device(0)
         out = run_l1(args)
+    elif args.prep:
+        import torch
+        torch.cuda.set_device(0)
+        out = run_prep(args)
     else:
         if world > 1:
             import torch

@@ -261,6 +261,36 @@ int msot_unet_adam_step(msot_unet_t net, double lr, int step, void *stream);
 int msot_unet_check(msot_unet_t net);
 
 /* ------------------------------------------------------------------------ */
+/* Raw-sinogram pre-processing, in the order of
+ * reconstruction_example_script.m:24-26, along the time axis of every column
+ * ([n_cols][T_raw] FP32 on the device, t fastest = MATLAB T x D x W):
+ *   crop_first_n_signals.m:12          the first n_crop samples are dropped;
+ *   apply_butterworth_window_to_sinogram.m:5-9  (window_order > 0)
+ *       x = mean + (x - mean) |h|, h the order-window_order Butterworth
+ *       band-pass with cut-offs [window_low, window_high] / T (in samples,
+ *       T = T_raw - n_crop) evaluated at T points of [0, pi);
+ *   filter_butter_zero_phase.m:16-48 with use_fft = true (fmin or fmax > 0,
+ *       Hz; <= 0 switches that half off): demean when fmin > 0, then
+ *       ifft(|H|^2 fft(x)) with H the order-8 low-pass at fmax times the
+ *       order-2 high-pass at fmin on T whole-circle bins.
+ * The plan holds the window, the T x T circulant of ifft(|H|^2) and a
+ * [max_cols][T] workspace.  d_out may equal d_raw unless n_crop > 0 without
+ * the filter.  The reference's filtfilt branch (use_fft = false) is not
+ * provided. */
+typedef struct msot_prep *msot_prep_t;
+int msot_prep_create(int T_raw, int n_crop, int window_order, double window_low,
+                     double window_high, double fs, double fmin, double fmax, int max_cols,
+                     msot_prep_t *prep);
+int msot_prep_apply(msot_prep_t prep, const float *d_raw, float *d_out, int n_cols, void *stream);
+int msot_prep_destroy(msot_prep_t prep);
+/* Host only: |H(e^{iw})| of the digital Butterworth filter the pre-processing
+ * designs (type 0 low-pass, 1 high-pass, 2 band-pass [wn1, wn2]; cut-offs in
+ * units of the Nyquist frequency), at w = pi k / n (whole = 0) or 2 pi k / n
+ * (whole = 1), k = 0 .. n - 1. */
+int msot_butter_response(int order, int type, double wn1, double wn2, int n, int whole,
+                         double *mag);
+
+/* ------------------------------------------------------------------------ */
 /* Instrumentation (no counterpart in the reference, whose only timing is
  * tic/toc, e.g. rec_nn_with_L2_reg.m:44-49). */
 

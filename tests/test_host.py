@@ -86,3 +86,33 @@ def test_mex_gateways_compile_against_the_mex_api(name, tmp_path):
                         os.path.join(ROOT, "oracle", "mex_shim"), "-I",
                         os.path.join(ROOT, "include"), src], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.parametrize("order,btype,wn,n,whole", [
+    (8, "low", 2 * 12e6 / 4e7, 2030, True),      # filter_butter_zero_phase low-pass
+    (2, "high", 2 * 1e5 / 4e7, 2030, True),      # and high-pass
+    (2, "bandpass", (300 / 2030, 1830 / 2030), 2030, False),  # the sinogram window
+    (4, "bandpass", (0.1, 0.45), 777, False),
+    (3, "low", 0.2, 64, False),
+])
+def test_butterworth_design_matches_scipy(order, btype, wn, n, whole):
+    # the library's own Butterworth design (host code, no GPU) against
+    # scipy.signal's, evaluated on the same grid
+    import scipy.signal as sps
+    from msot_gb300 import _lib
+    from msot_gb300.preprocess import butter_response
+    _lib.load(build_if_missing=True)
+    got = butter_response(order, btype, wn, n, whole)
+    z, p, k = sps.butter(order, wn, btype, output="zpk")
+    _, h = sps.freqz_zpk(z, p, k, worN=n, whole=whole)
+    assert np.max(np.abs(got - np.abs(h))) <= 1e-10 * max(1.0, np.abs(h).max())
+
+
+def test_butterworth_window_matches_oracle():
+    from oracle import preprocess as Q
+    from msot_gb300 import _lib
+    from msot_gb300.preprocess import butter_response
+    _lib.load(build_if_missing=True)
+    T = 2030
+    got = butter_response(2, "bandpass", (300 / T, (T - 200) / T), T)
+    assert np.max(np.abs(got - Q.butter_window(T, 2, 300, T - 200))) <= 1e-10
