@@ -108,6 +108,21 @@ int msot_interp_transpose(msot_plan_t plan, const float *d_raw, float *d_coeffs,
 int msot_interp_transpose_noalloc(msot_plan_t plan, const float *d_raw, float *d_coeffs,
                                   int batch, void *stream);
 
+/* Travel-time table of two speeds of sound on the GPU (FP64): the medium
+ * (c_below) and the coupling medium (c_above) are separated by the membrane
+ * z = sum_k membrane[k] x^k (n_coef <= 8).  A pixel with z > m(x) reaches a
+ * detector along the path through (x_m, m(x_m)) minimising
+ * |p - q| / c_below + |q - d| / c_above over x_m in [-radius, radius]
+ * (refraction.m:8-19, fermat_principle.m:17-24, there by fminbnd; here a
+ * golden-section search to the FP64 limit), other pixels straight at c_above
+ * (refraction.m:20-24).  travel as msot_travel_times; x_mem (may be NULL)
+ * receives x_m, NaN where the path does not cross the membrane
+ * (calculate_travel_time.m's x_membrane_intersections).  Synchronous. */
+int msot_travel_times_dual(int n_det, double radius, double coverage_deg, const double *x, int nx,
+                           const double *z, int nz, double c_below, double c_above,
+                           const double *membrane, int n_coef, double fs, double delay,
+                           double n_crop, double *travel, double *x_mem);
+
 /* Travel-time table of a single speed of sound on the GPU (FP64):
  * MSOTmodel.m:350-382 with calculate_travel_time's straight rays and the arc
  * detector positions of Probe.m:112-116.  x (nx) and z (nz) are the pixel

@@ -191,6 +191,127 @@ extern "C" int msot_travel_times(int n_det, double radius, double coverage_deg, 
 }
 
 // ---------------------------------------------------------------------------
+// Dual speed of sound: refraction at the membrane z = m(x) = sum_k a_k x^k
+// ---------------------------------------------------------------------------
+constexpr int MEM_MAX_COEF = 8;
+constexpr int FERMAT_ITERS = 64;  // golden-section steps: 0.618^64 ~ 4e-14 of 2 R
+
+__device__ __forceinline__ double mem_z(const double *a, int n, double x) {
+    double z = 0.0;
+    for (int k = n - 1; k >= 0; --k) z = fma(z, x, a[k]);
+    return z;
+}
+__device__ __forceinline__ double fermat_time(double x, double px, double pz, double dx, double dz,
+                                              const double *a, int n, double inv_cb,
+                                              double inv_ca) {
+    const double mz = mem_z(a, n, x);
+    const double ux = px - x, uz = pz - mz, vx = x - dx, vz = mz - dz;
+    return sqrt(ux * ux + uz * uz) * inv_cb + sqrt(vx * vx + vz * vz) * inv_ca;
+}
+
+// refraction.m:8-24 / fermat_principle.m:17-24: a pixel below the membrane
+// (z > m(x)) reaches detector d along the path through the membrane point
+// (x_m, m(x_m)) that minimises |p - q| / c_below + |q - d| / c_above over
+// x_m in [-R, R] (golden-section search, FP64); a pixel on the detector side
+// travels straight at c_above (x_m = NaN).  out[d][p] = t fs - offset.
+__global__ void k_travel_times_dual(const double *__restrict__ xd, const double *__restrict__ zd,
+                                    const double *__restrict__ xv, const double *__restrict__ zv,
+                                    int nx, int nz, const double *__restrict__ coef, int ncoef,
+                                    double radius, double inv_cb, double inv_ca, double fs,
+                                    double offset, double *__restrict__ out,
+                                    double *__restrict__ xmem) {
+    __shared__ double a[MEM_MAX_COEF];
+    if (threadIdx.x < MEM_MAX_COEF) a[threadIdx.x] = threadIdx.x < ncoef ? coef[threadIdx.x] : 0.0;
+    __syncthreads();
+    const int P = nx * nz;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int d = blockIdx.y;
+    if (p >= P) return;
+    const int ix = p / nz, iz = p - ix * nz;
+    const double px = xv[ix], pz = zv[iz], dx = xd[d], dz = zd[d];
+    double t, xm;
+    if (pz > mem_z(a, ncoef, px)) {
+        const double g = 0.6180339887498949;  // (sqrt(5) - 1) / 2
+        double lo = -radius, hi = radius;
+        double x1 = hi - g * (hi - lo), x2 = lo + g * (hi - lo);
+        double f1 = fermat_time(x1, px, pz, dx, dz, a, ncoef, inv_cb, inv_ca);
+        double f2 = fermat_time(x2, px, pz, dx, dz, a, ncoef, inv_cb, inv_ca);
+        for (int it = 0; it < FERMAT_ITERS; ++it) {
+            if (f1 < f2) {
+                hi = x2;
+                x2 = x1;
+                f2 = f1;
+                x1 = hi - g * (hi - lo);
+                f1 = fermat_time(x1, px, pz, dx, dz, a, ncoef, inv_cb, inv_ca);
+            } else {
+                lo = x1;
+                x1 = x2;
+                f1 = f2;
+                x2 = lo + g * (hi - lo);
+                f2 = fermat_time(x2, px, pz, dx, dz, a, ncoef, inv_cb, inv_ca);
+            }
+        }
+        if (f1 < f2) {
+            t = f1;
+            xm = x1;
+        } else {
+            t = f2;
+            xm = x2;
+        }
+    } else {
+        const double ux = dx - px, uz = dz - pz;
+        t = sqrt(ux * ux + uz * uz) * inv_ca;
+        xm = __longlong_as_double(0x7ff8000000000000ll);  // NaN: no intersection
+    }
+    out[(size_t)d * P + p] = t * fs - offset;
+    if (xmem) xmem[(size_t)d * P + p] = xm;
+}
+
+extern "C" int msot_travel_times_dual(int n_det, double radius, double coverage_deg,
+                                      const double *x, int nx, const double *z, int nz,
+                                      double c_below, double c_above, const double *membrane,
+                                      int n_coef, double fs, double delay, double n_crop,
+                                      double *travel, double *x_mem) {
+    if (n_det < 2 || nx <= 0 || nz <= 0 || !x || !z || !travel || !(c_below > 0.0) ||
+        !(c_above > 0.0) || !(fs > 0.0) || !(radius > 0.0) || !membrane || n_coef < 1 ||
+        n_coef > MEM_MAX_COEF) {
+        set_error("travel_times_dual: bad arguments (1 to %d membrane coefficients)",
+                  MEM_MAX_COEF);
+        return MSOT_EINVAL;
+    }
+    std::vector<double> xd(n_det), zd(n_det);
+    const double off = (180.0 - coverage_deg) / 2.0, step = coverage_deg / (n_det - 1);
+    for (int k = 0; k < n_det; ++k) {
+        const double ang = (off + step * k) * (M_PI / 180.0);
+        xd[k] = radius * std::cos(ang);
+        zd[k] = -radius * std::sin(ang);
+    }
+    const size_t P = (size_t)nx * nz, N = P * n_det;
+    DevArrays m;
+    double *dxd = m.get<double>(n_det), *dzd = m.get<double>(n_det);
+    double *dx = m.get<double>(nx), *dz = m.get<double>(nz), *dc = m.get<double>(n_coef);
+    double *dout = m.get<double>(N), *dxm = x_mem ? m.get<double>(N) : nullptr;
+    if (!dxd || !dzd || !dx || !dz || !dc || !dout || (x_mem && !dxm)) {
+        set_error("travel_times_dual: device allocation failed");
+        return MSOT_ENOMEM;
+    }
+    MSOT_CUDA_TRY(cudaMemcpy(dxd, xd.data(), sizeof(double) * n_det, cudaMemcpyHostToDevice));
+    MSOT_CUDA_TRY(cudaMemcpy(dzd, zd.data(), sizeof(double) * n_det, cudaMemcpyHostToDevice));
+    MSOT_CUDA_TRY(cudaMemcpy(dx, x, sizeof(double) * nx, cudaMemcpyHostToDevice));
+    MSOT_CUDA_TRY(cudaMemcpy(dz, z, sizeof(double) * nz, cudaMemcpyHostToDevice));
+    MSOT_CUDA_TRY(cudaMemcpy(dc, membrane, sizeof(double) * n_coef, cudaMemcpyHostToDevice));
+    const dim3 grid((unsigned)((P + 255) / 256), (unsigned)n_det);
+    KLAUNCH(k_travel_times_dual<<<grid, 256>>>(dxd, dzd, dx, dz, nx, nz, dc, n_coef, radius,
+                                               1.0 / c_below, 1.0 / c_above, fs, delay + n_crop,
+                                               dout, dxm));
+    MSOT_LAUNCH_CHECK();
+    MSOT_CUDA_TRY(cudaMemcpy(travel, dout, sizeof(double) * N, cudaMemcpyDeviceToHost));
+    if (x_mem)
+        MSOT_CUDA_TRY(cudaMemcpy(x_mem, dxm, sizeof(double) * N, cudaMemcpyDeviceToHost));
+    return MSOT_OK;
+}
+
+// ---------------------------------------------------------------------------
 // SPMR tables
 // ---------------------------------------------------------------------------
 namespace {

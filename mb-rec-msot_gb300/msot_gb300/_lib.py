@@ -110,6 +110,9 @@ SIGNATURES = {
     "msot_unet_gradients": (C.c_int, [_vp, _vp, _vp, C.c_int, _dp, C.POINTER(C.c_float), _vp]),
     "msot_unet_adam_step": (C.c_int, [_vp, C.c_double, C.c_int, _vp]),
     "msot_unet_check": (C.c_int, [_vp]),
+    "msot_travel_times_dual": (C.c_int, [C.c_int, C.c_double, C.c_double, _dp, C.c_int, _dp,
+                                         C.c_int, C.c_double, C.c_double, _dp, C.c_int,
+                                         C.c_double, C.c_double, C.c_double, _dp, _dp]),
     "msot_prep_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                    C.c_double, C.c_double, C.c_int, C.POINTER(_vp)]),
     "msot_prep_apply": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp]),

@@ -55,6 +55,11 @@ class Probe:
     delay: float = 0.0
     eir: np.ndarray | None = None
     eir_length: int = 257
+    # dual speed of sound (Probe.membrane, Probe.coupling.speedOfSound): the
+    # membrane z = sum_k membrane[k] x^k (metres; up to 8 coefficients) and the
+    # speed of sound of the coupling medium between membrane and detectors
+    membrane: tuple | None = None
+    coupling_speed_of_sound: float | None = None
 
     @classmethod
     def example_system(cls, eir=None):
@@ -194,11 +199,33 @@ def travel_times(probe: Probe, disc: Discretization, c: float, n_crop: int = 0) 
     return out
 
 
+def travel_times_dual(probe: Probe, disc: Discretization, c_below: float, c_above: float,
+                      membrane, n_crop: int = 0):
+    """([n_det][nx*nz] fractional sample indices, membrane intersections x_m)
+    for two speeds of sound split by the membrane (refraction.m:8-24,
+    fermat_principle.m:17-24; MSOTmodel.m:380-381), computed by
+    msot_travel_times_dual on the GPU (FP64 Fermat minimisation)."""
+    P = disc.nx * disc.nz
+    out = np.empty((probe.n_det, P), dtype=np.float64)
+    xm = np.empty((probe.n_det, P), dtype=np.float64)
+    x = np.ascontiguousarray(disc.x, dtype=np.float64)
+    z = np.ascontiguousarray(disc.z, dtype=np.float64)
+    a = np.ascontiguousarray(np.atleast_1d(membrane), dtype=np.float64)
+    D = C.POINTER(C.c_double)
+    _lib.check(_lib.load().msot_travel_times_dual(
+        int(probe.n_det), float(probe.radius), float(probe.angular_coverage),
+        x.ctypes.data_as(D), x.size, z.ctypes.data_as(D), z.size, float(c_below),
+        float(c_above), a.ctypes.data_as(D), a.size, float(probe.fs), float(probe.delay),
+        float(n_crop), out.ctypes.data_as(D), xm.ctypes.data_as(D)))
+    return out, xm
+
+
 class MSOTmodel:
     """MSOTmodel(probe, discretization, speed_of_sound, include_sir,
     use_single_speed_of_sound, num_cropped_samples_at_sinogram_start,
     filt_cutoff_min, filt_cutoff_max, model_normalization_factor)
-    (MSOTmodel.m:18) with single speed of sound.  SIR tables, when
+    (MSOTmodel.m:18); dual speed of sound (use_single_speed_of_sound False)
+    takes the membrane and coupling speed from the probe.  SIR tables, when
     include_sir, are given as ``sir_tables=(SPMR [NS, S], start_end [NS, 2]
     1-based, SPMRIndices [n_det, P] 1-based)``.  ``max_batch`` sizes the
     plan's scratch for batched applies and solves."""
@@ -208,8 +235,14 @@ class MSOTmodel:
                  num_cropped_samples_at_sinogram_start: int = 0, filt_cutoff_min: float = 1e5,
                  filt_cutoff_max: float = 12e6, model_normalization_factor: float | None = None,
                  sir_tables=None, max_batch: int = 1, norm_iterations: int = 100):
-        if not use_single_speed_of_sound:
-            raise NotImplementedError("dual speed of sound is not part of this build")
+        self.use_single_speed_of_sound = bool(use_single_speed_of_sound)
+        if not self.use_single_speed_of_sound:
+            if probe.membrane is None or probe.coupling_speed_of_sound is None:
+                raise ValueError("dual speed of sound needs probe.membrane and "
+                                 "probe.coupling_speed_of_sound")
+            if include_sir:
+                raise NotImplementedError("SIR with dual speed of sound (virtual-source SPMR "
+                                          "mapping, MSOTmodel.m:579-596) is not provided")
         self.Probe = probe
         self.Discretization = discretization
         self.c = float(speed_of_sound)
@@ -219,13 +252,20 @@ class MSOTmodel:
         self.n_t = int(probe.n_samples - self.n_crop)
         self.max_batch = int(max_batch)
         disc = discretization
-        # travel-time indices (MSOTmodel.m:380-381; straight rays, refraction.m:327),
-        # computed on the GPU in FP64
-        self.travel = travel_times(probe, disc, self.c, self.n_crop)
+        # travel-time indices (MSOTmodel.m:380-381; straight rays, refraction.m:327,
+        # or refracted at the membrane), computed on the GPU in FP64
+        self.x_membrane_intersections = None
+        if self.use_single_speed_of_sound:
+            self.travel = travel_times(probe, disc, self.c, self.n_crop)
+            c_ir = self.c
+        else:
+            self.travel, self.x_membrane_intersections = travel_times_dual(
+                probe, disc, self.c, probe.coupling_speed_of_sound, probe.membrane, self.n_crop)
+            c_ir = float(probe.coupling_speed_of_sound)  # MSOTmodel.m:331-335
         # interpolation radius (MSOTmodel.m:36-38)
         self.radius = float(disc.dz / (self.c / probe.fs))
         self.ir = np.ascontiguousarray(
-            model_impulse_response(probe, disc, self.c, self.fmin, self.fmax, self.include_sir),
+            model_impulse_response(probe, disc, c_ir, self.fmin, self.fmax, self.include_sir),
             dtype=np.float64)
         self.pre_x, self.pre_z = (np.ascontiguousarray(t, dtype=np.float64)
                                   for t in disc.prefilter_taps())

@@ -11,6 +11,7 @@ product.  It restates, in FP64:
                                       shift_inv_proj.m:66-71
   * project / transpose-project       Discretization.m:54-72
   * single-SoS travel-time indices    MSOTmodel.m:350-382, refraction.m:324-328
+  * dual-SoS (Fermat) travel times    refraction.m:8-24, fermat_principle.m:17-24
   * interpolation radius              MSOTmodel.m:35-38
   * the impulse response (no SIR)     MSOTmodel.m:329-348
   * the impulse response (with SIR)   MSOTmodel.m:320-327
@@ -251,6 +252,49 @@ def travel_time_indices(probe: ArcProbe, grid: Grid, c: float, n_crop: int = 0) 
     return dist / c * probe.fs - probe.delay - n_crop
 
 
+def travel_time_indices_dual(probe: ArcProbe, grid: Grid, c_below: float, c_above: float,
+                             membrane, n_crop: int = 0):
+    """(D, P) fractional sample indices and membrane intersections x_m for
+    two speeds of sound separated by the membrane z = sum_k a_k x^k
+    (refraction.m:8-24, fermat_principle.m:17-24, MSOTmodel.m:380-381).  A
+    pixel with z > m(x) takes the path through (x_m, m(x_m)) that minimises
+    |p - q| / c_below + |q - d| / c_above over [-R, R]: here a vectorised
+    golden-section search to 1e-13 R, checked against scipy's bounded Brent
+    method by the oracle tests; other pixels travel straight at c_above
+    (x_m = NaN)."""
+    a = np.asarray(membrane, dtype=np.float64)
+    m = lambda x: np.polynomial.polynomial.polyval(x, a)
+    xd, zd = probe.positions()
+    X, Z = grid.pixel_xz()
+    D, P = xd.size, X.size
+    px, pz = np.broadcast_to(X[None, :], (D, P)), np.broadcast_to(Z[None, :], (D, P))
+    dx, dz = np.broadcast_to(xd[:, None], (D, P)), np.broadcast_to(zd[:, None], (D, P))
+
+    def T(x):
+        mz = m(x)
+        return (np.hypot(px - x, pz - mz) / c_below + np.hypot(x - dx, mz - dz) / c_above)
+
+    R = probe.radius
+    g = (np.sqrt(5.0) - 1.0) / 2.0
+    lo, hi = np.full((D, P), -R), np.full((D, P), R)
+    x1, x2 = hi - g * (hi - lo), lo + g * (hi - lo)
+    f1, f2 = T(x1), T(x2)
+    while np.max(hi - lo) > 1e-13 * R:
+        left = f1 < f2
+        hi = np.where(left, x2, hi)
+        lo = np.where(left, lo, x1)
+        xn = np.where(left, hi - g * (hi - lo), lo + g * (hi - lo))
+        fn = T(xn)
+        x2, f2, x1, f1 = (np.where(left, x1, xn), np.where(left, f1, fn),
+                          np.where(left, xn, x2), np.where(left, fn, f2))
+    xm = np.where(f1 < f2, x1, x2)
+    t = np.minimum(f1, f2)
+    below = pz > m(px)
+    t = np.where(below, t, np.hypot(dx - px, dz - pz) / c_above)
+    xm = np.where(below, xm, np.nan)
+    return t * probe.fs - probe.delay - n_crop, xm
+
+
 def interpolation_radius(grid: Grid, probe: ArcProbe, c: float) -> float:
     """MSOTmodel.m:36-38."""
     _, z = grid.vectors()
@@ -276,15 +320,25 @@ class Model:
     norm: float | None = None
     lib: object = None
     sir_tables: object = None  # (sir_ns, start_end_ns2, sir_idx_dp) when include_sir
+    # dual speed of sound: membrane polynomial coefficients and the coupling
+    # medium's speed of sound (Probe.membrane, Probe.coupling.speedOfSound)
+    membrane: object = None
+    c_coupling: float | None = None
     travel: np.ndarray = field(init=False)
     radius: float = field(init=False)
     ir: np.ndarray = field(init=False)
     pre: np.ndarray = field(init=False)
 
     def __post_init__(self):
-        self.travel = travel_time_indices(self.probe, self.grid, self.c, self.n_crop)
+        if self.membrane is None:
+            self.travel = travel_time_indices(self.probe, self.grid, self.c, self.n_crop)
+            c_ir = self.c
+        else:
+            self.travel, _ = travel_time_indices_dual(self.probe, self.grid, self.c,
+                                                      self.c_coupling, self.membrane, self.n_crop)
+            c_ir = self.c_coupling  # MSOTmodel.m:331-335
         self.radius = interpolation_radius(self.grid, self.probe, self.c)
-        self.ir = impulse_response(self.probe, self.grid, self.c, self.fmin, self.fmax,
+        self.ir = impulse_response(self.probe, self.grid, c_ir, self.fmin, self.fmax,
                                    self.include_sir)
         self.pre = prefilter(self.grid)
         if self.lib is None:

@@ -185,3 +185,27 @@ def test_spmr_oracle_tables_are_consistent():
     h = S // 2
     assert np.all(np.abs(np.abs(tab).argmax(axis=1) - h) <= h)
     assert idx.min() >= 1 and idx.max() <= NS
+
+
+def test_dual_sos_travel_times_against_bounded_brent_and_snell():
+    # the oracle's vectorised golden-section Fermat search against scipy's
+    # bounded Brent minimiser on sampled pixel-detector pairs, and Snell's law
+    # at the intersection of a flat membrane
+    from scipy.optimize import minimize_scalar
+    probe = M.ArcProbe(n_det=16, radius=0.040, coverage_deg=135.0, n_samples=2030)
+    grid = M.Grid(12, 12, (-0.006, 0.006, -0.006, 0.006))
+    cb, ca, z0 = 1560.0, 1480.0, -0.012
+    tau, xm = M.travel_time_indices_dual(probe, grid, cb, ca, [z0])
+    xd, zd = probe.positions()
+    X, Z = grid.pixel_xz()
+    rng = np.random.default_rng(0)
+    for _ in range(40):
+        d, p = int(rng.integers(16)), int(rng.integers(X.size))
+        f = lambda x: np.hypot(X[p] - x, Z[p] - z0) / cb + np.hypot(x - xd[d], z0 - zd[d]) / ca
+        r = minimize_scalar(f, bounds=(-0.04, 0.04), method="bounded",
+                            options={"xatol": 1e-14})
+        assert abs(tau[d, p] - r.fun * probe.fs) <= 1e-6
+        # Snell: sin(theta_below) / c_below = sin(theta_above) / c_above
+        s1 = (xm[d, p] - X[p]) / np.hypot(xm[d, p] - X[p], z0 - Z[p])
+        s2 = (xd[d] - xm[d, p]) / np.hypot(xd[d] - xm[d, p], zd[d] - z0)
+        assert abs(s1 / cb - s2 / ca) <= 1e-9
