@@ -117,11 +117,16 @@ int msot_interp_transpose_noalloc(msot_plan_t plan, const float *d_raw, float *d
  * golden-section search to the FP64 limit), other pixels straight at c_above
  * (refraction.m:20-24).  travel as msot_travel_times; x_mem (may be NULL)
  * receives x_m, NaN where the path does not cross the membrane
- * (calculate_travel_time.m's x_membrane_intersections).  Synchronous. */
+ * (calculate_travel_time.m's x_membrane_intersections); virt_x / virt_z
+ * (both or neither NULL) the virtual sources of MSOTmodel.m:585-594: on the
+ * ray from the detector through the membrane point at the distance
+ * t * c_above, the pixel itself where x_m is NaN.  Host [n_det][nx*nz].
+ * Synchronous. */
 int msot_travel_times_dual(int n_det, double radius, double coverage_deg, const double *x, int nx,
                            const double *z, int nz, double c_below, double c_above,
                            const double *membrane, int n_coef, double fs, double delay,
-                           double n_crop, double *travel, double *x_mem);
+                           double n_crop, double *travel, double *x_mem, double *virt_x,
+                           double *virt_z);
 
 /* Travel-time table of a single speed of sound on the GPU (FP64):
  * MSOTmodel.m:350-382 with calculate_travel_time's straight rays and the arc
@@ -156,6 +161,11 @@ typedef struct msot_spmr_spec {
     double elem_elev_radius;    /* elevation focus radius [m]; 0 = flat element */
     int sub_x, sub_y;           /* point sources along the width / the height */
     int half_window;            /* DAC samples each side of the travel time (45 in the reference) */
+    /* dual speed of sound (MSOTmodel.m:579-596): host [n_det][nx*nz] virtual
+     * source positions (msot_travel_times_dual) used for the polar mapping in
+     * place of the pixels, with c the coupling medium's speed; both NULL for
+     * a single speed of sound */
+    const double *virt_x, *virt_z;
 } msot_spmr_spec;
 typedef struct msot_spmr_info {
     double d_min, d_step, a_step_deg;  /* polar grid (MSOTmodel.m:600-613) */

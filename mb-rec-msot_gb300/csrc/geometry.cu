@@ -61,14 +61,18 @@ __global__ void k_travel_times(const double *__restrict__ xd, const double *__re
 // (non-negative doubles order like their bit patterns)
 __global__ void k_spmr_polar(const double *__restrict__ xd, const double *__restrict__ zd,
                              const double *__restrict__ xv, const double *__restrict__ zv,
-                             int nx, int nz, double *__restrict__ r_out,
+                             int nx, int nz, const double *__restrict__ virt_x,
+                             const double *__restrict__ virt_z, double *__restrict__ r_out,
                              double *__restrict__ th_out, unsigned long long *ext) {
     const int P = nx * nz;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const int d = blockIdx.y;
     if (p >= P) return;
     const int ix = p / nz, iz = p - ix * nz;
-    const double ax = __dadd_rn(xd[d], -xv[ix]), az = __dadd_rn(zd[d], -zv[iz]);
+    // the pixel, or its virtual source for detector d (dual speed of sound)
+    const double px = virt_x ? virt_x[(size_t)d * P + p] : xv[ix];
+    const double pz = virt_z ? virt_z[(size_t)d * P + p] : zv[iz];
+    const double ax = __dadd_rn(xd[d], -px), az = __dadd_rn(zd[d], -pz);
     const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(az, az)));
     const double nd = __dsqrt_rn(__dadd_rn(__dmul_rn(xd[d], xd[d]), __dmul_rn(zd[d], zd[d])));
     double cs = __ddiv_rn(__dadd_rn(__dmul_rn(ax, xd[d]), __dmul_rn(az, zd[d])), __dmul_rn(nd, r));
@@ -219,7 +223,8 @@ __global__ void k_travel_times_dual(const double *__restrict__ xd, const double 
                                     int nx, int nz, const double *__restrict__ coef, int ncoef,
                                     double radius, double inv_cb, double inv_ca, double fs,
                                     double offset, double *__restrict__ out,
-                                    double *__restrict__ xmem) {
+                                    double *__restrict__ xmem, double *__restrict__ vxo,
+                                    double *__restrict__ vzo) {
     __shared__ double a[MEM_MAX_COEF];
     if (threadIdx.x < MEM_MAX_COEF) a[threadIdx.x] = threadIdx.x < ncoef ? coef[threadIdx.x] : 0.0;
     __syncthreads();
@@ -265,16 +270,31 @@ __global__ void k_travel_times_dual(const double *__restrict__ xd, const double 
     }
     out[(size_t)d * P + p] = t * fs - offset;
     if (xmem) xmem[(size_t)d * P + p] = xm;
+    if (vxo) {
+        // MSOTmodel.m:585-594: the virtual source on the ray from the detector
+        // through the membrane point, at the distance t c_above; the pixel
+        // itself where the path does not cross the membrane
+        double vx = px, vz = pz;
+        if (xm == xm) {
+            const double qx = xm - dx, qz = mem_z(a, ncoef, xm) - dz;
+            const double s = t / (inv_ca * sqrt(qx * qx + qz * qz));
+            vx = dx + qx * s;
+            vz = dz + qz * s;
+        }
+        vxo[(size_t)d * P + p] = vx;
+        vzo[(size_t)d * P + p] = vz;
+    }
 }
 
 extern "C" int msot_travel_times_dual(int n_det, double radius, double coverage_deg,
                                       const double *x, int nx, const double *z, int nz,
                                       double c_below, double c_above, const double *membrane,
                                       int n_coef, double fs, double delay, double n_crop,
-                                      double *travel, double *x_mem) {
+                                      double *travel, double *x_mem, double *virt_x,
+                                      double *virt_z) {
     if (n_det < 2 || nx <= 0 || nz <= 0 || !x || !z || !travel || !(c_below > 0.0) ||
         !(c_above > 0.0) || !(fs > 0.0) || !(radius > 0.0) || !membrane || n_coef < 1 ||
-        n_coef > MEM_MAX_COEF) {
+        n_coef > MEM_MAX_COEF || (!virt_x != !virt_z)) {
         set_error("travel_times_dual: bad arguments (1 to %d membrane coefficients)",
                   MEM_MAX_COEF);
         return MSOT_EINVAL;
@@ -291,7 +311,9 @@ extern "C" int msot_travel_times_dual(int n_det, double radius, double coverage_
     double *dxd = m.get<double>(n_det), *dzd = m.get<double>(n_det);
     double *dx = m.get<double>(nx), *dz = m.get<double>(nz), *dc = m.get<double>(n_coef);
     double *dout = m.get<double>(N), *dxm = x_mem ? m.get<double>(N) : nullptr;
-    if (!dxd || !dzd || !dx || !dz || !dc || !dout || (x_mem && !dxm)) {
+    double *dvx = virt_x ? m.get<double>(N) : nullptr, *dvz = virt_z ? m.get<double>(N) : nullptr;
+    if (!dxd || !dzd || !dx || !dz || !dc || !dout || (x_mem && !dxm) || (virt_x && !dvx) ||
+        (virt_z && !dvz)) {
         set_error("travel_times_dual: device allocation failed");
         return MSOT_ENOMEM;
     }
@@ -303,11 +325,15 @@ extern "C" int msot_travel_times_dual(int n_det, double radius, double coverage_
     const dim3 grid((unsigned)((P + 255) / 256), (unsigned)n_det);
     KLAUNCH(k_travel_times_dual<<<grid, 256>>>(dxd, dzd, dx, dz, nx, nz, dc, n_coef, radius,
                                                1.0 / c_below, 1.0 / c_above, fs, delay + n_crop,
-                                               dout, dxm));
+                                               dout, dxm, dvx, dvz));
     MSOT_LAUNCH_CHECK();
     MSOT_CUDA_TRY(cudaMemcpy(travel, dout, sizeof(double) * N, cudaMemcpyDeviceToHost));
     if (x_mem)
         MSOT_CUDA_TRY(cudaMemcpy(x_mem, dxm, sizeof(double) * N, cudaMemcpyDeviceToHost));
+    if (virt_x) {
+        MSOT_CUDA_TRY(cudaMemcpy(virt_x, dvx, sizeof(double) * N, cudaMemcpyDeviceToHost));
+        MSOT_CUDA_TRY(cudaMemcpy(virt_z, dvz, sizeof(double) * N, cudaMemcpyDeviceToHost));
+    }
     return MSOT_OK;
 }
 
@@ -386,7 +412,8 @@ int spmr_validate(const msot_spmr_spec *s) {
     if (!s || s->n_det < 2 || s->nx < 2 || s->nz < 2 || !s->x || !s->z || !(s->c > 0) ||
         !(s->fs > 0) || !(s->pixel_sigma > 0) || !(s->elem_width > 0) ||
         !(s->elem_height > 0) || s->sub_x < 1 || s->sub_y < 1 || s->sub_x * s->sub_y > 4096 ||
-        s->half_window < 1 || s->half_window > 4096 || s->elem_elev_radius < 0) {
+        s->half_window < 1 || s->half_window > 4096 || s->elem_elev_radius < 0 ||
+        (!s->virt_x != !s->virt_z)) {
         set_error("spmr: bad specification");
         return MSOT_EINVAL;
     }
@@ -450,7 +477,10 @@ int spmr_run(const msot_spmr_spec *s, msot_spmr_info *info, double *sir, int32_t
            *dth = m.get<double>((size_t)P * D);
     unsigned long long *dext = m.get<unsigned long long>(3);
     int *derr = m.get<int>(1);
-    if (!dxd || !dzd || !dx || !dz || !dr || !dth || !dext || !derr) {
+    double *dvx = s->virt_x ? m.get<double>((size_t)P * D) : nullptr;
+    double *dvz = s->virt_x ? m.get<double>((size_t)P * D) : nullptr;
+    if (!dxd || !dzd || !dx || !dz || !dr || !dth || !dext || !derr ||
+        (s->virt_x && (!dvx || !dvz))) {
         set_error("spmr: device allocation failed");
         return MSOT_ENOMEM;
     }
@@ -461,8 +491,12 @@ int spmr_run(const msot_spmr_spec *s, msot_spmr_info *info, double *sir, int32_t
     const unsigned long long ext0[3] = {~0ull, 0ull, 0ull};
     MSOT_CUDA_TRY(cudaMemcpy(dext, ext0, sizeof(ext0), cudaMemcpyHostToDevice));
     MSOT_CUDA_TRY(cudaMemset(derr, 0, sizeof(int)));
+    if (s->virt_x) {
+        MSOT_CUDA_TRY(cudaMemcpy(dvx, s->virt_x, sizeof(double) * P * D, cudaMemcpyHostToDevice));
+        MSOT_CUDA_TRY(cudaMemcpy(dvz, s->virt_z, sizeof(double) * P * D, cudaMemcpyHostToDevice));
+    }
     KLAUNCH(k_spmr_polar<<<dim3((unsigned)((P + 255) / 256), (unsigned)D), 256>>>(
-        dxd, dzd, dx, dz, nx, nz, dr, dth, dext));
+        dxd, dzd, dx, dz, nx, nz, dvx, dvz, dr, dth, dext));
     MSOT_LAUNCH_CHECK();
     unsigned long long ext[3];
     MSOT_CUDA_TRY(cudaMemcpy(ext, dext, sizeof(ext), cudaMemcpyDeviceToHost));

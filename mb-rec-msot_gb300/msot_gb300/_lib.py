@@ -59,7 +59,7 @@ class SpmrSpec(C.Structure):
         ("c", C.c_double), ("fs", C.c_double), ("pixel_sigma", C.c_double),
         ("elem_width", C.c_double), ("elem_height", C.c_double),
         ("elem_elev_radius", C.c_double), ("sub_x", C.c_int), ("sub_y", C.c_int),
-        ("half_window", C.c_int),
+        ("half_window", C.c_int), ("virt_x", _dp), ("virt_z", _dp),
     ]
 
 
@@ -112,7 +112,8 @@ SIGNATURES = {
     "msot_unet_check": (C.c_int, [_vp]),
     "msot_travel_times_dual": (C.c_int, [C.c_int, C.c_double, C.c_double, _dp, C.c_int, _dp,
                                          C.c_int, C.c_double, C.c_double, _dp, C.c_int,
-                                         C.c_double, C.c_double, C.c_double, _dp, _dp]),
+                                         C.c_double, C.c_double, C.c_double, _dp, _dp, _dp,
+                                         _dp]),
     "msot_prep_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                    C.c_double, C.c_double, C.c_int, C.POINTER(_vp)]),
     "msot_prep_apply": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp]),

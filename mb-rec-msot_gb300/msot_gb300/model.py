@@ -200,14 +200,18 @@ def travel_times(probe: Probe, disc: Discretization, c: float, n_crop: int = 0) 
 
 
 def travel_times_dual(probe: Probe, disc: Discretization, c_below: float, c_above: float,
-                      membrane, n_crop: int = 0):
+                      membrane, n_crop: int = 0, virtual: bool = False):
     """([n_det][nx*nz] fractional sample indices, membrane intersections x_m)
     for two speeds of sound split by the membrane (refraction.m:8-24,
     fermat_principle.m:17-24; MSOTmodel.m:380-381), computed by
-    msot_travel_times_dual on the GPU (FP64 Fermat minimisation)."""
+    msot_travel_times_dual on the GPU (FP64 Fermat minimisation); with
+    ``virtual`` also the virtual sources (virt_x, virt_z) of
+    MSOTmodel.m:585-594."""
     P = disc.nx * disc.nz
     out = np.empty((probe.n_det, P), dtype=np.float64)
     xm = np.empty((probe.n_det, P), dtype=np.float64)
+    vx = np.empty((probe.n_det, P), dtype=np.float64) if virtual else None
+    vz = np.empty((probe.n_det, P), dtype=np.float64) if virtual else None
     x = np.ascontiguousarray(disc.x, dtype=np.float64)
     z = np.ascontiguousarray(disc.z, dtype=np.float64)
     a = np.ascontiguousarray(np.atleast_1d(membrane), dtype=np.float64)
@@ -216,8 +220,9 @@ def travel_times_dual(probe: Probe, disc: Discretization, c_below: float, c_abov
         int(probe.n_det), float(probe.radius), float(probe.angular_coverage),
         x.ctypes.data_as(D), x.size, z.ctypes.data_as(D), z.size, float(c_below),
         float(c_above), a.ctypes.data_as(D), a.size, float(probe.fs), float(probe.delay),
-        float(n_crop), out.ctypes.data_as(D), xm.ctypes.data_as(D)))
-    return out, xm
+        float(n_crop), out.ctypes.data_as(D), xm.ctypes.data_as(D),
+        vx.ctypes.data_as(D) if virtual else None, vz.ctypes.data_as(D) if virtual else None))
+    return (out, xm, vx, vz) if virtual else (out, xm)
 
 
 class MSOTmodel:
@@ -240,9 +245,6 @@ class MSOTmodel:
             if probe.membrane is None or probe.coupling_speed_of_sound is None:
                 raise ValueError("dual speed of sound needs probe.membrane and "
                                  "probe.coupling_speed_of_sound")
-            if include_sir:
-                raise NotImplementedError("SIR with dual speed of sound (virtual-source SPMR "
-                                          "mapping, MSOTmodel.m:579-596) is not provided")
         self.Probe = probe
         self.Discretization = discretization
         self.c = float(speed_of_sound)

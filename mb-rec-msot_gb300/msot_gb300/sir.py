@@ -17,7 +17,7 @@ import numpy as np
 from . import _lib
 
 
-def _spec(probe, disc, c, element, sub, half_window):
+def _spec(probe, disc, c, element, sub, half_window, virtual=None):
     width, height, elev_radius = element
     x = np.ascontiguousarray(disc.x, dtype=np.float64)
     z = np.ascontiguousarray(disc.z, dtype=np.float64)
@@ -31,19 +31,28 @@ def _spec(probe, disc, c, element, sub, half_window):
     s.elem_elev_radius = float(elev_radius or 0.0)
     s.sub_x, s.sub_y = int(sub[0]), int(sub[1])
     s.half_window = int(half_window)
-    return s, (x, z)
+    keep = [x, z]
+    if virtual is not None:
+        vx, vz = (np.ascontiguousarray(v, dtype=np.float64) for v in virtual)
+        if vx.shape != (probe.n_det, disc.nx * disc.nz) or vz.shape != vx.shape:
+            raise ValueError("virtual sources must be [n_det][nx*nz]")
+        s.virt_x, s.virt_z = vx.ctypes.data_as(_lib._dp), vz.ctypes.data_as(_lib._dp)
+        keep += [vx, vz]
+    return s, keep
 
 
 def spmr_tables(probe, disc, c: float, element=(0.25e-3, 10e-3, 0.0), sub=(8, 8),
-                half_window: int = 45):
+                half_window: int = 45, virtual=None):
     """Returns (sir [NS][S], start_end [NS][2], sir_idx [n_det][P], info) in the
     layout MSOTmodel(include_sir=True, sir_tables=(sir, start_end, sir_idx))
     takes.  The half window grows (as calculate_polarSPMR.m:115-139 does) until
-    every column's response fits."""
+    every column's response fits.  With two speeds of sound pass c = the
+    coupling medium's speed and virtual = (virt_x, virt_z) from
+    virtual_sources (MSOTmodel.m:579-596)."""
     L = _lib.load()
     hw = int(half_window)
     while True:
-        s, keep = _spec(probe, disc, c, element, sub, hw)
+        s, keep = _spec(probe, disc, c, element, sub, hw, virtual)
         info = _lib.SpmrInfo()
         rc = L.msot_spmr_query(C.byref(s), C.byref(info))
         if rc == -2 and b"widen" in (L.msot_last_error() or b"") and hw < 4096:
@@ -59,3 +68,13 @@ def spmr_tables(probe, disc, c: float, element=(0.25e-3, 10e-3, 0.0), sub=(8, 8)
     meta = dict(d_min=info.d_min, d_step=info.d_step, a_step_deg=info.a_step_deg,
                 n_dist=info.n_dist, n_angle=info.n_angle, half_window=hw)
     return sir, se, idx, meta
+
+
+def virtual_sources(probe, disc, c_below: float):
+    """(virt_x, virt_z) [n_det][nx*nz]: the virtual source of every pixel for
+    every detector with two speeds of sound (MSOTmodel.m:585-594), from
+    msot_travel_times_dual with the probe's membrane and coupling speed."""
+    from .model import travel_times_dual
+    _, _, vx, vz = travel_times_dual(probe, disc, c_below, probe.coupling_speed_of_sound,
+                                     probe.membrane, virtual=True)
+    return vx, vz

@@ -295,6 +295,25 @@ def travel_time_indices_dual(probe: ArcProbe, grid: Grid, c_below: float, c_abov
     return t * probe.fs - probe.delay - n_crop, xm
 
 
+def virtual_sources(probe: ArcProbe, grid: Grid, c_below: float, c_above: float, membrane):
+    """MSOTmodel.m:585-594: (virt_x, virt_z) [D][P], the point at distance
+    t * c_above from the detector on its ray through the membrane
+    intersection; the pixel itself where the path does not cross."""
+    tau, xm = travel_time_indices_dual(probe, grid, c_below, c_above, membrane)
+    t = (tau + probe.delay) / probe.fs
+    xd, zd = probe.positions()
+    X, Z = grid.pixel_xz()
+    zm = np.polynomial.polynomial.polyval(xm, np.asarray(membrane, dtype=np.float64))
+    qx, qz = xm - xd[:, None], zm - zd[:, None]
+    n = np.hypot(qx, qz)
+    vx = xd[:, None] + qx / n * t * c_above
+    vz = zd[:, None] + qz / n * t * c_above
+    nan = np.isnan(xm)
+    vx = np.where(nan, np.broadcast_to(X[None, :], vx.shape), vx)
+    vz = np.where(nan, np.broadcast_to(Z[None, :], vz.shape), vz)
+    return vx, vz
+
+
 def interpolation_radius(grid: Grid, probe: ArcProbe, c: float) -> float:
     """MSOTmodel.m:36-38."""
     _, z = grid.vectors()

@@ -70,9 +70,11 @@ def _round(v):
 
 
 def spmr_tables(n_det, radius, coverage_deg, x, z, c, fs, sigma, width, height, elev_radius,
-                sx, sy, half_window=45):
+                sx, sy, half_window=45, virtual=None):
     """Returns (sir [NS][S], start_end [NS][2] 1-based, idx [D][P] 1-based,
-    info dict)."""
+    info dict).  virtual = (virt_x, virt_z) [D][P] replaces the pixels in the
+    polar mapping (two speeds of sound, MSOTmodel.m:579-596; c is then the
+    coupling medium's speed)."""
     x = np.asarray(x, dtype=np.float64)
     z = np.asarray(z, dtype=np.float64)
     off = (180.0 - coverage_deg) / 2.0
@@ -80,8 +82,12 @@ def spmr_tables(n_det, radius, coverage_deg, x, z, c, fs, sigma, width, height, 
     xd, zd = radius * np.cos(ang), -radius * np.sin(ang)
     X, Z = np.meshgrid(x, z, indexing="ij")
     X, Z = X.ravel(), Z.ravel()  # p = ix * nz + iz
-    ax = xd[:, None] - X[None, :]
-    az = zd[:, None] - Z[None, :]
+    if virtual is not None:
+        ax = xd[:, None] - np.asarray(virtual[0], dtype=np.float64)
+        az = zd[:, None] - np.asarray(virtual[1], dtype=np.float64)
+    else:
+        ax = xd[:, None] - X[None, :]
+        az = zd[:, None] - Z[None, :]
     r = np.sqrt(ax * ax + az * az)
     nd = np.sqrt(xd * xd + zd * zd)[:, None]
     th = np.arccos(np.clip((ax * xd[:, None] + az * zd[:, None]) / (nd * r), -1.0, 1.0))

@@ -68,3 +68,49 @@ def test_dual_sos_needs_membrane_and_coupling_speed(cuda):
     from msot_gb300 import Discretization, MSOTmodel, Probe
     with pytest.raises(ValueError):
         MSOTmodel(Probe(n_det=16), Discretization([-0.003, 0.003], 16), CB, False, False)
+
+
+def test_virtual_sources_match_oracle(cuda):
+    from msot_gb300.model import travel_times_dual
+    mem = (-0.014, 0.0, 3.0)
+    p, d, op, og = _geom(24, 32, 0.0127, mem)
+    tau, xm, vx, vz = travel_times_dual(p, d, CB, CA, mem, virtual=True)
+    rx, rz = M.virtual_sources(op, og, CB, CA, mem)
+    # the travel time is stationary in x_m, so two searches agree on x_m (and
+    # the ray direction through it) only to ~1e-9 m: bar 1e-8 m
+    assert np.max(np.abs(vx - rx)) <= 1e-8 and np.max(np.abs(vz - rz)) <= 1e-8
+    # the virtual source lies at distance t * c_coupling from its detector
+    xd, zd = op.positions()
+    dist = np.hypot(vx - xd[:, None], vz - zd[:, None])
+    assert np.max(np.abs(dist - tau / p.fs * CA)) <= 1e-12
+
+
+def test_dual_sos_with_sir_matches_oracle(cuda):
+    # SPMR tables from the virtual sources (MSOTmodel.m:579-596) with the
+    # coupling speed, then the SIR operator on the Fermat travel times
+    import torch
+    from oracle import sir as Q
+    from msot_gb300 import MSOTmodel
+    from msot_gb300.sir import spmr_tables, virtual_sources
+    mem = (-0.014, 0.0, 3.0)
+    n, D = 24, 32
+    p, d, op, og = _geom(n, D, 0.004, mem)
+    virt = virtual_sources(p, d, CB)
+    sir, se, idx, meta = spmr_tables(p, d, CA, element=(0.25e-3, 10e-3, 0.0), sub=(4, 4),
+                                     half_window=60, virtual=virt)
+    rsir, rse, ridx, info = Q.spmr_tables(D, 0.040, 135.0, d.x, d.z, CA, p.fs, d.sigma, 0.25e-3,
+                                          10e-3, 0.0, 4, 4, half_window=meta["half_window"],
+                                          virtual=M.virtual_sources(op, og, CB, CA, mem))
+    assert rel(sir, rsir) <= 1e-9
+    assert np.array_equal(se, rse) and np.array_equal(idx, ridx)
+    pm = MSOTmodel(p, d, CB, True, False, 0, 1e5, 12e6, 1.0, sir_tables=(sir, se, idx),
+                   max_batch=2)
+    om = M.Model(op, og, c=CB, norm=1.0, include_sir=True, membrane=mem, c_coupling=CA)
+    om.sir_tables = (sir, se, idx)
+    rng = np.random.default_rng(6)
+    x = rng.random((2, n, n))
+    y = pm.forward(torch.tensor(x, dtype=torch.float32)).cpu().numpy()
+    assert rel(y, om.forward(x)) < 1e-5
+    s = rng.standard_normal((2, D, 2030))
+    assert rel(pm.transpose(torch.tensor(s, dtype=torch.float32)).cpu().numpy(),
+               om.transpose(s)) < 1e-5
