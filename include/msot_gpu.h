@@ -210,6 +210,24 @@ int msot_rec_nn_with_L2_reg_warm(msot_plan_t plan, const float *d_b, float *d_re
                                  const float *d_v0, int coupled, double *err_img,
                                  double *err_reg, void *stream);
 
+/* rec_nn_with_L2_reg.m:1 with both regularisers of the reference's overview
+ * script (reconstruction_overview_script.m:46-54): RegL2 = identity weighted
+ * by lambdaL2 and RegL2_2 = RegL2T_2 = laplacian_per_wavelength (MATLAB
+ * del2 per image; the reference passes it as its own transpose) weighted by
+ * lambdaL2_2 (combine_forward_and_transpose_with_two_regs.m:8-14).  As in
+ * incorporate_l2_reg_into_model_functions.m:8-18 the Laplacian term enters
+ * only when lambdaL2 > 0 as well.  err_reg2 (optional host, batch doubles)
+ * receives lCurveErrReg_2 = ||del2(rec)||^2. */
+int msot_rec_nn_with_L2_reg_2(msot_plan_t plan, const float *d_b, float *d_rec, int batch,
+                              int num_iter, double lambdaL2, double lambdaL2_2, const float *d_x0,
+                              int coupled, double *err_img, double *err_reg, double *err_reg2,
+                              void *stream);
+/* laplacian_per_wavelength.m:4-8: d_out[w] = del2(d_in[w], 1) for images
+ * [batch][nx][nz] (z fastest): (second differences along x + along z) / 4,
+ * the end values extrapolated linearly from the interior. */
+int msot_laplacian_per_wavelength(const float *d_in, float *d_out, int batch, int nx, int nz,
+                                  void *stream);
+
 /* rec_nn_with_L1_eye_reg.m:1 */
 int msot_rec_nn_with_L1_eye_reg(msot_plan_t plan, const float *d_b, float *d_rec, int batch,
                                 int num_iter, double reg, const float *d_x0, int coupled,

@@ -93,12 +93,14 @@ __global__ void k_sumsq(const float *__restrict__ x, const float *__restrict__ y
 
 // LSQR init, image parts: ur = -sl*sr*w ; ub = sb*(w+vm) - sb*w.
 // part: sum ur^2 + ub^2 ; part2: sum (w+vm)^2 (for ||b_aug||).
+// (lw, ul: the Laplacian block, u_lap = -sl*sr2*del2(w); null without it)
 __global__ void k_l2_init_img(const float *__restrict__ wv, const float *__restrict__ vm,
                               float *__restrict__ ur, float *__restrict__ ub, size_t N,
                               double sl, double sr, double sb, int has_reg, double *part,
-                              double *part2) {
+                              double *part2, const float *__restrict__ lw,
+                              float *__restrict__ ul, double sr2) {
     float a1 = 0.f, a2 = 0.f;
-    const float c_r = (float)(-sl * sr), c_b = (float)sb;
+    const float c_r = (float)(-sl * sr), c_b = (float)sb, c_l2 = (float)(-sl * sr2);
     FOR_CHUNK(N) {
         const size_t k = base + i;
         const float wd = wv[k], s = wd + vm[k];
@@ -108,50 +110,68 @@ __global__ void k_l2_init_img(const float *__restrict__ wv, const float *__restr
         ub[k] = bb;
         a1 = fmaf(bb, bb, has_reg ? fmaf(r, r, a1) : a1);
         a2 = fmaf(s, s, a2);
+        if (lw) {
+            const float r2 = c_l2 * lw[k];
+            ul[k] = r2;
+            a1 = fmaf(r2, r2, a1);
+        }
     }
     STORE_PARTIAL((double)a1, part);
     STORE_PARTIAL((double)a2, part2);
 }
 
 // LSQR step, image parts: ur = sl*sr*v - gamma*ur ; ub = sb*v - gamma*ub
+// (lv = del2(v), ul: the Laplacian block u_lap = sl*sr2*del2(v) - gamma*u_lap)
 __global__ void k_l2_u_img(const float *__restrict__ v, float *__restrict__ ur,
                            float *__restrict__ ub, size_t N, double sl, double sr, double sb,
                            int has_reg, const Scal *__restrict__ sc, int coupled,
-                           double *part) {
+                           double *part, const float *__restrict__ lv, float *__restrict__ ul,
+                           double sr2) {
     float acc = 0.f;
     const Scal &q = sc[grp(blockIdx.y, coupled)];
     const float g = (float)q.gamma, c_r = (float)(sl * sr), c_b = (float)sb;
+    const float c_l2 = (float)(sl * sr2);
     const bool done = q.done;
     FOR_CHUNK(N) {
         const size_t k = base + i;
         const float vd = v[k];
-        float r = has_reg ? ur[k] : 0.f, bb = ub[k];
+        float r = has_reg ? ur[k] : 0.f, bb = ub[k], r2 = lv ? ul[k] : 0.f;
         if (!done) {
             r = fmaf(c_r, vd, -g * r);
             bb = fmaf(c_b, vd, -g * bb);
             if (has_reg) ur[k] = r;
             ub[k] = bb;
+            if (lv) {
+                r2 = fmaf(c_l2, lv[k], -g * r2);
+                ul[k] = r2;
+            }
         }
-        acc = fmaf(bb, bb, fmaf(r, r, acc));
+        acc = fmaf(bb, bb, fmaf(r, r, fmaf(r2, r2, acc)));
     }
     STORE_PARTIAL((double)acc, part);
 }
 
 // vt = (sl*(At_us + sr*ur) + sb*ub) / beta ; v = vt - beta*v_old (first: v_old = 0)
+// (lul = del2(u_lap): the Laplacian block's transpose, as the reference
+// passes it, adds sl*sr2*del2(u_lap))
 __global__ void k_l2_v_img(const float *__restrict__ atu, const float *__restrict__ ur,
                            const float *__restrict__ ub, float *__restrict__ v, size_t N,
                            double sl, double sr, double sb, int has_reg, int first,
-                           const Scal *__restrict__ sc, int coupled, double *part) {
+                           const Scal *__restrict__ sc, int coupled, double *part,
+                           const float *__restrict__ lul, double sr2) {
     float acc = 0.f;
     const Scal &q = sc[grp(blockIdx.y, coupled)];
     const bool done = q.done;
     const float ib = (float)(1.0 / q.beta), be = (float)q.beta;
     const float c_l = (float)sl, c_r = (float)(sl * sr), c_b = (float)sb;
+    const float c_l2 = (float)(sl * sr2);
     FOR_CHUNK(N) {
         const size_t k = base + i;
         float vv = v[k];
         if (!done) {
-            float vt = fmaf(c_l, atu[k], fmaf(c_b, ub[k], has_reg ? c_r * ur[k] : 0.f)) * ib;
+            float reg = has_reg ? c_r * ur[k] : 0.f;
+            if (lul) reg = fmaf(c_l2, lul[k], reg);
+            float vt = fmaf(c_l, atu[k], fmaf(c_b, ub[k], reg)) * ib;
             if (!first) vt = fmaf(-be, vv, vt);
             vv = vt;
             v[k] = vv;
@@ -159,6 +179,28 @@ __global__ void k_l2_v_img(const float *__restrict__ atu, const float *__restric
         acc = fmaf(vv, vv, acc);
     }
     STORE_PARTIAL((double)acc, part);
+}
+
+// MATLAB del2(U, 1) of every image [W][nx][nz] (z fastest): (the second
+// differences along z + along x) / 4, the end values of each line
+// extrapolated linearly from the interior (n > 3), copied (n == 3), zero
+// (n < 3) -- laplacian_per_wavelength.m:4-8
+__device__ __forceinline__ float del2_line(const float *u, int i, int n, int stride) {
+    if (n < 3) return 0.f;
+    auto D = [&](int k) { return u[(k + 1) * stride] - 2.f * u[k * stride] + u[(k - 1) * stride]; };
+    if (i > 0 && i < n - 1) return D(i);
+    if (n == 3) return D(1);
+    return i == 0 ? 2.f * D(1) - D(2) : 2.f * D(n - 2) - D(n - 3);
+}
+__global__ void k_del2(const float *__restrict__ in, float *__restrict__ out, int nx, int nz) {
+    const size_t N = (size_t)nx * nz;
+    FOR_CHUNK(N) {
+        const int ix = (int)(i / nz), iz = (int)(i % nz);
+        const float *img = in + base;
+        const float gz = del2_line(img + (size_t)ix * nz, iz, nz, 1);
+        const float gx = del2_line(img + iz, ix, nx, nz);
+        out[base + i] = 0.25f * (gx + gz);
+    }
 }
 
 // Sum of the partials of group g, computed by the whole warp (lane-strided,
@@ -399,12 +441,16 @@ static int group_sumsq(const Ctx &c, const float *x, const float *y, size_t N, i
 
 // One outer iteration of nnls_L2_less: lsqr(maxit = 2, x0 = w), clip, multiplier.
 static int l2_outer(const Ctx &c, const float *b, float *wv, float *vm, double sr,
-                    int has_reg, const double *normb2) {
+                    int has_reg, const double *normb2, double sr2) {
     const double sl = 1.0, sb = std::sqrt(1e-3);
     Work &k = c.wk;
     float *us = k.s1, *tmp_s = k.s2;
     float *ur = k.i[0], *ub = k.i[1], *v = k.i[2], *d = k.i[3], *x = k.i[4], *xmin = k.i[5],
           *tmp_i = k.i[6];
+    // second regulariser (Laplacian): residual block ul, del2 results in tl
+    const bool lap = sr2 > 0.0;
+    float *ul = lap ? k.i[9] : nullptr, *tl = lap ? k.i[10] : nullptr;
+    const int nx = c.pl.nx, nz = c.pl.nz;
     const size_t ns = c.NS / c.W, ni = c.NI / c.W;
     const dim3 gs(c.nbs, c.W), gi(c.nbi, c.W);
     const int G = c.coupled ? 1 : c.W;
@@ -423,15 +469,17 @@ static int l2_outer(const Ctx &c, const float *b, float *wv, float *vm, double s
         KLAUNCH(k_sino_update<<<gs, RED_THREADS, 0, st>>>(tmp_s, b, us, ns, 0, sl, k.sc,
                                                           c.coupled, c.P(0)));
     }
+    if (lap) KLAUNCH(k_del2<<<gi, RED_THREADS, 0, st>>>(wv, tl, nx, nz));
     KLAUNCH(k_l2_init_img<<<gi, RED_THREADS, 0, st>>>(wv, vm, ur, ub, ni, sl, sr, sb, has_reg, c.P(1),
-                                              c.P(2)));
+                                              c.P(2), tl, ul, sr2));
     KLAUNCH(k_l2_scalar<<<1, 1024, 0, st>>>(k.sc, 0, c.P(0), nps, c.P(1), c.nbi, c.P(2), c.nbi, normb2,
                                    sl, sb, c.W, c.coupled, 1e-8));
     MSOT_LAUNCH_CHECK();
     // v = A_aug^T u / beta
     TRY(apply_transpose(c.pl, us, tmp_i, c.W, st));
+    if (lap) KLAUNCH(k_del2<<<gi, RED_THREADS, 0, st>>>(ul, tl, nx, nz));
     KLAUNCH(k_l2_v_img<<<gi, RED_THREADS, 0, st>>>(tmp_i, ur, ub, v, ni, sl, sr, sb, has_reg, 1, k.sc,
-                                           c.coupled, c.P(1)));
+                                           c.coupled, c.P(1), tl, sr2));
     KLAUNCH(k_l2_scalar<<<1, 1024, 0, st>>>(k.sc, 1, c.P(1), c.nbi, nullptr, 0, nullptr, 0, nullptr, sl,
                                    sb, c.W, c.coupled, 1e-8));
     KLAUNCH(k_l2_scale_v<<<gi, RED_THREADS, 0, st>>>(v, d, x, xmin, wv, ni, 1, k.sc, c.coupled));
@@ -446,8 +494,9 @@ static int l2_outer(const Ctx &c, const float *b, float *wv, float *vm, double s
             KLAUNCH(k_sino_update<<<gs, RED_THREADS, 0, st>>>(tmp_s, nullptr, us, ns, 1, sl, k.sc,
                                                               c.coupled, c.P(0)));
         }
+        if (lap) KLAUNCH(k_del2<<<gi, RED_THREADS, 0, st>>>(v, tl, nx, nz));
         KLAUNCH(k_l2_u_img<<<gi, RED_THREADS, 0, st>>>(v, ur, ub, ni, sl, sr, sb, has_reg, k.sc,
-                                               c.coupled, c.P(1)));
+                                               c.coupled, c.P(1), tl, ul, sr2));
         KLAUNCH(k_l2_scalar<<<1, 1024, 0, st>>>(k.sc, 2, c.P(0), nps, c.P(1), c.nbi, nullptr, 0,
                                        nullptr, sl, sb, c.W, c.coupled, 1e-8));
         KLAUNCH(k_l2_dx<<<gi, RED_THREADS, 0, st>>>(v, d, x, xmin, ni, k.sc, c.coupled));
@@ -455,8 +504,9 @@ static int l2_outer(const Ctx &c, const float *b, float *wv, float *vm, double s
         MSOT_LAUNCH_CHECK();
         if (it == 1) break;  // the last A^T of lsqr only feeds its stopping test
         TRY(apply_transpose(c.pl, us, tmp_i, c.W, st));
+        if (lap) KLAUNCH(k_del2<<<gi, RED_THREADS, 0, st>>>(ul, tl, nx, nz));
         KLAUNCH(k_l2_v_img<<<gi, RED_THREADS, 0, st>>>(tmp_i, ur, ub, v, ni, sl, sr, sb, has_reg, 0,
-                                               k.sc, c.coupled, c.P(1)));
+                                               k.sc, c.coupled, c.P(1), tl, sr2));
         KLAUNCH(k_l2_scalar<<<1, 1024, 0, st>>>(k.sc, 1, c.P(1), c.nbi, nullptr, 0, nullptr, 0, nullptr,
                                        sl, sb, c.W, c.coupled, 1e-8));
         KLAUNCH(k_l2_scale_v<<<gi, RED_THREADS, 0, st>>>(v, d, x, xmin, wv, ni, 0, k.sc, c.coupled));
@@ -477,7 +527,7 @@ struct SolverCache {
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
     cudaGraphExec_t l2_exec = nullptr;
     int l2_W = -1, l2_has_reg = -1, l2_coupled = -1;
-    double l2_sr = -1.0;
+    double l2_sr = -1.0, l2_sr2 = -1.0;
     long l2_kernels = 0;  // kernel nodes in the captured iteration
 };
 
@@ -530,7 +580,8 @@ static long count_kernel_nodes(cudaGraph_t g) {
 
 static int solve_l2(Plan &pl, const float *b_in, float *rec, int W, int num_iter,
                     double lambdaL2, const float *x0, const float *v0, int coupled,
-                    double *err_img, double *err_reg, cudaStream_t user) {
+                    double *err_img, double *err_reg, cudaStream_t user,
+                    double lambdaL2_2 = 0.0, double *err_reg2 = nullptr) {
     int rc;
     SolverCache *sc = cache_for(pl, W, rc);
     if (rc) return rc;
@@ -543,6 +594,9 @@ static int solve_l2(Plan &pl, const float *b_in, float *rec, int W, int num_iter
     Ctx c{pl, W, coupled, st, NS, NI, nblk_for(NS / W), nblk_for(NI / W), wk};
     const int has_reg = lambdaL2 > 0;
     const double sr = has_reg ? std::sqrt(lambdaL2) : 0.0;
+    // incorporate_l2_reg_into_model_functions.m:8-18: the second term only
+    // together with the first
+    const double sr2 = has_reg && lambdaL2_2 > 0 ? std::sqrt(lambdaL2_2) : 0.0;
     float *wv = wk.i[7], *vm = wk.i[8];
     const float *b = wk.s3;
     do {
@@ -566,17 +620,17 @@ static int solve_l2(Plan &pl, const float *b_in, float *rec, int W, int num_iter
         int it = 0;
         const bool use_graph = !profiling_enabled() && num_iter > 1;
         const bool have = sc->l2_exec && sc->l2_W == W && sc->l2_has_reg == has_reg &&
-                          sc->l2_coupled == coupled && sc->l2_sr == sr;
+                          sc->l2_coupled == coupled && sc->l2_sr == sr && sc->l2_sr2 == sr2;
         if (use_graph && !have) {
             // first iteration eagerly (sets kernel attributes), then capture one
-            if ((rc = l2_outer(c, b, wv, vm, sr, has_reg, wk.gsum))) break;
+            if ((rc = l2_outer(c, b, wv, vm, sr, has_reg, wk.gsum, sr2))) break;
             ++it;
             if (sc->l2_exec) cudaGraphExecDestroy(sc->l2_exec);
             sc->l2_exec = nullptr;
             cudaGraph_t g = nullptr;
             MSOT_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
             const long before = g_launch_count.load();
-            rc = l2_outer(c, b, wv, vm, sr, has_reg, wk.gsum);
+            rc = l2_outer(c, b, wv, vm, sr, has_reg, wk.gsum, sr2);
             g_launch_count -= g_launch_count.load() - before;  // counted per replay below
             cudaError_t ce = cudaStreamEndCapture(st, &g);
             if (rc || ce != cudaSuccess) {
@@ -600,6 +654,7 @@ static int solve_l2(Plan &pl, const float *b_in, float *rec, int W, int num_iter
             sc->l2_has_reg = has_reg;
             sc->l2_coupled = coupled;
             sc->l2_sr = sr;
+            sc->l2_sr2 = sr2;
         }
         if (use_graph) {
             for (; it < num_iter; ++it) {
@@ -608,7 +663,7 @@ static int solve_l2(Plan &pl, const float *b_in, float *rec, int W, int num_iter
             }
         } else {
             for (; it < num_iter && rc == MSOT_OK; ++it)
-                rc = l2_outer(c, b, wv, vm, sr, has_reg, wk.gsum);
+                rc = l2_outer(c, b, wv, vm, sr, has_reg, wk.gsum, sr2);
             if (rc) break;
         }
         KLAUNCH(k_copy<<<256, 256, 0, st>>>(wv, rec, NI));
@@ -627,6 +682,17 @@ static int solve_l2(Plan &pl, const float *b_in, float *rec, int W, int num_iter
                 if ((rc = group_sumsq(ci, rec, nullptr, NI, c.nbi, e))) break;
                 for (int w = 0; w < W; ++w) err_reg[w] = has_reg ? e[w] : 0.0;
             }
+        }
+        if (err_reg2) {
+            // lCurveErrReg_2 = ||del2(rec)||^2 (rec_nn_with_L2_reg.m:58-63)
+            std::vector<double> e;
+            if (sr2 > 0.0) {
+                KLAUNCH(k_del2<<<dim3(c.nbi, W), RED_THREADS, 0, st>>>(rec, wk.i[10], pl.nx, pl.nz));
+                Ctx ci = c;
+                ci.coupled = 0;
+                if ((rc = group_sumsq(ci, wk.i[10], nullptr, NI, c.nbi, e))) break;
+            }
+            for (int w = 0; w < W; ++w) err_reg2[w] = sr2 > 0.0 ? e[w] : 0.0;
         }
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) {
@@ -988,6 +1054,37 @@ extern "C" int msot_rec_nn_with_L2_reg_warm(msot_plan_t plan, const float *d_b, 
     }
     return solve_l2(plan->p, d_b, d_rec, batch, num_iter, lambdaL2, d_w0, d_v0,
                     coupled ? 1 : 0, err_img, err_reg, (cudaStream_t)stream);
+}
+
+extern "C" int msot_rec_nn_with_L2_reg_2(msot_plan_t plan, const float *d_b, float *d_rec,
+                                         int batch, int num_iter, double lambdaL2,
+                                         double lambdaL2_2, const float *d_x0, int coupled,
+                                         double *err_img, double *err_reg, double *err_reg2,
+                                         void *stream) {
+    if (!plan || !d_b || !d_rec || batch <= 0 || num_iter < 0) {
+        set_error("rec_nn_with_L2_reg_2: bad arguments");
+        return MSOT_EINVAL;
+    }
+    if (batch > plan->p.max_batch) {
+        set_error("batch %d exceeds the plan's max_batch %d", batch, plan->p.max_batch);
+        return MSOT_EINVAL;
+    }
+    return solve_l2(plan->p, d_b, d_rec, batch, num_iter, lambdaL2, d_x0, nullptr,
+                    coupled ? 1 : 0, err_img, err_reg, (cudaStream_t)stream, lambdaL2_2,
+                    err_reg2);
+}
+
+extern "C" int msot_laplacian_per_wavelength(const float *d_in, float *d_out, int batch, int nx,
+                                             int nz, void *stream) {
+    if (!d_in || !d_out || d_in == d_out || batch <= 0 || nx <= 0 || nz <= 0) {
+        set_error("laplacian_per_wavelength: bad arguments (in and out must differ)");
+        return MSOT_EINVAL;
+    }
+    const size_t N = (size_t)nx * nz;
+    KLAUNCH(k_del2<<<dim3(nblk_for(N), batch), RED_THREADS, 0, (cudaStream_t)stream>>>(
+        d_in, d_out, nx, nz));
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
 }
 
 extern "C" int msot_rec_nn_with_L1_eye_reg(msot_plan_t plan, const float *d_b, float *d_rec,

@@ -114,6 +114,9 @@ SIGNATURES = {
                                          C.c_int, C.c_double, C.c_double, _dp, C.c_int,
                                          C.c_double, C.c_double, C.c_double, _dp, _dp, _dp,
                                          _dp]),
+    "msot_rec_nn_with_L2_reg_2": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_double,
+                                            C.c_double, _vp, C.c_int, _dp, _dp, _dp, _vp]),
+    "msot_laplacian_per_wavelength": (C.c_int, [_vp, _vp, C.c_int, C.c_int, C.c_int, _vp]),
     "msot_prep_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                    C.c_double, C.c_double, C.c_int, C.POINTER(_vp)]),
     "msot_prep_apply": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp]),

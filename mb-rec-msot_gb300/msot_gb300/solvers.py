@@ -58,19 +58,32 @@ def rec_nn_with_L2_reg(model: MSOTmodel, data_filt, num_iter_nn_outer: int, lamb
                        RegL2="identity", RegL2T="identity", lambdaL2_2=None, RegL2_2=None,
                        RegL2T_2=None, *, x0=None, v0=None, coupled: bool = False, stream=None):
     """rec_nn_with_L2_reg.m:1.  Returns (rec_img, lCurveErrImg, lCurveErrReg,
-    lCurveErrReg_2, err, t) like the reference; lCurveErr* are per-instance
+    lCurveErrReg_2, err, t) like the reference.  RegL2 is the identity;
+    RegL2_2 / RegL2T_2 (with lambdaL2_2 > 0 and lambdaL2 > 0, as the reference
+    requires) is laplacian_per_wavelength.  lCurveErr* are per-instance
     numpy arrays (one value when coupled), err is empty (the reference only
     fills it when calculate_objective_per_iter is set, which it hard-codes
     to false) and t is the wall time of the solve in seconds."""
     if lambdaL2 and lambdaL2 > 0 and RegL2 not in ("identity", None):
         raise NotImplementedError("only the identity L2 regulariser is supported")
-    if lambdaL2_2 and lambdaL2_2 > 0:
-        raise NotImplementedError("the second (Laplacian) L2 term is not part of this build")
+    two = bool(lambdaL2_2 and lambdaL2_2 > 0)
+    if two and not (_is_laplacian(RegL2_2) and _is_laplacian(RegL2T_2 or RegL2_2)):
+        raise NotImplementedError("the second L2 regulariser must be laplacian_per_wavelength")
     b, W, x0p, rec = _prep(model, data_filt, x0)
     e1 = np.zeros(W)
     e2 = np.zeros(W)
+    e3 = np.zeros(W)
     t0 = time.perf_counter()
-    if v0 is not None:
+    if two:
+        if v0 is not None:
+            raise NotImplementedError("v0 with the second regulariser")
+        _lib.check(_lib.load().msot_rec_nn_with_L2_reg_2(
+            model.plan, C.c_void_p(b.data_ptr()), C.c_void_p(rec.data_ptr()), W,
+            int(num_iter_nn_outer), float(lambdaL2 or 0.0), float(lambdaL2_2),
+            C.c_void_p(x0p.data_ptr()) if x0p is not None else None, 1 if coupled else 0,
+            e1.ctypes.data_as(C.POINTER(C.c_double)), e2.ctypes.data_as(C.POINTER(C.c_double)),
+            e3.ctypes.data_as(C.POINTER(C.c_double)), _stream_ptr(stream)))
+    elif v0 is not None:
         if x0p is None:
             raise ValueError("v0 needs x0")
         v0p = torch.as_tensor(v0).to(device=b.device, dtype=torch.float32)
@@ -90,8 +103,28 @@ def rec_nn_with_L2_reg(model: MSOTmodel, data_filt, num_iter_nn_outer: int, lamb
             _stream_ptr(stream)))
     t = time.perf_counter() - t0
     if coupled:
-        e1, e2 = np.array([e1.sum()]), np.array([e2.sum()])
-    return rec, e1, e2, np.zeros_like(e1), np.zeros(0), t
+        e1, e2, e3 = np.array([e1.sum()]), np.array([e2.sum()]), np.array([e3.sum()])
+    return rec, e1, e2, e3, np.zeros(0), t
+
+
+def laplacian_per_wavelength(x, *, stream=None):
+    """laplacian_per_wavelength.m:1-9: MATLAB del2(x(:, :, wl), 1) for every
+    image of a batch (W, nx, nz) on the GPU (msot_laplacian_per_wavelength)."""
+    t = torch.as_tensor(x)
+    if not t.is_cuda:
+        t = t.cuda()
+    t = t.to(torch.float32).contiguous()
+    if t.dim() == 2:
+        t = t.unsqueeze(0)
+    out = torch.empty_like(t)
+    _lib.check(_lib.load().msot_laplacian_per_wavelength(
+        C.c_void_p(t.data_ptr()), C.c_void_p(out.data_ptr()), t.shape[0], t.shape[1], t.shape[2],
+        _stream_ptr(stream)))
+    return out
+
+
+def _is_laplacian(reg) -> bool:
+    return reg is laplacian_per_wavelength or reg == "laplacian"
 
 
 def rec_nn_with_L1_eye_reg(model: MSOTmodel, data_filt, num_iter: int, regParam: float, *,

