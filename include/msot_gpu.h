@@ -341,6 +341,8 @@ int msot_butter_response(int order, int type, double wn1, double wn2, int n, int
  * float summation order):
  *   "tv_prox_cluster"  CTAs per image of the shared-memory SB_ITV2 kernel
  *                      (1, 2, 4, 8, 16; 0 = automatic).
+ *   "conv_min_blocks"  register cap of the IR convolution, as resident CTAs
+ *                      per SM: 3 (default), 4, or 1 (uncapped).
  *   "unet_tensor_cores" 1 (default) = U-Net 3x3 convolutions on the tensor
  *                      cores where the shape allows, 0 = CUDA cores only
  *                      (FP32 activations, no TF32 rounding). */

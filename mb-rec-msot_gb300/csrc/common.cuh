@@ -91,6 +91,8 @@ const char *set_error(const char *fmt, ...);
 
 // tensor-core convolutions of the warm-start U-Net on (1) or off (0); unet.cu
 extern std::atomic<int> g_unet_tc;
+// register cap (minimum resident CTAs per SM) of the IR convolution; operator.cu
+extern std::atomic<int> g_conv_min_blocks;
 
 // launch counter (every kernel launch of the library goes through KLAUNCH)
 extern std::atomic<long long> g_launch_count;

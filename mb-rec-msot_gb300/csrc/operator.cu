@@ -705,8 +705,8 @@ struct ConvEpi {
 // one warp per transform (two real columns), 32-point FFTs in registers and
 // two warp-local transposes through padded shared memory per direction.
 // EPI != 0 requires every CTA's columns to lie in one instance.
-template <int FPC, int EPI = 0>
-__global__ void __launch_bounds__(32 * FPC) k_conv_fft1k(const float *__restrict__ in,
+template <int FPC, int EPI = 0, int MINB = 1>
+__global__ void __launch_bounds__(32 * FPC, MINB) k_conv_fft1k(const float *__restrict__ in,
                                                          float *__restrict__ out,
                                                          const float2 *__restrict__ tw,
                                                          const float2 *__restrict__ H, int C,
@@ -1120,6 +1120,11 @@ int launch_sir_adjoint(const Plan &pl, const float *raw, float *x, int W, float 
 }
 
 constexpr int CONV_FPC = 4;
+// minimum resident CTAs per SM the convolution is compiled for (register
+// cap): 1 = unconstrained (172 registers, 2 CTAs fit), 3 (168 registers, no
+// spills), 4 (128 registers, small spills); msot_tune_set("conv_min_blocks")
+std::atomic<int> g_conv_min_blocks{3};
+static int conv_min_blocks() { return g_conv_min_blocks.load(); }
 
 int launch_conv(const Plan &pl, const float *in, float *out, int W, bool transpose,
                 cudaStream_t st) {
@@ -1134,8 +1139,19 @@ int launch_conv(const Plan &pl, const float *in, float *out, int W, bool transpo
         if (pl.fft_log4n == 5) {
             constexpr int FPC = CONV_FPC;
             dim3 g1(div_up(pl.T, V), div_up(div_up(C, 2), FPC));
-            KLAUNCH(k_conv_fft1k<FPC><<<g1, 32 * FPC, 0, st>>>(in, out, pl.fft_tw, H, C, pl.T,
-                                                               pl.L));
+            switch (conv_min_blocks()) {
+            case 3:
+                KLAUNCH(k_conv_fft1k<FPC, 0, 3><<<g1, 32 * FPC, 0, st>>>(in, out, pl.fft_tw, H, C,
+                                                                         pl.T, pl.L));
+                break;
+            case 4:
+                KLAUNCH(k_conv_fft1k<FPC, 0, 4><<<g1, 32 * FPC, 0, st>>>(in, out, pl.fft_tw, H, C,
+                                                                         pl.T, pl.L));
+                break;
+            default:
+                KLAUNCH(k_conv_fft1k<FPC><<<g1, 32 * FPC, 0, st>>>(in, out, pl.fft_tw, H, C, pl.T,
+                                                                   pl.L));
+            }
         } else {
             if ((rc = set_smem(k_conv_fft<6>, smem)) != MSOT_OK) return rc;
             KLAUNCH(k_conv_fft<6><<<grid, N / 4, smem, st>>>(in, out, pl.fft_tw, H, C, pl.T,
@@ -1251,12 +1267,20 @@ int apply_forward_update(const Plan &pl, const float *img, float *u, const float
     e.nparts = (pl.D / (2 * CONV_FPC)) * (int)g1.x;
     e.part = part;
     *nparts = e.nparts;
-    if (mode == 0)
-        KLAUNCH(k_conv_fft1k<CONV_FPC, 1><<<g1, 32 * CONV_FPC, 0, st>>>(
-            pl.scr_sino, u, pl.fft_tw, pl.fft_hf, C, pl.T, pl.L, e));
-    else
-        KLAUNCH(k_conv_fft1k<CONV_FPC, 2><<<g1, 32 * CONV_FPC, 0, st>>>(
-            pl.scr_sino, u, pl.fft_tw, pl.fft_hf, C, pl.T, pl.L, e));
+    const int mb = conv_min_blocks();
+#define CONV_EPI_LAUNCH(EPI, MB)                                                           \
+    KLAUNCH(k_conv_fft1k<CONV_FPC, EPI, MB><<<g1, 32 * CONV_FPC, 0, st>>>(                 \
+        pl.scr_sino, u, pl.fft_tw, pl.fft_hf, C, pl.T, pl.L, e))
+    if (mode == 0) {
+        if (mb == 3) CONV_EPI_LAUNCH(1, 3);
+        else if (mb == 4) CONV_EPI_LAUNCH(1, 4);
+        else CONV_EPI_LAUNCH(1, 1);
+    } else {
+        if (mb == 3) CONV_EPI_LAUNCH(2, 3);
+        else if (mb == 4) CONV_EPI_LAUNCH(2, 4);
+        else CONV_EPI_LAUNCH(2, 1);
+    }
+#undef CONV_EPI_LAUNCH
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
 }
