@@ -260,6 +260,7 @@ def run_ours(args, rank, world):
     L = _lib.load()
     B = args.batch
     model = build_model(B)
+    tuning = model.autotune(B)  # kernel variants timed on this geometry and batch
     x_true, b = make_data(model, B, seed=1000 + rank)
     flush = torch.empty(512 * 1024 * 1024 // 4, device="cuda")
     dist = None
@@ -359,6 +360,7 @@ def run_ours(args, rank, world):
         "data": "synthetic (seeded disk+vessel phantoms, 1% noise)",
         "config": workload_config(B, world), "clocks": clk.summary(), "e2e": e2e,
         "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
+        "autotune": tuning,
         "rel_error_vs_fp64": acc, "host": platform.machine(),
     }
 
@@ -649,6 +651,7 @@ def run_tv(args):
             continue
         disc = Discretization([-0.0127, 0.0127], n)
         model = MSOTmodel(probe, disc, 1500.0, False, True, 0, 1e5, 12e6, None, max_batch=B)
+        tuning = model.autotune(B)
         maps = {}
         imgs = np.empty((len(inst), n, n), dtype=np.float32)
         for i, (f, l) in enumerate(inst):
@@ -677,7 +680,7 @@ def run_tv(args):
             if n == min(grids) and c0 == 0:
                 rec0 = rec[0].cpu().numpy().astype(np.float64)
         per_grid[str(n)] = {"instances": len(inst), "ms": ms_grid,
-                            "recons_per_s": len(inst) / (ms_grid / 1e3)}
+                            "recons_per_s": len(inst) / (ms_grid / 1e3), "autotune": tuning}
         total_ms += ms_grid
         if n == min(grids) and not args.no_oracle:
             ref, t_cpu = oracle_tv_solve(model, first_b, n_iter, reg, os.cpu_count() or 1)

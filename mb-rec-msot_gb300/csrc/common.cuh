@@ -60,6 +60,10 @@ struct Plan {
     int adj_groups_max = 0;        // detector groups the partial buffer is sized for
     float *scr_part = nullptr;     // [adj_groups_max][max_batch][P] adjoint partial sums
     struct SolverCache *solver = nullptr;  // solver workspace and captured CUDA graphs
+    // variants chosen by msot_autotune for this plan (0 = the built-in choice)
+    int tune_fwd_wt = 0;      // instances per CTA of the DAS forward (8, 4, 2)
+    int tune_conv_mb = 0;     // register cap of the IR convolution (1, 3, 4)
+    int tune_tv_cluster = 0;  // CTAs per image of the SB_ITV2 cluster kernel
     // IR
     int L = 0, Lh = 0;
     float *ir_fwd = nullptr, *ir_adj = nullptr;
@@ -185,6 +189,7 @@ int apply_forward_update(const Plan &pl, const float *img, float *u, const float
                          int *nparts, cudaStream_t st);
 bool forward_update_fusable(const Plan &pl, int W);
 void solver_cache_free(Plan &pl);  // solver.cu
+void solver_cache_invalidate(Plan &pl);  // drops the captured solver graphs (solver.cu)
 bool profiling_enabled();          // timing.cu
 int apply_transpose(const Plan &pl, const float *sino, float *img, int W, cudaStream_t st);
 

@@ -994,7 +994,8 @@ static int das_fwd_f(const Plan &pl, const float *xpm, float *raw, int W, float 
 int launch_das_forward(const Plan &pl, const float *xpm, float *raw, int W, float scale,
                        cudaStream_t st) {
     TimedScope ts_(KID_INTERP_FWD, st);
-    const int wt = pick_wt(W, 1, 8);
+    int wt = pick_wt(W, 1, 8);
+    if (pl.tune_fwd_wt && W % pl.tune_fwd_wt == 0) wt = pl.tune_fwd_wt;
     switch (wt) {
         case 8: return das_fwd_f<8>(pl, xpm, raw, W, scale, st);
         case 4: return das_fwd_f<4>(pl, xpm, raw, W, scale, st);
@@ -1124,7 +1125,9 @@ constexpr int CONV_FPC = 4;
 // cap): 1 = unconstrained (172 registers, 2 CTAs fit), 3 (168 registers, no
 // spills), 4 (128 registers, small spills); msot_tune_set("conv_min_blocks")
 std::atomic<int> g_conv_min_blocks{3};
-static int conv_min_blocks() { return g_conv_min_blocks.load(); }
+static int conv_min_blocks(const Plan &pl) {
+    return pl.tune_conv_mb ? pl.tune_conv_mb : g_conv_min_blocks.load();
+}
 
 int launch_conv(const Plan &pl, const float *in, float *out, int W, bool transpose,
                 cudaStream_t st) {
@@ -1139,7 +1142,7 @@ int launch_conv(const Plan &pl, const float *in, float *out, int W, bool transpo
         if (pl.fft_log4n == 5) {
             constexpr int FPC = CONV_FPC;
             dim3 g1(div_up(pl.T, V), div_up(div_up(C, 2), FPC));
-            switch (conv_min_blocks()) {
+            switch (conv_min_blocks(pl)) {
             case 3:
                 KLAUNCH(k_conv_fft1k<FPC, 0, 3><<<g1, 32 * FPC, 0, st>>>(in, out, pl.fft_tw, H, C,
                                                                          pl.T, pl.L));
@@ -1267,7 +1270,7 @@ int apply_forward_update(const Plan &pl, const float *img, float *u, const float
     e.nparts = (pl.D / (2 * CONV_FPC)) * (int)g1.x;
     e.part = part;
     *nparts = e.nparts;
-    const int mb = conv_min_blocks();
+    const int mb = conv_min_blocks(pl);
 #define CONV_EPI_LAUNCH(EPI, MB)                                                           \
     KLAUNCH(k_conv_fft1k<CONV_FPC, EPI, MB><<<g1, 32 * CONV_FPC, 0, st>>>(                 \
         pl.scr_sino, u, pl.fft_tw, pl.fft_hf, C, pl.T, pl.L, e))

@@ -554,6 +554,13 @@ static SolverCache *cache_for(Plan &pl, int W, int &rc) {
     return sc;
 }
 
+void solver_cache_invalidate(Plan &pl) {
+    if (!pl.solver) return;
+    if (pl.solver->l2_exec) cudaGraphExecDestroy(pl.solver->l2_exec);
+    pl.solver->l2_exec = nullptr;
+    pl.solver->l2_W = -1;
+}
+
 void solver_cache_free(Plan &pl) {
     if (!pl.solver) return;
     if (pl.solver->l2_exec) cudaGraphExecDestroy(pl.solver->l2_exec);

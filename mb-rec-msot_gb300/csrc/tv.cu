@@ -1170,10 +1170,10 @@ struct TvcGeom {
 
 std::atomic<int> g_tv_cluster{0};  // forced cluster size (msot_tune_set), 0 = automatic
 
-TvcGeom tvc_geometry(int N) {
+TvcGeom tvc_geometry(int N, int force = 0) {
     TvcGeom g;
     if (N > TVC_THREADS) return g;
-    if (const int Cf = g_tv_cluster.load()) {
+    if (const int Cf = force ? force : g_tv_cluster.load()) {
         const int nloc = (N + Cf - 1) / Cf;
         const size_t bytes = (size_t)TVC_NV * nloc * N * sizeof(float);
         if (bytes <= 225 * 1024) {
@@ -1289,9 +1289,9 @@ cudaError_t tvc_launch_gm(const float *z, const TvState *sv, double mu, int coup
 // global-memory kernel on `work` (TV_NVEC vectors per image)
 
 int tv_prox(const float *z, const TvState *sv, double mu, int coupled, float *out, float *work,
-            int W, int N, cudaStream_t st) {
+            int W, int N, cudaStream_t st, int cluster) {
     TimedScope ts(KID_TV_PROX, st);
-    const TvcGeom gm = tvc_geometry(N);
+    const TvcGeom gm = tvc_geometry(N, cluster);
     if (g_prox_path.load() == 0 && gm.C) {
         bool fits = false;
         const cudaError_t e = tvc_launch(gm, z, sv, mu, coupled, out, W, N, st, fits);
@@ -1349,7 +1349,7 @@ int msot_sb_itv2(const float *d_g, float *d_u, int batch, int n, double mu, void
         set_error("sb_itv2: device allocation failed");
         return MSOT_ENOMEM;
     }
-    int rc = tv_prox(d_g, nullptr, mu, 1, d_u, work, batch, n, st);
+    int rc = tv_prox(d_g, nullptr, mu, 1, d_u, work, batch, n, st, 0);
     if (rc) return rc;
     MSOT_CUDA_TRY(cudaStreamSynchronize(st));
     return MSOT_OK;
@@ -1467,7 +1467,7 @@ int msot_rec_nn_with_TV_reg(msot_plan_t plan, const float *d_b, float *d_rec, in
         for (int k = 0; k < sparsa_iter; ++k) {
             TV_CK(apply_transpose(pl, rs, atr, W, st));
             KLAUNCH(k_tv_z<<<grid, TV_RED, 0, st>>>(x, atr, ri, sv, coupled, z, P, sl, sb));
-            TV_CK(tv_prox(z, sv, 0.0, coupled, xn, work, W, N, st));
+            TV_CK(tv_prox(z, sv, 0.0, coupled, xn, work, W, N, st, pl.tune_tv_cluster));
             KLAUNCH(k_tv_step<<<grid, TV_RED, 0, st>>>(x, xn, ri, dx, sv, coupled, N, sb, W, part));
             MSOT_LAUNCH_CHECK();
             TV_CK(apply_forward(pl, dx, As, W, st));
@@ -1497,3 +1497,127 @@ int msot_rec_nn_with_TV_reg(msot_plan_t plan, const float *d_b, float *d_rec, in
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Autotuner: times the variants of the plan's hot kernels on its own geometry
+// and batch and keeps the fastest in the plan (Plan::tune_*).
+// ---------------------------------------------------------------------------
+namespace msot {
+
+// deterministic pseudo-random fill in [0, 1) (integer hash of the index)
+__global__ void k_tune_fill(float *a, size_t n, uint32_t seed) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        uint32_t h = (uint32_t)i * 2654435761u ^ seed;
+        h ^= h >> 16;
+        h *= 2246822519u;
+        h ^= h >> 13;
+        a[i] = (float)(h >> 8) * (1.0f / 16777216.0f);
+    }
+}
+
+// mean time of `reps` runs of fn after one warm-up, CUDA events on st
+template <class F>
+static int tune_time(cudaStream_t st, int reps, double &ms, F fn) {
+    int rc = fn();
+    if (rc) return rc;
+    cudaEvent_t a, b;
+    MSOT_CUDA_TRY(cudaEventCreate(&a));
+    MSOT_CUDA_TRY(cudaEventCreate(&b));
+    cudaEventRecord(a, st);
+    for (int r = 0; r < reps && rc == MSOT_OK; ++r) rc = fn();
+    cudaEventRecord(b, st);
+    const cudaError_t e = cudaEventSynchronize(b);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (rc) return rc;
+    if (e != cudaSuccess) {
+        set_error("autotune: %s", cudaGetErrorString(e));
+        return MSOT_ECUDA;
+    }
+    ms = t / reps;
+    return MSOT_OK;
+}
+
+}  // namespace msot
+
+extern "C" int msot_autotune(msot_plan_t plan, int batch, void *stream, msot_tuning *out) {
+    if (!plan || batch <= 0 || batch > plan->p.max_batch) {
+        set_error("autotune: bad arguments (batch 1 .. max_batch)");
+        return MSOT_EINVAL;
+    }
+    Plan &pl = plan->p;
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t NI = (size_t)batch * pl.P, NS = (size_t)batch * pl.D * pl.T;
+    const bool tv_ok = pl.nx == pl.nz;
+    DevBufs b;
+    float *img = b.get<float>(NI), *img2 = b.get<float>(NI), *sino = b.get<float>(NS);
+    float *work = tv_ok ? b.get<float>((size_t)batch * TV_NVEC * pl.P) : nullptr;
+    if (!b.ok) {
+        set_error("autotune: device allocation failed");
+        return MSOT_ENOMEM;
+    }
+    KLAUNCH(k_tune_fill<<<1024, 256, 0, st>>>(img, NI, 12345u));
+    KLAUNCH(k_tune_fill<<<1024, 256, 0, st>>>(sino, NS, 777u));
+    MSOT_LAUNCH_CHECK();
+    int rc;
+    msot_tuning res{};
+    // DAS forward: instances per CTA (apply_forward: prefilter, forward, conv)
+    {
+        double best = 1e30;
+        int pick = 0;
+        for (int wt : {8, 4, 2}) {
+            if (batch % wt) continue;
+            pl.tune_fwd_wt = wt;
+            double ms;
+            if ((rc = tune_time(st, 3, ms, [&] { return apply_forward(pl, img, sino, batch, st); })))
+                return rc;
+            if (ms < best) best = ms, pick = wt;
+        }
+        pl.tune_fwd_wt = pick;
+        res.fwd_wt = pick;
+        res.fwd_ms = pick ? best : 0.0;
+    }
+    // IR convolution register cap (apply_transpose: conv, adjoint, prefilter)
+    {
+        double best = 1e30;
+        int pick = 3;
+        for (int mb : {1, 3, 4}) {
+            pl.tune_conv_mb = mb;
+            double ms;
+            if ((rc = tune_time(st, 3, ms,
+                                [&] { return apply_transpose(pl, sino, img2, batch, st); })))
+                return rc;
+            if (ms < best) best = ms, pick = mb;
+        }
+        pl.tune_conv_mb = pick;
+        res.conv_min_blocks = pick;
+        res.transpose_ms = best;
+    }
+    // SB_ITV2 cluster size (square grids): the automatic choice and every forced
+    // size whose vectors fit in shared memory
+    res.tv_cluster = 0;
+    if (tv_ok) {
+        double best = 1e30;
+        int pick = 0;
+        for (int C : {0, 1, 2, 4, 8, 16}) {
+            if (C && !tvc_geometry(pl.nx, C).C) continue;
+            double ms;
+            if ((rc = tune_time(st, 2, ms, [&] {
+                     return tv_prox(img, nullptr, 0.05, 1, img2, work, batch, pl.nx, st, C);
+                 })))
+                return rc;
+            if (ms < best) best = ms, pick = C;
+        }
+        pl.tune_tv_cluster = pick;
+        res.tv_cluster = pick;
+        res.tv_prox_ms = best;
+    }
+    // the solvers' captured graphs hold the old kernels
+    solver_cache_invalidate(pl);
+    if (out) *out = res;
+    MSOT_CUDA_TRY(cudaStreamSynchronize(st));
+    return MSOT_OK;
+}

@@ -63,6 +63,11 @@ class SpmrSpec(C.Structure):
     ]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("fwd_wt", C.c_int), ("conv_min_blocks", C.c_int), ("tv_cluster", C.c_int),
+                ("fwd_ms", C.c_double), ("transpose_ms", C.c_double), ("tv_prox_ms", C.c_double)]
+
+
 class SpmrInfo(C.Structure):
     _fields_ = [
         ("d_min", C.c_double), ("d_step", C.c_double), ("a_step_deg", C.c_double),
@@ -117,6 +122,7 @@ SIGNATURES = {
     "msot_rec_nn_with_L2_reg_2": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_double,
                                             C.c_double, _vp, C.c_int, _dp, _dp, _dp, _vp]),
     "msot_laplacian_per_wavelength": (C.c_int, [_vp, _vp, C.c_int, C.c_int, C.c_int, _vp]),
+    "msot_autotune": (C.c_int, [_vp, C.c_int, _vp, C.POINTER(Tuning)]),
     "msot_prep_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                    C.c_double, C.c_double, C.c_int, C.POINTER(_vp)]),
     "msot_prep_apply": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp]),

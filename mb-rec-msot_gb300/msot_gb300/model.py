@@ -328,6 +328,14 @@ class MSOTmodel:
     def plan(self):
         return self._plan
 
+    def autotune(self, batch: int | None = None, stream=None) -> dict:
+        """msot_autotune: time the kernel variants on this model's geometry at
+        ``batch`` instances (default max_batch) and keep the fastest."""
+        t = _lib.Tuning()
+        _lib.check(_lib.load().msot_autotune(self.plan, int(batch or self.max_batch),
+                                             _stream_ptr(stream), C.byref(t)))
+        return {f: getattr(t, f) for f, _ in t._fields_}
+
     def estimate_sigma_max(self, iters: int = 100, seed: int = 0) -> float:
         out = C.c_double()
         _lib.check(_lib.load().msot_estimate_norm(self._plan, int(iters), int(seed),

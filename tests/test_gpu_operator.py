@@ -176,3 +176,24 @@ def test_travel_times_on_gpu_match_oracle(cuda):
         ref = M.travel_time_indices(M.config1_probe(), M.config_grid(n), 1500.0, crop)
         assert tau.shape == ref.shape
         assert np.max(np.abs(tau - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+def test_autotune_keeps_results(cuda):
+    # the autotuner only picks among variants that differ in float summation
+    # order: the operator still matches the oracle, the solve its untuned self
+    import torch
+    from msot_gb300 import rec_nn_with_L2_reg
+    pm, om = make_pair(n=48, n_det=64, n_samples=1200, radius=0.02, fov_half=0.0063, norm=1.0,
+                       max_batch=8)
+    rng = np.random.default_rng(8)
+    x = rng.random((8, 48, 48))
+    b = torch.tensor(om.forward(x), dtype=torch.float32)
+    before = rec_nn_with_L2_reg(pm, b, 10, 1e-2)[0].cpu().numpy()
+    t = pm.autotune(8)
+    assert t["fwd_wt"] in (2, 4, 8) and t["conv_min_blocks"] in (1, 3, 4)
+    assert t["tv_cluster"] in (0, 1, 2, 4, 8, 16)
+    assert t["fwd_ms"] > 0 and t["transpose_ms"] > 0 and t["tv_prox_ms"] > 0
+    y = pm.forward(torch.tensor(x, dtype=torch.float32)).cpu().numpy()
+    assert rel(y, om.forward(x)) < 1e-5
+    after = rec_nn_with_L2_reg(pm, b, 10, 1e-2)[0].cpu().numpy()
+    assert rel(after, before) < 1e-5
