@@ -230,7 +230,8 @@ class MSOTmodel:
     use_single_speed_of_sound, num_cropped_samples_at_sinogram_start,
     filt_cutoff_min, filt_cutoff_max, model_normalization_factor)
     (MSOTmodel.m:18); dual speed of sound (use_single_speed_of_sound False)
-    takes the membrane and coupling speed from the probe.  SIR tables, when
+    takes the membrane and coupling speed from the probe.  cache_dir keeps
+    the travel-time tables on disk (msot_gb300.cache).  SIR tables, when
     include_sir, are given as ``sir_tables=(SPMR [NS, S], start_end [NS, 2]
     1-based, SPMRIndices [n_det, P] 1-based)``.  ``max_batch`` sizes the
     plan's scratch for batched applies and solves."""
@@ -239,7 +240,8 @@ class MSOTmodel:
                  include_sir: bool = False, use_single_speed_of_sound: bool = True,
                  num_cropped_samples_at_sinogram_start: int = 0, filt_cutoff_min: float = 1e5,
                  filt_cutoff_max: float = 12e6, model_normalization_factor: float | None = None,
-                 sir_tables=None, max_batch: int = 1, norm_iterations: int = 100):
+                 sir_tables=None, max_batch: int = 1, norm_iterations: int = 100,
+                 cache_dir: str | None = None):
         self.use_single_speed_of_sound = bool(use_single_speed_of_sound)
         if not self.use_single_speed_of_sound:
             if probe.membrane is None or probe.coupling_speed_of_sound is None:
@@ -256,14 +258,21 @@ class MSOTmodel:
         disc = discretization
         # travel-time indices (MSOTmodel.m:380-381; straight rays, refraction.m:327,
         # or refracted at the membrane), computed on the GPU in FP64
-        self.x_membrane_intersections = None
         if self.use_single_speed_of_sound:
-            self.travel = travel_times(probe, disc, self.c, self.n_crop)
+            compute = lambda: (travel_times(probe, disc, self.c, self.n_crop), None)
             c_ir = self.c
         else:
-            self.travel, self.x_membrane_intersections = travel_times_dual(
-                probe, disc, self.c, probe.coupling_speed_of_sound, probe.membrane, self.n_crop)
+            compute = lambda: travel_times_dual(probe, disc, self.c, probe.coupling_speed_of_sound,
+                                                probe.membrane, self.n_crop)
             c_ir = float(probe.coupling_speed_of_sound)  # MSOTmodel.m:331-335
+        if cache_dir:
+            # acoustic_file_<hash> of MSOTmodel.m:350-379
+            from . import cache
+            self.travel, self.x_membrane_intersections = cache.acoustic_tables(
+                cache_dir, probe, disc, self.c, self.n_crop, self.use_single_speed_of_sound,
+                compute)
+        else:
+            self.travel, self.x_membrane_intersections = compute()
         # interpolation radius (MSOTmodel.m:36-38)
         self.radius = float(disc.dz / (self.c / probe.fs))
         self.ir = np.ascontiguousarray(

@@ -42,13 +42,23 @@ def _spec(probe, disc, c, element, sub, half_window, virtual=None):
 
 
 def spmr_tables(probe, disc, c: float, element=(0.25e-3, 10e-3, 0.0), sub=(8, 8),
-                half_window: int = 45, virtual=None):
+                half_window: int = 45, virtual=None, cache_dir=None):
     """Returns (sir [NS][S], start_end [NS][2], sir_idx [n_det][P], info) in the
     layout MSOTmodel(include_sir=True, sir_tables=(sir, start_end, sir_idx))
     takes.  The half window grows (as calculate_polarSPMR.m:115-139 does) until
     every column's response fits.  With two speeds of sound pass c = the
     coupling medium's speed and virtual = (virt_x, virt_z) from
-    virtual_sources (MSOTmodel.m:579-596)."""
+    virtual_sources (MSOTmodel.m:579-596).  cache_dir keeps the tables on
+    disk keyed by every input (msot_gb300.cache)."""
+    if cache_dir:
+        from . import cache
+        xd, zd = probe.detector_positions()
+        fields = dict(detector_x=xd, detector_z=zd, x=disc.x, z=disc.z, c=c, fs=probe.fs,
+                      sigma=disc.sigma, element=element, sub=sub, half_window=half_window)
+        if virtual is not None:
+            fields.update(virt_x=np.ravel(virtual[0]), virt_z=np.ravel(virtual[1]))
+        return cache.spmr_tables(cache_dir, fields, lambda: spmr_tables(
+            probe, disc, c, element, sub, half_window, virtual))
     L = _lib.load()
     hw = int(half_window)
     while True:

@@ -197,3 +197,20 @@ def test_autotune_keeps_results(cuda):
     assert rel(y, om.forward(x)) < 1e-5
     after = rec_nn_with_L2_reg(pm, b, 10, 1e-2)[0].cpu().numpy()
     assert rel(after, before) < 1e-5
+
+
+def test_model_tables_from_disk_cache(cuda, tmp_path):
+    # a second model of the same geometry loads the travel-time table written
+    # by the first (acoustic_file_<key>.npz) and applies the same operator
+    import os
+    import torch
+    from msot_gb300 import Discretization, MSOTmodel, Probe
+    p = Probe(n_det=32, radius=0.02, n_samples=1200)
+    d = Discretization([-0.004, 0.004], 24)
+    m1 = MSOTmodel(p, d, 1500.0, model_normalization_factor=1.0, cache_dir=str(tmp_path))
+    files = os.listdir(tmp_path)
+    assert len(files) == 1 and files[0].startswith("acoustic_file_")
+    m2 = MSOTmodel(p, d, 1500.0, model_normalization_factor=1.0, cache_dir=str(tmp_path))
+    assert np.array_equal(m1.travel, m2.travel)
+    x = torch.rand((1, 24, 24))
+    assert torch.equal(m1.forward(x), m2.forward(x))

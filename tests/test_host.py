@@ -116,3 +116,43 @@ def test_butterworth_window_matches_oracle():
     T = 2030
     got = butter_response(2, "bandpass", (300 / T, (T - 200) / T), T)
     assert np.max(np.abs(got - Q.butter_window(T, 2, 300, T - 200))) <= 1e-10
+
+
+def test_table_cache_round_trip_and_collision(tmp_path):
+    # the acoustic-table cache (MSOTmodel.m:289-308, 350-379): stored on the
+    # first call, loaded (without computing) on the second, a file written for
+    # other fields is a hash collision
+    from msot_gb300 import Discretization, Probe
+    from msot_gb300 import cache
+    probe = Probe(n_det=8)
+    disc = Discretization([-0.003, 0.003], 6)
+    calls = []
+
+    def compute():
+        calls.append(1)
+        return np.arange(8 * 36, dtype=np.float64).reshape(8, 36), None
+
+    t1, x1 = cache.acoustic_tables(str(tmp_path), probe, disc, 1500.0, 0, True, compute)
+    t2, x2 = cache.acoustic_tables(str(tmp_path), probe, disc, 1500.0, 0, True, compute)
+    assert len(calls) == 1 and np.array_equal(t1, t2) and x2 is None
+    # a different speed of sound is another key (no collision, computed again)
+    cache.acoustic_tables(str(tmp_path), probe, disc, 1510.0, 0, True, compute)
+    assert len(calls) == 2
+    # tamper with a stored field: loading reports the collision
+    import glob
+    f = sorted(glob.glob(str(tmp_path / "acoustic_file_*.npz")))[0]
+    with np.load(f) as z:
+        data = {k: z[k] for k in z.files}
+    data["field_region_x"] = data["field_region_x"] + 1.0
+    np.savez(f, **data)
+    with pytest.raises(RuntimeError, match="collision"):
+        for c in (1500.0, 1510.0):
+            cache.acoustic_tables(str(tmp_path), probe, disc, c, 0, True, compute)
+    # SPMR tables: exact-match reuse
+    spec = dict(c=1500.0, sub=(8, 8))
+    mk = lambda: (np.ones((3, 5)), np.ones((3, 2), np.int32), np.ones((8, 36), np.int32),
+                  dict(d_min=0.01, d_step=1e-4, a_step_deg=0.1, n_dist=3, n_angle=1,
+                       half_window=45))
+    a = cache.spmr_tables(str(tmp_path), spec, mk)
+    b = cache.spmr_tables(str(tmp_path), spec, lambda: 1 / 0)
+    assert np.array_equal(a[0], b[0]) and b[3]["half_window"] == 45 and b[3]["n_dist"] == 3
