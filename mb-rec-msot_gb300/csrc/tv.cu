@@ -1413,6 +1413,39 @@ int msot_itv(const float *d_x, double *itv, int batch, int n, void *stream) {
     return MSOT_OK;
 }
 
+}  // extern "C"
+
+namespace {
+// a non-blocking stream that starts after the work queued on `user` and
+// makes `user` wait for everything queued on it when it closes
+struct TvStream {
+    cudaStream_t s = nullptr, user = nullptr;
+    cudaEvent_t ev = nullptr;
+    int open(cudaStream_t u) {
+        user = u;
+        if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+            set_error("rec_nn_with_TV_reg: stream creation failed");
+            return MSOT_ECUDA;
+        }
+        cudaEventRecord(ev, user);
+        cudaStreamWaitEvent(s, ev, 0);
+        return MSOT_OK;
+    }
+    ~TvStream() {
+        if (s) {
+            cudaEventRecord(ev, s);
+            cudaStreamWaitEvent(user, ev, 0);
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+        if (ev) cudaEventDestroy(ev);
+    }
+};
+}  // namespace
+
+extern "C" {
+
 int msot_rec_nn_with_TV_reg(msot_plan_t plan, const float *d_b, float *d_rec, int batch,
                             int num_iter, double reg, int sparsa_iter, const float *d_x0,
                             int coupled, double *err_img, double *err_reg, void *stream) {
@@ -1452,46 +1485,96 @@ int msot_rec_nn_with_TV_reg(msot_plan_t plan, const float *d_b, float *d_rec, in
     int rc = MSOT_OK;
 #define TV_CK(expr)                                                                        \
     if ((rc = (expr)) != MSOT_OK) return rc
-    if (d_x0)
-        MSOT_CUDA_TRY(cudaMemcpyAsync(wv, d_x0, NI * sizeof(float), cudaMemcpyDeviceToDevice, st));
-    else
-        MSOT_CUDA_TRY(cudaMemsetAsync(wv, 0, NI * sizeof(float), st));
-    MSOT_CUDA_TRY(cudaMemsetAsync(vm, 0, NI * sizeof(float), st));
-    for (int outer = 0; outer < num_iter; ++outer) {
-        KLAUNCH(k_tv_begin<<<grid, TV_RED, 0, st>>>(wv, vm, x, ri, N, sb, W, part));
+    // One outer iteration is a fixed launch sequence with device-side scalars
+    // (no host synchronisation): the first runs eagerly (kernel attributes),
+    // the next is captured once as a CUDA graph on a private stream and
+    // replayed for the remaining iterations.
+    auto outer_step = [&](cudaStream_t s) -> int {
+        int r;
+        KLAUNCH(k_tv_begin<<<grid, TV_RED, 0, s>>>(wv, vm, x, ri, N, sb, W, part));
         MSOT_LAUNCH_CHECK();
-        TV_CK(apply_forward(pl, x, As, W, st));
-        KLAUNCH(k_tv_rs0<<<grid, TV_RED, 0, st>>>(d_b, As, rs, ns, sl, W, part));
-        KLAUNCH(k_tv_scalar<<<1, 64, 0, st>>>(0, part, G, W, coupled, reg, 1.0, TV_BETA, 1e-8, sv));
+        if ((r = apply_forward(pl, x, As, W, s))) return r;
+        KLAUNCH(k_tv_rs0<<<grid, TV_RED, 0, s>>>(d_b, As, rs, ns, sl, W, part));
+        KLAUNCH(k_tv_scalar<<<1, 64, 0, s>>>(0, part, G, W, coupled, reg, 1.0, TV_BETA, 1e-8, sv));
         MSOT_LAUNCH_CHECK();
         for (int k = 0; k < sparsa_iter; ++k) {
-            TV_CK(apply_transpose(pl, rs, atr, W, st));
-            KLAUNCH(k_tv_z<<<grid, TV_RED, 0, st>>>(x, atr, ri, sv, coupled, z, P, sl, sb));
-            TV_CK(tv_prox(z, sv, 0.0, coupled, xn, work, W, N, st, pl.tune_tv_cluster));
-            KLAUNCH(k_tv_step<<<grid, TV_RED, 0, st>>>(x, xn, ri, dx, sv, coupled, N, sb, W, part));
+            if ((r = apply_transpose(pl, rs, atr, W, s))) return r;
+            KLAUNCH(k_tv_z<<<grid, TV_RED, 0, s>>>(x, atr, ri, sv, coupled, z, P, sl, sb));
+            if ((r = tv_prox(z, sv, 0.0, coupled, xn, work, W, N, s, pl.tune_tv_cluster)))
+                return r;
+            KLAUNCH(k_tv_step<<<grid, TV_RED, 0, s>>>(x, xn, ri, dx, sv, coupled, N, sb, W, part));
             MSOT_LAUNCH_CHECK();
-            TV_CK(apply_forward(pl, dx, As, W, st));
-            KLAUNCH(k_tv_rs<<<grid, TV_RED, 0, st>>>(rs, As, ns, sl, W, part));
-            KLAUNCH(k_tv_scalar<<<1, 64, 0, st>>>(1, part, G, W, coupled, reg, 1.0, TV_BETA, 1e-8, sv));
+            if ((r = apply_forward(pl, dx, As, W, s))) return r;
+            KLAUNCH(k_tv_rs<<<grid, TV_RED, 0, s>>>(rs, As, ns, sl, W, part));
+            KLAUNCH(k_tv_scalar<<<1, 64, 0, s>>>(1, part, G, W, coupled, reg, 1.0, TV_BETA, 1e-8,
+                                                 sv));
             MSOT_LAUNCH_CHECK();
         }
-        KLAUNCH(k_tv_outer<<<go, 256, 0, st>>>(x, wv, vm, NI));
+        KLAUNCH(k_tv_outer<<<go, 256, 0, s>>>(x, wv, vm, NI));
         MSOT_LAUNCH_CHECK();
+        return MSOT_OK;
+    };
+    TvStream ps;  // private capturable stream, ordered after the caller's work
+    if ((rc = ps.open(st))) return rc;
+    const cudaStream_t cs = ps.s;
+    if (d_x0)
+        MSOT_CUDA_TRY(cudaMemcpyAsync(wv, d_x0, NI * sizeof(float), cudaMemcpyDeviceToDevice, cs));
+    else
+        MSOT_CUDA_TRY(cudaMemsetAsync(wv, 0, NI * sizeof(float), cs));
+    MSOT_CUDA_TRY(cudaMemsetAsync(vm, 0, NI * sizeof(float), cs));
+    int outer = 0;
+    if (num_iter > 0) {
+        TV_CK(outer_step(cs));
+        ++outer;
     }
-    MSOT_CUDA_TRY(cudaMemcpyAsync(d_rec, wv, NI * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    if (num_iter > 1 && !profiling_enabled()) {
+        cudaGraph_t g = nullptr;
+        MSOT_CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed));
+        const long before = g_launch_count.load();
+        rc = outer_step(cs);
+        const long captured = g_launch_count.load() - before;
+        g_launch_count -= captured;  // counted per replay below
+        cudaError_t ce = cudaStreamEndCapture(cs, &g);
+        if (rc == MSOT_OK && ce != cudaSuccess) {
+            set_error("rec_nn_with_TV_reg: graph capture failed: %s", cudaGetErrorString(ce));
+            rc = MSOT_ECUDA;
+        }
+        cudaGraphExec_t ge = nullptr;
+        if (rc == MSOT_OK) {
+            ce = cudaGraphInstantiate(&ge, g, 0);
+            if (ce != cudaSuccess) {
+                set_error("rec_nn_with_TV_reg: graph instantiation failed: %s",
+                          cudaGetErrorString(ce));
+                rc = MSOT_ECUDA;
+            }
+        }
+        if (g) cudaGraphDestroy(g);
+        for (; rc == MSOT_OK && outer < num_iter; ++outer) {
+            ce = cudaGraphLaunch(ge, cs);
+            if (ce != cudaSuccess) {
+                set_error("rec_nn_with_TV_reg: graph launch failed: %s", cudaGetErrorString(ce));
+                rc = MSOT_ECUDA;
+            }
+            g_launch_count += captured;
+        }
+        if (ge) cudaGraphExecDestroy(ge);
+        if (rc) return rc;
+    }
+    for (; outer < num_iter; ++outer) TV_CK(outer_step(cs));
+    MSOT_CUDA_TRY(cudaMemcpyAsync(d_rec, wv, NI * sizeof(float), cudaMemcpyDeviceToDevice, cs));
     if (err_img || err_reg) {
         std::vector<double> h;
         if (err_img) {
-            TV_CK(apply_forward(pl, wv, As, W, st));
-            TV_CK(tv_sums(As, d_b, ns, 0, W, part, dout, h, st));
+            TV_CK(apply_forward(pl, wv, As, W, cs));
+            TV_CK(tv_sums(As, d_b, ns, 0, W, part, dout, h, cs));
             for (int w = 0; w < W; ++w) err_img[w] = h[w];
         }
         if (err_reg) {
-            TV_CK(tv_sums(wv, nullptr, P, N, W, part, dout, h, st));
+            TV_CK(tv_sums(wv, nullptr, P, N, W, part, dout, h, cs));
             for (int w = 0; w < W; ++w) err_reg[w] = h[w];
         }
     }
-    MSOT_CUDA_TRY(cudaStreamSynchronize(st));
+    MSOT_CUDA_TRY(cudaStreamSynchronize(cs));
 #undef TV_CK
     return MSOT_OK;
 }
