@@ -355,6 +355,8 @@ int msot_autotune(msot_plan_t plan, int batch, void *stream, msot_tuning *out);
  * float summation order):
  *   "tv_prox_cluster"  CTAs per image of the shared-memory SB_ITV2 kernel
  *                      (1, 2, 4, 8, 16; 0 = automatic).
+ *   "adj_prefetch"     1 (default) = the DAS adjoint loads the next detector's
+ *                      samples into registers during the current one; 0 = off.
  *   "conv_min_blocks"  register cap of the IR convolution, as resident CTAs
  *                      per SM: 3 (default), 4, or 1 (uncapped).
  *   "unet_tensor_cores" 1 (default) = U-Net 3x3 convolutions on the tensor

@@ -97,6 +97,8 @@ const char *set_error(const char *fmt, ...);
 extern std::atomic<int> g_unet_tc;
 // register cap (minimum resident CTAs per SM) of the IR convolution; operator.cu
 extern std::atomic<int> g_conv_min_blocks;
+// next-detector register prefetch of the DAS adjoint on (1) or off (0); operator.cu
+extern std::atomic<int> g_adj_prefetch;
 
 // launch counter (every kernel launch of the library goes through KLAUNCH)
 extern std::atomic<long long> g_launch_count;

@@ -315,8 +315,12 @@ __global__ void __launch_bounds__(256) k_das_fwd3(const int32_t *__restrict__ of
 // window), and every thread adds U + f V + e1 s[b-F] + e2 s[b+F+1] to its 16
 // pixels.  Groups write partial images; k_sum_parts adds them in fixed order.
 constexpr int ADJ_BPT = 4;  // buckets per thread when building Q
+std::atomic<int> g_adj_prefetch{1};  // next-detector prefetch in k_das_adj4 (msot_tune_set)
 
-template <int WT, int F>
+// PF > 0: the segment of the next detector is loaded into registers (PF
+// samples per instance per thread; needs SL <= PF * BLK_THREADS) while the
+// current one is filtered and gathered.
+template <int WT, int F, int PF = 0>
 __global__ void __launch_bounds__(BLK_THREADS, 3) k_das_adj4(
     const int32_t *__restrict__ btau, const int2 *__restrict__ bspan,
     const float *__restrict__ s, float *__restrict__ part, int nx, int nz, int nbx, int D,
@@ -337,19 +341,52 @@ __global__ void __launch_bounds__(BLK_THREADS, 3) k_das_adj4(
 #pragma unroll
         for (int i = 0; i < WT; ++i) acc[k][i] = 0.f;
     const int d_begin = grp * det_per_group, d_end = min(D, d_begin + det_per_group);
+    float pre[PF > 0 ? WT : 1][PF > 0 ? PF : 1];
+    auto fetch = [&](int d) {
+        const int2 sq = __ldg(bspan + (size_t)blk * D + d);
+        const int nq = sq.y - sq.x + 1;
+        const int Lq = nq > 0 ? ((nq + ADJ_BPT - 1) / ADJ_BPT) * ADJ_BPT + 2 * F + 2 : 0;
+#pragma unroll
+        for (int w = 0; w < WT; ++w) {
+            const float *src = s + ((size_t)(w0 + w) * D + d) * T;
+#pragma unroll
+            for (int j = 0; j < PF; ++j) {
+                const int k = t + j * BLK_THREADS, tt = sq.x - F + k;
+                pre[w][j] = (k < Lq && tt >= 0 && tt < T) ? __ldg(src + tt) : 0.f;
+            }
+        }
+    };
+    if constexpr (PF > 0)
+        if (d_begin < d_end) fetch(d_begin);
     for (int d = d_begin; d < d_end; ++d) {
         const int2 sp = __ldg(bspan + (size_t)blk * D + d);
         const int nb = sp.y - sp.x + 1;
-        if (nb <= 0) continue;  // block outside the grid: uniform across the CTA
+        if (nb <= 0) {  // block outside the grid: uniform across the CTA
+            if constexpr (PF > 0)
+                if (d + 1 < d_end) fetch(d + 1);
+            continue;
+        }
         const int L = ((nb + ADJ_BPT - 1) / ADJ_BPT) * ADJ_BPT + 2 * F + 2;
-        for (int w = 0; w < WT; ++w) {
-            const float *src = s + ((size_t)(w0 + w) * D + d) * T;
-            for (int k = t; k < L; k += BLK_THREADS) {
-                const int tt = sp.x - F + k;
-                seg[w * SL + k] = (tt >= 0 && tt < T) ? __ldg(src + tt) : 0.f;
+        if constexpr (PF > 0) {
+#pragma unroll
+            for (int w = 0; w < WT; ++w)
+#pragma unroll
+                for (int j = 0; j < PF; ++j) {
+                    const int k = t + j * BLK_THREADS;
+                    if (k < L) seg[w * SL + k] = pre[w][j];
+                }
+        } else {
+            for (int w = 0; w < WT; ++w) {
+                const float *src = s + ((size_t)(w0 + w) * D + d) * T;
+                for (int k = t; k < L; k += BLK_THREADS) {
+                    const int tt = sp.x - F + k;
+                    seg[w * SL + k] = (tt >= 0 && tt < T) ? __ldg(src + tt) : 0.f;
+                }
             }
         }
         __syncthreads();
+        if constexpr (PF > 0)
+            if (d + 1 < d_end) fetch(d + 1);  // in flight during the filter and the gather
         // one bucket per thread: consecutive threads read consecutive samples
         for (int i = t; i < WT * nb; i += BLK_THREADS) {
             const int w = i / nb, bl = i - w * nb;
@@ -1012,7 +1049,6 @@ static int das_adj_launch(const Plan &pl, const float *raw, float *x, int W, flo
     const size_t smem = (size_t)((WT * SL + 3) & ~3) * sizeof(float) +
                         (size_t)WT * pl.blk_span_max * sizeof(float4);
     int rc;
-    if ((rc = set_smem(k_das_adj4<WT, F>, smem)) != MSOT_OK) return rc;
     const int base = pl.n_blk * (W / WT);
     int groups = std::max(1, std::min(pl.D, div_up(2 * 152, base)));
     groups = std::min(groups, std::max(1, pl.adj_groups_max * pl.max_batch / W));
@@ -1021,9 +1057,21 @@ static int das_adj_launch(const Plan &pl, const float *raw, float *x, int W, flo
     groups = div_up(pl.D, dpg);
     const size_t stride = (size_t)W * pl.P;
     dim3 grid(pl.n_blk, W / WT, groups);
-    KLAUNCH(k_das_adj4<WT, F><<<grid, BLK_THREADS, smem, st>>>(
-        pl.blk_tau, pl.blk_span, raw, pl.scr_part, pl.nx, pl.nz, pl.n_blk_x, pl.D, pl.T,
-        pl.frac_bits, pl.inv_r, pl.ce1, pl.ce2, pl.blk_span_max, dpg, stride));
+#define ADJ4_LAUNCH(PFV)                                                                   \
+    do {                                                                                   \
+        if ((rc = set_smem(k_das_adj4<WT, F, PFV>, smem)) != MSOT_OK) return rc;           \
+        KLAUNCH(k_das_adj4<WT, F, PFV><<<grid, BLK_THREADS, smem, st>>>(                   \
+            pl.blk_tau, pl.blk_span, raw, pl.scr_part, pl.nx, pl.nz, pl.n_blk_x, pl.D, pl.T, \
+            pl.frac_bits, pl.inv_r, pl.ce1, pl.ce2, pl.blk_span_max, dpg, stride));        \
+    } while (0)
+    // next-detector prefetch when the segment fits PF registers per instance
+    if (g_adj_prefetch.load() && SL <= 2 * BLK_THREADS)
+        ADJ4_LAUNCH(2);
+    else if (g_adj_prefetch.load() && SL <= 4 * BLK_THREADS)
+        ADJ4_LAUNCH(4);
+    else
+        ADJ4_LAUNCH(0);
+#undef ADJ4_LAUNCH
     MSOT_LAUNCH_CHECK();
     KLAUNCH(k_sum_parts<<<(unsigned)std::min<size_t>(4096, div_up((int)stride, 256)), 256, 0,
                           st>>>(pl.scr_part, x, stride, groups, stride, scale));

@@ -1366,6 +1366,10 @@ int msot_tv_prox_stats(long long *sweeps, long long *cg_steps) {
 }
 
 int msot_tune_set(const char *key, int value) {
+    if (key && std::strcmp(key, "adj_prefetch") == 0 && (value == 0 || value == 1)) {
+        msot::g_adj_prefetch.store(value);
+        return MSOT_OK;
+    }
     if (key && std::strcmp(key, "conv_min_blocks") == 0 &&
         (value == 1 || value == 3 || value == 4)) {
         msot::g_conv_min_blocks.store(value);

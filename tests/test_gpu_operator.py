@@ -206,11 +206,11 @@ def test_model_tables_from_disk_cache(cuda, tmp_path):
     import torch
     from msot_gb300 import Discretization, MSOTmodel, Probe
     p = Probe(n_det=32, radius=0.02, n_samples=1200)
-    d = Discretization([-0.004, 0.004], 24)
+    d = Discretization([-0.004, 0.004], 32)
     m1 = MSOTmodel(p, d, 1500.0, model_normalization_factor=1.0, cache_dir=str(tmp_path))
     files = os.listdir(tmp_path)
     assert len(files) == 1 and files[0].startswith("acoustic_file_")
     m2 = MSOTmodel(p, d, 1500.0, model_normalization_factor=1.0, cache_dir=str(tmp_path))
     assert np.array_equal(m1.travel, m2.travel)
-    x = torch.rand((1, 24, 24))
+    x = torch.rand((1, 32, 32))
     assert torch.equal(m1.forward(x), m2.forward(x))
