@@ -339,8 +339,9 @@ int msot_butter_response(int order, int type, double wn1, double wn2, int n, int
 
 /* Autotuner (no reference counterpart): times the variants of the plan's
  * hot kernels on its own geometry at `batch` instances -- instances per CTA
- * of the DAS forward (8, 4, 2), the register cap of the IR convolution (1, 3,
- * 4 resident CTAs per SM) and, for square grids, the CTAs per image of the
+ * of the DAS forward (8, 4, 2) and adjoint (2, 1), the register cap of the
+ * IR convolution (1, 3, 4 resident CTAs per SM) and, for square grids, the
+ * CTAs per image of the
  * SB_ITV2 cluster kernel (automatic, 1 .. 16) -- and keeps the fastest in
  * the plan (they change results only in float summation order).  Drops the
  * plan's captured solver graphs.  Not concurrent with other calls on the
@@ -348,6 +349,7 @@ int msot_butter_response(int order, int type, double wn1, double wn2, int n, int
 typedef struct msot_tuning {
     int fwd_wt, conv_min_blocks, tv_cluster;  /* 0 = the built-in choice */
     double fwd_ms, transpose_ms, tv_prox_ms;  /* per apply of the chosen variant */
+    int adj_wt;                               /* instances per CTA of the DAS adjoint */
 } msot_tuning;
 int msot_autotune(msot_plan_t plan, int batch, void *stream, msot_tuning *out);
 

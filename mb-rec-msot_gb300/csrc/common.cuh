@@ -62,6 +62,7 @@ struct Plan {
     struct SolverCache *solver = nullptr;  // solver workspace and captured CUDA graphs
     // variants chosen by msot_autotune for this plan (0 = the built-in choice)
     int tune_fwd_wt = 0;      // instances per CTA of the DAS forward (8, 4, 2)
+    int tune_adj_wt = 0;      // instances per CTA of the DAS adjoint (2, 1)
     int tune_conv_mb = 0;     // register cap of the IR convolution (1, 3, 4)
     int tune_tv_cluster = 0;  // CTAs per image of the SB_ITV2 cluster kernel
     // IR

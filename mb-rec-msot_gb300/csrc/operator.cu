@@ -1102,7 +1102,8 @@ static int das_adj_f(const Plan &pl, const float *raw, float *x, int W, float sc
 int launch_das_adjoint(const Plan &pl, const float *raw, float *x, int W, float scale,
                        cudaStream_t st) {
     TimedScope ts_(KID_INTERP_ADJ, st);
-    const int wt = pick_wt(W, 1, 2);
+    int wt = pick_wt(W, 1, 2);
+    if (pl.tune_adj_wt && W % pl.tune_adj_wt == 0) wt = pl.tune_adj_wt;
     if (wt == 2) return das_adj_f<2>(pl, raw, x, W, scale, st);
     return das_adj_f<1>(pl, raw, x, W, scale, st);
 }

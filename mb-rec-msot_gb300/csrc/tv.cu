@@ -1667,6 +1667,22 @@ extern "C" int msot_autotune(msot_plan_t plan, int batch, void *stream, msot_tun
         res.fwd_wt = pick;
         res.fwd_ms = pick ? best : 0.0;
     }
+    // DAS adjoint: instances per CTA (apply_transpose)
+    {
+        double best = 1e30;
+        int pick = 0;
+        for (int wt : {2, 1}) {
+            if (batch % wt) continue;
+            pl.tune_adj_wt = wt;
+            double ms;
+            if ((rc = tune_time(st, 3, ms,
+                                [&] { return apply_transpose(pl, sino, img2, batch, st); })))
+                return rc;
+            if (ms < best) best = ms, pick = wt;
+        }
+        pl.tune_adj_wt = pick;
+        res.adj_wt = pick;
+    }
     // IR convolution register cap (apply_transpose: conv, adjoint, prefilter)
     {
         double best = 1e30;

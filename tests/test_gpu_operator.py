@@ -191,6 +191,7 @@ def test_autotune_keeps_results(cuda):
     before = rec_nn_with_L2_reg(pm, b, 10, 1e-2)[0].cpu().numpy()
     t = pm.autotune(8)
     assert t["fwd_wt"] in (2, 4, 8) and t["conv_min_blocks"] in (1, 3, 4)
+    assert t["adj_wt"] in (1, 2)
     assert t["tv_cluster"] in (0, 1, 2, 4, 8, 16)
     assert t["fwd_ms"] > 0 and t["transpose_ms"] > 0 and t["tv_prox_ms"] > 0
     y = pm.forward(torch.tensor(x, dtype=torch.float32)).cpu().numpy()
