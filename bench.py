@@ -342,6 +342,18 @@ def run_ours(args, rank, world):
                 "peak_source": f"{peak_kind} hbm_gbs (copy)",
                 "avg_launch_us": avg_s * 1e6, "bytes_per_launch": alg,
                 "families_ms_per_solve": {k: round(v["ms"], 3) for k, v in fam.items()}}
+        if name == "interp_forward":
+            # the forward's real bound: every (pixel, detector) pair gathers the
+            # W values of its pixel from L2 (P D W 4 bytes per launch), against
+            # the measured random 32-byte-sector gather rate of an L2-resident
+            # buffer (msot_l2_gather_probe, 64 MiB)
+            g = C.c_double()
+            L.msot_l2_gather_probe(64 << 20, C.byref(g))
+            gather = 4.0 * N_GRID * N_GRID * N_DET * B
+            roof["l2_gather"] = {"achieved": gather / avg_s / 1e9, "peak": g.value,
+                                 "unit": "GB/s", "frac": gather / avg_s / 1e9 / g.value,
+                                 "bytes_per_launch": gather,
+                                 "peak_source": "measured: msot_l2_gather_probe, 64 MiB"}
     # --- FP64 oracle: accuracy of instance 0 + the CPU baseline sample ----------------
     acc = None
     cpu = None

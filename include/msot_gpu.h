@@ -375,6 +375,10 @@ int msot_tv_prox_stats(long long *sweeps, long long *cg_steps);
 long long msot_launch_count(void);
 /* on != 0: record a CUDA event pair around every launch of the hot kernel
  * families (reset on each call); 0 disables. */
+/* Throughput (GB/s) of random 32-byte-sector loads from a device buffer of
+ * buffer_bytes (1 .. 96 MiB) that stays resident in L2: the ceiling of the
+ * DAS interpolation kernels, whose gathers L2 serves.  Synchronous. */
+int msot_l2_gather_probe(size_t buffer_bytes, double *gbs);
 int msot_profile_enable(int on);
 /* Name of kernel family `kid` (0..6), NULL past the end. */
 const char *msot_profile_kernel_name(int kid);

@@ -220,7 +220,7 @@ __global__ void k_permute(const float *__restrict__ in, float *__restrict__ out,
 constexpr int FWD_UNR = 2;
 
 template <int WT, int F>
-__global__ void __launch_bounds__(256) k_das_fwd3(const int32_t *__restrict__ off,
+__global__ void __launch_bounds__(256, 4) k_das_fwd3(const int32_t *__restrict__ off,
                                                   const int2 *__restrict__ ent,
                                                   const float *__restrict__ xpm,
                                                   float *__restrict__ raw, int P, int D, int T,
@@ -233,6 +233,20 @@ __global__ void __launch_bounds__(256) k_das_fwd3(const int32_t *__restrict__ of
     const int t0 = blockIdx.x * TB;
     const int b_lo = t0 - F - 1;
     {
+        // no pixel of this detector falls in the CTA's buckets (outside its
+        // travel-time span): every output of the tile is zero
+        const int32_t *o = off + (size_t)d * (T + 1);
+        const int bl = max(b_lo, 0), bh = min(b_lo + NB, T);
+        if (bl >= bh || __ldg(o + bl) == __ldg(o + bh)) {
+            const int t = t0 + (int)threadIdx.x;
+            if ((int)threadIdx.x < TB && t < T) {
+#pragma unroll
+                for (int i = 0; i < WT; ++i) raw[((size_t)(w0 + i) * D + d) * T + t] = 0.f;
+            }
+            return;
+        }
+    }
+    {
         float m0[WT], m1[WT], m2[WT], m3[WT];
 #pragma unroll
         for (int i = 0; i < WT; ++i) m0[i] = m1[i] = m2[i] = m3[i] = 0.f;
@@ -243,12 +257,17 @@ __global__ void __launch_bounds__(256) k_das_fwd3(const int32_t *__restrict__ of
             const int2 *e = ent + (size_t)d * P;
             const int mask = (1 << fb) - 1;
             const float step = __int_as_float((127 - fb) << 23);  // 2^-fb
+            // the entries of the next group load while this group's gathers
+            // are in flight (one dependent latency per group, not two)
+            int2 qn[FWD_UNR];
+#pragma unroll
+            for (int u = 0; u < FWD_UNR; ++u)
+                qn[u] = j0 + u < j1 ? __ldg(e + j0 + u) : make_int2(0, -1);
             for (int j = j0; j < j1; j += FWD_UNR) {
                 int2 q[FWD_UNR];
                 float xv[FWD_UNR][WT];
 #pragma unroll
-                for (int u = 0; u < FWD_UNR; ++u)
-                    q[u] = j + u < j1 ? __ldg(e + j + u) : make_int2(0, -1);
+                for (int u = 0; u < FWD_UNR; ++u) q[u] = qn[u];
 #pragma unroll
                 for (int u = 0; u < FWD_UNR; ++u) {
                     const float *xp = xpm + (size_t)max(q[u].y, 0) * W + w0;
@@ -263,6 +282,9 @@ __global__ void __launch_bounds__(256) k_das_fwd3(const int32_t *__restrict__ of
                         for (int i = 0; i < WT; ++i) xv[u][i] = __ldg(xp + i);
                     }
                 }
+#pragma unroll
+                for (int u = 0; u < FWD_UNR; ++u)
+                    qn[u] = j + FWD_UNR + u < j1 ? __ldg(e + j + FWD_UNR + u) : make_int2(0, -1);
 #pragma unroll
                 for (int u = 0; u < FWD_UNR; ++u) {
                     if (q[u].y < 0) break;

@@ -100,3 +100,75 @@ int msot_profile_read(int kid, int *launches, double *total_ms) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// L2 gather probe: throughput of random 32-byte-sector loads from a buffer
+// that stays resident in L2 -- the ceiling of the DAS kernels, whose image
+// and sinogram gathers are served by L2, not HBM.
+// ---------------------------------------------------------------------------
+namespace msot {
+
+__global__ void k_l2_gather_probe(const float4 *__restrict__ buf, unsigned n_sectors, int iters,
+                                  unsigned seed, float *sink) {
+    unsigned h = seed ^ ((blockIdx.x * blockDim.x + threadIdx.x) * 2654435761u);
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int i = 0; i < iters; ++i) {
+        h = h * 1664525u + 1013904223u;
+        const unsigned s = h % n_sectors;
+        const float4 a = __ldg(buf + 2 * (size_t)s), b = __ldg(buf + 2 * (size_t)s + 1);
+        acc.x += a.x + b.x;
+        acc.y += a.y + b.y;
+        acc.z += a.z + b.z;
+        acc.w += a.w + b.w;
+    }
+    if (acc.x + acc.y + acc.z + acc.w == 1234.5f) sink[0] = acc.x;  // keeps the loads
+}
+
+}  // namespace msot
+
+extern "C" int msot_l2_gather_probe(size_t buffer_bytes, double *gbs) {
+    using namespace msot;
+    if (!gbs || buffer_bytes < 1024 * 1024 || buffer_bytes > (size_t)96 * 1024 * 1024) {
+        set_error("l2_gather_probe: buffer of 1 .. 96 MiB");
+        return MSOT_EINVAL;
+    }
+    float4 *buf = nullptr;
+    float *sink = nullptr;
+    MSOT_CUDA_TRY(cudaMalloc(&buf, buffer_bytes));
+    if (cudaMalloc(&sink, sizeof(float)) != cudaSuccess) {
+        cudaFree(buf);
+        set_error("l2_gather_probe: allocation failed");
+        return MSOT_ENOMEM;
+    }
+    const unsigned n_sectors = (unsigned)(buffer_bytes / 32);
+    cudaMemset(buf, 0, buffer_bytes);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const dim3 grid((unsigned)sms * 16), block(256);
+    const int iters = 64;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    for (int w = 0; w < 3; ++w)  // warm-up: brings the buffer into L2
+        KLAUNCH(k_l2_gather_probe<<<grid, block>>>(buf, n_sectors, iters, 7u + w, sink));
+    cudaEventRecord(a);
+    const int reps = 20;
+    for (int r = 0; r < reps; ++r)
+        KLAUNCH(k_l2_gather_probe<<<grid, block>>>(buf, n_sectors, iters, 100u + r, sink));
+    cudaEventRecord(b);
+    cudaError_t e = cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(buf);
+    cudaFree(sink);
+    if (e != cudaSuccess) {
+        set_error("l2_gather_probe: %s", cudaGetErrorString(e));
+        return MSOT_ECUDA;
+    }
+    const double bytes = (double)grid.x * block.x * iters * 32.0 * reps;
+    *gbs = bytes / (ms * 1e-3) / 1e9;
+    return MSOT_OK;
+}

@@ -123,6 +123,7 @@ SIGNATURES = {
     "msot_rec_nn_with_L2_reg_2": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_double,
                                             C.c_double, _vp, C.c_int, _dp, _dp, _dp, _vp]),
     "msot_laplacian_per_wavelength": (C.c_int, [_vp, _vp, C.c_int, C.c_int, C.c_int, _vp]),
+    "msot_l2_gather_probe": (C.c_int, [C.c_size_t, _dp]),
     "msot_autotune": (C.c_int, [_vp, C.c_int, _vp, C.POINTER(Tuning)]),
     "msot_prep_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                    C.c_double, C.c_double, C.c_int, C.POINTER(_vp)]),
