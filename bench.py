@@ -210,10 +210,10 @@ def oracle_solve(model, b_np, threads):
 
 # DRAM bytes (read + write) per launch of each family's kernel at batch 64,
 # from one ncu --set full capture of `bench.py --op --batch 64`
-NCU_TRAFFIC_B64 = {"interp_forward": 49.811712e6 + 85.703936e6,
-                   "interp_adjoint": 77.512192e6 + 3.013888e6,
-                   "ir_conv": 133.145344e6 + 84.419328e6,
-                   "prefilter": 4.203008e6}
+NCU_TRAFFIC_B64 = {"interp_forward": 47.80288e6 + 84.551168e6,
+                   "interp_adjoint": 77.48736e6 + 2.382336e6,
+                   "ir_conv": 133.204992e6 + 85.45408e6,
+                   "prefilter": 4.246784e6}
 
 
 def algorithmic_bytes(kid_name, batch):
