@@ -68,6 +68,8 @@ def parse():
     ap.add_argument("--ws-train-steps", type=int, default=3000)
     ap.add_argument("--ws-frames", type=int, default=256)
     ap.add_argument("--ws-input-iters", type=int, default=10)
+    ap.add_argument("--ws-backprojection", default="transpose", choices=["transpose", "waveeq"],
+                    help="network input when --ws-input-iters is 0")
     ap.add_argument("--unet", action="store_true",
                     help="warm-start U-Net alone (4 levels, 32 base channels, batch 16): "
                          "training steps and forward passes: one JSON line")
@@ -742,7 +744,7 @@ def run_warmstart(args):
     model = MSOTmodel(probe, Discretization([-h, h], n), 1500.0, False, True, 0, 1e5, 12e6, None,
                       max_batch=64)
     ws = LearnedWarmStart(model, LAMBDA, levels=4, base_channels=32, max_batch=16,
-                          input_iters=args.ws_input_iters)
+                          input_iters=args.ws_input_iters, backprojection=args.ws_backprojection)
     L = _lib.load()
     imgs = phantom_batch(model.Discretization, P + F, seed=11)
     (f, t, b), pair_ms = _event_ms(lambda: ws.make_pairs(imgs, 200, seed=12))
@@ -803,7 +805,11 @@ def run_warmstart(args):
         "config": {"workload": f"learned warm start, {n}x{n} px, {F} frames, 256-el arc, "
                                f"2030 samples, lambdaL2={LAMBDA}",
                    "grid": [n, n], "frames": F, "train_pairs": P,
-                   "input_iterations": args.ws_input_iters, "target_iterations": 200},
+                   "input_iterations": args.ws_input_iters,
+                   "input": ("plain iterate" if args.ws_input_iters else
+                             {"transpose": "A'b", "waveeq": "backproject_waveeq"}[
+                                 args.ws_backprojection]),
+                   "target_iterations": 200},
         "gpu_launches_dmas_cf": dm_launches,
     }
 

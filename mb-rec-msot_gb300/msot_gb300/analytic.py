@@ -60,7 +60,8 @@ def backproject_waveeq(sigMat, x, z, speed_of_sound, sampling_frequency,
     """backproject_waveeq.m:1.  psf: MATLAB m x n array (numpy (m, n), m along
     time); K: the bp_kernel matrix of the full acquisition times (numpy (Nt, Nt)
     with K[j, k] = MATLAB K(j, k), or a CUDA tensor already in column-major
-    order as returned by bp_kernel_device)."""
+    order as returned by bp_kernel_device).  The image is the reference's,
+    mirrored in x by its final fliplr (backproject_waveeq.m:49)."""
     s = _sig(sigMat)
     W, D, T = s.shape
     xv, zv = _vec(x), _vec(z)
@@ -81,3 +82,31 @@ def backproject_waveeq(sigMat, x, z, speed_of_sound, sampling_frequency,
         float(detector_radius), _dptr(psf_cm), psf.shape[0], psf.shape[1],
         C.c_void_p(Kd.data_ptr()), Kn, C.c_void_p(out.data_ptr()), _stream_ptr(stream)))
     return out
+
+
+def bp_kernel(t) -> np.ndarray:
+    """bp_kernel.m:1-12: K(t, t') = -Im trapz_lambda(H0(t lambda)
+    conj(H0(t' lambda)) lambda) with lambda = dl (1 .. Nt), dl = pi / (t_end -
+    t_1), H0 the Hankel function of the first kind.  With H0 = J0 + i Y0 the
+    imaginary part is real-valued: K = M - M^T, M = J0(t lambda) diag(w
+    lambda) Y0(t' lambda)^T (w the trapezoid weights) -- two real GEMMs on
+    the host in FP64."""
+    from scipy import special
+    t = np.asarray(t, dtype=np.float64).ravel()
+    n = t.size
+    dl = np.pi / (t[-1] - t[0])
+    lam = dl * np.arange(1, n + 1)
+    w = np.full(n, dl)
+    w[0] = w[-1] = dl / 2.0
+    arg = t[:, None] * lam[None, :]
+    J = special.j0(arg)
+    Y = special.y0(arg)
+    M = (J * (w * lam)[None, :]) @ Y.T
+    return M - M.T
+
+
+def bp_kernel_device(t, device="cuda"):
+    """bp_kernel(t) as the FP32 column-major CUDA tensor backproject_waveeq
+    takes directly."""
+    K = bp_kernel(t)
+    return torch.tensor(np.ascontiguousarray(K.T), dtype=torch.float32, device=device)

@@ -3,9 +3,10 @@ reference): a U-Net on the project's CUDA kernels (msot_unet_*), trained on
 pairs the plain GPU solver generates, whose prediction seeds both splitting
 variables of rec_nn_with_L2_reg (image w and multiplier v, kkt_multiplier).
 
-The network input f is either the backprojection A'b of a sinogram b
-(input_iters = 0) or the plain solver's iterate after input_iters
-iterations.  Input f / s, output x / (kappa s), with s = rms(f) per instance
+The network input f is a backprojection of the sinogram b (input_iters =
+0): A'b, or the backproject_waveeq image (backprojection = "waveeq", with
+the bp_kernel of the acquisition times and its x mirror undone) -- or the
+plain solver's iterate after input_iters iterations.  Input f / s, output x / (kappa s), with s = rms(f) per instance
 and kappa = median rms(x) / rms(f) over the training pairs, so one network
 serves any data scale; with ``residual`` (an iterate as input, kappa = 1)
 the network predicts the correction x / s - f / s.  The plain solver stays
@@ -104,7 +105,7 @@ class LearnedWarmStart:
 
     def __init__(self, model, lambdaL2: float = 0.0, net: UNet | None = None, levels=4,
                  base_channels=32, max_batch=16, seed=0, beta=1e-3, input_iters=0,
-                 residual=None):
+                 residual=None, backprojection: str = "transpose"):
         nx, nz = model.image_shape
         if nx != nz:
             raise ValueError("the warm-start network needs a square grid")
@@ -115,6 +116,10 @@ class LearnedWarmStart:
         if self.residual and self.input_iters <= 0:
             raise ValueError("the residual form needs an iterate as input (input_iters > 0)")
         self.kappa = 1.0 if self.residual else None
+        if backprojection not in ("transpose", "waveeq"):
+            raise ValueError("backprojection: 'transpose' or 'waveeq'")
+        self.backprojection = backprojection
+        self._K = None
 
     def _chunks(self, W):
         m = self.model.max_batch
@@ -132,10 +137,26 @@ class LearnedWarmStart:
         if self.input_iters > 0:
             f = torch.cat([rec_nn_with_L2_reg(self.model, b[i:j], self.input_iters, self.lam)[0]
                            for i, j in self._chunks(b.shape[0])])
+        elif self.backprojection == "waveeq":
+            f = self._waveeq(b)
         else:
             f = torch.cat([self.model.transpose(b[i:j]) for i, j in self._chunks(b.shape[0])])
         s = f.flatten(1).pow(2).mean(1).sqrt().clamp_min(1e-30)
         return (f / s.view(-1, 1, 1)).unsqueeze(1).contiguous(), s
+
+    def _waveeq(self, b):
+        """backproject_waveeq of b on the model's grid and probe (psf = 1),
+        with the x mirror of backproject_waveeq.m:49 undone so that the image
+        lines up with the model's pixels."""
+        from .analytic import backproject_waveeq, bp_kernel_device
+        m, d, p = self.model, self.model.Discretization, self.model.Probe
+        crop = m.n_crop + p.delay
+        if self._K is None:
+            nt = m.n_t + int(round(crop))
+            self._K = bp_kernel_device(np.arange(1, nt + 1) / p.fs)
+        out = backproject_waveeq(b, d.x, d.z, m.c, p.fs, crop, p.angular_coverage, p.radius,
+                                 np.array([[1.0]]), self._K)
+        return out.flip(1).contiguous()
 
     def make_pairs(self, images, iters=200, noise=0.01, seed=0):
         """Training pairs from phantoms (W, nx, nz): sinograms A x + noise

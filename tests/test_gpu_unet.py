@@ -163,3 +163,28 @@ def test_learned_warm_start_falls_back_to_zero_start(cuda):
     rec, fell = ws.solve(b, 5, torch.stack([bad[0], good[1]]))
     plain = rec_nn_with_L2_reg(model, b, 5, 1e-2)[0]
     assert float((rec[0] - plain[0]).norm() / plain[0].norm()) < 1e-5
+
+
+def test_waveeq_input_lines_up_with_the_image(cuda):
+    # the backproject_waveeq input (x mirror of backproject_waveeq.m:49
+    # undone) correlates with the phantom; the mirrored image does not
+    import torch
+    from msot_gb300 import Discretization, MSOTmodel, Probe
+    from msot_gb300.synthetic import gauss_pulse_eir
+    from msot_gb300.warmstart import LearnedWarmStart
+    n = 48
+    h = 0.2e-3 * (n - 1) / 2
+    probe = Probe(n_det=64, radius=0.02, angular_coverage=135.0, fs=4e7, n_samples=1200,
+                  eir=gauss_pulse_eir(), eir_length=257)
+    model = MSOTmodel(probe, Discretization([-h, h], n), 1500.0, model_normalization_factor=1.0,
+                      max_batch=2)
+    img = np.zeros((1, n, n), dtype=np.float32)
+    img[0, 10:16, 30:40] = 1.0
+    img[0, 30:34, 8:12] = 2.0
+    b = model.forward(torch.tensor(img, device="cuda"))
+    ws = LearnedWarmStart(model, 1e-2, levels=3, base_channels=8, max_batch=2,
+                          backprojection="waveeq")
+    f = ws.features(b)[0][0, 0].cpu().numpy()
+    corr = lambda a, c: float(np.corrcoef(a.ravel(), c.ravel())[0, 1])
+    assert corr(f, img[0]) > 0.3
+    assert abs(corr(f[::-1, :], img[0])) < 0.1

@@ -156,3 +156,15 @@ def test_table_cache_round_trip_and_collision(tmp_path):
     a = cache.spmr_tables(str(tmp_path), spec, mk)
     b = cache.spmr_tables(str(tmp_path), spec, lambda: 1 / 0)
     assert np.array_equal(a[0], b[0]) and b[3]["half_window"] == 45 and b[3]["n_dist"] == 3
+
+
+def test_bp_kernel_matches_oracle():
+    # the library's real-arithmetic form (K = M - M^T) against the oracle's
+    # complex Hankel product (bp_kernel.m:1-12)
+    from oracle import backprojection as B
+    from msot_gb300.analytic import bp_kernel
+    t = np.arange(1, 301) / 4e7
+    K = bp_kernel(t)
+    R = B.bp_kernel(t)
+    assert np.max(np.abs(K - R)) <= 1e-9 * np.abs(R).max()
+    assert np.max(np.abs(K + K.T)) <= 1e-12 * np.abs(K).max()
