@@ -777,6 +777,25 @@ def run_warmstart(args):
         if found is None and e <= target:
             found = (k, ms)
             break
+    # iterations each start needs for the accuracy of k plain iterations
+    plain_scan = []
+    for k in (5, 10, 20, 50, 100, 150, 200):
+        r, ms = _event_ms(lambda: solve(k))
+        plain_scan.append({"iterations": k, "rel_err": err(r), "ms": ms})
+    warm_errs = []
+    for k in (0, 1, 2, 5, 10, 20, 50, 100, 150, 200, 300):
+        if k == 0:
+            warm_errs.append((0, err(w0)))
+            continue
+        r = torch.cat([rec_nn_with_L2_reg(model, bt[i:i + 64], k, LAMBDA, x0=w0[i:i + 64],
+                                          v0=v0[i:i + 64])[0] for i in range(0, F, 64)])
+        warm_errs.append((k, err(r)))
+    crossover = []
+    for p in plain_scan:
+        need = next((k for k, e in warm_errs if e <= p["rel_err"]), None)
+        crossover.append({"plain_iterations": p["iterations"], "rel_err": p["rel_err"],
+                          "learned_input_plus_warm_iterations":
+                              None if need is None else args.ws_input_iters + need})
     n0 = L.msot_launch_count()
     dm_ms = _event_ms(lambda: reconstruct_dmas_cf(model, bt))[1]
     dm_launches = L.msot_launch_count() - n0
@@ -790,6 +809,7 @@ def run_warmstart(args):
                        "warm": (args.ws_input_iters + found[0]) if found else None,
                        "saved": (200 - args.ws_input_iters - found[0]) if found else None},
         "accuracy_target_rel_err_vs_1000_it": target, "warm_scan": scan,
+        "plain_scan": plain_scan, "iterations_to_plain_accuracy": crossover,
         "fallback_instances": int(fell.sum()),
         "equal_iterations": {"total": args.ws_input_iters + 10,
                              "plain_rel_err": eq, "warm_rel_err": scan[1]["rel_err"]
