@@ -141,34 +141,35 @@ extern "C" int msot_l2_gather_probe(size_t buffer_bytes, double *gbs) {
         return MSOT_ENOMEM;
     }
     const unsigned n_sectors = (unsigned)(buffer_bytes / 32);
-    cudaMemset(buf, 0, buffer_bytes);
     int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const dim3 grid((unsigned)sms * 16), block(256);
-    const int iters = 64;
-    cudaEvent_t a, b;
-    cudaEventCreate(&a);
-    cudaEventCreate(&b);
-    for (int w = 0; w < 3; ++w)  // warm-up: brings the buffer into L2
-        KLAUNCH(k_l2_gather_probe<<<grid, block>>>(buf, n_sectors, iters, 7u + w, sink));
-    cudaEventRecord(a);
-    const int reps = 20;
-    for (int r = 0; r < reps; ++r)
-        KLAUNCH(k_l2_gather_probe<<<grid, block>>>(buf, n_sectors, iters, 100u + r, sink));
-    cudaEventRecord(b);
-    cudaError_t e = cudaEventSynchronize(b);
+    cudaEvent_t a = nullptr, b = nullptr;
+    cudaError_t e = cudaMemset(buf, 0, buffer_bytes);
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaEventCreate(&a);
+    if (e == cudaSuccess) e = cudaEventCreate(&b);
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, a, b);
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
+    if (e == cudaSuccess) {
+        const dim3 grid((unsigned)sms * 16), block(256);
+        const int iters = 64, reps = 20;
+        for (int w = 0; w < 3; ++w)  // warm-up: brings the buffer into L2
+            KLAUNCH(k_l2_gather_probe<<<grid, block>>>(buf, n_sectors, iters, 7u + w, sink));
+        cudaEventRecord(a);
+        for (int r = 0; r < reps; ++r)
+            KLAUNCH(k_l2_gather_probe<<<grid, block>>>(buf, n_sectors, iters, 100u + r, sink));
+        cudaEventRecord(b);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaEventSynchronize(b);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+        *gbs = (double)grid.x * block.x * iters * 32.0 * reps / (ms * 1e-3) / 1e9;
+    }
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
     cudaFree(buf);
     cudaFree(sink);
     if (e != cudaSuccess) {
         set_error("l2_gather_probe: %s", cudaGetErrorString(e));
         return MSOT_ECUDA;
     }
-    const double bytes = (double)grid.x * block.x * iters * 32.0 * reps;
-    *gbs = bytes / (ms * 1e-3) / 1e9;
     return MSOT_OK;
 }
