@@ -255,6 +255,32 @@ def run_operator(args):
             "warmup": args.warmup, "impl": "ours-operator"}
 
 
+# ----------------------------------------------------------------------------
+# replicas over ranks: each rank solves its own batch (no data-path
+# collective); the step time is the slowest rank's
+# ----------------------------------------------------------------------------
+def rank_seed(rank: int) -> int:
+    """Seed of a rank's synthetic batch (distinct phantoms per replica)."""
+    return 1000 + int(rank)
+
+
+def max_over_ranks(x: float, dist=None) -> float:
+    """MAX of x over the ranks of the default process group (NCCL: on the
+    device; gloo: on the host); x itself without a group."""
+    if dist is None:
+        return float(x)
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(batch_per_rank: int, world: int, ms_per_step: float) -> float:
+    """Whole-job recons/s: every rank's batch per the slowest rank's step."""
+    return batch_per_rank * world / (ms_per_step / 1e3)
+
+
 def run_ours(args, rank, world):
     import torch
     from msot_gb300 import _lib, rec_nn_with_L2_reg
@@ -263,7 +289,7 @@ def run_ours(args, rank, world):
     B = args.batch
     model = build_model(B)
     tuning = model.autotune(B)  # kernel variants timed on this geometry and batch
-    x_true, b = make_data(model, B, seed=1000 + rank)
+    x_true, b = make_data(model, B, seed=rank_seed(rank))
     flush = torch.empty(512 * 1024 * 1024 // 4, device="cuda")
     dist = None
     if world > 1:
@@ -286,13 +312,9 @@ def run_ours(args, rank, world):
             ev[k][1].record()
         torch.cuda.synchronize()
     launches = L.msot_launch_count() - n0
-    ms = float(sum(a.elapsed_time(z) for a, z in ev))
-    if dist:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(float(sum(a.elapsed_time(z) for a, z in ev)), dist)
     ms_per_step = ms / args.steps
-    value = B * world / (ms_per_step / 1e3)
+    value = job_throughput(B, world, ms_per_step)
     # --- end to end through the public API with host buffers --------------------------
     b_host = b.cpu().pin_memory()
     rec_host = torch.empty((B, N_GRID, N_GRID), dtype=torch.float32).pin_memory()
@@ -305,12 +327,8 @@ def run_ours(args, rank, world):
         rec_host.copy_(r)
         torch.cuda.synchronize()
         e2e_ms += (time.perf_counter() - t0) * 1e3
-    e2e_ms /= args.steps
-    if dist:
-        t = torch.tensor([e2e_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e = {"value": B * world / (e2e_ms / 1e3), "unit": "recons/s",
+    e2e_ms = max_over_ranks(e2e_ms / args.steps, dist)
+    e2e = {"value": job_throughput(B, world, e2e_ms), "unit": "recons/s",
            "h2d_bytes_per_step": int(b_host.numel() * 4),
            "d2h_bytes_per_step": int(rec_host.numel() * 4)}
     # --- live per-kernel event timing (one instrumented solve) ------------------------
