@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-oracle", action="store_true", help="skip the FP64 oracle solve")
+    ap.add_argument("--clocks-csv", default=None,
+                    help="keep the nvidia-smi clock samples of the timed region in this file")
     ap.add_argument("--op", action="store_true",
                     help="time the operator alone: one step = A then A^T on the batch")
     ap.add_argument("--tv", action="store_true",
@@ -115,9 +117,12 @@ class Clocks:
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index=0):
+    def __init__(self, gpu_index=0, path=None):
+        """Samples every 200 ms into ``path`` (kept), or into a temporary file."""
+        import tempfile
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        self.keep = path is not None
+        self.path = path or os.path.join(tempfile.gettempdir(), f"clocks_bench_{os.getpid()}.csv")
         self.idx = gpu_index
 
     def __enter__(self):
@@ -158,6 +163,11 @@ class Clocks:
                 for n, v in zip(names, parts[5:9]):
                     if v.lower() == "active":
                         reasons.add(n)
+        if not self.keep:
+            try:
+                os.remove(self.path)
+            except OSError:
+                pass
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
                 "reasons": sorted(reasons), "samples": len(sm)}
 
@@ -304,7 +314,7 @@ def run_ours(args, rank, world):
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    with Clocks(torch.cuda.current_device()) as clk:
+    with Clocks(torch.cuda.current_device(), args.clocks_csv) as clk:
         for k in range(args.steps):
             flush.zero_()
             ev[k][0].record()
