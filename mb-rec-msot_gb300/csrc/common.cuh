@@ -93,6 +93,11 @@ struct Plan {
 };
 
 const char *set_error(const char *fmt, ...);
+// Raises a kernel's maximum dynamic shared memory to `bytes` if it is below
+// (never lowers it): the attribute is process-wide per function, so plans of
+// different sizes used from several threads must not shrink it between
+// another thread's setting and launch.  Thread-safe.  plan.cu
+cudaError_t raise_max_dynamic_smem(const void *func, size_t bytes);
 
 // tensor-core convolutions of the warm-start U-Net on (1) or off (0); unet.cu
 extern std::atomic<int> g_unet_tc;

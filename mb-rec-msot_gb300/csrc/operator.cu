@@ -944,8 +944,7 @@ static int pick_wt(int W, int T, int max_wt) {
 template <class K>
 static int set_smem(K kern, size_t bytes) {
     if (bytes > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)bytes);
+        cudaError_t e = raise_max_dynamic_smem((const void *)kern, bytes);
         if (e != cudaSuccess) {
             set_error("cudaFuncSetAttribute(smem=%zu): %s", bytes, cudaGetErrorString(e));
             return MSOT_ECUDA;
@@ -974,8 +973,7 @@ static int prefilter2d_km(const Plan &pl, const float *in, float *out, int W, bo
     constexpr int NC = PF_TX + 2 * KM;
     const size_t smem = (size_t)(2 * NC * (pl.nz | 1) + 2 * (2 * KM + 1)) * sizeof(float);
     if (smem > 200 * 1024) return 1;
-    MSOT_CUDA_TRY(cudaFuncSetAttribute(k_prefilter2d<KM>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MSOT_CUDA_TRY(raise_max_dynamic_smem((const void *)k_prefilter2d<KM>, smem));
     const dim3 grid((unsigned)((pl.nx + PF_TX - 1) / PF_TX), (unsigned)W);
     KLAUNCH(k_prefilter2d<KM><<<grid, PF_THREADS, smem, st>>>(
         in, out, pl.pre_x, pl.pre_z, pl.Kx, pl.Kz, pl.nx, pl.nz, W, transpose ? 1 : 0, out_mode));

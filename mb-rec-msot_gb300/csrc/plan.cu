@@ -11,6 +11,10 @@
 #include <cstring>
 #include <vector>
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "common.cuh"
 
 namespace msot {
@@ -23,6 +27,20 @@ const char *set_error(const char *fmt, ...) {
     vsnprintf(g_err, sizeof g_err, fmt, ap);
     va_end(ap);
     return g_err;
+}
+
+cudaError_t raise_max_dynamic_smem(const void *func, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, size_t> current;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t &c = current[{dev, func}];
+    if (bytes <= c) return cudaSuccess;
+    e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) c = bytes;
+    return e;
 }
 
 template <class T>

@@ -1202,8 +1202,7 @@ TvcGeom tvc_geometry(int N, int force = 0) {
 template <class K>
 static cudaError_t tvc_config(K kern, const TvcGeom &gm, int W, cudaStream_t st,
                               cudaLaunchConfig_t &cfg, cudaLaunchAttribute *at, bool &fits) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)gm.smem);
+    cudaError_t e = raise_max_dynamic_smem((const void *)kern, gm.smem);
     if (e != cudaSuccess) return e;
     if (gm.C > 8) {
         e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);

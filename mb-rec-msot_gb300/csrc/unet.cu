@@ -899,8 +899,7 @@ template <int NT>
 int conv3_tc(const float *in, int Ci, const float *wpk, const float *bias, float *out, int Co,
              int S, int N, int relu, cudaStream_t st) {
     const size_t smem = tc_smem_bytes(NT);
-    MSOT_CUDA_TRY(cudaFuncSetAttribute(k_conv3_tc<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
+    MSOT_CUDA_TRY(raise_max_dynamic_smem((const void *)k_conv3_tc<NT>, smem));
     const int tx = (S + TC_TX - 1) / TC_TX, ty = (S + TC_TY - 1) / TC_TY;
     const int vec = (S % 4 == 0) && ((uintptr_t)in % 16 == 0);
     dim3 grid(tx * ty, Co / NT, N);
@@ -951,9 +950,7 @@ int conv_bwd(msot_unet *u, const ConvL &c, const float *x, const float *y, const
         const int tx = (c.S + TC_TX - 1) / TC_TX, ty = (c.S + TC_TY - 1) / TC_TY;
         const int tiles = tx * ty, cog = (c.Co + 127) / 128, cig = (c.Ci + 31) / 32;
         const int splits = std::max(1, std::min(N * tiles, 148 / (cog * cig)));
-        MSOT_CUDA_TRY(cudaFuncSetAttribute(k_conv3_dw_tc,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)DW_SMEM));
+        MSOT_CUDA_TRY(raise_max_dynamic_smem((const void *)k_conv3_dw_tc, DW_SMEM));
         const int vec = (c.S % 4 == 0) && ((uintptr_t)x % 16 == 0) && ((uintptr_t)dy_pre % 16 == 0);
         KLAUNCH(k_conv3_dw_tc<<<dim3(cog, cig, splits), TC_THREADS, DW_SMEM, st>>>(
             x, c.Ci, dy_pre, c.Co, u->grad + c.w_off, c.S, c.S, N, tx, tiles, splits, vec));
