@@ -6,10 +6,11 @@ variables of rec_nn_with_L2_reg (image w and multiplier v, kkt_multiplier).
 The network input f is a backprojection of the sinogram b (input_iters =
 0): A'b, or the backproject_waveeq image (backprojection = "waveeq", with
 the bp_kernel of the acquisition times and its x mirror undone) -- or the
-plain solver's iterate after input_iters iterations.  Input f / s, output x / (kappa s), with s = rms(f) per instance
-and kappa = median rms(x) / rms(f) over the training pairs, so one network
-serves any data scale; with ``residual`` (an iterate as input, kappa = 1)
-the network predicts the correction x / s - f / s.  The plain solver stays
+plain solver's iterate after input_iters iterations.  Input f / s, output
+x / (kappa s), with s = rms(f) per instance and kappa = median rms(x) /
+rms(f) over the training pairs, so one network serves any data scale; with
+``residual`` (an iterate as input, kappa = 1) the network predicts the
+correction x / s - f / s.  The plain solver stays
 the fallback: an instance whose prediction has a larger objective
 |A x0 - b|^2 + lambda |x0|^2 than the zero start (|b|^2) is started from zero.
 """
@@ -132,7 +133,8 @@ class LearnedWarmStart:
         return b.to(torch.float32).reshape(-1, *self.model.sinogram_shape).contiguous()
 
     def features(self, b):
-        """(f / s as (W, 1, n, n), s (W,)); f = A'b or the plain iterate."""
+        """(f / s as (W, 1, n, n), s (W,)); f = the plain iterate, A'b or the
+        backproject_waveeq image (see the module docstring)."""
         b = self._sino(b)
         if self.input_iters > 0:
             f = torch.cat([rec_nn_with_L2_reg(self.model, b[i:j], self.input_iters, self.lam)[0]
