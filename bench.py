@@ -541,7 +541,8 @@ def run_sweep(args):
             line[k] = {"gbs": alg_bytes / sec / 1e9, "hbm_frac": alg_bytes / sec / 1e9 / peak,
                        "tflops": flops / sec / 1e12,
                        "fp32_frac_nominal": flops / sec / 1e12 / FP32_NOMINAL_TFLOPS}
-        line["peak_source"] = f"{peak_kind} hbm_gbs (copy); FP32 nominal {FP32_NOMINAL_TFLOPS:.1f} TF/s"
+        line["peak_source"] = (f"{peak_kind} hbm_gbs (copy); "
+                               f"FP32 nominal {FP32_NOMINAL_TFLOPS:.1f} TF/s")
         out.append(line)
         print(json.dumps(line), flush=True)
         del model
@@ -667,7 +668,8 @@ def run_prep(args):
             "gemm_tflops": flops / (ms * 1e9), "steps": args.steps, "warmup": args.warmup,
             "gpu_launches_per_step": (L.msot_launch_count() - n0) // args.steps,
             "dtype": "f32", "data": "synthetic Gaussian noise",
-            "config": {"workload": f"crop {n_crop}, window, zero-phase filter; {W} x {D} x {T_raw}"}}
+            "config": {"workload": f"crop {n_crop}, window, zero-phase filter; "
+                                   f"{W} x {D} x {T_raw}"}}
 
 
 def run_tv(args):
@@ -938,7 +940,8 @@ def run_unet(args):
     except Exception:
         bf16 = None
     return {"metric": "U-Net training images/s", "value": B / (train_ms / 1e3), "unit": "images/s",
-            "ms_per_step": train_ms, "forward_ms": fwd_ms, "forward_images_per_s": B / (fwd_ms / 1e3),
+            "ms_per_step": train_ms, "forward_ms": fwd_ms,
+            "forward_images_per_s": B / (fwd_ms / 1e3),
             "train_tflops": 3 * fl / (train_ms * 1e9), "forward_tflops": fl / (fwd_ms * 1e9),
             "peak_bf16_tflops_measured": bf16,
             "peak_tf32_tflops_est": bf16 / 2 if bf16 else None,

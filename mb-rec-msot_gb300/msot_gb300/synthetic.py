@@ -36,7 +36,8 @@ def phantom(disc, rng: np.random.Generator, n_disks=(5, 15), r_disk=(0.3e-3, 3e-
         across = -(X - px) * np.sin(th) + (Z - pz) * np.cos(th)
         along = (X - px) * np.cos(th) + (Z - pz) * np.sin(th)
         length = rng.uniform(0.3, 0.8) * (x1 - x0)
-        img += rng.uniform(*amp) * np.exp(-across ** 2 / (2 * sig * sig)) * (np.abs(along) <= length / 2)
+        img += (rng.uniform(*amp) * np.exp(-across ** 2 / (2 * sig * sig))
+                * (np.abs(along) <= length / 2))
     return img
 
 
@@ -59,7 +60,8 @@ def phantom_batch(disc, count: int, seed: int = 0, device="cuda", n_disks=(5, 15
         cx, cz = (2 * u(count) - 1) * half, (2 * u(count) - 1) * half
         rad = r_disk[0] + u(count) * (r_disk[1] - r_disk[0])
         a = (amp[0] + u(count) * (amp[1] - amp[0])) * (k < nd)
-        inside = (X - cx.view(-1, 1, 1)) ** 2 + (Z - cz.view(-1, 1, 1)) ** 2 <= (rad ** 2).view(-1, 1, 1)
+        inside = ((X - cx.view(-1, 1, 1)) ** 2 + (Z - cz.view(-1, 1, 1)) ** 2
+                  <= (rad ** 2).view(-1, 1, 1))
         img += a.view(-1, 1, 1) * inside
     sig = vessel_width / 2.355
     for _ in range(n_vessels):

@@ -26,7 +26,8 @@ def test_port_das_matches_reference_bitwise(port, golden, W):
 def test_port_sir_matches_reference_bitwise(port, golden, W):
     g = golden
     r, T = float(g["radius"]), int(g["sir_T"])
-    y = port.forward_sir(g[f"sir_img_w{W}"], g["sir_idx"], g["sir_tau"], g["sir"], T, g["sir_se"], r)
+    y = port.forward_sir(g[f"sir_img_w{W}"], g["sir_idx"], g["sir_tau"], g["sir"], T,
+                         g["sir_se"], r)
     assert np.array_equal(y, g[f"sir_fwd_w{W}"])
     x = port.transpose_sir(g[f"sir_sig_w{W}"], g["sir_idx"], g["sir_tau"], g["sir"], g["sir_se"], r)
     assert np.array_equal(x, g[f"sir_adj_w{W}"])
