@@ -210,3 +210,46 @@ def test_dual_sos_travel_times_against_bounded_brent_and_snell():
         s1 = (xm[d, p] - X[p]) / np.hypot(xm[d, p] - X[p], z0 - Z[p])
         s2 = (xd[d] - xm[d, p]) / np.hypot(xd[d] - xm[d, p], zd[d] - z0)
         assert abs(s1 / cb - s2 / ca) <= 1e-9
+
+
+def test_del2_restatement_properties():
+    # MATLAB del2(U, 1) of x^2 + y^2 is 1 everywhere (the end values come from
+    # linear extrapolation, exact for quadratics), of a linear field 0; lines
+    # of 3 copy the centre, shorter lines give 0
+    from oracle import solvers as S
+    X, Y = np.meshgrid(np.arange(7.0), np.arange(5.0), indexing="ij")
+    assert np.allclose(S.del2(X ** 2 + Y ** 2), 1.0)
+    assert np.allclose(S.del2(3.0 * X - 2.0 * Y + 1.0), 0.0)
+    u = np.random.default_rng(1).standard_normal((3, 2))
+    d = S.del2(u)
+    col = (u[2] - 2 * u[1] + u[0]) / 4.0  # the n = 3 axis, copied to its ends; n = 2 axis: 0
+    assert np.allclose(d, np.broadcast_to(col, (3, 2)))
+
+
+def test_virtual_sources_restatement():
+    # the virtual source lies at distance t c_coupling from its detector, and
+    # is the pixel itself when the path does not cross the membrane
+    probe = M.ArcProbe(n_det=12, radius=0.040, coverage_deg=135.0, n_samples=2030)
+    grid = M.Grid(10, 10, (-0.006, 0.006, -0.006, 0.006))
+    mem = (-0.004, 0.1)  # cuts the grid: some pixels lie on the detector side
+    tau, xm = M.travel_time_indices_dual(probe, grid, 1560.0, 1480.0, mem)
+    vx, vz = M.virtual_sources(probe, grid, 1560.0, 1480.0, mem)
+    xd, zd = probe.positions()
+    d = np.hypot(vx - xd[:, None], vz - zd[:, None])
+    assert np.allclose(d, tau / probe.fs * 1480.0, rtol=0, atol=1e-12)
+    X, Z = grid.pixel_xz()
+    direct = np.isnan(xm)
+    assert direct.any() and (~direct).any()
+    assert np.array_equal(vx[direct], np.broadcast_to(X, vx.shape)[direct])
+
+
+def test_spmr_with_pixels_as_virtual_sources_is_unchanged():
+    from oracle import sir as Q
+    x = np.linspace(-0.002, 0.002, 8)
+    z = np.linspace(-0.002, 0.002, 8)
+    args = (8, 0.040, 135.0, x, z, 1500.0, 4e7, 0.00029, 0.25e-3, 10e-3, 0.0, 2, 2)
+    a = Q.spmr_tables(*args, half_window=60)
+    X, Z = np.meshgrid(x, z, indexing="ij")
+    virt = (np.broadcast_to(X.ravel(), (8, 64)), np.broadcast_to(Z.ravel(), (8, 64)))
+    b = Q.spmr_tables(*args, half_window=60, virtual=virt)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
