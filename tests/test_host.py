@@ -168,3 +168,50 @@ def test_bp_kernel_matches_oracle():
     R = B.bp_kernel(t)
     assert np.max(np.abs(K - R)) <= 1e-9 * np.abs(R).max()
     assert np.max(np.abs(K + K.T)) <= 1e-12 * np.abs(K).max()
+
+
+def test_new_entry_points_reject_bad_arguments_without_a_device():
+    # argument checks run before any device work, so they hold on any host
+    from msot_gb300 import _lib
+    L = _lib.load(build_if_missing=True)
+    D = ctypes.POINTER(ctypes.c_double)
+    out = (ctypes.c_double * 16)()
+    x = (ctypes.c_double * 4)(0.0, 1e-3, 2e-3, 3e-3)
+    a = (ctypes.c_double * 9)(*([0.0] * 9))
+    h = ctypes.c_void_p()
+    cases = [
+        # pre-processing: low >= high, cut-off above Nyquist, nothing left after the crop
+        (lambda: L.msot_prep_create(100, 0, 2, 50.0, 40.0, 4e7, 0.0, 0.0, 4, ctypes.byref(h)),
+         b"prep_create"),
+        (lambda: L.msot_prep_create(100, 0, 0, 0.0, 0.0, 4e7, 0.0, 3e7, 4, ctypes.byref(h)),
+         b"prep_create"),
+        (lambda: L.msot_prep_create(10, 9, 0, 0.0, 0.0, 0.0, 0.0, 0.0, 4, ctypes.byref(h)),
+         b"prep_create"),
+        (lambda: L.msot_prep_apply(None, None, None, 1, None), b"prep_apply"),
+        (lambda: L.msot_butter_response(8, 0, 1.5, 0.0, 16, 0, ctypes.cast(out, D)),
+         b"butter_response"),
+        # dual speed of sound: no or too many membrane coefficients, one of the
+        # two virtual-source outputs
+        (lambda: L.msot_travel_times_dual(4, 0.04, 135.0, x, 4, x, 4, 1500.0, 1480.0, a, 0,
+                                          4e7, 0.0, 0.0, ctypes.cast(out, D), None, None, None),
+         b"travel_times_dual"),
+        (lambda: L.msot_travel_times_dual(4, 0.04, 135.0, x, 4, x, 4, 1500.0, 1480.0, a, 9,
+                                          4e7, 0.0, 0.0, ctypes.cast(out, D), None, None, None),
+         b"travel_times_dual"),
+        (lambda: L.msot_travel_times_dual(4, 0.04, 135.0, x, 4, x, 4, 1500.0, 1480.0, a, 2,
+                                          4e7, 0.0, 0.0, ctypes.cast(out, D), None,
+                                          ctypes.cast(out, D), None),
+         b"travel_times_dual"),
+        (lambda: L.msot_rec_nn_with_L2_reg_2(None, None, None, 1, 1, 1e-2, 1e-2, None, 0, None,
+                                             None, None, None), b"rec_nn_with_L2_reg_2"),
+        (lambda: L.msot_laplacian_per_wavelength(None, None, 1, 4, 4, None),
+         b"laplacian_per_wavelength"),
+        (lambda: L.msot_autotune(None, 1, None, None), b"autotune"),
+        (lambda: L.msot_l2_gather_probe(1024, ctypes.cast(out, D)), b"l2_gather_probe"),
+        (lambda: L.msot_tune_set(b"no_such_knob", 1), b"tune_set"),
+        (lambda: L.msot_tune_set(b"conv_min_blocks", 2), b"tune_set"),
+    ]
+    for call, where in cases:
+        rc = call()
+        assert rc == -1, where
+        assert where in L.msot_last_error(), (where, L.msot_last_error())
