@@ -390,7 +390,7 @@ def run_ours(args, rank, world):
     # --- FP64 oracle: accuracy of instance 0 + the CPU baseline sample ----------------
     acc = None
     cpu = None
-    if not args.no_oracle:
+    if not args.no_oracle and world == 1:  # rank 0 at N = 1 only
         threads = os.cpu_count() or 1
         ref, t_cpu = oracle_solve(model, b[0].cpu().numpy(), threads)
         got = rec[0].cpu().numpy().astype(np.float64)
