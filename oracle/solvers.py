@@ -18,7 +18,10 @@ are restated here from their published algorithms:
     no continuation, no debiasing, StopCriterion 1 (relative change of the
     objective below ToleranceA).
 Parity against MATLAB for these is therefore unpinned; the GPU solvers are
-pinned against these restatements.
+pinned against these restatements.  The LSQR and CGS restatements are
+checked step by step against scipy.sparse.linalg's lsqr and cgs, independent
+implementations of the same published algorithms (tests/test_oracle.py);
+SpaRSA has no such second implementation here.
 
 Solver sources restated:
   rec_nn_with_L2_reg.m:1-66, nnls_L2_less.m:27-143 (aug operator :145-167),

@@ -119,9 +119,10 @@ def test_lsqr_restatement_matches_scipy():
     A = rng.standard_normal((40, 15))
     b = rng.standard_normal(40)
     x0 = rng.standard_normal(15)
-    ours = S.lsqr(lambda v: A @ v, lambda u: A.T @ u, b, 1e-12, 3, x0)
-    ref = sp_lsqr(A, b, atol=0, btol=0, iter_lim=3, x0=x0)[0]
-    assert np.allclose(ours, ref, rtol=1e-10, atol=1e-12)
+    for k in range(1, 13):
+        ours = S.lsqr(lambda v: A @ v, lambda u: A.T @ u, b, 1e-12, k, x0)
+        ref = sp_lsqr(A, b, atol=0, btol=0, iter_lim=k, x0=x0)[0]
+        assert np.allclose(ours, ref, rtol=1e-10, atol=1e-12), k
 
 
 def test_cgs_restatement_solves_spd_system():
@@ -134,6 +135,28 @@ def test_cgs_restatement_solves_spd_system():
     # not converged after 2 steps: returns the iterate of smallest residual
     x2 = S.cgs(lambda v: A @ v, b, 1e-12, 2)
     assert np.linalg.norm(A @ x2 - b) <= np.linalg.norm(b)
+
+
+def test_cgs_iterates_match_scipy():
+    """Each CGS step against scipy's independent implementation of the same
+    algorithm (Templates form, x0 = 0) on a non-symmetric system whose
+    residual is not monotone: after k steps the restatement returns scipy's
+    iterate of smallest residual among its first k."""
+    from scipy.sparse.linalg import cgs as sp_cgs
+    rng = np.random.default_rng(7)
+    n = 30
+    A = 4 * np.eye(n) + 0.5 * rng.standard_normal((n, n))
+    b = rng.standard_normal(n)
+    its = []
+    sp_cgs(A, b, x0=np.zeros(n), rtol=1e-14, atol=0, maxiter=12,
+           callback=lambda x: its.append(x.copy()))
+    assert len(its) == 12
+    res = [np.linalg.norm(b - A @ x) for x in its]
+    assert any(res[k + 1] > res[k] for k in range(11))  # non-monotone case
+    for k in range(1, 13):
+        ours = S.cgs(lambda v: A @ v, b, 1e-14, k)
+        j = int(np.argmin(res[:k]))
+        assert np.abs(ours - its[j]).max() < 1e-11
 
 
 def test_l2_nnls_oracle_is_nonnegative_and_fits():
