@@ -169,6 +169,54 @@ def test_l2_nnls_oracle_is_nonnegative_and_fits():
     assert e_img < 0.1 * np.linalg.norm(b) ** 2
 
 
+def test_l2_nnls_oracle_converges_to_scipy_nnls():
+    """The splitting of nnls_L2_less.m:93-141 (beta = 1e-3, two LSQR steps
+    per iteration) approaches the minimiser of |A x - b|^2 + lambda |x|^2,
+    x >= 0, that scipy's active-set NNLS (Lawson & Hanson) finds on the
+    augmented system; A has unit norm as the normalised model does."""
+    from scipy.optimize import nnls
+    rng = np.random.default_rng(0)
+    A = rng.standard_normal((60, 30))
+    A /= np.linalg.norm(A, 2)
+    lam = 1e-2
+    xt = np.maximum(rng.standard_normal(30), 0)
+    b = A @ xt + 0.05 * rng.standard_normal(60)
+    xa, _ = nnls(np.vstack([A, np.sqrt(lam) * np.eye(30)]), np.concatenate([b, np.zeros(30)]))
+    assert (xa == 0).sum() >= 3  # active constraints present
+    errs = []
+    for it in (50, 200, 1000):
+        rec, _, _ = S.rec_nn_with_L2_reg(lambda v: A @ v, lambda u: A.T @ u, b, 30, it, lam)
+        errs.append(np.linalg.norm(rec - xa) / np.linalg.norm(xa))
+    assert errs[0] > errs[1] > errs[2] and errs[2] < 2e-4
+
+
+def test_l1_nnls_oracle_minimises_nonnegative_lasso():
+    """nnls_L1_eye_matrix_less.m:76-107 is split Bregman for
+    min 1/2 |A u - b|^2 + eta sum(u), u >= 0.  With an accurate inner solve
+    (30 CGS steps) it reaches the minimiser that projected FISTA finds.  The
+    reference's own setting (2 CGS steps from zero per iteration) stalls about
+    1 % away from it on this problem: the inexact inner solve moves the fixed
+    point, a property of the reference's algorithm that the GPU solver
+    reproduces."""
+    rng = np.random.default_rng(0)
+    A = rng.standard_normal((60, 30))
+    A /= np.linalg.norm(A, 2)
+    xt = np.maximum(rng.standard_normal(30), 0)
+    b = A @ xt + 0.05 * rng.standard_normal(60)
+    eta = 1e-2
+    x, z, t = np.zeros(30), np.zeros(30), 1.0
+    for _ in range(20000):  # step 1/L with L = |A|^2 = 1
+        xn = np.maximum(z - (A.T @ (A @ z - b) + eta), 0.0)
+        tn = (1 + np.sqrt(1 + 4 * t * t)) / 2
+        z, x, t = xn + (t - 1) / tn * (xn - x), xn, tn
+    assert (x == 0).sum() >= 3
+    fwd, adj = (lambda v: A @ v), (lambda u: A.T @ u)
+    rec = S.nnls_L1_eye_matrix_less(fwd, adj, b, A.T @ b, eta, 1.0, 1000, 30)
+    assert np.linalg.norm(rec - x) <= 1e-6 * np.linalg.norm(x)
+    rec2 = S.rec_nn_with_L1_eye_reg(fwd, adj, b, 1000, eta)[0]
+    assert 1e-3 < np.linalg.norm(rec2 - x) / np.linalg.norm(x) < 5e-2
+
+
 def test_sb_itv2_reduces_tv():
     rng = np.random.default_rng(6)
     n = 12
@@ -178,6 +226,73 @@ def test_sb_itv2_reduces_tv():
     g += 0.1 * rng.standard_normal((n, n))
     u = S.sb_itv2(g, 0.05, B, Bt, BtB).reshape(n, n, order="F")
     assert S.itv(u) < S.itv(g)
+
+
+def test_sb_itv2_minimises_isotropic_tv_objective():
+    """Split Bregman with lambda = 1 (SB_ITV2.m:20-40) minimises
+    E(u) = mu * sum_i |(B u)_i|_2 + 1/2 |u - g|^2 over the DiffOper
+    gradient B.  An independent solver of the same objective (the
+    Chambolle-Pock primal-dual iteration, dual constraint |p_i| <= mu) gives
+    the reference minimum."""
+    rng = np.random.default_rng(6)
+    n = 12
+    N = n * n
+    B, Bt, BtB = S.diff_oper(n)
+    g = np.zeros((n, n))
+    g[3:8, 4:9] = 1.0
+    g += 0.1 * rng.standard_normal((n, n))
+    gf = g.ravel(order="F")
+    mu = 0.05
+
+    def energy(u):
+        Bu = B @ u
+        return mu * np.sum(np.hypot(Bu[:N], Bu[N:])) + 0.5 * np.sum((u - gf) ** 2)
+
+    u, ub, p = gf.copy(), gf.copy(), np.zeros(2 * N)
+    tau = sig = 0.34  # tau * sigma * |B|^2 < 1 with |B|^2 <= 8
+    for _ in range(20000):
+        p = p + sig * (B @ ub)
+        f = np.maximum(1.0, np.hypot(p[:N], p[N:]) / mu)
+        p = p / np.concatenate([f, f])
+        un = (u - tau * (Bt @ p) + tau * gf) / (1 + tau)
+        ub, u = 2 * un - u, un
+    e_ref = energy(u)
+    us = S.sb_itv2(g, mu, B, Bt, BtB, tol=1e-6, max_outer=2000)
+    assert abs(energy(us) - e_ref) <= 1e-5 * e_ref
+    assert np.linalg.norm(us - u) <= 1e-4 * np.linalg.norm(u)
+    # the reference's own stopping tolerance (1e-3) stays within 1e-3 of it
+    assert energy(S.sb_itv2(g, mu, B, Bt, BtB)) <= (1 + 1e-3) * e_ref
+
+
+def test_sparsa_reaches_the_lasso_minimiser():
+    """The SpaRSA restatement (Barzilai-Borwein prox-gradient) with the
+    soft-threshold prox converges to the minimiser of
+    1/2 |y - A x|^2 + tau |x|_1 that an independent method (FISTA, Beck &
+    Teboulle 2009) finds."""
+    rng = np.random.default_rng(8)
+    m, n = 60, 40
+    A = rng.standard_normal((m, n)) / np.sqrt(m)
+    xt = np.zeros(n)
+    xt[rng.choice(n, 6, replace=False)] = rng.standard_normal(6)
+    y = A @ xt + 0.01 * rng.standard_normal(m)
+    tau = 0.02
+
+    def soft(v, t):
+        return np.sign(v) * np.maximum(np.abs(v) - t, 0.0)
+
+    def objective(x):
+        return 0.5 * np.sum((y - A @ x) ** 2) + tau * np.abs(x).sum()
+
+    L = np.linalg.norm(A, 2) ** 2
+    x, z, t = np.zeros(n), np.zeros(n), 1.0
+    for _ in range(20000):
+        xn = soft(z - (A.T @ (A @ z - y)) / L, tau / L)
+        tn = (1 + np.sqrt(1 + 4 * t * t)) / 2
+        z, x, t = xn + (t - 1) / tn * (xn - x), xn, tn
+    xs = S.sparsa(y, lambda v: A @ v, lambda u: A.T @ u, tau, soft, lambda v: np.abs(v).sum(),
+                  np.zeros(n), 200, tol=1e-14)
+    assert abs(objective(xs) - objective(x)) <= 1e-12 * objective(x)
+    assert np.linalg.norm(xs - x) <= 1e-7 * np.linalg.norm(x)
 
 
 def test_bp_kernel_is_antisymmetric_and_dmas_identity():
