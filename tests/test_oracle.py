@@ -113,6 +113,42 @@ def test_convolve_ir_matches_direct_fir():
     assert np.allclose(y, direct, rtol=0, atol=1e-12)
 
 
+@pytest.mark.parametrize("fmin,fmax", [(1e5, 12e6), (0.0, 12e6), (5e5, 0.0)])
+def test_fft_zero_phase_filter_equals_forward_backward_iir(fmin, fmax):
+    """filter_butter_zero_phase.m:26-48 (use_fft = true) multiplies the
+    spectrum by |H|^2 on the whole circle.  For a pulse whose filtered tails
+    stay inside the record that equals running the Butterworth sections
+    forward and then backward in the time domain (after the mean removal the
+    reference applies with a high-pass)."""
+    import scipy.signal as sps
+    fs, n = 4e7, 8192
+    t = np.arange(n)
+    x = np.exp(-0.5 * ((t - n / 2) / 6.0) ** 2) * np.sin(2 * np.pi * 5e6 * t / fs)
+    y = M.filter_butter_zero_phase(x[:, None], fs, fmin, fmax)[:, 0]
+    xs = x - x.mean() if fmin > 0 else x
+    secs = []
+    if fmax > 0:
+        secs.append(sps.butter(8, fmax * 2 / fs, "low", output="sos"))
+    if fmin > 0:
+        secs.append(sps.butter(2, fmin * 2 / fs, "high", output="sos"))
+    sos = np.vstack(secs)
+    ff = sps.sosfilt(sos, sps.sosfilt(sos, xs)[::-1])[::-1]
+    assert np.abs(y - ff).max() <= 1e-12 * np.abs(y).max()
+
+
+def test_sigma_max_estimate_matches_svd():
+    """The power iteration standing in for svds(A, 1) (MSOTmodel.m:277-278)
+    against the largest singular value of a dense matrix with a clear gap."""
+    rng = np.random.default_rng(9)
+    U, _ = np.linalg.qr(rng.standard_normal((50, 20)))
+    V, _ = np.linalg.qr(rng.standard_normal((20, 20)))
+    s = np.linspace(0.1, 1.0, 20)
+    s[-1] = 2.0
+    A = (U * s) @ V.T
+    est = M.estimate_sigma_max(lambda v: A @ v, lambda u: A.T @ u, (20,), iters=60)
+    assert abs(est - np.linalg.svd(A, compute_uv=False)[0]) <= 1e-12 * 2.0
+
+
 def test_lsqr_restatement_matches_scipy():
     from scipy.sparse.linalg import lsqr as sp_lsqr
     rng = np.random.default_rng(3)
