@@ -396,6 +396,34 @@ def test_model_and_analytic_geometries_agree():
         assert abs(i - i0) <= 1 and abs(j - j0) <= 1
 
 
+def test_spmr_antialias_response_matches_butterworth_design():
+    """calculate_polarSPMR.m:50-54,73: |freqz|^2 of butter(8, fs_dac / f_field,
+    'low') on the whole circle; the restatement writes it in closed form
+    (bilinear Butterworth), checked here against scipy's design."""
+    import scipy.signal as sps
+    from oracle import sir as O
+    fs, n = 4e7, 1 << 16
+    f = np.arange(n) / n
+    with np.errstate(divide="ignore", over="ignore"):
+        ratio = np.tan(np.pi * f) / np.tan(np.pi * (fs / 2.0) / O.FSF)
+        h2 = 1.0 / (1.0 + ratio ** 16)
+    h2[n // 2] = 0.0
+    _, h = sps.sosfreqz(sps.butter(8, fs / O.FSF, "low", output="sos"), worN=n, whole=True)
+    assert np.abs(np.abs(h) ** 2 - h2).max() < 1e-10
+    # and nshape_filtered applies exactly this response to the N-shape
+    sigma, c = 1e-5, 1500.0  # decays within the default 200 field samples
+    g, M = O.nshape_filtered(sigma, c, fs)
+    m = np.arange(-M, M + 2)
+    circ = np.zeros(O.NF)
+    circ[m % O.NF] = g
+    j = np.arange(-200, 201)
+    t = j / O.FSF
+    q = np.zeros(O.NF)
+    q[j % O.NF] = np.exp(-(c * t) ** 2 / (2 * sigma ** 2)) * (-t)
+    ref = np.real(np.fft.ifft(np.fft.fft(q) * h2))
+    assert np.abs(circ - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
 def test_spmr_oracle_tables_are_consistent():
     # SPMR generator restatement (parity with the reference's Field II tables
     # is unpinned): every column peaks near its travel time, start <= end
