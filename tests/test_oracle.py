@@ -40,6 +40,47 @@ def test_reference_library_reproduces_golden(golden):
     assert np.array_equal(ref.forward_das(golden["das_img_w5"], tau, T, r), golden["das_fwd_w5"])
 
 
+@pytest.mark.skipif(not native.ref_available(), reason="reference MEX not compiled on this host")
+@pytest.mark.parametrize("seed", range(12))
+def test_port_matches_reference_on_random_geometries(port, seed):
+    """Beyond the committed golden vectors: the C restatement against the
+    reference MEX code itself on seeded random arcs, grids, interpolation
+    radii (1 to 8 samples), batch sizes and thread counts, bit for bit, for
+    all four operators."""
+    from tests.golden.make_golden import small_geometry
+    ref = native.ref()
+    rng = np.random.default_rng(1000 + seed)
+    nx, nz = int(rng.integers(3, 30)), int(rng.integers(3, 30))
+    n_det = int(rng.integers(2, 40))
+    pitch = float(rng.uniform(0.04e-3, 0.3e-3))
+    tau, r = small_geometry(nx, nz, n_det, R=float(rng.uniform(0.006, 0.03)),
+                            cov=float(rng.uniform(60, 270)), pitch=pitch)
+    D, P = tau.shape
+    W = int(rng.choice([1, 2, 4, 7]))
+    T = int(np.ceil(tau.max() + r)) + int(rng.integers(2, 30))
+    threads = int(rng.choice([1, 3, 8]))
+    for lib in (port, ref):
+        lib.set_threads(threads)
+    img = rng.random((P, W))
+    sig = rng.standard_normal((D, T, W))
+    assert np.array_equal(port.forward_das(img, tau, T, r), ref.forward_das(img, tau, T, r))
+    assert np.array_equal(port.transpose_das(sig, tau, r), ref.transpose_das(sig, tau, r))
+    S, NS = int(rng.integers(5, 60)), int(rng.integers(1, 20))
+    sir = rng.standard_normal((NS, S))
+    se = np.zeros((NS, 2), dtype=np.int32)
+    for k in range(NS):
+        a = int(rng.integers(1, S + 1))
+        se[k] = (a, int(rng.integers(a, S + 1)))
+    idx = rng.integers(1, NS + 1, size=(D, P)).astype(np.int32)
+    tau_s = tau - (tau.min() - 3.0)
+    Ts = int(np.ceil(tau_s.max())) + int(rng.integers(1, 20))
+    sig_s = rng.standard_normal((D, Ts, W))
+    assert np.array_equal(port.forward_sir(img, idx, tau_s, sir, Ts, se, r),
+                          ref.forward_sir(img, idx, tau_s, sir, Ts, se, r))
+    assert np.array_equal(port.transpose_sir(sig_s, idx, tau_s, sir, se, r),
+                          ref.transpose_sir(sig_s, idx, tau_s, sir, se, r))
+
+
 def test_port_rejects_out_of_range_taps(port, golden):
     tau, r, T = golden["tau"], float(golden["radius"]), int(golden["T"])
     bad = tau.copy()
