@@ -38,6 +38,7 @@ for _p in (ROOT, os.path.join(ROOT, "mb-rec-msot_gb300")):
 
 METRIC = "NNLS recons/s at <=1e-3 rel. error vs FP64: learned+batched vs plain, 1 GB300"
 N_GRID, N_DET, N_T, N_ITER, LAMBDA = 128, 256, 2030, 50, 1e-2
+ONE_THREAD_ITERS = 2  # outer iterations of the single-thread CPU sample
 HBM_FALLBACK_GBS = 6800.0
 
 
@@ -202,9 +203,10 @@ def make_data(model, batch, seed):
     return x, y.contiguous()
 
 
-def oracle_solve(model, b_np, threads):
+def oracle_solve(model, b_np, threads, n_iter=None):
     """CPU-baseline leg: FP64 oracle solve of one instance with the same model
-    parameters as the GPU plan; its result is also the accuracy reference."""
+    parameters as the GPU plan (n_iter outer iterations, default the
+    workload's); the full solve is also the accuracy reference."""
     from oracle import model as M
     from oracle import native
     from oracle import solvers as S
@@ -219,7 +221,8 @@ def oracle_solve(model, b_np, threads):
     fwd = lambda v: om.forward(v.reshape(1, g.nx, g.nz)).ravel()
     adj = lambda y: om.transpose(y.reshape(1, p.n_det, -1)).ravel()
     t0 = time.perf_counter()
-    rec, _, _ = S.rec_nn_with_L2_reg(fwd, adj, b_np.astype(np.float64).ravel(), P, N_ITER, LAMBDA)
+    rec, _, _ = S.rec_nn_with_L2_reg(fwd, adj, b_np.astype(np.float64).ravel(), P,
+                                     N_ITER if n_iter is None else int(n_iter), LAMBDA)
     return rec.reshape(g.nx, g.nz), time.perf_counter() - t0
 
 
@@ -398,6 +401,12 @@ def run_ours(args, rank, world):
         cpu = {"value": 1.0 / t_cpu, "unit": "recons/s", "cores": threads, "kind": "port",
                "sample": "one full 50-iteration FP64 solve of instance 0 (C restatement of the "
                          "MEX kernels + numpy FFT wrappers/LSQR)"}
+        _, t_one = oracle_solve(model, b[0].cpu().numpy(), 1, ONE_THREAD_ITERS)
+        cpu["single_thread"] = {
+            "value": (ONE_THREAD_ITERS / N_ITER) / t_one, "unit": "recons/s", "cores": 1,
+            "sample": f"{ONE_THREAD_ITERS} of the {N_ITER} outer iterations of instance 0 with "
+                      f"the C kernels on one thread; recons/s = ({ONE_THREAD_ITERS}/{N_ITER}) / "
+                      "time"}
     return {
         "metric": METRIC, "value": value, "unit": "recons/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,

@@ -1,11 +1,14 @@
-"""bench.py's reference arm on the host (no GPU): the JSON line it prints and
-its behaviour on ranks other than 0.  The arm times the reference's CPU
-implementation of the batched L2 solve (the compiled MEX kernels where they
-built, else their C restatement) inside the FP64 solver restatement."""
+"""bench.py on the host (no GPU): the reference arm's JSON line and its
+behaviour on ranks other than 0, and the GPU arm's CPU-baseline helper.  The
+reference arm times the reference's CPU implementation of the batched L2
+solve (the compiled MEX kernels where they built, else their C restatement)
+inside the FP64 solver restatement."""
 import json
 import os
 import subprocess
 import sys
+
+import numpy as np
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -46,3 +49,26 @@ def test_reference_arm_is_silent_on_other_ranks():
     r = _bench({"RANK": "1", "WORLD_SIZE": "2"}, "--steps", "1", "--warmup", "0")
     assert r.returncode == 0, r.stderr[-2000:]
     assert r.stdout.strip() == ""
+
+
+def test_cpu_baseline_leg_runs_a_bounded_sample():
+    """The GPU arm's CPU-baseline helper on a stand-in for the model's
+    attributes (no device needed): the full solve and the short
+    single-thread sample both run the FP64 oracle on the same geometry."""
+    from types import SimpleNamespace
+
+    import bench
+    from oracle import model as M
+    disc = SimpleNamespace(nx=24, nz=24, fov=(-0.003, 0.003, -0.003, 0.003))
+    probe = SimpleNamespace(n_det=32, radius=0.02, angular_coverage=135.0, fs=4e7,
+                            n_samples=900, delay=0.0, eir=None, eir_length=65)
+    model = SimpleNamespace(Discretization=disc, Probe=probe, c=1500.0, fmin=1e5, fmax=12e6,
+                            norm=1.0)
+    om = M.Model(M.ArcProbe(n_det=32, radius=0.02, coverage_deg=135.0, n_samples=900,
+                            eir_length=65), M.Grid(24, 24, disc.fov), c=1500.0, norm=1.0)
+    rng = np.random.default_rng(3)
+    b = om.forward(rng.random((1, 24, 24)))[0]
+    rec, t_full = bench.oracle_solve(model, b, 2, 6)
+    assert rec.shape == (24, 24) and rec.min() >= 0 and t_full > 0
+    _, t_one = bench.oracle_solve(model, b, 1, bench.ONE_THREAD_ITERS)
+    assert t_one > 0
