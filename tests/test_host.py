@@ -215,3 +215,38 @@ def test_new_entry_points_reject_bad_arguments_without_a_device():
         rc = call()
         assert rc == -1, where
         assert where in L.msot_last_error(), (where, L.msot_last_error())
+
+
+def test_last_error_is_per_thread():
+    """msot_last_error() reports the calling thread's own last failure: two
+    threads that fail in different entry points at the same time each read
+    their own message (argument checks only, no device work)."""
+    import threading
+    from msot_gb300 import _lib
+    L = _lib.load(build_if_missing=True)
+    start = threading.Barrier(2)
+    seen = {}
+
+    def worker(name, call, where):
+        start.wait()
+        msgs = []
+        for _ in range(200):
+            assert call() == -1
+            msgs.append(L.msot_last_error())
+        seen[name] = (where, msgs)
+
+    h = ctypes.c_void_p()
+    threads = [
+        threading.Thread(target=worker, args=(
+            "plan", lambda: L.msot_plan_create(None, ctypes.byref(h)), b"plan")),
+        threading.Thread(target=worker, args=(
+            "tune", lambda: L.msot_tune_set(b"no_such_knob", 1), b"tune_set")),
+    ]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert set(seen) == {"plan", "tune"}
+    for where, msgs in seen.values():
+        assert all(where in m for m in msgs), (where, set(msgs))
+    assert not any(b"tune_set" in m for m in seen["plan"][1])
