@@ -9,18 +9,14 @@
  */
 #include "mex.h"
 #include "msot_gpu.h"
+#include "msot_mex_inputs.h"
+
+static const msot_mex_input kInputs[] = {
+    {false, "image"}, {false, "travelTimes"}, {true, "numTimesteps"},
+    {false, "circularInterpolationRadiusInSamples"}};
 
 void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
-    if (nrhs != 4) mexErrMsgIdAndTxt("forwardMex:nrhs", "four inputs required.");
-    if (!mxIsDouble(prhs[0]) || mxIsComplex(prhs[0]))
-        mexErrMsgIdAndTxt("forwardMex:notDouble", "image must be type double.");
-    if (!mxIsDouble(prhs[1]) || mxIsComplex(prhs[1]))
-        mexErrMsgIdAndTxt("forwardMex:notDouble", "travelTimes must be type double.");
-    if (!mxIsInt32(prhs[2]))
-        mexErrMsgIdAndTxt("forwardMex:notInt32", "numTimesteps must be type int32.");
-    if (!mxIsDouble(prhs[3]) || mxIsComplex(prhs[3]))
-        mexErrMsgIdAndTxt("forwardMex:notDouble",
-                          "circularInterpolationRadiusInSamples must be type double.");
+    msot_mex_check_inputs(nrhs, prhs, kInputs, 4);
     const int W = (int)mxGetM(prhs[0]), P = (int)mxGetN(prhs[0]);
     const int D = (int)mxGetN(prhs[1]);
     const int T = (int)mxGetScalar(prhs[2]);

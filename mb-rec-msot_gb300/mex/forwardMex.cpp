@@ -5,13 +5,15 @@
  */
 #include "mex.h"
 #include "msot_gpu.h"
+#include "msot_mex_inputs.h"
+
+static const msot_mex_input kInputs[] = {
+    {false, "image"}, {true, "sirIndices"}, {false, "travelTimes"}, {false, "sir"},
+    {true, "numTimesteps"}, {true, "sirTimestepsStartAndEnd"},
+    {false, "circularInterpolationRadiusInSamples"}};
 
 void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
-    if (nrhs != 7) mexErrMsgIdAndTxt("forwardMex:nrhs", "seven inputs required.");
-    if (!mxIsDouble(prhs[0]) || !mxIsInt32(prhs[1]) || !mxIsDouble(prhs[2]) ||
-        !mxIsDouble(prhs[3]) || !mxIsInt32(prhs[4]) || !mxIsInt32(prhs[5]) ||
-        !mxIsDouble(prhs[6]))
-        mexErrMsgIdAndTxt("forwardMex:class", "wrong input class (see forwardMex.cpp:30-50).");
+    msot_mex_check_inputs(nrhs, prhs, kInputs, 7);
     const int W = (int)mxGetM(prhs[0]), P = (int)mxGetN(prhs[0]);
     const int D = (int)mxGetN(prhs[1]);
     const int S = (int)mxGetM(prhs[3]), NS = (int)mxGetN(prhs[3]);

@@ -6,12 +6,13 @@
  */
 #include "mex.h"
 #include "msot_gpu.h"
+#include "msot_mex_inputs.h"
+
+static const msot_mex_input kInputs[] = {
+    {false, "sigMat"}, {false, "travelTimes"}, {false, "circularInterpolationRadiusInSamples"}};
 
 void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
-    if (nrhs != 3) mexErrMsgIdAndTxt("forwardMex:nrhs", "three inputs required.");
-    for (int i = 0; i < 3; ++i)
-        if (!mxIsDouble(prhs[i]) || mxIsComplex(prhs[i]))
-            mexErrMsgIdAndTxt("forwardMex:notDouble", "inputs must be type double.");
+    msot_mex_check_inputs(nrhs, prhs, kInputs, 3);
     const int W = (int)mxGetM(prhs[0]);
     const int T = (int)mxGetDimensions(prhs[0])[1];
     const int P = (int)mxGetM(prhs[1]), D = (int)mxGetN(prhs[1]);

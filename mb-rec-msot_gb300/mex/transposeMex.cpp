@@ -5,12 +5,14 @@
  */
 #include "mex.h"
 #include "msot_gpu.h"
+#include "msot_mex_inputs.h"
+
+static const msot_mex_input kInputs[] = {
+    {false, "sigMat"}, {true, "sirIndices"}, {false, "travelTimes"}, {false, "sir"},
+    {true, "sirTimestepsStartAndEnd"}, {false, "circularInterpolationRadiusInSamples"}};
 
 void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
-    if (nrhs != 6) mexErrMsgIdAndTxt("forwardMex:nrhs", "six inputs required.");
-    if (!mxIsDouble(prhs[0]) || !mxIsInt32(prhs[1]) || !mxIsDouble(prhs[2]) ||
-        !mxIsDouble(prhs[3]) || !mxIsInt32(prhs[4]) || !mxIsDouble(prhs[5]))
-        mexErrMsgIdAndTxt("forwardMex:class", "wrong input class (see transposeMex.cpp:30-50).");
+    msot_mex_check_inputs(nrhs, prhs, kInputs, 6);
     const int W = (int)mxGetM(prhs[0]);
     const int T = (int)mxGetDimensions(prhs[0])[1];
     const int P = (int)mxGetM(prhs[1]), D = (int)mxGetN(prhs[1]);

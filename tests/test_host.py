@@ -250,3 +250,58 @@ def test_last_error_is_per_thread():
     for where, msgs in seen.values():
         assert all(where in m for m in msgs), (where, set(msgs))
     assert not any(b"tune_set" in m for m in seen["plan"][1])
+
+
+def test_mex_gateways_raise_the_reference_error_ids(tmp_path):
+    """Each gateway, given one input of the wrong class at a time, raises the
+    error ID and message the reference's MEX raises for it
+    (forwardMex.cpp:30-50, transposeMex.cpp:30-47,
+    forwardDelayAndSumMex.cpp:27-38, transposeDelayAndSumMex.cpp:26-34).
+    Where the reference's MEX code was compiled (x86 hosts) the harness calls
+    it too and the two must agree line by line; elsewhere the gateways are
+    checked against the expected IDs.  No device work: every call stops at
+    the class check."""
+    import shutil
+    import subprocess
+    from msot_gb300 import _build, _lib
+    from oracle import native
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    lib = _lib.lib_path()
+    if not os.path.exists(lib):
+        _build.build()
+    shim = os.path.join(ROOT, "oracle", "mex_shim")
+    inc = os.path.join(ROOT, "include")
+    objs = []
+    for name in ("forwardDelayAndSumMex", "transposeDelayAndSumMex", "forwardMex",
+                 "transposeMex"):
+        o = str(tmp_path / f"{name}.o")
+        src = os.path.join(ROOT, "mb-rec-msot_gb300", "mex", name + ".cpp")
+        subprocess.run(["g++", "-std=c++17", "-O1", "-fPIC", f"-DmexFunction=gw_{name}",
+                        "-I", shim, "-I", inc, "-c", src, "-o", o], check=True)
+        objs.append(o)
+    with_ref = native.ref_available()
+    exe = str(tmp_path / "harness")
+    cmd = ["g++", "-std=c++17", "-O1", "-I", shim,
+           os.path.join(ROOT, "tests", "mex_error_harness.cpp"), *objs, "-o", exe,
+           "-L", os.path.dirname(lib), "-lmsotgpu", "-Wl,-rpath," + os.path.dirname(lib)]
+    if with_ref:
+        cmd[3:3] = ["-DWITH_REF"]
+        cmd += [native.REF_PATH, "-Wl,-rpath," + os.path.dirname(native.REF_PATH), "-fopenmp"]
+    subprocess.run(cmd, check=True)
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.splitlines()
+    rows = {}
+    for line in out:
+        who, name, k, rest = line.split(" ", 3)
+        rows[(who, name, int(k))] = rest
+    classes = {"forwardDelayAndSumMex": "ddid", "transposeDelayAndSumMex": "ddd",
+               "forwardMex": "diddiid", "transposeMex": "diddid"}
+    for name, cl in classes.items():
+        for k, c in enumerate(cl):
+            got = rows[("gw", name, k)]
+            want_id = "forwardMex:notInt32" if c == "i" else "forwardMex:notDouble"
+            assert got.startswith(want_id + "|"), (name, k, got)
+            assert got.endswith(" must be type int32." if c == "i" else " must be type double.")
+            if with_ref:
+                assert got == rows[("ref", name, k)], (name, k, got, rows[("ref", name, k)])
+        assert rows[("gw", name, -1)].startswith("forwardMex:nrhs|"), name
