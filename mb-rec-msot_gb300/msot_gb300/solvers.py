@@ -167,19 +167,35 @@ def rec_nn_with_TV_reg(model: MSOTmodel, data_filt, num_iter: int, regParam: flo
     return rec, e1, e2, np.zeros(0), t
 
 
-def SB_ITV2(g, mu: float, *, stream=None):
-    """SB_ITV2.m:1 on a batch of square images g [W, n, n] (or one [n, n])."""
+def SB_ITV2(g, mu: float, B=None, Bt=None, BtB=None, *, stream=None):
+    """SB_ITV2.m:1 on a batch of square images g [W, n, n] (or one [n, n]).
+
+    B, Bt, BtB: the reference's caller passes DiffOper(n) (PsiForTVReg.m:6,
+    rec_nn_with_TV_reg.m:41); the kernel applies that operator itself, so
+    they are accepted for the signature and only their shapes are checked."""
     t = torch.as_tensor(g)
+    if t.dim() < 2 or t.shape[-1] != t.shape[-2]:
+        raise ValueError("SB_ITV2 needs square images")
+    n2 = t.shape[-1] * t.shape[-1]
+    for name, op, shape in (("B", B, (2 * n2, n2)), ("Bt", Bt, (n2, 2 * n2)),
+                            ("BtB", BtB, (n2, n2))):
+        if op is not None and tuple(op.shape) != shape:
+            raise ValueError(f"{name} must be DiffOper({t.shape[-1]}) of shape {shape}")
     if not t.is_cuda:
         t = t.cuda()
     squeeze = t.dim() == 2
     t = t.to(torch.float32).reshape(-1, t.shape[-2], t.shape[-1]).contiguous()
-    if t.shape[-1] != t.shape[-2]:
-        raise ValueError("SB_ITV2 needs square images")
     u = torch.empty_like(t)
     _lib.check(_lib.load().msot_sb_itv2(C.c_void_p(t.data_ptr()), C.c_void_p(u.data_ptr()),
                                         t.shape[0], t.shape[-1], float(mu), _stream_ptr(stream)))
     return u[0] if squeeze else u
+
+
+def SB_ITV(g, mu: float, *, stream=None):
+    """SB_ITV.m:1: SB_ITV2 with the difference operator built inside (the
+    denoising library's own entry point; its progress prints are not
+    reproduced)."""
+    return SB_ITV2(g, mu, stream=stream)
 
 
 def ITV(x, *, stream=None):

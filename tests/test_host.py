@@ -305,3 +305,22 @@ def test_mex_gateways_raise_the_reference_error_ids(tmp_path):
             if with_ref:
                 assert got == rows[("ref", name, k)], (name, k, got, rows[("ref", name, k)])
         assert rows[("gw", name, -1)].startswith("forwardMex:nrhs|"), name
+
+
+def test_sb_itv2_mirror_takes_the_reference_signature():
+    """SB_ITV2(g, mu, B, Bt, BtB) as PsiForTVReg.m:6 calls it: the operators
+    of DiffOper(n) are accepted (the kernel applies that operator itself) and
+    operators of another size are refused before any device work; SB_ITV is
+    the library's own two-argument entry point."""
+    import inspect
+    import msot_gb300 as m
+    from oracle import solvers as S
+    assert list(inspect.signature(m.SB_ITV2).parameters)[:5] == ["g", "mu", "B", "Bt", "BtB"]
+    assert list(inspect.signature(m.SB_ITV).parameters)[:2] == ["g", "mu"]
+    B, Bt, BtB = S.diff_oper(5)
+    g = np.zeros((6, 6))
+    for bad in ((B, None, None), (None, Bt, None), (None, None, BtB)):
+        with pytest.raises(ValueError, match="DiffOper"):
+            m.SB_ITV2(g, 0.1, *bad)
+    with pytest.raises(ValueError, match="square"):
+        m.SB_ITV2(np.zeros((6, 5)), 0.1)
