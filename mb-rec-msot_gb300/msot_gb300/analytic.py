@@ -3,7 +3,9 @@ signatures (reconstruction_backprojection/).
 
 Layouts: sigMat [W, D, T] (== MATLAB T x D x W) as a torch CUDA tensor or
 numpy array; fov given by the pixel coordinate vectors x (columns) and z
-(rows) of the meshgrid (Discretization.m:28-34); images [W, nx, nz].
+(rows) of the meshgrid (Discretization.m:28-34), or by the meshgrid matrices
+themselves as the reference passes them (region.xPositionsFov /
+zPositionsFov, Nz x Nx, reconstruct_dmas_cf.m:6-7); images [W, nx, nz].
 """
 from __future__ import annotations
 
@@ -30,13 +32,29 @@ def _vec(v):
     return np.ascontiguousarray(np.asarray(v, dtype=np.float64).ravel())
 
 
+def _fov_axis(v, axis: str) -> np.ndarray:
+    """The coordinate vector of one fov argument: a vector as given, or from
+    an Nz x Nx meshgrid matrix its first row (x: constant down each column)
+    or its first column (z: constant along each row)."""
+    a = np.asarray(v, dtype=np.float64)
+    if a.ndim <= 1 or min(a.shape) == 1:
+        return _vec(a)
+    if a.ndim != 2:
+        raise ValueError(f"fov_{axis} must be a vector or an Nz x Nx meshgrid matrix")
+    vec = a[0, :] if axis == "x" else a[:, 0]
+    grid = np.broadcast_to(vec[None, :] if axis == "x" else vec[:, None], a.shape)
+    if not np.array_equal(a, grid):
+        raise ValueError(f"fov_{axis} is not a meshgrid of {axis} coordinates")
+    return _vec(vec)
+
+
 def dmas_cf(sigMat, x, z, speed_of_sound, sampling_frequency,
             cropped_or_unrecorded_signals_at_sinogram_start, angular_coverage, detector_radius,
             stream=None):
     """dmas_cf.m:19: returns (p0_rec_dmas_cf, p0_rec_dmas, cf, p0_rec_das)."""
     s = _sig(sigMat)
     W, D, T = s.shape
-    xv, zv = _vec(x), _vec(z)
+    xv, zv = _fov_axis(x, "x"), _fov_axis(z, "z")
     outs = [torch.empty((W, xv.size, zv.size), device=s.device) for _ in range(4)]
     _lib.check(_lib.load().msot_dmas_cf(
         C.c_void_p(s.data_ptr()), W, D, T, _dptr(xv), xv.size, _dptr(zv), zv.size,
@@ -64,7 +82,7 @@ def backproject_waveeq(sigMat, x, z, speed_of_sound, sampling_frequency,
     mirrored in x by its final fliplr (backproject_waveeq.m:49)."""
     s = _sig(sigMat)
     W, D, T = s.shape
-    xv, zv = _vec(x), _vec(z)
+    xv, zv = _fov_axis(x, "x"), _fov_axis(z, "z")
     psf = np.atleast_2d(np.asarray(psf, dtype=np.float64))
     psf_cm = np.ascontiguousarray(psf.T)  # column-major m x n
     if isinstance(K, torch.Tensor) and K.is_cuda:

@@ -12,6 +12,7 @@ from __future__ import annotations
 
 import ctypes as C
 from dataclasses import dataclass
+from types import SimpleNamespace
 
 import numpy as np
 import torch
@@ -105,6 +106,15 @@ class Discretization:
         self.dx = self.x[1] - self.x[0]
         self.dz = self.z[1] - self.z[0]
         self.sigma = round(min(self.dx, self.dz) / 2 * 1e6) / 1e6
+        # region.xPositionsFov / zPositionsFov: the Nz x Nx meshgrid matrices
+        # of Discretization.m:34, for code written against the MATLAB class
+        X, Z = np.meshgrid(self.x, self.z)
+        self.region = SimpleNamespace(xPositionsFov=X, zPositionsFov=Z)
+        self.sizeOfPixelGrid = (self.nx, self.nz)
+
+    @property
+    def numberOfPixels(self) -> int:
+        return self.nx * self.nz
 
     @property
     def number_of_pixels(self) -> int:

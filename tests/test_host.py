@@ -324,3 +324,37 @@ def test_sb_itv2_mirror_takes_the_reference_signature():
             m.SB_ITV2(g, 0.1, *bad)
     with pytest.raises(ValueError, match="square"):
         m.SB_ITV2(np.zeros((6, 5)), 0.1)
+
+
+def test_analytic_mirror_accepts_the_reference_meshgrids():
+    """dmas_cf / backproject_waveeq receive region.xPositionsFov and
+    zPositionsFov, Nz x Nx meshgrid matrices (reconstruct_dmas_cf.m:6-7);
+    the mirror reads the same coordinate vectors from them as from plain
+    vectors, and refuses a matrix that is not a meshgrid."""
+    from msot_gb300 import analytic as A
+    x = np.linspace(-1e-3, 1e-3, 7)
+    z = np.linspace(-2e-3, 1e-3, 5)
+    X, Z = np.meshgrid(x, z)  # Nz x Nx, as MATLAB's meshgrid
+    assert np.array_equal(A._fov_axis(X, "x"), x)
+    assert np.array_equal(A._fov_axis(Z, "z"), z)
+    assert np.array_equal(A._fov_axis(x, "x"), x)
+    assert np.array_equal(A._fov_axis(z[:, None], "z"), z)
+    with pytest.raises(ValueError, match="meshgrid"):
+        A._fov_axis(Z, "x")
+    with pytest.raises(ValueError, match="meshgrid"):
+        A._fov_axis(np.random.default_rng(0).random((5, 7)), "z")
+
+
+def test_discretization_exposes_the_reference_region():
+    """Discretization.region.xPositionsFov / zPositionsFov are MATLAB's
+    meshgrid(x, z) (Discretization.m:34), Nz x Nx, and numberOfPixels /
+    sizeOfPixelGrid follow the reference's names."""
+    from msot_gb300 import Discretization
+    from msot_gb300 import analytic as A
+    d = Discretization([-0.005, 0.005, -0.004, 0.006], (9, 7))
+    X, Z = d.region.xPositionsFov, d.region.zPositionsFov
+    assert X.shape == (7, 9) and Z.shape == (7, 9)
+    assert np.array_equal(X[0], d.x) and np.array_equal(Z[:, 0], d.z)
+    assert d.numberOfPixels == 63 and d.sizeOfPixelGrid == (9, 7)
+    assert np.array_equal(A._fov_axis(X, "x"), d.x)
+    assert np.array_equal(A._fov_axis(Z, "z"), d.z)
