@@ -16,11 +16,13 @@
  *   - Host-buffer entry points (msot_mex_*) take FP64 arrays in exactly the
  *     column-major layouts of the reference MEX functions and do all device
  *     transfers themselves.
- *   - A plan is immutable after creation and may be used from several host
- *     threads on different streams, except for the functions documented as
- *     using the plan's scratch (msot_forward, msot_transpose,
- *     msot_interp_transpose and the solvers), which must not overlap on the
- *     GPU for one plan.
+ *   - A plan's tables are immutable after creation and the plan may be used
+ *     from several host threads on different streams, except for the
+ *     functions documented as using the plan's scratch (msot_forward,
+ *     msot_transpose, msot_interp_transpose and the solvers, which also keep
+ *     their captured graphs in the plan), which must not overlap on the GPU
+ *     for one plan, and msot_autotune, which changes the plan's kernel
+ *     choices and runs alone on it.
  */
 #ifndef MSOT_GPU_H
 #define MSOT_GPU_H
