@@ -358,3 +358,64 @@ def test_discretization_exposes_the_reference_region():
     assert d.numberOfPixels == 63 and d.sizeOfPixelGrid == (9, 7)
     assert np.array_equal(A._fov_axis(X, "x"), d.x)
     assert np.array_equal(A._fov_axis(Z, "z"), d.z)
+
+
+class _FakeLib:
+    """Records the C-ABI calls a Python wrapper makes (returns MSOT_OK)."""
+
+    def __init__(self):
+        self.calls = []
+
+    def __getattr__(self, name):
+        def call(*args):
+            self.calls.append((name, args))
+            return 0
+        return call
+
+
+def _host_only(monkeypatch):
+    """Run the wrappers' host logic without a device: tensors stay on the
+    CPU and the library is a recorder."""
+    import torch
+    from msot_gb300 import _lib, analytic, solvers
+    fake = _FakeLib()
+    monkeypatch.setattr(_lib, "load", lambda *a, **k: fake)
+    monkeypatch.setattr(torch.Tensor, "cuda", lambda self, *a, **k: self)
+    monkeypatch.setattr(analytic, "_stream_ptr", lambda stream=None: None)
+    monkeypatch.setattr(solvers, "_stream_ptr", lambda stream=None: None)
+    return fake
+
+
+def test_analytic_wrappers_pass_the_grid_sizes(monkeypatch):
+    """dmas_cf and backproject_waveeq hand the library the sinogram shape and
+    the fov vector lengths, whether the fov comes as vectors or as the
+    reference's meshgrids."""
+    from msot_gb300 import analytic as A
+    fake = _host_only(monkeypatch)
+    x = np.linspace(-1e-3, 1e-3, 7)
+    z = np.linspace(-2e-3, 1e-3, 5)
+    X, Z = np.meshgrid(x, z)
+    sig = np.zeros((3, 16, 40), dtype=np.float32)
+    for fx, fz in ((x, z), (X, Z)):
+        outs = A.dmas_cf(sig, fx, fz, 1500.0, 4e7, 0, 135.0, 0.04)
+        name, args = fake.calls[-1]
+        assert name == "msot_dmas_cf" and args[1:4] == (3, 16, 40)
+        assert args[5] == 7 and args[7] == 5
+        assert all(tuple(o.shape) == (3, 7, 5) for o in outs)
+        out = A.backproject_waveeq(sig, fx, fz, 1500.0, 4e7, 0, 135.0, 0.04, np.ones((1, 1)),
+                                   np.eye(40))
+        name, args = fake.calls[-1]
+        assert name == "msot_backproject_waveeq" and args[1:4] == (3, 16, 40)
+        assert args[5] == 7 and args[7] == 5 and tuple(out.shape) == (3, 7, 5)
+
+
+def test_sb_itv2_wrapper_passes_batch_and_size(monkeypatch):
+    from msot_gb300 import solvers as S
+    from oracle import solvers as OS
+    fake = _host_only(monkeypatch)
+    B, Bt, BtB = OS.diff_oper(6)
+    u = S.SB_ITV2(np.zeros((4, 6, 6)), 0.05, B, Bt, BtB)
+    name, args = fake.calls[-1]
+    assert name == "msot_sb_itv2" and args[2:5] == (4, 6, 0.05)
+    assert tuple(u.shape) == (4, 6, 6)
+    assert tuple(S.SB_ITV(np.zeros((6, 6)), 0.05).shape) == (6, 6)
