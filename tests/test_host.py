@@ -419,3 +419,53 @@ def test_sb_itv2_wrapper_passes_batch_and_size(monkeypatch):
     assert name == "msot_sb_itv2" and args[2:5] == (4, 6, 0.05)
     assert tuple(u.shape) == (4, 6, 6)
     assert tuple(S.SB_ITV(np.zeros((6, 6)), 0.05).shape) == (6, 6)
+
+
+def test_model_and_solver_wrappers_marshal_the_plan(monkeypatch):
+    """MSOTmodel's host logic without a device: the plan descriptor carries
+    the grid, T = samples - crop, the interpolation radius of
+    MSOTmodel.m:36-38 (dz / (c / fs)), an odd IR and the prefilter taps; the
+    operators and rec_nn_with_L2_reg pass batch, iterations and lambda; the
+    batch limit is enforced on the host."""
+    from msot_gb300 import MSOTmodel, Discretization, Probe, rec_nn_with_L2_reg
+    from msot_gb300 import model as Mo
+    fake = _host_only(monkeypatch)
+    monkeypatch.setattr(Mo, "_stream_ptr", lambda stream=None: None)
+    probe = Probe(n_det=32, radius=0.02, angular_coverage=135.0, n_samples=900, eir_length=65)
+    disc = Discretization([-0.003, 0.003, -0.002, 0.002], (24, 20))
+    m = MSOTmodel(probe, disc, 1500.0, False, True, 10, 1e5, 12e6, 2.5, max_batch=4)
+    creates = [a for n, a in fake.calls if n == "msot_plan_create"]
+    d = creates[-1][0]._obj
+    assert (d.nx, d.nz, d.n_det, d.n_t, d.max_batch) == (24, 20, 32, 890, 4)
+    assert abs(d.radius - disc.dz / (1500.0 / probe.fs)) < 1e-12
+    assert d.ir_len % 2 == 1 and d.pre_len_x % 2 == 1 and d.pre_len_z % 2 == 1
+    assert d.norm == 2.5
+    y = m.Funcs.applyForward(np.zeros((3, 24, 20), dtype=np.float32))
+    name, args = fake.calls[-1]
+    assert name == "msot_forward" and args[3] == 3 and tuple(y.shape) == (3, 32, 890)
+    x = m.Funcs.applyTranspose(y)
+    assert fake.calls[-1][0] == "msot_transpose" and tuple(x.shape) == (3, 24, 20)
+    with pytest.raises(ValueError, match="max_batch"):
+        m.Funcs.applyForward(np.zeros((5, 24, 20), dtype=np.float32))
+    rec = rec_nn_with_L2_reg(m, np.zeros((2, 32, 890), dtype=np.float32), 7, 1e-2)[0]
+    name, args = fake.calls[-1]
+    assert name == "msot_rec_nn_with_L2_reg" and args[3:6] == (2, 7, 1e-2)
+    assert tuple(rec.shape) == (2, 24, 20)
+
+
+def test_preprocessor_splits_batches_into_max_cols(monkeypatch):
+    """Preprocessor applies a batch of columns in chunks of at most max_cols
+    (the scratch it was created for), covering every column once."""
+    from msot_gb300 import preprocess as P
+    fake = _host_only(monkeypatch)
+    monkeypatch.setattr(P, "_stream_ptr", lambda stream=None: None)
+    p = P.Preprocessor(100, 10, (2, 20.0, 70.0), 4e7, 1e5, 12e6, max_cols=7)
+    name, args = [c for c in fake.calls if c[0] == "msot_prep_create"][-1]
+    assert args[:3] == (100, 10, 2) and args[8] == 7
+    x = np.zeros((3, 5, 100), dtype=np.float32)  # 15 columns
+    out = p(x)
+    applies = [a for n, a in fake.calls if n == "msot_prep_apply"]
+    assert [a[3] for a in applies] == [7, 7, 1]
+    assert tuple(out.shape) == (3, 5, 90)
+    with pytest.raises(ValueError, match="samples"):
+        p(np.zeros((2, 99), dtype=np.float32))
