@@ -203,7 +203,7 @@ int msot_rec_nn_with_L2_reg(msot_plan_t plan, const float *d_b, float *d_rec, in
                             double *err_img, double *err_reg, void *stream);
 
 /* Warm start of both splitting variables of nnls_L2_less (no reference
- * counterpart: the reference starts w and v from zero, nnls_L2_less.m:94-95).
+ * counterpart: the reference starts w and v from zero, nnls_L2_less.m:28-29).
  * d_w0 seeds the image w, d_v0 the multiplier v; at the method's fixed point
  * v = (A'(A w - b) + lambdaL2 w) / beta on the zero set of w and 0 elsewhere
  * (beta = 1e-3), which is what a consistent warm start supplies. */
@@ -309,7 +309,7 @@ int msot_unet_check(msot_unet_t net);
 /* Raw-sinogram pre-processing, in the order of
  * reconstruction_example_script.m:24-26, along the time axis of every column
  * ([n_cols][T_raw] FP32 on the device, t fastest = MATLAB T x D x W):
- *   crop_first_n_signals.m:12          the first n_crop samples are dropped;
+ *   crop_first_n_signals.m:2          the first n_crop samples are dropped;
  *   apply_butterworth_window_to_sinogram.m:5-9  (window_order > 0)
  *       x = mean + (x - mean) |h|, h the order-window_order Butterworth
  *       band-pass with cut-offs [window_low, window_high] / T (in samples,

@@ -1,7 +1,7 @@
 // geometry.cu -- the model's geometry tables on the GPU.
 //
 //   msot_travel_times <- MSOTmodel.m:350-382 (calculate_travel_time with one
-//                        speed of sound: straight rays, refraction.m:327):
+//                        speed of sound: straight rays, refraction.m:20-24):
 //                        tau[d][p] = |x_p - x_d| / c * fs - delay - n_crop,
 //                        detector angles from Probe.m:112-116.
 //

@@ -6,7 +6,7 @@
 //                 pixel model, applied here as two short stencils.
 //   k_das_fwd     forwardDelayAndSumMex.cpp:72-103: scatter of tri-interpolated
 //                 pixels into one detector column held in shared memory.
-//   k_das_adj     transposeDelayAndSumMex.cpp:67-100: gather per pixel over all
+//   k_das_adj     transposeDelayAndSumMex.cpp:67-97: gather per pixel over all
 //                 detectors, 8x8 pixel patch x 4 detector groups per CTA.
 //   k_sir_fwd     forwardMex.cpp:118-160 (SIR column convolved with the tri
 //                 taps, samples outside [0, T) dropped).
@@ -536,7 +536,7 @@ __global__ void __launch_bounds__(256) k_sir_fwd(const int32_t *__restrict__ tau
 // ---------------------------------------------------------------------------
 // SIR adjoint: per (pixel, detector) v_k = sum_i f[i] y[tb + i + k - S/2] for
 // k in the SIR column's [start, end], x += sum_k h[k] v_k; y outside [0, T)
-// counts as zero (transposeMex.cpp:298).
+// counts as zero (transposeMex.cpp:136).
 // ---------------------------------------------------------------------------
 template <int WT, int NT>
 __global__ void __launch_bounds__(256) k_sir_adj(const int32_t *__restrict__ tiles,

@@ -1,6 +1,6 @@
 // preprocess.cu -- raw-sinogram pre-processing on the GPU, in the order of
 // reconstruction_example_script.m:24-26:
-//   crop_first_n_signals.m:12               drop the first n_crop samples
+//   crop_first_n_signals.m:2               drop the first n_crop samples
 //   apply_butterworth_window_to_sinogram.m:5-9
 //       x <- mean + (x - mean) |h(t)|, h = freqz of an order-n Butterworth
 //       band-pass with cut-offs [low, high] / T (in samples), T points on

@@ -8,11 +8,11 @@
 // reconstructions), or the whole batch shares one set (coupled = the W
 // wavelengths of one reference call, whose lsqr/cgs see one stacked vector).
 //
-//   rec_nn_with_L2_reg  -> rec_nn_with_L2_reg.m:24-63, nnls_L2_less.m:93-141,
+//   rec_nn_with_L2_reg  -> rec_nn_with_L2_reg.m:24-63, nnls_L2_less.m:27-101,
 //                          lsqr (Paige & Saunders) on [sqrt(lam) [A; sqrt(lamL2) I];
 //                          sqrt(beta) I] with maxit 2, x0 = w, tol 1e-8.
 //   rec_nn_with_L1_eye  -> rec_nn_with_L1_eye_reg.m:21-47,
-//                          nnls_L1_eye_matrix_less.m:76-107, cgs on lam A^T A + I.
+//                          nnls_L1_eye_matrix_less.m:26-65, cgs on lam A^T A + I.
 //   estimate_norm       -> the sigma_max of MSOTmodel.m:277-278 by power
 //                          iteration.
 #include <cmath>

@@ -266,7 +266,7 @@ class MSOTmodel:
         self.n_t = int(probe.n_samples - self.n_crop)
         self.max_batch = int(max_batch)
         disc = discretization
-        # travel-time indices (MSOTmodel.m:380-381; straight rays, refraction.m:327,
+        # travel-time indices (MSOTmodel.m:380-381; straight rays, refraction.m:20-24,
         # or refracted at the membrane), computed on the GPU in FP64
         if self.use_single_speed_of_sound:
             compute = lambda: (travel_times(probe, disc, self.c, self.n_crop), None)

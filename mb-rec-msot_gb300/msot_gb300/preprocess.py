@@ -61,7 +61,7 @@ class Preprocessor:
 
 
 def crop_first_n_signals(data_raw, n_signals_to_crop: int):
-    """crop_first_n_signals.m:11-13 (time is the last axis here)."""
+    """crop_first_n_signals.m:1-3 (time is the last axis here)."""
     x = _columns(data_raw)
     return x[..., int(n_signals_to_crop):].contiguous()
 

@@ -7,7 +7,7 @@ slices are W independent reconstructions (one reference call each); with
 ``coupled=True`` they are the wavelengths of ONE reference call (the
 reference's lsqr/cgs then see one stacked vector).  ``x0`` is an optional
 warm start (the reference's L2/TV cores always start from zero,
-nnls_L2_less.m:94).
+nnls_L2_less.m:28-29).
 """
 from __future__ import annotations
 

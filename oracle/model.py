@@ -10,7 +10,7 @@ product.  It restates, in FP64:
   * the shift-invariant prefilter     Discretization.m:46-51, :74-86,
                                       shift_inv_proj.m:66-71
   * project / transpose-project       Discretization.m:54-72
-  * single-SoS travel-time indices    MSOTmodel.m:350-382, refraction.m:324-328
+  * single-SoS travel-time indices    MSOTmodel.m:350-382, refraction.m:20-24
   * dual-SoS (Fermat) travel times    refraction.m:8-24, fermat_principle.m:17-24
   * interpolation radius              MSOTmodel.m:35-38
   * the impulse response (no SIR)     MSOTmodel.m:329-348
@@ -245,7 +245,7 @@ def convolve_ir_transpose(sino_wdt: np.ndarray, ir: np.ndarray) -> np.ndarray:
 # ----------------------------------------------------------------------------
 def travel_time_indices(probe: ArcProbe, grid: Grid, c: float, n_crop: int = 0) -> np.ndarray:
     """(D, P) fractional sample indices, MSOTmodel.m:380-381 with straight
-    rays (refraction.m:327): |x_p - x_d| / c * fs - delay - n_crop."""
+    rays (refraction.m:23): |x_p - x_d| / c * fs - delay - n_crop."""
     xd, zd = probe.positions()
     X, Z = grid.pixel_xz()
     dist = np.sqrt((xd[:, None] - X[None, :]) ** 2 + (zd[:, None] - Z[None, :]) ** 2)

@@ -12,7 +12,7 @@
  * any host (the reference itself needs x86 AVX intrinsics and does not build
  * on aarch64):
  *   orc_forward_das    <- forwardDelayAndSumMex.cpp:72-103
- *   orc_transpose_das  <- transposeDelayAndSumMex.cpp:67-100
+ *   orc_transpose_das  <- transposeDelayAndSumMex.cpp:67-97
  *   orc_forward_sir    <- forwardMex.cpp:100-161
  *   orc_transpose_sir  <- transposeMex.cpp:97-158 (file lines 259-320 of the
  *                         concatenated listing; loop over pixels outermost)

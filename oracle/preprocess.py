@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY ("the oracle"): imported by tests/ only.
 
-  * crop_first_n_signals.m:11-13
+  * crop_first_n_signals.m:1-3
   * apply_butterworth_window_to_sinogram.m:1-10 (butter band-pass, zp2tf,
     freqz at T points of [0, pi), |h|)
   * filter_butter_zero_phase.m:16-48 (use_fft = true), via

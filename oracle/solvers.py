@@ -24,10 +24,10 @@ implementations of the same published algorithms (tests/test_oracle.py);
 SpaRSA has no such second implementation here.
 
 Solver sources restated:
-  rec_nn_with_L2_reg.m:1-66, nnls_L2_less.m:27-143 (aug operator :145-167),
+  rec_nn_with_L2_reg.m:1-66, nnls_L2_less.m:27-77 (aug operator :79-101),
   incorporate_l2_reg_into_model_functions.m:1-23,
   combine_forward_and_transpose_with_reg.m:1-10,
-  rec_nn_with_L1_eye_reg.m:1-49, nnls_L1_eye_matrix_less.m:26-115,
+  rec_nn_with_L1_eye_reg.m:1-49, nnls_L1_eye_matrix_less.m:26-65,
   rec_nn_with_TV_reg.m:1-55, nnls_sparsa_based_reg_matrix_less.m:31-86,
   PsiForTVReg.m, PhiForTVReg.m, SplitBregmanTVdenoising/SB_ITV2.m:20-40,
   DiffOper.m:1-7, ITV.m:5-6.
@@ -134,9 +134,9 @@ def cgs(Aop, b, tol, maxit):
 # L2-regularised NNLS
 # ----------------------------------------------------------------------------
 def nnls_L2_less(Aaug, Aaug_t, target, n_img, lam, beta, n_iter, n_inner, w0=None):
-    """nnls_L2_less.m:93-141.  ``Aaug`` is the operator [A; sqrt(lamL2) I]
+    """nnls_L2_less.m:27-72 (loop :51-72).  ``Aaug`` is the operator [A; sqrt(lamL2) I]
     (combine_forward_and_transpose_with_reg.m), target = [b; 0].  w0 seeds the
-    iterate (the reference starts from zero, nnls_L2_less.m:94)."""
+    iterate (the reference starts from zero, nnls_L2_less.m:28-29)."""
     w = np.zeros(n_img) if w0 is None else np.array(w0, dtype=np.float64)
     v = np.zeros(n_img)
     m = target.size
@@ -235,7 +235,7 @@ def rec_nn_with_L2_reg(fwd, adj, b, n_img, num_iter, lambdaL2, w0=None, lambdaL2
 # L1 (identity) NNLS by split Bregman
 # ----------------------------------------------------------------------------
 def nnls_L1_eye_matrix_less(fwd, adj, b, u0, eta, lam, n_iter, cg_iter):
-    """nnls_L1_eye_matrix_less.m:76-107: d = P(u - bp);
+    """nnls_L1_eye_matrix_less.m:26-57 (loop :38-54): d = P(u - bp);
     rhs = P(d) + bp + lam A^T b - lam eta; u = cgs(lam A^T A + I, rhs, 1e-8, 2);
     bp += P(d) - u."""
     bp = np.zeros_like(u0)

@@ -247,7 +247,7 @@ def test_l2_nnls_oracle_is_nonnegative_and_fits():
 
 
 def test_l2_nnls_oracle_converges_to_scipy_nnls():
-    """The splitting of nnls_L2_less.m:93-141 (beta = 1e-3, two LSQR steps
+    """The splitting of nnls_L2_less.m:51-72 (beta = 1e-3, two LSQR steps
     per iteration) approaches the minimiser of |A x - b|^2 + lambda |x|^2,
     x >= 0, that scipy's active-set NNLS (Lawson & Hanson) finds on the
     augmented system; A has unit norm as the normalised model does."""
@@ -268,7 +268,7 @@ def test_l2_nnls_oracle_converges_to_scipy_nnls():
 
 
 def test_l1_nnls_oracle_minimises_nonnegative_lasso():
-    """nnls_L1_eye_matrix_less.m:76-107 is split Bregman for
+    """nnls_L1_eye_matrix_less.m:38-54 is split Bregman for
     min 1/2 |A u - b|^2 + eta sum(u), u >= 0.  With an accurate inner solve
     (30 CGS steps) it reaches the minimiser that projected FISTA finds.  The
     reference's own setting (2 CGS steps from zero per iteration) stalls about
