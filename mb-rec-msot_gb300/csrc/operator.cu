@@ -1,18 +1,31 @@
 // operator.cu -- sm_103a kernels of the model-based operator A and A^T.
 //
-//   k_prefilter   separable circular prefilter (Discretization.m:54-72); the
-//                 2-D filter conj(phi_hat/|phi_hat|^2) of shift_inv_proj.m:67-71
-//                 factors into one circular filter per axis for the Gaussian
-//                 pixel model, applied here as two short stencils.
-//   k_das_fwd     forwardDelayAndSumMex.cpp:72-103: scatter of tri-interpolated
-//                 pixels into one detector column held in shared memory.
-//   k_das_adj     transposeDelayAndSumMex.cpp:67-97: gather per pixel over all
-//                 detectors, 8x8 pixel patch x 4 detector groups per CTA.
+//   k_prefilter2d  the prefilter of Discretization.m:54-72 in one pass: the
+//                  2-D filter conj(phi_hat/|phi_hat|^2) of shift_inv_proj.m:67-71
+//                  factors into one circular filter per axis for the Gaussian
+//                  pixel model; both axes from a shared-memory tile.
+//                  k_prefilter (one axis per launch) serves single-axis plans
+//                  and the SIR path's pixel order.
+//   k_to_pixmajor / k_permute  instance-major image -> the pixel-major (and,
+//                  with SIR, tile-permuted) order the interpolation gathers.
+//   k_das_fwd3     forwardDelayAndSumMex.cpp:72-103 restated exactly by the
+//                  bucket decomposition of the tri taps: per (time tile,
+//                  detector, instances) CTA, bucket moments over the pixels
+//                  whose travel time falls in each sample, then the 2F+2-tap
+//                  filter over the moments; no atomics.
+//   k_das_adj4 + k_sum_parts  transposeDelayAndSumMex.cpp:67-97: per 64x64
+//                  pixel block and detector group, the block's sinogram span
+//                  filtered once into bucket tables in shared memory; groups'
+//                  partial images summed in fixed order.
 //   k_sir_fwd     forwardMex.cpp:118-160 (SIR column convolved with the tri
 //                 taps, samples outside [0, T) dropped).
 //   k_sir_adj     transposeMex.cpp:115-158 (its exact adjoint).
-//   k_conv        convolve_with_IR / transpose_convolve_with_IR
-//                 (MSOTmodel.m:259-269) as a direct FIR over each detector column.
+//   k_conv_fft1k  convolve_with_IR / transpose_convolve_with_IR
+//                 (MSOTmodel.m:259-269) by overlap-save with 1024-point FFTs,
+//                 two real columns per complex transform; with EPI set it also
+//                 writes the L2 solver's LSQR sinogram update (IRs up to 513
+//                 taps).  k_conv_fft (4096 points) takes IRs of 514-2049
+//                 taps, the direct FIR k_conv longer ones.
 //
 // Fixed-point travel times: tau_fx = tau * 2^fb (int32).  The taps of a
 // (pixel, detector) pair are t in [ceil((tau_fx - r_fx)/2^fb),

@@ -1,7 +1,9 @@
 // timing.cu -- kernel launch counter and optional CUDA-event timing of the
 // hot kernels (used by the benchmark to measure the dominant kernel's
 // duration live, and by tests).  Off by default: when disabled a timed scope
-// costs one branch.
+// costs one branch.  Also the L2 gather probe (k_l2_gather_probe): the rate
+// of random 32-byte loads from an L2-resident buffer, the ceiling of the DAS
+// interpolation kernels.
 #include <atomic>
 #include <mutex>
 #include <vector>

@@ -6,7 +6,14 @@
 //                 cgs(I + B'B, g - B'(b - d), 1e-5, 100) from zero, outer loop
 //                 until ||u_prev - u|| / ||u|| <= 1e-3 (capped at TV_SB_MAX
 //                 sweeps).  One CTA per image runs the whole prox on the
-//                 device (bounded loops, no host round trips).
+//                 device (bounded loops, no host round trips), vectors in
+//                 global memory.
+//   k_tv_prox_cl / k_tv_prox_cl4  the same prox by one thread-block cluster
+//                 per image, the image split into column slabs held in
+//                 shared memory (neighbours over distributed shared memory);
+//                 cl4 handles 4 z-pixels per thread, and its GM form keeps
+//                 the vectors in an L2-resident workspace for images too large
+//                 for shared memory.  k_tv_prox is the fallback.
 //   k_itv      <- ITV.m:5-6 (isotropic TV with MATLAB's gradient: central
 //                 differences inside, one-sided at the borders).
 //   msot_rec_nn_with_TV_reg <- rec_nn_with_TV_reg.m:20-54 and
@@ -22,6 +29,9 @@
 // the first block differences along z, the second along x, so (I + B'B) is a
 // five-point stencil with one-sided rows at the borders.  Where SB_ITV2.m:34
 // divides 0 by 0 (|Bu + b| = 0) the shrinkage here writes d = 0.
+//
+// msot_autotune (k_tune_fill fills its timing inputs) is also here: it times
+// the kernel variants of a plan on its own geometry.
 //
 // All SpaRSA scalars (objective, alpha, mu = tau/alpha, stop flags) live on
 // the device, so an outer iteration is a fixed launch sequence with no host
