@@ -476,9 +476,11 @@ __global__ void k_sum_parts(const float *__restrict__ part, float *__restrict__ 
 }
 
 // ---------------------------------------------------------------------------
-// SIR forward: as k_das_fwd, but each (pixel, detector) pair deposits the
-// SIR column convolved with its NT tri taps: e[m] = sum_i f[i] h[m - i],
-// output sample tb + m - S/2, dropped outside [0, T) (forwardMex.cpp:139).
+// SIR forward: CTA = (detector, pixel slice, WT instances) with the
+// detector's output column [WT][T] in shared memory; each (pixel, detector)
+// pair deposits the SIR column convolved with its NT tri taps,
+// e[m] = sum_i f[i] h[m - i], at output sample tb + m - S/2 by shared-memory
+// atomics, dropped outside [0, T) (forwardMex.cpp:139).
 // ---------------------------------------------------------------------------
 template <int WT, int NT>
 __global__ void __launch_bounds__(256) k_sir_fwd(const int32_t *__restrict__ tau_pi,
