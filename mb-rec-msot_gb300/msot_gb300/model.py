@@ -84,6 +84,29 @@ class Probe:
             raise ValueError("EIR length must be odd")
         return e
 
+    # Read-only views under the MATLAB class's field names (Probe.m:101-127),
+    # for code written against the reference's model struct.
+    @property
+    def detector(self):
+        xd, zd = self.detector_positions()
+        return SimpleNamespace(numOfTransducers=self.n_det, radius=self.radius,
+                               angularCoverage=self.angular_coverage,
+                               xPositionsOfTransducers=xd, zPositionsOfTransducers=zd,
+                               EIR=self.eir_taps())
+
+    @property
+    def DAC(self):
+        return SimpleNamespace(numRecordedSamplesPerTransducer=self.n_samples,
+                               delayBeforeRecording=self.delay, frequency=self.fs)
+
+    @property
+    def coupling(self):
+        return SimpleNamespace(speedOfSound=self.coupling_speed_of_sound)
+
+    @property
+    def eirLength(self) -> int:
+        return int(self.eir_taps().size)
+
 
 # ----------------------------------------------------------------------------
 # Discretization (Discretization.m)
@@ -360,6 +383,33 @@ class MSOTmodel:
         _lib.check(_lib.load().msot_estimate_norm(self._plan, int(iters), int(seed),
                                                   C.byref(out), _stream_ptr()))
         return float(out.value)
+
+    # --- the reference's model struct fields (MSOTmodel.m:18-48), read-only -------
+    @property
+    def Medium(self):
+        return SimpleNamespace(speedOfSound=self.c)
+
+    @property
+    def DataPreprocessing(self):
+        return SimpleNamespace(numCroppedSamplesAtSinogramStart=self.n_crop,
+                               filtCutoffMin=self.fmin, filtCutoffMax=self.fmax)
+
+    @property
+    def Data(self):
+        """numTimeSamplesPerTransducer, absoluteTravelTimeIndices ([n_det][P],
+        memory-identical to MATLAB's P x D) and
+        circularInterpolationRadiusInSamples."""
+        return SimpleNamespace(numTimeSamplesPerTransducer=self.n_t,
+                               absoluteTravelTimeIndices=self.travel,
+                               circularInterpolationRadiusInSamples=self.radius)
+
+    @property
+    def useSingleSpeedOfSound(self) -> bool:
+        return self.use_single_speed_of_sound
+
+    @property
+    def includeSir(self) -> bool:
+        return self.include_sir
 
     # --- operators ----------------------------------------------------------------
     @property

@@ -469,3 +469,41 @@ def test_preprocessor_splits_batches_into_max_cols(monkeypatch):
     assert tuple(out.shape) == (3, 5, 90)
     with pytest.raises(ValueError, match="samples"):
         p(np.zeros((2, 99), dtype=np.float32))
+
+
+def test_model_struct_views_run_reference_style_code(monkeypatch):
+    """Code written against the reference's model struct runs on the mirror:
+    reconstruct_dmas_cf.m:4-12 reads the fov meshgrids, Medium, DAC,
+    DataPreprocessing and detector fields; the views carry the mirror's
+    values (host logic only, library calls recorded)."""
+    from msot_gb300 import MSOTmodel, Discretization, Probe
+    from msot_gb300 import analytic as A
+    from msot_gb300 import model as Mo
+    fake = _host_only(monkeypatch)
+    monkeypatch.setattr(Mo, "_stream_ptr", lambda stream=None: None)
+    probe = Probe(n_det=32, radius=0.02, angular_coverage=135.0, n_samples=900, delay=3.0,
+                  eir_length=65)
+    model = MSOTmodel(probe, Discretization([-0.003, 0.003], 24), 1480.0, False, True, 10, 1e5,
+                      12e6, 1.0)
+    assert model.Probe.detector.numOfTransducers == 32 and model.Probe.eirLength == 65
+    assert model.Probe.DAC.frequency == probe.fs and model.Probe.DAC.delayBeforeRecording == 3.0
+    assert model.Medium.speedOfSound == 1480.0
+    assert model.DataPreprocessing.numCroppedSamplesAtSinogramStart == 10
+    assert model.Data.numTimeSamplesPerTransducer == 890
+    assert model.Data.circularInterpolationRadiusInSamples == model.radius
+    assert model.useSingleSpeedOfSound and not model.includeSir
+    sinogram = np.zeros((1, 32, 890), dtype=np.float32)
+    A.dmas_cf(sinogram,
+              model.Discretization.region.xPositionsFov,
+              model.Discretization.region.zPositionsFov,
+              model.Medium.speedOfSound,
+              model.Probe.DAC.frequency,
+              model.DataPreprocessing.numCroppedSamplesAtSinogramStart
+              + model.Probe.DAC.delayBeforeRecording,
+              model.Probe.detector.angularCoverage,
+              model.Probe.detector.radius)
+    name, args = fake.calls[-1]
+    assert name == "msot_dmas_cf" and args[5] == 24 and args[7] == 24
+    assert args[8:13] == (1480.0, probe.fs, 13.0, 135.0, 0.02)
+    A.reconstruct_dmas_cf(model, sinogram)
+    assert fake.calls[-1][1][8:13] == args[8:13]
