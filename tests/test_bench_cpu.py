@@ -72,3 +72,21 @@ def test_cpu_baseline_leg_runs_a_bounded_sample():
     assert rec.shape == (24, 24) and rec.min() >= 0 and t_full > 0
     _, t_one = bench.oracle_solve(model, b, 1, bench.ONE_THREAD_ITERS)
     assert t_one > 0
+
+
+def test_clock_summary_parses_the_nvidia_smi_samples(tmp_path):
+    """The clocks object bench.py attaches to its JSON line: median SM clock
+    under load, the maximum clock, and every throttle reason seen Active."""
+    import bench
+    path = tmp_path / "clocks.csv"
+    path.write_text(
+        "0, 2070, 2070, 900.1, 0x0, Not Active, Not Active, Not Active, Not Active\n"
+        "0, 1980, 2070, 1390.5, 0x4, Not Active, Not Active, Not Active, Active\n"
+        "0, 2070, 2070, 1200.0, 0x0, Not Active, Not Active, Not Active, Not Active\n"
+        "garbage line\n")
+    c = bench.Clocks(0, str(path))
+    c.proc = object()  # samples already written; no nvidia-smi here
+    s = c.summary()
+    assert s["sm_mhz"] == 2070.0 and s["sm_max_mhz"] == 2070.0 and s["samples"] == 3
+    assert s["reasons"] == ["sw_power_cap"]
+    assert path.exists()  # a file the caller named is kept
