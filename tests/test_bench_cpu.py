@@ -90,3 +90,19 @@ def test_clock_summary_parses_the_nvidia_smi_samples(tmp_path):
     assert s["sm_mhz"] == 2070.0 and s["sm_max_mhz"] == 2070.0 and s["samples"] == 3
     assert s["reasons"] == ["sw_power_cap"]
     assert path.exists()  # a file the caller named is kept
+
+
+def test_roofline_bytes_per_launch():
+    """Algorithmic bytes behind roofline.achieved at the bench's batch of 64:
+    FP32 travel table 4PD + image 4PW + sinogram 4TDW for an interpolation
+    launch (about 154 MB), read + write of the sinogram for the IR
+    convolution, of the image for the prefilter."""
+    import bench
+    P, D, T, W = 128 * 128, 256, 2030, 64
+    fwd = bench.algorithmic_bytes("interp_forward", W)
+    assert fwd == 4 * P * D + 4 * P * W + 4 * T * D * W
+    assert abs(fwd / 1e6 - 154.0) < 1.0
+    assert bench.algorithmic_bytes("interp_adjoint", W) == fwd
+    assert bench.algorithmic_bytes("ir_conv", W) == 8 * T * D * W
+    assert bench.algorithmic_bytes("prefilter", W) == 8 * P * W
+    assert bench.algorithmic_bytes("something_else", W) is None
