@@ -23,6 +23,16 @@ product.  It restates, in FP64:
 Layout: sinograms are numpy (W, D, T) C-order (== MATLAB T x D x W) and
 images (W, Nx, Nz) C-order (== MATLAB Nz x Nx x W); pixel p = ix*Nz + iz.
 
+Pins: the interpolation inside forward / transpose runs through the C
+restatement of the MEX loops (msot_oracle.c), bit-identical to the
+reference's compiled MEX code.  The MATLAB wrapper steps around it have no
+MATLAB run to compare with (parity unpinned against MATLAB itself); they are
+checked against independent computations in tests/test_oracle.py instead.
+Those checks are: the separable prefilter against the 2-D FFT prefilter, the
+FFT zero-phase filter against forward-backward IIR filtering, the adjoint
+test, the power-iteration norm against an SVD, and one pixel's sinogram
+located by both this model's transpose and the analytic reconstructors.
+
 Deviations recorded for the synthetic probe used by this project: the EIR
 length is a probe property (odd, e.g. 257) instead of the reference's fixed
 201 (Probe.m:13); the crop uses floor(L/2) of that length, so the output keeps
