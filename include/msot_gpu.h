@@ -197,7 +197,11 @@ int msot_estimate_norm(msot_plan_t plan, int iters, uint64_t seed, double *sigma
  * always starts from zero).  err_img/err_reg (optional host arrays of
  * `batch` doubles) receive lCurveErrImg / lCurveErrReg per instance. */
 
-/* rec_nn_with_L2_reg.m:1 with RegL2 = identity (lambdaL2 <= 0: no reg). */
+/* rec_nn_with_L2_reg.m:1 with RegL2 = identity (lambdaL2 <= 0: no reg).
+ * When err_img is given and an instance's final residual ||A x - b||^2 is
+ * NaN or Inf (NaN / Inf in its data or start), returns MSOT_ENONFINITE naming
+ * the first such instance; the images are still written.  The same holds
+ * for the _warm and _2 forms below. */
 int msot_rec_nn_with_L2_reg(msot_plan_t plan, const float *d_b, float *d_rec, int batch,
                             int num_iter, double lambdaL2, const float *d_x0, int coupled,
                             double *err_img, double *err_reg, void *stream);

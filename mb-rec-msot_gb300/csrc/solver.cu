@@ -606,6 +606,7 @@ static int solve_l2(Plan &pl, const float *b_in, float *rec, int W, int num_iter
     const double sr2 = has_reg && lambdaL2_2 > 0 ? std::sqrt(lambdaL2_2) : 0.0;
     float *wv = wk.i[7], *vm = wk.i[8];
     const float *b = wk.s3;
+    int nonfinite = -1;  // first instance whose final residual is NaN / Inf
     do {
         MSOT_CUDA_TRY(cudaMemcpyAsync(wk.s3, b_in, NS * sizeof(float), cudaMemcpyDeviceToDevice, st));
         if (x0)
@@ -681,7 +682,10 @@ static int solve_l2(Plan &pl, const float *b_in, float *rec, int W, int num_iter
                 Ctx ci = c;
                 ci.coupled = 0;
                 if ((rc = group_sumsq(ci, wk.s2, b, NS, c.nbs, e))) break;
-                for (int w = 0; w < W; ++w) err_img[w] = e[w];
+                for (int w = 0; w < W; ++w) {
+                    err_img[w] = e[w];
+                    if (nonfinite < 0 && !std::isfinite(e[w])) nonfinite = w;
+                }
             }
             if (err_reg) {
                 Ctx ci = c;
@@ -707,6 +711,13 @@ static int solve_l2(Plan &pl, const float *b_in, float *rec, int W, int num_iter
             rc = MSOT_ECUDA;
         }
     } while (0);
+    if (rc == MSOT_OK && nonfinite >= 0) {
+        // the reference returns the NaN image silently; here the caller learns
+        // of it (the image is still written)
+        set_error("rec_nn_with_L2_reg: non-finite residual ||A x - b||^2 for instance %d "
+                  "(NaN or Inf in the data or the start)", nonfinite);
+        rc = MSOT_ENONFINITE;
+    }
     cudaEventRecord(sc->ev_out, st);
     cudaStreamWaitEvent(user, sc->ev_out, 0);
     return rc;

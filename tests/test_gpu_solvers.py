@@ -179,3 +179,20 @@ def test_l2_second_regulariser_needs_the_first(norm_pair):
                            laplacian_per_wavelength)[0]
     p = rec_nn_with_L2_reg(pm, bt, 5, 0.0)[0]
     assert torch.equal(a, p)
+
+
+def test_l2_solver_reports_nonfinite_data(norm_pair):
+    """A NaN in one instance's sinogram: the solve returns MSOT_ENONFINITE
+    naming that instance (the reference would return a NaN image silently),
+    and the plan solves finite data normally afterwards."""
+    import torch
+    from msot_gb300 import rec_nn_with_L2_reg
+    from msot_gb300._lib import MsotError
+    pm, om = norm_pair
+    _, b = _data(om, 64, 3, 23)
+    bad = torch.tensor(b, dtype=torch.float32)
+    bad[1, 5, 100] = float("nan")
+    with pytest.raises(MsotError, match="non-finite residual .* instance 1"):
+        rec_nn_with_L2_reg(pm, bad, 5, 1e-2)
+    rec, e_img, _, _, _, _ = rec_nn_with_L2_reg(pm, torch.tensor(b, dtype=torch.float32), 5, 1e-2)
+    assert torch.isfinite(rec).all() and np.isfinite(e_img).all()
