@@ -234,7 +234,8 @@ int msot_rec_nn_with_L2_reg_2(msot_plan_t plan, const float *d_b, float *d_rec, 
 int msot_laplacian_per_wavelength(const float *d_in, float *d_out, int batch, int nx, int nz,
                                   void *stream);
 
-/* rec_nn_with_L1_eye_reg.m:1 */
+/* rec_nn_with_L1_eye_reg.m:1.  MSOT_ENONFINITE as for the L2 solver when an
+ * instance's final residual is NaN or Inf (err_img given). */
 int msot_rec_nn_with_L1_eye_reg(msot_plan_t plan, const float *d_b, float *d_rec, int batch,
                                 int num_iter, double reg, const float *d_x0, int coupled,
                                 double *err_img, double *err_reg, void *stream);

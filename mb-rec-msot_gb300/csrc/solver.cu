@@ -911,6 +911,7 @@ static int solve_l1(const Plan &pl, const float *b, float *rec, int W, int num_i
     float *vh = rhs;
     int rc = MSOT_OK;
     float *atmp = nullptr, *uh = nullptr;
+    int nonfinite = -1;  // first instance whose final residual is NaN / Inf
     do {
         if (cudaMalloc(&atmp, NI * sizeof(float)) != cudaSuccess ||
             cudaMalloc(&uh, NI * sizeof(float)) != cudaSuccess) {
@@ -961,7 +962,10 @@ static int solve_l1(const Plan &pl, const float *b, float *rec, int W, int num_i
             if (err_img) {
                 if ((rc = apply_forward(pl, rec, wk.s2, W, st))) break;
                 if ((rc = group_sumsq(ci, wk.s2, b, NS, c.nbs, e))) break;
-                for (int w = 0; w < W; ++w) err_img[w] = e[w];
+                for (int w = 0; w < W; ++w) {
+                    err_img[w] = e[w];
+                    if (nonfinite < 0 && !std::isfinite(e[w])) nonfinite = w;
+                }
             }
             if (err_reg) {
                 std::vector<float> h(NI);
@@ -981,6 +985,11 @@ static int solve_l1(const Plan &pl, const float *b, float *rec, int W, int num_i
             rc = MSOT_ECUDA;
         }
     } while (0);
+    if (rc == MSOT_OK && nonfinite >= 0) {
+        set_error("rec_nn_with_L1_eye_reg: non-finite residual ||A x - b||^2 for instance %d "
+                  "(NaN or Inf in the data or the start)", nonfinite);
+        rc = MSOT_ENONFINITE;
+    }
     cudaFree(atmp);
     cudaFree(uh);
     free_work(wk);

@@ -196,3 +196,20 @@ def test_l2_solver_reports_nonfinite_data(norm_pair):
         rec_nn_with_L2_reg(pm, bad, 5, 1e-2)
     rec, e_img, _, _, _, _ = rec_nn_with_L2_reg(pm, torch.tensor(b, dtype=torch.float32), 5, 1e-2)
     assert torch.isfinite(rec).all() and np.isfinite(e_img).all()
+
+
+def test_l1_solver_reports_nonfinite_data(norm_pair):
+    """As for L2: a NaN in one instance's sinogram gives MSOT_ENONFINITE
+    naming it, and finite data solve normally afterwards."""
+    import torch
+    from msot_gb300 import rec_nn_with_L1_eye_reg
+    from msot_gb300._lib import MsotError
+    pm, om = norm_pair
+    _, b = _data(om, 64, 3, 24)
+    bad = torch.tensor(b, dtype=torch.float32)
+    bad[2, 7, 300] = float("inf")
+    with pytest.raises(MsotError, match="non-finite residual .* instance 2"):
+        rec_nn_with_L1_eye_reg(pm, bad, 3, 1e-3)
+    rec, e_img, _, _, _ = rec_nn_with_L1_eye_reg(pm, torch.tensor(b, dtype=torch.float32), 3,
+                                                 1e-3)
+    assert torch.isfinite(rec).all() and np.isfinite(e_img).all()
