@@ -72,6 +72,11 @@ def test_cpu_baseline_leg_runs_a_bounded_sample():
     assert rec.shape == (24, 24) and rec.min() >= 0 and t_full > 0
     _, t_one = bench.oracle_solve(model, b, 1, bench.ONE_THREAD_ITERS)
     assert t_one > 0
+    # the TV and L1 modes' oracle legs on the same stand-in
+    rec_tv, t_tv = bench.oracle_tv_solve(model, b, 2, 5e-3, 2)
+    assert rec_tv.shape == (24, 24) and rec_tv.min() >= 0 and t_tv > 0
+    rec_l1, t_l1 = bench.oracle_l1_solve(model, b, 3, 1e-3, 2)
+    assert rec_l1.shape == (24, 24) and np.isfinite(rec_l1).all() and t_l1 > 0
 
 
 def test_clock_summary_parses_the_nvidia_smi_samples(tmp_path):
