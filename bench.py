@@ -471,7 +471,17 @@ def run_reference(args, rank):
     }
 
 
-FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12  # FMA pipe, nominal max clock
+def fp32_nominal_tflops() -> float:
+    """FP32 FMA-pipe rate of the current device at the measured maximum SM
+    clock: SMs x 128 lanes x 2 flops x clock."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            mhz = float(json.load(f)["sm_max_mhz"])
+    except Exception:
+        mhz = 2070.0
+    return sms * 128 * 2 * float(mhz) * 1e6 / 1e12
 
 
 def run_sweep(args):
@@ -549,9 +559,9 @@ def run_sweep(args):
             sec = res[k] / 1e3
             line[k] = {"gbs": alg_bytes / sec / 1e9, "hbm_frac": alg_bytes / sec / 1e9 / peak,
                        "tflops": flops / sec / 1e12,
-                       "fp32_frac_nominal": flops / sec / 1e12 / FP32_NOMINAL_TFLOPS}
+                       "fp32_frac_nominal": flops / sec / 1e12 / fp32_nominal_tflops()}
         line["peak_source"] = (f"{peak_kind} hbm_gbs (copy); "
-                               f"FP32 nominal {FP32_NOMINAL_TFLOPS:.1f} TF/s")
+                               f"FP32 nominal {fp32_nominal_tflops():.1f} TF/s")
         out.append(line)
         print(json.dumps(line), flush=True)
         del model

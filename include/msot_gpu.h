@@ -9,6 +9,8 @@
  *     No C++ exception crosses this boundary.
  *   - Device pointers are CUDA device memory of the current device; `stream`
  *     is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *   - A plan belongs to the device that was current when it was created;
+ *     a call on it with another device current returns MSOT_EINVAL.
  *   - Batched layouts are instance-major and FP32:
  *       image     [batch][nx][nz]       (pixel p = ix*nz + iz, MATLAB Nz x Nx)
  *       sinogram  [batch][n_det][n_t]   (MATLAB T x D x W)
@@ -99,14 +101,23 @@ int msot_interp_transpose(msot_plan_t plan, const float *d_raw, float *d_coeffs,
  * counterpart in the reference.  It is for callers that are not allowed to
  * allocate device memory, e.g. a host application whose device memory is
  * owned by another allocator or that runs under a fixed memory budget.  Its
- * partial sums live in a 16 MiB array inside the library (held on every
- * device that loads the library until the process exits) instead of the
- * plan's scratch, so the call performs no cudaMalloc / cudaFree.  Limit:
- * batch * nx * nz <= 4 Mi (4194304) elements, else MSOT_ERANGE.  The first
- * call on a device looks up the array's device address (cudaGetSymbolAddress)
- * with that device current; make that first call before any stream capture.
- * All calls share the one array: calls that overlap on the GPU (other streams
- * or threads) race and must be serialised by the caller. */
+ * partial sums live in a 16 MiB array inside the library instead of the
+ * plan's scratch, so the call performs no cudaMalloc / cudaFree.  The array
+ * belongs to the library's operator module: it is allocated when CUDA loads
+ * that module on a device and held there until the process exits.  Under
+ * lazy module loading (CUDA's default) that load can be the first call of
+ * this function on the device, so a caller with a fixed budget makes one
+ * warm-up call (or sets CUDA_MODULE_LOADING=EAGER) before its budget
+ * applies.  Limit: batch * nx * nz <= 4 Mi (4194304) elements, else
+ * MSOT_ERANGE.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current and keeps it for
+ * the process: this assumes the device's primary context (the CUDA runtime's
+ * own), with no cudaDeviceReset afterwards; make that first call before any
+ * stream capture.  The current device must be the plan's.  All calls share
+ * the one array: calls that overlap on the GPU (other streams or threads)
+ * race and must be serialised by the caller.  The detector groups differ
+ * from msot_interp_transpose's, so the result equals it up to the order of
+ * the FP32 partial sums, not bit for bit. */
 int msot_interp_transpose_noalloc(msot_plan_t plan, const float *d_raw, float *d_coeffs,
                                   int batch, void *stream);
 

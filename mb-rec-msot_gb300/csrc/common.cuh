@@ -32,6 +32,7 @@ constexpr int BLK_X = 64, BLK_Z = 64, BLK = BLK_X * BLK_Z;  // adjoint pixel blo
 constexpr int BLK_THREADS = 256, BLK_PPT = BLK / BLK_THREADS;  // 16 pixels per thread
 
 struct Plan {
+    int device = -1;   // CUDA device the plan's tables live on (current at creation)
     int nx, nz, P, D, T;
     double radius;
     int frac_bits;     // fixed-point fraction bits of tau
@@ -202,6 +203,15 @@ bool profiling_enabled();          // timing.cu
 int apply_transpose(const Plan &pl, const float *sino, float *img, int W, cudaStream_t st);
 
 inline int div_up(int a, int b) { return (a + b - 1) / b; }
+
+// MSOT_OK when the current device is the one the plan was created on, else
+// MSOT_EINVAL with a message naming `who`: every kernel of a call reads the
+// plan's tables, which live on that device only.  plan.cu
+int check_plan_device(const Plan &pl, const char *who);
+
+// Streaming multiprocessors of the current device (queried once per device,
+// cached; 1 if the query fails).  Launch heuristics size grids by it.  plan.cu
+int sm_count();
 
 }  // namespace msot
 

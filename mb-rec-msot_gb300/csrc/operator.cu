@@ -1018,7 +1018,7 @@ static int fwd_split(const Plan &pl, int nwt) {
     // enough CTAs to fill the GPU twice over
     int ctas = pl.D * nwt;
     int ns = 1;
-    while (ctas * ns < 2 * 152 && ns < 8) ns *= 2;
+    while (ctas * ns < 2 * sm_count() && ns < 8) ns *= 2;
     return ns;
 }
 
@@ -1085,7 +1085,7 @@ static int das_adj_launch(const Plan &pl, const float *raw, float *x, int W, flo
                         (size_t)WT * pl.blk_span_max * sizeof(float4);
     int rc;
     const int base = pl.n_blk * (W / WT);
-    int groups = std::max(1, std::min(pl.D, div_up(2 * 152, base)));
+    int groups = std::max(1, std::min(pl.D, div_up(2 * sm_count(), base)));
     groups = std::min(groups, std::max(1, pl.adj_groups_max * pl.max_batch / W));
     groups = std::min(groups, pl.adj_groups_max);
     const int dpg = div_up(pl.D, groups);
@@ -1448,7 +1448,7 @@ static int das_adj_launch_fixed(const Plan &pl, const float *raw, float *x, int 
     if ((rc = set_smem(k_das_adj4<WT, F>, smem)) != MSOT_OK) return rc;
     const size_t stride = (size_t)W * pl.P;
     const int base = pl.n_blk * (W / WT);
-    int groups = std::max(1, std::min(pl.D, div_up(2 * 152, base)));
+    int groups = std::max(1, std::min(pl.D, div_up(2 * sm_count(), base)));
     groups = std::min<size_t>(groups, NOALLOC_PART_FLOATS / stride);
     const int dpg = div_up(pl.D, groups);
     groups = div_up(pl.D, dpg);
@@ -1500,7 +1500,7 @@ static int check_batch(msot_plan_t plan, int batch, const void *a, const void *b
         set_error("batch %d exceeds the plan's max_batch %d", batch, plan->p.max_batch);
         return MSOT_EINVAL;
     }
-    return MSOT_OK;
+    return check_plan_device(plan->p, "operator");
 }
 
 extern "C" {
@@ -1550,6 +1550,7 @@ int msot_interp_transpose_noalloc(msot_plan_t plan, const float *d_raw, float *d
                   "supported");
         return MSOT_EINVAL;
     }
+    if (int rc0 = check_plan_device(pl, "interp_transpose_noalloc")) return rc0;
     if ((size_t)batch * pl.P > NOALLOC_PART_FLOATS) {
         set_error("interp_transpose_noalloc: batch x pixels = %zu exceeds the fixed scratch of "
                   "%zu floats",

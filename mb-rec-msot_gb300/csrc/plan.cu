@@ -29,6 +29,32 @@ const char *set_error(const char *fmt, ...) {
     return g_err;
 }
 
+int check_plan_device(const Plan &pl, const char *who) {
+    int dev = -1;
+    MSOT_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev != pl.device) {
+        set_error("%s: the plan was created on device %d but device %d is current", who,
+                  pl.device, dev);
+        return MSOT_EINVAL;
+    }
+    return MSOT_OK;
+}
+
+int sm_count() {
+    static std::atomic<int> cached[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 1;
+    if (dev < 64) {
+        const int c = cached[dev].load(std::memory_order_relaxed);
+        if (c > 0) return c;
+    }
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+        return 1;
+    if (dev < 64) cached[dev].store(n, std::memory_order_relaxed);
+    return n;
+}
+
 cudaError_t raise_max_dynamic_smem(const void *func, size_t bytes) {
     static std::mutex mu;
     static std::map<std::pair<int, const void *>, size_t> current;
@@ -104,6 +130,7 @@ static int build(const msot_plan_desc *d, Plan &p) {
         set_error("plan: grid too large");
         return MSOT_EINVAL;
     }
+    MSOT_CUDA_TRY(cudaGetDevice(&p.device));
     p.nx = d->nx;
     p.nz = d->nz;
     p.P = d->nx * d->nz;

@@ -1063,6 +1063,7 @@ extern "C" int msot_rec_nn_with_L2_reg(msot_plan_t plan, const float *d_b, float
         set_error("batch %d exceeds the plan's max_batch %d", batch, plan->p.max_batch);
         return MSOT_EINVAL;
     }
+    if (int rc = check_plan_device(plan->p, "solver")) return rc;
     return solve_l2(plan->p, d_b, d_rec, batch, num_iter, lambdaL2, d_x0, nullptr,
                     coupled ? 1 : 0, err_img, err_reg, (cudaStream_t)stream);
 }
@@ -1079,6 +1080,7 @@ extern "C" int msot_rec_nn_with_L2_reg_warm(msot_plan_t plan, const float *d_b, 
         set_error("batch %d exceeds the plan's max_batch %d", batch, plan->p.max_batch);
         return MSOT_EINVAL;
     }
+    if (int rc = check_plan_device(plan->p, "solver")) return rc;
     return solve_l2(plan->p, d_b, d_rec, batch, num_iter, lambdaL2, d_w0, d_v0,
                     coupled ? 1 : 0, err_img, err_reg, (cudaStream_t)stream);
 }
@@ -1096,6 +1098,7 @@ extern "C" int msot_rec_nn_with_L2_reg_2(msot_plan_t plan, const float *d_b, flo
         set_error("batch %d exceeds the plan's max_batch %d", batch, plan->p.max_batch);
         return MSOT_EINVAL;
     }
+    if (int rc = check_plan_device(plan->p, "solver")) return rc;
     return solve_l2(plan->p, d_b, d_rec, batch, num_iter, lambdaL2, d_x0, nullptr,
                     coupled ? 1 : 0, err_img, err_reg, (cudaStream_t)stream, lambdaL2_2,
                     err_reg2);
@@ -1126,6 +1129,7 @@ extern "C" int msot_rec_nn_with_L1_eye_reg(msot_plan_t plan, const float *d_b, f
         set_error("batch %d exceeds the plan's max_batch %d", batch, plan->p.max_batch);
         return MSOT_EINVAL;
     }
+    if (int rc = check_plan_device(plan->p, "solver")) return rc;
     return solve_l1(plan->p, d_b, d_rec, batch, num_iter, reg, d_x0, coupled ? 1 : 0, err_img,
                     err_reg, (cudaStream_t)stream);
 }
@@ -1136,5 +1140,6 @@ extern "C" int msot_estimate_norm(msot_plan_t plan, int iters, uint64_t seed, do
         set_error("estimate_norm: bad arguments");
         return MSOT_EINVAL;
     }
+    if (int rc = check_plan_device(plan->p, "estimate_norm")) return rc;
     return estimate_norm(plan->p, iters, seed, sigma_max, (cudaStream_t)stream);
 }

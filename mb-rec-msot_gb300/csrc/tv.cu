@@ -1165,7 +1165,9 @@ struct DevBufs {
     }
 };
 
-int blocks_per_instance(int W) { return std::max(1, std::min(64, (4 * 152 + W - 1) / W)); }
+int blocks_per_instance(int W) {
+    return std::max(1, std::min(64, (4 * sm_count() + W - 1) / W));
+}
 
 // 0: cluster path where it fits, 1: force the global-memory kernel
 std::atomic<int> g_prox_path{0};
@@ -1468,6 +1470,7 @@ int msot_rec_nn_with_TV_reg(msot_plan_t plan, const float *d_b, float *d_rec, in
         return MSOT_EINVAL;
     }
     const Plan &pl = plan->p;
+    if (int rc = check_plan_device(pl, "rec_nn_with_TV_reg")) return rc;
     if (pl.nx != pl.nz) {
         set_error("This TV implementation works only with square images!");
         return MSOT_EINVAL;
@@ -1645,6 +1648,7 @@ extern "C" int msot_autotune(msot_plan_t plan, int batch, void *stream, msot_tun
         return MSOT_EINVAL;
     }
     Plan &pl = plan->p;
+    if (int rc = check_plan_device(pl, "autotune")) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     const size_t NI = (size_t)batch * pl.P, NS = (size_t)batch * pl.D * pl.T;
     const bool tv_ok = pl.nx == pl.nz;

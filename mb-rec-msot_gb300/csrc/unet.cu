@@ -949,7 +949,7 @@ int conv_bwd(msot_unet *u, const ConvL &c, const float *x, const float *y, const
     if (g_unet_tc.load() && c.Ci >= 8) {
         const int tx = (c.S + TC_TX - 1) / TC_TX, ty = (c.S + TC_TY - 1) / TC_TY;
         const int tiles = tx * ty, cog = (c.Co + 127) / 128, cig = (c.Ci + 31) / 32;
-        const int splits = std::max(1, std::min(N * tiles, 148 / (cog * cig)));
+        const int splits = std::max(1, std::min(N * tiles, (sm_count() - 4) / (cog * cig)));
         MSOT_CUDA_TRY(raise_max_dynamic_smem((const void *)k_conv3_dw_tc, DW_SMEM));
         const int vec = (c.S % 4 == 0) && ((uintptr_t)x % 16 == 0) && ((uintptr_t)dy_pre % 16 == 0);
         KLAUNCH(k_conv3_dw_tc<<<dim3(cog, cig, splits), TC_THREADS, DW_SMEM, st>>>(
@@ -958,7 +958,7 @@ int conv_bwd(msot_unet *u, const ConvL &c, const float *x, const float *y, const
         const int tx = (c.S + CT - 1) / CT, tiles = tx * tx;
         const int cog = (c.Co + COT - 1) / COT, cig = (c.Ci + CIT - 1) / CIT;
         const int splits =
-            std::max(1, std::min(N * tiles, (4 * 152 + cog * cig - 1) / (cog * cig)));
+            std::max(1, std::min(N * tiles, (4 * sm_count() + cog * cig - 1) / (cog * cig)));
         KLAUNCH(k_conv3_dw<<<dim3(cog, cig, splits), 256, 0, st>>>(
             x, c.Ci, dy_pre, c.Co, u->grad + c.w_off, c.S, c.S, N, tx, tiles, splits));
     }
