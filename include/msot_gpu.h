@@ -356,8 +356,10 @@ int msot_butter_response(int order, int type, double wn1, double wn2, int n, int
  * tic/toc, e.g. rec_nn_with_L2_reg.m:44-49). */
 
 /* Autotuner (no reference counterpart): times the variants of the plan's
- * hot kernels on its own geometry at `batch` instances -- instances per CTA
- * of the DAS forward (8, 4, 2) and adjoint (2, 1), the register cap of the
+ * hot kernels on its own geometry at `batch` instances -- the DAS forward's
+ * kernel (image values staged in shared memory per time tile and detector
+ * group, or gathered per detector) and instances per CTA (8, 4, 2), the DAS
+ * adjoint's instances per CTA (2, 1), the register cap of the
  * IR convolution (1, 3, 4 resident CTAs per SM) and, for square grids, the
  * CTAs per image of the
  * SB_ITV2 cluster kernel (automatic, 1 .. 16) -- and keeps the fastest in
@@ -368,6 +370,7 @@ typedef struct msot_tuning {
     int fwd_wt, conv_min_blocks, tv_cluster;  /* 0 = the built-in choice */
     double fwd_ms, transpose_ms, tv_prox_ms;  /* per apply of the chosen variant */
     int adj_wt;                               /* instances per CTA of the DAS adjoint */
+    int fwd_staged;                           /* DAS forward: 1 staged, 2 per-detector buckets */
 } msot_tuning;
 int msot_autotune(msot_plan_t plan, int batch, void *stream, msot_tuning *out);
 
@@ -375,6 +378,13 @@ int msot_autotune(msot_plan_t plan, int batch, void *stream, msot_tuning *out);
  * float summation order):
  *   "tv_prox_cluster"  CTAs per image of the shared-memory SB_ITV2 kernel
  *                      (1, 2, 4, 8, 16; 0 = automatic).
+ *   "fwd_staged"       1 (default) = the DAS forward stages each CTA's image
+ *                      values in shared memory where the plan's tables fit,
+ *                      0 = per-detector L2 gathers (plans autotuned keep their pick).
+ *   "fwd_staged_tile", "fwd_staged_group"  time samples per CTA (8 .. 64) and
+ *                      detectors per CTA (1 .. 16) of the staged forward's
+ *                      tables in plans created afterwards; 0 (default) = the
+ *                      plan picks the shape that fits shared memory.
  *   "adj_prefetch"     1 (default) = the DAS adjoint loads the next detector's
  *                      samples into registers during the current one; 0 = off.
  *   "conv_min_blocks"  register cap of the IR convolution, as resident CTAs

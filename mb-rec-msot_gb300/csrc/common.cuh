@@ -19,6 +19,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cuda_runtime.h>
+#include <vector>
 
 #include "../../include/msot_gpu.h"
 
@@ -52,6 +53,17 @@ struct Plan {
     float ce1 = 0.f, ce2 = 0.f;    // (r - F)/r and (F + 1 - r)/r
     int32_t *fwd_off = nullptr;    // [D][T+1] CSR offsets of bucket b = floor(tau)
     int2 *fwd_ent = nullptr;       // [D][P] (tau fixed point, pixel) sorted by bucket
+    // staged forward (das_fwd_staged.cu): CTA = (time tile of st_tt samples,
+    // group of st_g detectors); st_tt == 0 when the plan has no such tables
+    int st_tt = 0, st_g = 0, st_ntiles = 0, st_ngroups = 0, st_ib = 0;
+    int st_umax = 0;               // largest pixel union of a CTA
+    int st_ent_cap = 0;            // largest entry count of a CTA, rounded up to 4
+    int st_off_stride = 0;         // ints per CTA in st_off
+    int st_threads = 0;            // threads per CTA
+    int4 *st_info = nullptr;       // [n_cta] {u_off, nU, e_off, n_ent}
+    int32_t *st_u = nullptr;       // pixel unions, ascending per CTA
+    int32_t *st_off = nullptr;     // [n_cta][st_off_stride] entry offsets per (detector, bucket)
+    uint32_t *st_ent = nullptr;    // entries (tau fraction << st_ib) | index in the union
     // adjoint pixel blocks of BLK_Z x BLK_X pixels; thread t of a CTA owns
     // the pixels (iz = t % BLK_Z, ix = t / BLK_Z + 4k), k < BLK_PPT
     int n_blk_x = 0, n_blk_z = 0, n_blk = 0;
@@ -66,6 +78,7 @@ struct Plan {
     int tune_adj_wt = 0;      // instances per CTA of the DAS adjoint (2, 1)
     int tune_conv_mb = 0;     // register cap of the IR convolution (1, 3, 4)
     int tune_tv_cluster = 0;  // CTAs per image of the SB_ITV2 cluster kernel
+    int tune_fwd_staged = 0;  // DAS forward kernel: 1 staged, 2 k_das_fwd3, 0 = g_fwd_staged
     // IR
     int L = 0, Lh = 0;
     float *ir_fwd = nullptr, *ir_adj = nullptr;
@@ -208,6 +221,37 @@ inline int div_up(int a, int b) { return (a + b - 1) / b; }
 // MSOT_EINVAL with a message naming `who`: every kernel of a call reads the
 // plan's tables, which live on that device only.  plan.cu
 int check_plan_device(const Plan &pl, const char *who);
+
+// time tile / detector group forced on the staged forward tables of plans
+// created from now on (0 = chosen by the plan); das_fwd_staged.cu
+extern std::atomic<int> g_st_force_tt, g_st_force_g;
+// staged DAS forward (das_fwd_staged.cu): builds the plan's st_* tables
+// from the fixed-point travel times tfx [D][P] and the per-detector bucket
+// CSR (foff [D][T+1], fent [D][P]); leaves st_tt = 0 when no tile shape fits
+int build_fwd_staged(Plan &p, const int32_t *tfx, const int32_t *foff, const int2 *fent,
+                     size_t &bytes);
+// the host-side tables of the staged forward before upload
+struct StTables {
+    int tt = 0, g = 0, ntiles = 0, ngroups = 0, ib = 0, umax = 0, ent_cap = 0, off_stride = 0,
+        threads = 0;
+    std::vector<int4> info;
+    std::vector<int32_t> ulist, offs;
+    std::vector<uint32_t> ent;
+};
+int build_fwd_staged_host(const Plan &p, const int32_t *tfx, const int32_t *foff,
+                          const int2 *fent, int dev_smem, StTables &t);
+size_t st_smem_bytes(const Plan &p, int wt);
+bool fwd_staged_fits(const Plan &p, int wt);
+// xt in the [W/wt][P][wt] layout of das_fwd_wt
+int launch_das_forward_staged(const Plan &p, const float *xt, float *raw, int W, int wt,
+                              float scale, cudaStream_t st);
+// reads (and with clear != 0 resets) the staged forward's timeout flag
+int fwd_staged_error(int clear);
+// staged forward on (1, default) or off (0); operator.cu
+extern std::atomic<int> g_fwd_staged;
+// instances per CTA of the DAS forward at batch W: the interpolation input is
+// laid out [W/wt][P][wt] (pixel-major within an instance tile).  operator.cu
+int das_fwd_wt(const Plan &pl, int W);
 
 // Streaming multiprocessors of the current device (queried once per device,
 // cached; 1 if the query fails).  Launch heuristics size grids by it.  plan.cu

@@ -52,12 +52,12 @@ __device__ __forceinline__ float tri_weight(int t, int32_t tau, int fb, float c1
 // ---------------------------------------------------------------------------
 // Prefilter: out = scale * sum_k h[k] in[w][pix - k (circular)] along one
 // axis.  Output layout: out_mode 0 = [W][P]; 1 = [W][P] with pixel perm[j] at
-// position j (scatter order); 2 = pixel-major [P][W].
+// position j (scatter order); 2 = [W/wt][P][wt] (pixel-major per instance tile).
 // ---------------------------------------------------------------------------
 __global__ void k_prefilter(const float *__restrict__ in, float *__restrict__ out,
                             const float *__restrict__ taps, int K, int nx, int nz, int W,
                             int along_x, int transpose, float scale,
-                            const int32_t *__restrict__ perm, int out_mode) {
+                            const int32_t *__restrict__ perm, int out_mode, int wt) {
     const int P = nx * nz;
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long)W * P) return;
@@ -83,7 +83,7 @@ __global__ void k_prefilter(const float *__restrict__ in, float *__restrict__ ou
         acc = fmaf(h, __ldg(src + s), acc);
     }
     if (out_mode == 2)
-        out[(size_t)j * W + w] = acc * scale;
+        out[((size_t)(w / wt) * P + j) * wt + w % wt] = acc * scale;
     else
         out[(size_t)w * P + j] = acc * scale;
 }
@@ -95,7 +95,7 @@ __global__ void k_prefilter(const float *__restrict__ in, float *__restrict__ ou
 // buffer, then filters along x into the TX output columns.  Each thread
 // slides a register window over 8 consecutive outputs, so a tap costs one
 // FMA and (8 + 2 KM) / 8 / (2 KM + 1) shared loads.  Taps are zero-padded to
-// the compile-time half width KM >= K.  out_mode 0 = [W][P], 2 = [P][W].
+// the compile-time half width KM >= K.  out_mode 0 = [W][P], 2 = [W/wt][P][wt].
 // ---------------------------------------------------------------------------
 constexpr int PF_TX = 32, PF_R = 8, PF_THREADS = 256;
 
@@ -108,7 +108,7 @@ template <int KM>
 __global__ void __launch_bounds__(PF_THREADS) k_prefilter2d(
     const float *__restrict__ in, float *__restrict__ out, const float *__restrict__ taps_x,
     const float *__restrict__ taps_z, int Kx, int Kz, int nx, int nz, int W, int transpose,
-    int out_mode) {
+    int out_mode, int wt) {
     constexpr int NC = PF_TX + 2 * KM;  // staged columns
     constexpr int NTAP = 2 * KM + 1;
     constexpr int NW = PF_THREADS / 32;
@@ -185,20 +185,20 @@ __global__ void __launch_bounds__(PF_THREADS) k_prefilter2d(
             if (ix >= nx) break;
             const size_t p = (size_t)ix * nz + z;
             if (out_mode == 2)
-                out[p * W + w] = acc[j];
+                out[((size_t)(w / wt) * nx * nz + p) * wt + w % wt] = acc[j];
             else
                 out[(size_t)w * nx * nz + p] = acc[j];
         }
     }
 }
 
-// [W][P] -> pixel-major [P][W]
+// [W][P] -> [W/wt][P][wt] (pixel-major within each tile of wt instances)
 __global__ void k_to_pixmajor(const float *__restrict__ in, float *__restrict__ out, int P,
-                              int W) {
+                              int W, int wt) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long)W * P) return;
     const int w = (int)(idx / P), j = (int)(idx % P);
-    out[(size_t)j * W + w] = __ldg(in + idx);
+    out[((size_t)(w / wt) * P + j) * wt + w % wt] = __ldg(in + idx);
 }
 
 // [W][P] -> [W][P] in scatter order (out[w][j] = in[w][perm[j]])
@@ -226,7 +226,8 @@ __global__ void k_permute(const float *__restrict__ in, float *__restrict__ out,
 // V_b = sum beta_k s[b+k]; each (pixel, detector) then adds
 // U + f V + e1 s[b-F] + e2 s[b+F+1].
 // ---------------------------------------------------------------------------
-// CTA = (tile of TB = 256 - 2F - 2 output samples, detector, WT instances).
+// CTA = (tile of TB = 256 - 2F - 2 output samples, detector, WT instances);
+// the image is [W/WT][P][WT].
 // Phase 1: one bucket per thread reduces the four moments of its pixels,
 // loading FWD_UNR (entry, pixel) pairs at a time; phase 2: each output sample
 // applies the (2F+2)-tap filter over the bucket moments.
@@ -283,7 +284,7 @@ __global__ void __launch_bounds__(256, 4) k_das_fwd3(const int32_t *__restrict__
                 for (int u = 0; u < FWD_UNR; ++u) q[u] = qn[u];
 #pragma unroll
                 for (int u = 0; u < FWD_UNR; ++u) {
-                    const float *xp = xpm + (size_t)max(q[u].y, 0) * W + w0;
+                    const float *xp = xpm + ((size_t)blockIdx.z * P + max(q[u].y, 0)) * WT;
                     if constexpr (WT % 4 == 0) {
 #pragma unroll
                         for (int i = 0; i < WT; i += 4) {
@@ -974,8 +975,9 @@ int launch_prefilter(const Plan &pl, const float *in, float *out, int W, bool tr
     const int K = along_x ? pl.Kx : pl.Kz;
     const float *taps = along_x ? pl.pre_x : pl.pre_z;
     const long n = (long)W * pl.P;
+    const int wt = out_mode == 2 ? das_fwd_wt(pl, W) : 1;
     KLAUNCH(k_prefilter<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
-        in, out, taps, K, pl.nx, pl.nz, W, along_x, transpose, scale, pl.perm, out_mode));
+        in, out, taps, K, pl.nx, pl.nz, W, along_x, transpose, scale, pl.perm, out_mode, wt));
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
 }
@@ -990,8 +992,10 @@ static int prefilter2d_km(const Plan &pl, const float *in, float *out, int W, bo
     if (smem > 200 * 1024) return 1;
     MSOT_CUDA_TRY(raise_max_dynamic_smem((const void *)k_prefilter2d<KM>, smem));
     const dim3 grid((unsigned)((pl.nx + PF_TX - 1) / PF_TX), (unsigned)W);
+    const int wt = out_mode == 2 ? das_fwd_wt(pl, W) : 1;
     KLAUNCH(k_prefilter2d<KM><<<grid, PF_THREADS, smem, st>>>(
-        in, out, pl.pre_x, pl.pre_z, pl.Kx, pl.Kz, pl.nx, pl.nz, W, transpose ? 1 : 0, out_mode));
+        in, out, pl.pre_x, pl.pre_z, pl.Kx, pl.Kz, pl.nx, pl.nz, W, transpose ? 1 : 0, out_mode,
+        wt));
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
 }
@@ -1025,12 +1029,13 @@ static int fwd_split(const Plan &pl, int nwt) {
 int launch_to_pixmajor(const Plan &pl, const float *in, float *out, int W, cudaStream_t st) {
     TimedScope ts_(KID_PERMUTE, st);
     const long n = (long)W * pl.P;
-    KLAUNCH(k_to_pixmajor<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, pl.P, W));
+    KLAUNCH(k_to_pixmajor<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, pl.P, W,
+                                                                         das_fwd_wt(pl, W)));
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
 }
 
-// DAS forward by bucket moments; xpm is pixel-major [P][W].
+// DAS forward by bucket moments; xpm is [W/WT][P][WT].
 template <int WT, int F>
 static int das_fwd_launch(const Plan &pl, const float *xpm, float *raw, int W, float scale,
                           cudaStream_t st) {
@@ -1063,11 +1068,25 @@ static int das_fwd_f(const Plan &pl, const float *xpm, float *raw, int W, float 
     }
 }
 
+std::atomic<int> g_fwd_staged{1};
+
+int das_fwd_wt(const Plan &pl, int W) {
+    if (pl.tune_fwd_wt && W % pl.tune_fwd_wt == 0) return pl.tune_fwd_wt;
+    return pick_wt(W, 1, 8);
+}
+
+// the staged kernel (das_fwd_staged.cu) where the plan has its tables and
+// they fit shared memory at this instance tile, else k_das_fwd3
+static bool use_staged(const Plan &pl, int wt) {
+    const int sel = pl.tune_fwd_staged ? pl.tune_fwd_staged : (g_fwd_staged.load() ? 1 : 2);
+    return sel == 1 && fwd_staged_fits(pl, wt);
+}
+
 int launch_das_forward(const Plan &pl, const float *xpm, float *raw, int W, float scale,
                        cudaStream_t st) {
     TimedScope ts_(KID_INTERP_FWD, st);
-    int wt = pick_wt(W, 1, 8);
-    if (pl.tune_fwd_wt && W % pl.tune_fwd_wt == 0) wt = pl.tune_fwd_wt;
+    const int wt = das_fwd_wt(pl, W);
+    if (use_staged(pl, wt)) return launch_das_forward_staged(pl, xpm, raw, W, wt, scale, st);
     switch (wt) {
         case 8: return das_fwd_f<8>(pl, xpm, raw, W, scale, st);
         case 4: return das_fwd_f<4>(pl, xpm, raw, W, scale, st);

@@ -95,7 +95,8 @@ static void free_plan(Plan &p) {
     void *ptrs[] = {p.tau_tiles, p.tau_pi, p.perm, p.ir_fwd, p.ir_adj, p.pre_x, p.pre_z,
                     p.sir, p.sir_se, p.sir_tiles, p.sir_pi, p.scr_img0, p.scr_img1,
                     p.scr_sino, p.fwd_off, p.fwd_ent, p.blk_tau, p.blk_span,
-                    p.scr_part, p.fft_tw, p.fft_hf, p.fft_ha};
+                    p.scr_part, p.fft_tw, p.fft_hf, p.fft_ha, p.st_info, p.st_u,
+                    p.st_off, p.st_ent};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     p = Plan();
@@ -375,6 +376,8 @@ static int build(const msot_plan_desc *d, Plan &p) {
     UP(p.tau_pi, tpi);
     UP(p.perm, perm);
     if (!has_sir) {
+        if ((rc = build_fwd_staged(p, tfx.data(), foff.data(), fent.data(), B)) != MSOT_OK)
+            return rc;
         UP(p.fwd_off, foff);
         UP(p.fwd_ent, fent);
         UP(p.blk_tau, btau);

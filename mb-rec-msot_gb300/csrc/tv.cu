@@ -1390,6 +1390,20 @@ int msot_tune_set(const char *key, int value) {
         msot::g_unet_tc.store(value);
         return MSOT_OK;
     }
+    if (key && std::strcmp(key, "fwd_staged") == 0 && (value == 0 || value == 1)) {
+        msot::g_fwd_staged.store(value);
+        return MSOT_OK;
+    }
+    if (key && std::strcmp(key, "fwd_staged_tile") == 0 &&
+        (value == 0 || value == 8 || value == 16 || value == 32 || value == 64)) {
+        msot::g_st_force_tt.store(value);
+        return MSOT_OK;
+    }
+    if (key && std::strcmp(key, "fwd_staged_group") == 0 &&
+        (value == 0 || value == 1 || value == 2 || value == 4 || value == 8 || value == 16)) {
+        msot::g_st_force_g.store(value);
+        return MSOT_OK;
+    }
     if (key && std::strcmp(key, "tv_prox_cluster") == 0 &&
         (value == 0 || value == 1 || value == 2 || value == 4 || value == 8 || value == 16)) {
         g_tv_cluster.store(value);
@@ -1664,20 +1678,29 @@ extern "C" int msot_autotune(msot_plan_t plan, int batch, void *stream, msot_tun
     MSOT_LAUNCH_CHECK();
     int rc;
     msot_tuning res{};
-    // DAS forward: instances per CTA (apply_forward: prefilter, forward, conv)
+    // DAS forward: kernel (staged / per-detector buckets) and instances per
+    // CTA (apply_forward: prefilter, forward, conv)
     {
         double best = 1e30;
-        int pick = 0;
-        for (int wt : {8, 4, 2}) {
-            if (batch % wt) continue;
-            pl.tune_fwd_wt = wt;
-            double ms;
-            if ((rc = tune_time(st, 3, ms, [&] { return apply_forward(pl, img, sino, batch, st); })))
-                return rc;
-            if (ms < best) best = ms, pick = wt;
+        int pick = 0, pick_kernel = 0;
+        for (int kernel : {1, 2}) {
+            if (kernel == 1 && !pl.st_tt) continue;
+            for (int wt : {8, 4, 2}) {
+                if (batch % wt) continue;
+                if (kernel == 1 && !fwd_staged_fits(pl, wt)) continue;
+                pl.tune_fwd_wt = wt;
+                pl.tune_fwd_staged = kernel;
+                double ms;
+                if ((rc = tune_time(st, 3, ms,
+                                    [&] { return apply_forward(pl, img, sino, batch, st); })))
+                    return rc;
+                if (ms < best) best = ms, pick = wt, pick_kernel = kernel;
+            }
         }
         pl.tune_fwd_wt = pick;
+        pl.tune_fwd_staged = pick_kernel;
         res.fwd_wt = pick;
+        res.fwd_staged = pick_kernel;
         res.fwd_ms = pick ? best : 0.0;
     }
     // DAS adjoint: instances per CTA (apply_transpose)

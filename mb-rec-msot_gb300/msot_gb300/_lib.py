@@ -66,7 +66,7 @@ class SpmrSpec(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("fwd_wt", C.c_int), ("conv_min_blocks", C.c_int), ("tv_cluster", C.c_int),
                 ("fwd_ms", C.c_double), ("transpose_ms", C.c_double), ("tv_prox_ms", C.c_double),
-                ("adj_wt", C.c_int)]
+                ("adj_wt", C.c_int), ("fwd_staged", C.c_int)]
 
 
 class SpmrInfo(C.Structure):
