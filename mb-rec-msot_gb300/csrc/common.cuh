@@ -241,6 +241,7 @@ struct StTables {
 int build_fwd_staged_host(const Plan &p, const int32_t *tfx, const int32_t *foff,
                           const int2 *fent, int dev_smem, StTables &t);
 size_t st_smem_bytes(const Plan &p, int wt);
+int st_ent_region(const Plan &p, int wt);
 bool fwd_staged_fits(const Plan &p, int wt);
 // xt in the [W/wt][P][wt] layout of das_fwd_wt
 int launch_das_forward_staged(const Plan &p, const float *xt, float *raw, int W, int wt,

@@ -39,13 +39,14 @@ namespace msot {
 __device__ int g_fwd_st_err = 0;  // set by a CTA whose bulk-copy wait timed out
 
 template <int WT, int F>
-__global__ void __launch_bounds__(1024) k_das_fwd_st(
+__global__ void __launch_bounds__(384, 2) k_das_fwd_st(
     const int4 *__restrict__ info, const int32_t *__restrict__ ulist,
     const int32_t *__restrict__ offs, const uint32_t *__restrict__ ents,
     const float *__restrict__ xt, float *__restrict__ raw, int P, int D, int T, int G, int TT,
     int n_tiles, int off_stride, int ent_cap, int ib, int fb, float inv_r, float ce1, float ce2,
     float scale) {
     const int NBK = TT + 2 * F + 1;
+    const int NBKp = NBK | 1;  // odd row stride of the moments: conflict-free 8-byte loads
     extern __shared__ __align__(16) unsigned char st_smem[];
     uint32_t *s_ent = reinterpret_cast<uint32_t *>(st_smem);            // [ent_cap]
     int32_t *s_off = reinterpret_cast<int32_t *>(s_ent + ent_cap);        // [off_stride]
@@ -86,9 +87,15 @@ __global__ void __launch_bounds__(1024) k_das_fwd_st(
         for (int i = tid; i < inf.y; i += nthr) {
             const float *src = xsrc + (size_t)__ldg(U + i) * WT;
             const uint32_t dst = smem_u32(s_x + (size_t)i * WT);
-            if constexpr (WT >= 4) {
-#pragma unroll
-                for (int c = 0; c < WT / 4; ++c) cp_async16(dst + 16 * c, src + 4 * c);
+            if constexpr (WT == 8) {
+                // the two 16-byte halves swap places on every other group of
+                // four pixels, so that the 8-lane phases of a 16-byte load
+                // over random pixels spread over all eight bank groups
+                const int sw = (i >> 2) & 1;
+                cp_async16(dst + 16 * sw, src);
+                cp_async16(dst + 16 * (sw ^ 1), src + 4);
+            } else if constexpr (WT == 4) {
+                cp_async16(dst, src);
             } else if constexpr (WT == 2) {
                 cp_async8(dst, src);
             } else {
@@ -110,78 +117,155 @@ __global__ void __launch_bounds__(1024) k_das_fwd_st(
         return;
     }
 
-    // phase 1: one (detector, bucket) per thread reduces its four moments
-    const int j = tid / NBK, i = tid - j * NBK;
-    const bool active = j < G;
-    float m0[WT], m1[WT], m2[WT], m3[WT];
+    // phase 1: each (detector, bucket) pair reduces its four moments; the
+    // instances go in pairs through the packed FP32 unit (fma.rn.f32x2)
+    constexpr int WP = WT >= 2 ? WT / 2 : 1;  // instance pairs (WT = 1: one scalar)
+    const uint32_t umask = (1u << ib) - 1u;
+    const float step = __int_as_float((127 - fb) << 23);  // 2^-fb
+    float2 *M2v = reinterpret_cast<float2 *>(s_x);  // moments [G][4][WP][NBKp] (pairs)
+    float *M1s = s_x;                              // WT = 1: [G][4][NBKp]
+    const int npair = G * NBK;
+    // a thread keeps the moments of its pair in registers until every thread
+    // has stopped reading the staged image values (threads >= npair)
+    constexpr int MAXP = 1;
+    float2 acc[MAXP][4][WP];
+    int pj[MAXP], pi[MAXP];
 #pragma unroll
-    for (int w = 0; w < WT; ++w) m0[w] = m1[w] = m2[w] = m3[w] = 0.f;
-    if (active) {
-        const int lo = s_off[j * (NBK + 1) + i], hi = s_off[j * (NBK + 1) + i + 1];
-        const uint32_t umask = (1u << ib) - 1u;
-        const float step = __int_as_float((127 - fb) << 23);  // 2^-fb
+    for (int u = 0; u < MAXP; ++u) {
+        const int pr = tid + u * nthr;
+        pj[u] = pr < npair ? pr / NBK : -1;
+        pi[u] = pr < npair ? pr - pj[u] * NBK : 0;
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+#pragma unroll
+            for (int w = 0; w < WP; ++w) acc[u][m][w] = make_float2(0.f, 0.f);
+        if (pj[u] < 0) continue;
+        const int lo = s_off[pj[u] * (NBK + 1) + pi[u]], hi = s_off[pj[u] * (NBK + 1) + pi[u] + 1];
         for (int e = lo; e < hi; ++e) {
             const uint32_t q = s_ent[e];
             const float f = (float)(q >> ib) * step;
             const float *xp = s_x + (size_t)(q & umask) * WT;
-            float xv[WT];
-            if constexpr (WT >= 4) {
-#pragma unroll
-                for (int c = 0; c < WT; c += 4) {
-                    const float4 v = *reinterpret_cast<const float4 *>(xp + c);
-                    xv[c] = v.x; xv[c + 1] = v.y; xv[c + 2] = v.z; xv[c + 3] = v.w;
-                }
-            } else {
-#pragma unroll
-                for (int c = 0; c < WT; ++c) xv[c] = xp[c];
-            }
             const float e1 = fmaxf(0.f, fmaf(-f, inv_r, ce1));
             const float e2 = fmaxf(0.f, fmaf(f, inv_r, -ce2));
+            if constexpr (WT >= 2) {
+                float2 xv[WP];
+                if constexpr (WT == 8) {
+                    const int sw = (int)((q & umask) >> 2) & 1;
+                    const float4 v = *reinterpret_cast<const float4 *>(xp + 4 * sw);
+                    const float4 v2 = *reinterpret_cast<const float4 *>(xp + 4 * (sw ^ 1));
+                    xv[0] = make_float2(v.x, v.y);
+                    xv[1] = make_float2(v.z, v.w);
+                    xv[2] = make_float2(v2.x, v2.y);
+                    xv[3] = make_float2(v2.z, v2.w);
+                } else if constexpr (WT == 4) {
+                    const float4 v = *reinterpret_cast<const float4 *>(xp);
+                    xv[0] = make_float2(v.x, v.y);
+                    xv[1] = make_float2(v.z, v.w);
+                } else {
+                    xv[0] = *reinterpret_cast<const float2 *>(xp);
+                }
+                const float2 f2 = make_float2(f, f), e12 = make_float2(e1, e1),
+                             e22 = make_float2(e2, e2);
 #pragma unroll
-            for (int w = 0; w < WT; ++w) {
-                m0[w] += xv[w];
-                m1[w] = fmaf(f, xv[w], m1[w]);
-                m2[w] = fmaf(e1, xv[w], m2[w]);
-                m3[w] = fmaf(e2, xv[w], m3[w]);
+                for (int w = 0; w < WP; ++w) {
+                    acc[u][0][w] = fadd2(acc[u][0][w], xv[w]);
+                    acc[u][1][w] = ffma2(f2, xv[w], acc[u][1][w]);
+                    acc[u][2][w] = ffma2(e12, xv[w], acc[u][2][w]);
+                    acc[u][3][w] = ffma2(e22, xv[w], acc[u][3][w]);
+                }
+            } else {
+                const float xv = xp[0];
+                acc[u][0][0].x += xv;
+                acc[u][1][0].x = fmaf(f, xv, acc[u][1][0].x);
+                acc[u][2][0].x = fmaf(e1, xv, acc[u][2][0].x);
+                acc[u][3][0].x = fmaf(e2, xv, acc[u][3][0].x);
             }
         }
     }
     __syncthreads();  // every thread is done with the staged image values
-    float *M = s_x;   // moments [G][4][WT][NBK]
-    if (active) {
 #pragma unroll
-        for (int w = 0; w < WT; ++w) {
-            M[((j * 4 + 0) * WT + w) * NBK + i] = m0[w];
-            M[((j * 4 + 1) * WT + w) * NBK + i] = m1[w];
-            M[((j * 4 + 2) * WT + w) * NBK + i] = m2[w];
-            M[((j * 4 + 3) * WT + w) * NBK + i] = m3[w];
-        }
+    for (int u = 0; u < MAXP; ++u) {
+        if (pj[u] < 0) continue;
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+#pragma unroll
+            for (int w = 0; w < WP; ++w) {
+                if constexpr (WT >= 2)
+                    M2v[((pj[u] * 4 + m) * WP + w) * NBKp + pi[u]] = acc[u][m][w];
+                else
+                    M1s[(pj[u] * 4 + m) * NBKp + pi[u]] = acc[u][m][0].x;
+            }
     }
     __syncthreads();
 
     // phase 2: output t (local tl) reads buckets t - F - 1 .. t + F, i.e.
-    // local indices tl .. tl + 2F + 1; lanes run along t (coalesced stores)
-    for (int o = tid; o < G * WT * TT; o += nthr) {
-        const int tl = o % TT, r = o / TT, w = r % WT, jj = r / WT;
-        const int d = d0 + jj, t = t0 + tl;
-        if (d >= D || t >= T) continue;
-        const float *M0 = M + ((jj * 4 + 0) * WT + w) * NBK + tl + F + 1;
-        const float *M1 = M + ((jj * 4 + 1) * WT + w) * NBK + tl + F + 1;
-        float acc = M[((jj * 4 + 2) * WT + w) * NBK + tl + 2 * F + 1] +
-                    M[((jj * 4 + 3) * WT + w) * NBK + tl];
+    // local indices tl .. tl + 2F + 1.  A thread filters FB = 4 consecutive
+    // outputs of one (detector, instance pair) from one window of 2F + 3
+    // moments: outputs tl0 + u read M0 / M1 at tl0 + 1 + (u + F - k).
+    // Consecutive threads take consecutive (detector, pair) rows (odd row
+    // stride: distinct banks); the tile goes through shared memory (over the
+    // entries, no longer needed) so that the global stores run along t.
+    constexpr int FB = 4;
+    const int ntb = TT / FB, nrow = G * WP, TTp = TT + 1;
+    float *s_out = reinterpret_cast<float *>(s_ent);  // [G][WT][TTp]
+    for (int it = tid; it < nrow * ntb; it += nthr) {
+        const int r = it % nrow, tb = it / nrow, wp = r % WP, jj = r / WP;
+        const int tl0 = tb * FB;
+        float2 v0[2 * F + 3], v1[2 * F + 3], a2[FB], a3[FB];
+        if constexpr (WT >= 2) {
+            const float2 *B0 = M2v + ((jj * 4 + 0) * WP + wp) * NBKp + tl0 + 1;
+            const float2 *B1 = M2v + ((jj * 4 + 1) * WP + wp) * NBKp + tl0 + 1;
+            const float2 *B2 = M2v + ((jj * 4 + 2) * WP + wp) * NBKp + tl0 + 2 * F + 1;
+            const float2 *B3 = M2v + ((jj * 4 + 3) * WP + wp) * NBKp + tl0;
 #pragma unroll
-        for (int kk = -(F - 1); kk <= F; ++kk) {
-            const float a = 1.f - (float)(kk < 0 ? -kk : kk) * inv_r;
-            acc = fmaf(a, M0[-kk], acc);
-            acc = kk <= 0 ? acc - inv_r * M1[-kk] : fmaf(inv_r, M1[-kk], acc);
+            for (int c = 0; c < 2 * F + 3; ++c) v0[c] = B0[c], v1[c] = B1[c];
+#pragma unroll
+            for (int u = 0; u < FB; ++u) a2[u] = B2[u], a3[u] = B3[u];
+        } else {
+            const float *B0 = M1s + (jj * 4 + 0) * NBKp + tl0 + 1;
+            const float *B1 = M1s + (jj * 4 + 1) * NBKp + tl0 + 1;
+            const float *B2 = M1s + (jj * 4 + 2) * NBKp + tl0 + 2 * F + 1;
+            const float *B3 = M1s + (jj * 4 + 3) * NBKp + tl0;
+#pragma unroll
+            for (int c = 0; c < 2 * F + 3; ++c)
+                v0[c] = make_float2(B0[c], 0.f), v1[c] = make_float2(B1[c], 0.f);
+#pragma unroll
+            for (int u = 0; u < FB; ++u)
+                a2[u] = make_float2(B2[u], 0.f), a3[u] = make_float2(B3[u], 0.f);
         }
-        raw[((size_t)(w0 + w) * D + d) * T + t] = acc * scale;
+        const float2 pr = make_float2(inv_r, inv_r), nr = make_float2(-inv_r, -inv_r);
+        float *o0 = s_out + (jj * WT + (WT >= 2 ? 2 * wp : 0)) * TTp + tl0;
+#pragma unroll
+        for (int u = 0; u < FB; ++u) {
+            float2 y = fadd2(a2[u], a3[u]);
+#pragma unroll
+            for (int kk = -(F - 1); kk <= F; ++kk) {
+                const float a = 1.f - (float)(kk < 0 ? -kk : kk) * inv_r;
+                y = ffma2(make_float2(a, a), v0[u + F - kk], y);
+                y = ffma2(kk <= 0 ? nr : pr, v1[u + F - kk], y);
+            }
+            o0[u] = y.x * scale;
+            if constexpr (WT >= 2) o0[TTp + u] = y.y * scale;
+        }
+    }
+    __syncthreads();
+    for (int o = tid; o < G * WT * TT; o += nthr) {
+        const int tl = o % TT, rw = o / TT, w = rw % WT, jj = rw / WT;
+        const int d = d0 + jj, t = t0 + tl;
+        if (d < D && t < T) raw[((size_t)(w0 + w) * D + d) * T + t] = s_out[rw * TTp + tl];
     }
 }
 
 // ---------------------------------------------------------------------------
 // host: table construction at plan creation
 // ---------------------------------------------------------------------------
+// words of the entries region: the entries, then (after the moments) the
+// output tile [G][wt][TT + 1]; a multiple of 4
+int st_ent_region(const Plan &p, int wt) {
+    const int out = p.st_g * wt * (p.st_tt + 1);
+    return (std::max(p.st_ent_cap, out) + 3) & ~3;
+}
+
 static inline int floor_div(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
 
 // tiles k whose bucket range [k TT - F - 1, k TT + TT + F) holds bucket b
@@ -193,9 +277,9 @@ static inline void st_tile_range(int b, int TT, int F, int n_tiles, int &k0, int
 }
 
 size_t st_smem_bytes(const Plan &p, int wt) {
-    const int NBK = p.st_tt + 2 * p.F + 1;
-    const size_t xs = std::max((size_t)p.st_umax * wt, (size_t)p.st_g * 4 * wt * NBK);
-    return (size_t)p.st_ent_cap * 4 + (size_t)p.st_off_stride * 4 + 16 + xs * 4;
+    const int NBKp = (p.st_tt + 2 * p.F + 1) | 1;
+    const size_t xs = std::max((size_t)p.st_umax * wt, (size_t)p.st_g * 4 * wt * NBKp);
+    return (size_t)st_ent_region(p, wt) * 4 + (size_t)p.st_off_stride * 4 + 16 + xs * 4;
 }
 
 namespace {
@@ -274,13 +358,14 @@ int build_fwd_staged_host(const Plan &p, const int32_t *tfx, const int32_t *foff
             for (int TT : tts)
                 for (int G : gs) {
                     const int NBK = TT + 2 * p.F + 1;
-                    if (G * NBK > 1024 || G * NBK < min_threads || G > p.D) continue;
+                    if (G * NBK > 384 || G * NBK < min_threads || G > p.D) continue;
                     const StScan s = st_scan(p, tfx, TT, G, std::max(1, step8 * 8 / G));
                     const size_t umax = sample ? (size_t)s.umax * 5 / 4 : (size_t)s.umax;
                     const size_t emax = sample ? (size_t)s.emax * 5 / 4 + 64 : (size_t)s.emax;
                     if (umax >= ((size_t)1 << ib)) continue;
-                    const size_t xs = std::max(umax * 8, (size_t)G * 4 * 8 * NBK);
-                    const size_t need = ((emax + 3) & ~(size_t)3) * 4 +
+                    const size_t xs = std::max(umax * 8, (size_t)G * 4 * 8 * (NBK | 1));
+                    const size_t er = std::max(emax, (size_t)G * 8 * (TT + 1));
+                    const size_t need = ((er + 3) & ~(size_t)3) * 4 +
                                         (size_t)((G * (NBK + 1) + 3) & ~3) * 4 + 16 + xs * 4;
                     if (need > budget) continue;
                     if (best_cost < 0 || s.cost < best_cost) {
@@ -368,7 +453,7 @@ int build_fwd_staged_host(const Plan &p, const int32_t *tfx, const int32_t *foff
     t.umax = umax;
     t.ent_cap = (emax + 3) & ~3;
     t.off_stride = off_stride;
-    t.threads = std::min(1024, (G * NBK + 31) / 32 * 32);
+    t.threads = std::min(384, (G * NBK + 31) / 32 * 32);
     return MSOT_OK;
 }
 
@@ -434,8 +519,8 @@ static int st_launch(const Plan &p, const float *xt, float *raw, int W, float sc
     const dim3 grid((unsigned)(p.st_ntiles * p.st_ngroups), (unsigned)(W / WT));
     KLAUNCH(k_das_fwd_st<WT, F><<<grid, p.st_threads, smem, st>>>(
         p.st_info, p.st_u, p.st_off, p.st_ent, xt, raw, p.P, p.D, p.T, p.st_g, p.st_tt,
-        p.st_ntiles, p.st_off_stride, p.st_ent_cap, p.st_ib, p.frac_bits, p.inv_r, p.ce1, p.ce2,
-        scale));
+        p.st_ntiles, p.st_off_stride, st_ent_region(p, WT), p.st_ib, p.frac_bits, p.inv_r, p.ce1,
+        p.ce2, scale));
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
 }

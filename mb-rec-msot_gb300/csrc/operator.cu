@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(256, 4) k_das_fwd3(const int32_t *__restrict__
         for (int k = -(F - 1); k <= F; ++k) {
             const float a = 1.f - (float)(k < 0 ? -k : k) * inv_r;
             acc = fmaf(a, M0[-k], acc);
-            acc = k <= 0 ? acc - inv_r * M1[-k] : fmaf(inv_r, M1[-k], acc);
+            acc = fmaf(k <= 0 ? -inv_r : inv_r, M1[-k], acc);
         }
         raw[((size_t)(w0 + i) * D + d) * T + t] = acc * scale;
     }
