@@ -414,6 +414,69 @@ const char *msot_profile_kernel_name(int kid);
 int msot_profile_read(int kid, int *launches, double *total_ms);
 
 /* ------------------------------------------------------------------------ */
+/* MATLAB-level drop-in (host buffers, FP64, MATLAB memory layouts).  The MEX
+ * gateways mex/msot_model_mex.cpp, mex/rec_nn_with_L2_reg.cpp,
+ * mex/rec_nn_with_L1_eye_reg.cpp and mex/rec_nn_with_TV_reg.cpp wrap these. */
+
+/* 1 when `plan` was created and not yet destroyed (a registry of live
+ * plans: MEX callers hand plans to MATLAB as integer handles), else 0. */
+int msot_plan_valid(msot_plan_t plan);
+
+/* The fields of the reference's model object a plan is built from
+ * (MSOTmodel.m:18-48): Discretization.sizeOfPixelGrid = [nx nz];
+ * Data.absoluteTravelTimeIndices (P x D), circularInterpolationRadiusInSamples,
+ * numTimeSamplesPerTransducer; Data.IRHat (interleaved complex, n_hat
+ * entries, the length-(T + L - 1) transform of the IR, MSOTmodel.m:338-346)
+ * with Probe.eirLength = L; Discretization.prefilter (interleaved complex
+ * nz x nx, column-major, Discretization.m:47-51); Data.SPMR /
+ * SPMRTimestepIndexStartAndEnd / SPMRIndices when includeSir. */
+typedef struct msot_model_fields {
+    int nx, nz, n_det, n_t;
+    double radius;
+    const double *travel;     /* P x D */
+    const double *ir_hat;     /* NULL: no IR convolution */
+    int n_hat, eir_length;
+    const double *prefilter;  /* NULL: no prefilter */
+    int sir_len, n_sir;       /* 0: no SIR */
+    const double *sir;
+    const int32_t *sir_start_end, *sir_idx;
+    double norm;              /* model normalisation factor; <= 0: sigma_max is
+                                 estimated (power iteration, 100 steps), as the
+                                 reference runs svds when none is given
+                                 (MSOTmodel.m:273-279) */
+    int max_batch;            /* largest wavelength stack per call */
+} msot_model_fields;
+/* Plan of a reference model: IR taps = the first eirLength samples of
+ * ifft(IRHat) (the rest must vanish, else MSOT_EINVAL); prefilter taps = the
+ * two circular factors of ifft2(prefilter), which is separable for the
+ * Gaussian pixel model, truncated below 1e-13 of the centre. */
+int msot_plan_create_from_model(const msot_model_fields *fields, msot_plan_t *plan);
+/* The plan's normalisation factor (0 for an invalid handle). */
+double msot_plan_norm(msot_plan_t plan);
+
+/* model.Funcs.applyForward (transpose = 0: image Nz x Nx x W -> sinogram
+ * T x D x W) and applyTranspose (transpose = 1: the reverse), FP64 host
+ * arrays; W <= the plan's max_batch.  Synchronous. */
+int msot_host_apply(msot_plan_t plan, int transpose, const double *in, int W, double *out);
+
+/* The solvers on a T x D x W stack data (FP64 host), one reference call:
+ * the W wavelengths are solved coupled and the outputs are sums over the
+ * stack; rec receives Nz x Nx x W.  rec_nn_with_L2_reg.m:1 (RegL2 the
+ * identity weighted by lambdaL2 > 0, RegL2_2 laplacian_per_wavelength
+ * weighted by lambdaL2_2 > 0 and used only with lambdaL2 > 0, as the
+ * reference does; err_reg2 may be NULL, else it receives ||del2(rec)||^2). */
+int msot_host_rec_nn_with_L2_reg(msot_plan_t plan, const double *data, int W, int num_iter,
+                                 double lambdaL2, double lambdaL2_2, double *rec,
+                                 double *err_img, double *err_reg, double *err_reg2);
+/* rec_nn_with_L1_eye_reg.m:1 (err_reg = ||rec||_1). */
+int msot_host_rec_nn_with_L1_eye_reg(msot_plan_t plan, const double *data, int W, int num_iter,
+                                     double reg, double *rec, double *err_img,
+                                     double *err_reg);
+/* rec_nn_with_TV_reg.m:1 (square grids; err_reg = the summed ITV). */
+int msot_host_rec_nn_with_TV_reg(msot_plan_t plan, const double *data, int W, int num_iter,
+                                 double reg, double *rec, double *err_img, double *err_reg);
+
+/* ------------------------------------------------------------------------ */
 /* Host-buffer entry points with the reference MEX contracts (FP64 in/out,
  * column-major, MATLAB-owned inputs; output written to caller memory that
  * MATLAB allocated with mxCreate*).  Arithmetic is FP32 on the GPU. */

@@ -241,13 +241,11 @@ struct StTables {
 int build_fwd_staged_host(const Plan &p, const int32_t *tfx, const int32_t *foff,
                           const int2 *fent, int dev_smem, StTables &t);
 size_t st_smem_bytes(const Plan &p, int wt);
-int st_ent_region(const Plan &p, int wt);
+int st_x_words(const Plan &p, int wt);
 bool fwd_staged_fits(const Plan &p, int wt);
 // xt in the [W/wt][P][wt] layout of das_fwd_wt
 int launch_das_forward_staged(const Plan &p, const float *xt, float *raw, int W, int wt,
                               float scale, cudaStream_t st);
-// reads (and with clear != 0 resets) the staged forward's timeout flag
-int fwd_staged_error(int clear);
 // staged forward on (1, default) or off (0); operator.cu
 extern std::atomic<int> g_fwd_staged;
 // instances per CTA of the DAS forward at batch W: the interpolation input is

@@ -15,18 +15,20 @@
 // into shared memory once (16-byte cp.async) and every detector of the group
 // reads it there.  Adjacent detectors see nearly the same band of pixels, so
 // the union is little larger than one detector's band and the L2 traffic
-// drops by about G.
+// drops by about G.  Each thread reduces the moments of one (detector,
+// bucket) from shared memory, two instances per packed FP32 instruction
+// (fma.rn.f32x2); the filter runs four outputs per thread from one register
+// window of moments, and the output tile leaves through shared memory.
 //
-// Per CTA the plan stores (concatenated, each CTA's part 16-byte aligned):
+// Per CTA the plan stores (concatenated):
 //   st_info  {u_off, nU, e_off, n_ent}
 //   st_u     the union's pixel indices, ascending
 //   st_off   [G][NBK + 1] offsets of the CTA's entries per (detector, bucket)
 //   st_ent   entries (tau fraction << ib) | index in U, bucket-sorted, pixels
 //            ascending within a bucket (the order of k_das_fwd3's walk, so the
 //            two kernels give identical sums)
-// with NBK = TT + 2F + 1 buckets spanning [k TT - F - 1, k TT + TT + F).  The
-// entries and offsets arrive by two bulk copies (TMA engine) on one mbarrier
-// while the image values are in flight.
+// with NBK = TT + 2F + 1 buckets spanning [k TT - F - 1, k TT + TT + F).  TT
+// and G are powers of two.  The entries and offsets are read through L1.
 #include <algorithm>
 #include <atomic>
 #include <vector>
@@ -36,49 +38,85 @@
 
 namespace msot {
 
-__device__ int g_fwd_st_err = 0;  // set by a CTA whose bulk-copy wait timed out
+// image values of entry q (index in the union in its low bits) as instance
+// pairs
+template <int WT>
+__device__ __forceinline__ void load_x(const float *s_x, uint32_t q, uint32_t umask,
+                                       float2 (&xv)[WT >= 2 ? WT / 2 : 1]) {
+    const float *xp = s_x + (size_t)(q & umask) * WT;
+    if constexpr (WT >= 4) {
+#pragma unroll
+        for (int c = 0; c < WT / 4; ++c) {
+            const float4 v = *reinterpret_cast<const float4 *>(xp + 4 * c);
+            xv[2 * c] = make_float2(v.x, v.y);
+            xv[2 * c + 1] = make_float2(v.z, v.w);
+        }
+    } else if constexpr (WT == 2) {
+        xv[0] = *reinterpret_cast<const float2 *>(xp);
+    } else {
+        xv[0] = make_float2(xp[0], 0.f);
+    }
+}
 
+// the four bucket moments of one entry: sum x, sum f x, sum e1 x, sum e2 x,
+// instance pairs through the packed FP32 unit (fma.rn.f32x2)
+template <int WT>
+__device__ __forceinline__ void accumulate(float2 (&acc)[4][WT >= 2 ? WT / 2 : 1], uint32_t q,
+                                           const float2 (&xv)[WT >= 2 ? WT / 2 : 1], int ib,
+                                           float step, float inv_r, float ce1, float ce2) {
+    constexpr int WP = WT >= 2 ? WT / 2 : 1;
+    const float f = (float)(q >> ib) * step;
+    const float e1 = fmaxf(0.f, fmaf(-f, inv_r, ce1));
+    const float e2 = fmaxf(0.f, fmaf(f, inv_r, -ce2));
+    if constexpr (WT >= 2) {
+        const float2 f2 = make_float2(f, f), e12 = make_float2(e1, e1), e22 = make_float2(e2, e2);
+#pragma unroll
+        for (int w = 0; w < WP; ++w) {
+            acc[0][w] = fadd2(acc[0][w], xv[w]);
+            acc[1][w] = ffma2(f2, xv[w], acc[1][w]);
+            acc[2][w] = ffma2(e12, xv[w], acc[2][w]);
+            acc[3][w] = ffma2(e22, xv[w], acc[3][w]);
+        }
+    } else {
+        acc[0][0].x += xv[0].x;
+        acc[1][0].x = fmaf(f, xv[0].x, acc[1][0].x);
+        acc[2][0].x = fmaf(e1, xv[0].x, acc[2][0].x);
+        acc[3][0].x = fmaf(e2, xv[0].x, acc[3][0].x);
+    }
+}
+
+// TT = 1 << lg_tt output samples and G = 1 << lg_g detectors per CTA; the
+// shared memory holds the union's image values [nU][WT] (x_words floats,
+// later the moments) and the output tile [G][WT][TT + 1].
 template <int WT, int F>
-__global__ void __launch_bounds__(384, 2) k_das_fwd_st(
+__global__ void __launch_bounds__(384, WT >= 16 ? 1 : 2) k_das_fwd_st(
     const int4 *__restrict__ info, const int32_t *__restrict__ ulist,
     const int32_t *__restrict__ offs, const uint32_t *__restrict__ ents,
-    const float *__restrict__ xt, float *__restrict__ raw, int P, int D, int T, int G, int TT,
-    int n_tiles, int off_stride, int ent_cap, int ib, int fb, float inv_r, float ce1, float ce2,
-    float scale) {
+    const float *__restrict__ xt, float *__restrict__ raw, int P, int D, int T, int lg_g,
+    int lg_tt, int n_tiles, int off_stride, int x_words, int ib, int fb, float inv_r, float ce1,
+    float ce2, float scale) {
+    constexpr int WP = WT >= 2 ? WT / 2 : 1;  // instance pairs (WT = 1: one scalar)
+    const int G = 1 << lg_g, TT = 1 << lg_tt;
     const int NBK = TT + 2 * F + 1;
     const int NBKp = NBK | 1;  // odd row stride of the moments: conflict-free 8-byte loads
-    extern __shared__ __align__(16) unsigned char st_smem[];
-    uint32_t *s_ent = reinterpret_cast<uint32_t *>(st_smem);            // [ent_cap]
-    int32_t *s_off = reinterpret_cast<int32_t *>(s_ent + ent_cap);        // [off_stride]
-    uint64_t *s_bar = reinterpret_cast<uint64_t *>(s_off + off_stride);   // mbarrier
-    int *s_flag = reinterpret_cast<int *>(s_bar + 1);                     // wait failed
-    float *s_x = reinterpret_cast<float *>(s_bar + 2);  // [nU][WT], then the moments
+    extern __shared__ __align__(16) float st_smem[];
+    float *s_x = st_smem;                        // [nU][WT], then the moments
+    float *s_out = st_smem + x_words;            // [G][WT][TT + 1]
     const int cta = blockIdx.x, g = cta / n_tiles, k = cta - g * n_tiles;
-    const int d0 = g * G, t0 = k * TT, w0 = blockIdx.y * WT;
+    const int d0 = g << lg_g, t0 = k << lg_tt, w0 = blockIdx.y * WT;
     const int tid = threadIdx.x, nthr = blockDim.x;
+    const int lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
     const int4 inf = __ldg(info + cta);  // u_off, nU, e_off, n_ent
     if (inf.w == 0) {
-        // no pixel of the group falls in the tile: its outputs are zero
-        for (int o = tid; o < G * WT * TT; o += nthr) {
-            const int tl = o % TT, r = o / TT, w = r % WT, j = r / WT;
-            const int d = d0 + j, t = t0 + tl;
-            if (d < D && t < T) raw[((size_t)(w0 + w) * D + d) * T + t] = 0.f;
+        // no pixel of the group falls in the tile: zero rows, lanes along t
+        for (int rw = warp; rw < G * WT; rw += nwarp) {
+            const int d = d0 + rw / WT, w = rw % WT;
+            if (d >= D) continue;
+            float *row = raw + ((size_t)(w0 + w) * D + d) * T;
+            for (int tl = lane; tl < TT; tl += 32)
+                if (t0 + tl < T) row[t0 + tl] = 0.f;
         }
         return;
-    }
-    const uint32_t bar = smem_u32(s_bar);
-    if (tid == 0) {
-        s_flag[0] = 0;
-        mbar_init(bar, 1);
-        mbar_init_fence();
-    }
-    __syncthreads();
-    if (tid == 0) {
-        const uint32_t ent_bytes = (uint32_t)((inf.w + 3) & ~3) * 4u;
-        const uint32_t off_bytes = (uint32_t)off_stride * 4u;
-        mbar_arrive_expect_tx(bar, ent_bytes + off_bytes);
-        bulk_g2s(smem_u32(s_ent), ents + inf.z, ent_bytes, bar);
-        bulk_g2s(smem_u32(s_off), offs + (size_t)cta * off_stride, off_bytes, bar);
     }
     // the union's image values, WT instances per pixel ([W/WT][P][WT] layout)
     {
@@ -87,15 +125,9 @@ __global__ void __launch_bounds__(384, 2) k_das_fwd_st(
         for (int i = tid; i < inf.y; i += nthr) {
             const float *src = xsrc + (size_t)__ldg(U + i) * WT;
             const uint32_t dst = smem_u32(s_x + (size_t)i * WT);
-            if constexpr (WT == 8) {
-                // the two 16-byte halves swap places on every other group of
-                // four pixels, so that the 8-lane phases of a 16-byte load
-                // over random pixels spread over all eight bank groups
-                const int sw = (i >> 2) & 1;
-                cp_async16(dst + 16 * sw, src);
-                cp_async16(dst + 16 * (sw ^ 1), src + 4);
-            } else if constexpr (WT == 4) {
-                cp_async16(dst, src);
+            if constexpr (WT >= 4) {
+#pragma unroll
+                for (int c = 0; c < WT / 4; ++c) cp_async16(dst + 16 * c, src + 4 * c);
             } else if constexpr (WT == 2) {
                 cp_async8(dst, src);
             } else {
@@ -103,97 +135,57 @@ __global__ void __launch_bounds__(384, 2) k_das_fwd_st(
             }
         }
     }
-    cp_async_wait_all();
-    if (!mbar_wait_bounded(bar, 0)) s_flag[0] = 1;
-    __syncthreads();
-    if (s_flag[0]) {
-        // the bulk copies did not complete within the bound: report, wait
-        // once more (bounded) for the copies still landing here, skip the tile
-        if (tid == 0) {
-            atomicExch(&g_fwd_st_err, 1);
-            mbar_wait_bounded(bar, 0);
-        }
-        __syncthreads();
-        return;
+    // this thread's (detector, bucket) and the bounds of its entries (read
+    // through L1 while the image values are in flight)
+    const int j = tid / NBK, i = tid - j * NBK;
+    const bool active = j < G;
+    int lo = 0, hi = 0;
+    if (active) {
+        const int32_t *o = offs + (size_t)cta * off_stride + j * (NBK + 1) + i;
+        lo = __ldg(o);
+        hi = __ldg(o + 1);
     }
+    cp_async_wait_all();
+    __syncthreads();
 
-    // phase 1: each (detector, bucket) pair reduces its four moments; the
-    // instances go in pairs through the packed FP32 unit (fma.rn.f32x2)
-    constexpr int WP = WT >= 2 ? WT / 2 : 1;  // instance pairs (WT = 1: one scalar)
+    // phase 1: the thread's bucket moments, two entries per step
     const uint32_t umask = (1u << ib) - 1u;
     const float step = __int_as_float((127 - fb) << 23);  // 2^-fb
-    float2 *M2v = reinterpret_cast<float2 *>(s_x);  // moments [G][4][WP][NBKp] (pairs)
-    float *M1s = s_x;                              // WT = 1: [G][4][NBKp]
-    const int npair = G * NBK;
-    // a thread keeps the moments of its pair in registers until every thread
-    // has stopped reading the staged image values (threads >= npair)
-    constexpr int MAXP = 1;
-    float2 acc[MAXP][4][WP];
-    int pj[MAXP], pi[MAXP];
+    float2 acc[4][WP];
 #pragma unroll
-    for (int u = 0; u < MAXP; ++u) {
-        const int pr = tid + u * nthr;
-        pj[u] = pr < npair ? pr / NBK : -1;
-        pi[u] = pr < npair ? pr - pj[u] * NBK : 0;
+    for (int m = 0; m < 4; ++m)
 #pragma unroll
-        for (int m = 0; m < 4; ++m)
-#pragma unroll
-            for (int w = 0; w < WP; ++w) acc[u][m][w] = make_float2(0.f, 0.f);
-        if (pj[u] < 0) continue;
-        const int lo = s_off[pj[u] * (NBK + 1) + pi[u]], hi = s_off[pj[u] * (NBK + 1) + pi[u] + 1];
-        for (int e = lo; e < hi; ++e) {
-            const uint32_t q = s_ent[e];
-            const float f = (float)(q >> ib) * step;
-            const float *xp = s_x + (size_t)(q & umask) * WT;
-            const float e1 = fmaxf(0.f, fmaf(-f, inv_r, ce1));
-            const float e2 = fmaxf(0.f, fmaf(f, inv_r, -ce2));
-            if constexpr (WT >= 2) {
-                float2 xv[WP];
-                if constexpr (WT == 8) {
-                    const int sw = (int)((q & umask) >> 2) & 1;
-                    const float4 v = *reinterpret_cast<const float4 *>(xp + 4 * sw);
-                    const float4 v2 = *reinterpret_cast<const float4 *>(xp + 4 * (sw ^ 1));
-                    xv[0] = make_float2(v.x, v.y);
-                    xv[1] = make_float2(v.z, v.w);
-                    xv[2] = make_float2(v2.x, v2.y);
-                    xv[3] = make_float2(v2.z, v2.w);
-                } else if constexpr (WT == 4) {
-                    const float4 v = *reinterpret_cast<const float4 *>(xp);
-                    xv[0] = make_float2(v.x, v.y);
-                    xv[1] = make_float2(v.z, v.w);
-                } else {
-                    xv[0] = *reinterpret_cast<const float2 *>(xp);
-                }
-                const float2 f2 = make_float2(f, f), e12 = make_float2(e1, e1),
-                             e22 = make_float2(e2, e2);
-#pragma unroll
-                for (int w = 0; w < WP; ++w) {
-                    acc[u][0][w] = fadd2(acc[u][0][w], xv[w]);
-                    acc[u][1][w] = ffma2(f2, xv[w], acc[u][1][w]);
-                    acc[u][2][w] = ffma2(e12, xv[w], acc[u][2][w]);
-                    acc[u][3][w] = ffma2(e22, xv[w], acc[u][3][w]);
-                }
-            } else {
-                const float xv = xp[0];
-                acc[u][0][0].x += xv;
-                acc[u][1][0].x = fmaf(f, xv, acc[u][1][0].x);
-                acc[u][2][0].x = fmaf(e1, xv, acc[u][2][0].x);
-                acc[u][3][0].x = fmaf(e2, xv, acc[u][3][0].x);
-            }
+        for (int w = 0; w < WP; ++w) acc[m][w] = make_float2(0.f, 0.f);
+    {
+        const uint32_t *E = ents + inf.z;
+        int e = lo;
+        for (; e + 1 < hi; e += 2) {
+            const uint32_t qa = __ldg(E + e), qb = __ldg(E + e + 1);
+            float2 xa[WP], xb[WP];
+            load_x<WT>(s_x, qa, umask, xa);
+            load_x<WT>(s_x, qb, umask, xb);
+            accumulate<WT>(acc, qa, xa, ib, step, inv_r, ce1, ce2);
+            accumulate<WT>(acc, qb, xb, ib, step, inv_r, ce1, ce2);
+        }
+        if (e < hi) {
+            const uint32_t qa = __ldg(E + e);
+            float2 xa[WP];
+            load_x<WT>(s_x, qa, umask, xa);
+            accumulate<WT>(acc, qa, xa, ib, step, inv_r, ce1, ce2);
         }
     }
     __syncthreads();  // every thread is done with the staged image values
-#pragma unroll
-    for (int u = 0; u < MAXP; ++u) {
-        if (pj[u] < 0) continue;
+    float2 *M2v = reinterpret_cast<float2 *>(s_x);  // moments [G][4][WP][NBKp] (pairs)
+    float *M1s = s_x;                              // WT = 1: [G][4][NBKp]
+    if (active) {
 #pragma unroll
         for (int m = 0; m < 4; ++m)
 #pragma unroll
             for (int w = 0; w < WP; ++w) {
                 if constexpr (WT >= 2)
-                    M2v[((pj[u] * 4 + m) * WP + w) * NBKp + pi[u]] = acc[u][m][w];
+                    M2v[((j * 4 + m) * WP + w) * NBKp + i] = acc[m][w];
                 else
-                    M1s[(pj[u] * 4 + m) * NBKp + pi[u]] = acc[u][m][0].x;
+                    M1s[(j * 4 + m) * NBKp + i] = acc[m][0].x;
             }
     }
     __syncthreads();
@@ -203,13 +195,15 @@ __global__ void __launch_bounds__(384, 2) k_das_fwd_st(
     // outputs of one (detector, instance pair) from one window of 2F + 3
     // moments: outputs tl0 + u read M0 / M1 at tl0 + 1 + (u + F - k).
     // Consecutive threads take consecutive (detector, pair) rows (odd row
-    // stride: distinct banks); the tile goes through shared memory (over the
-    // entries, no longer needed) so that the global stores run along t.
+    // stride: distinct banks); the tile goes through shared memory so that
+    // the global stores run along t.
     constexpr int FB = 4;
-    const int ntb = TT / FB, nrow = G * WP, TTp = TT + 1;
-    float *s_out = reinterpret_cast<float *>(s_ent);  // [G][WT][TTp]
-    for (int it = tid; it < nrow * ntb; it += nthr) {
-        const int r = it % nrow, tb = it / nrow, wp = r % WP, jj = r / WP;
+    const int TTp = TT + 1;
+    const int lg_nrow = lg_g + (WP == 8 ? 3 : WP == 4 ? 2 : WP == 2 ? 1 : 0);
+    const int n_items = (G * WP) * (TT / FB);
+    for (int it = tid; it < n_items; it += nthr) {
+        const int r = it & ((1 << lg_nrow) - 1), tb = it >> lg_nrow;
+        const int wp = r % WP, jj = r / WP;
         const int tl0 = tb * FB;
         float2 v0[2 * F + 3], v1[2 * F + 3], a2[FB], a3[FB];
         if constexpr (WT >= 2) {
@@ -249,21 +243,24 @@ __global__ void __launch_bounds__(384, 2) k_das_fwd_st(
         }
     }
     __syncthreads();
-    for (int o = tid; o < G * WT * TT; o += nthr) {
-        const int tl = o % TT, rw = o / TT, w = rw % WT, jj = rw / WT;
-        const int d = d0 + jj, t = t0 + tl;
-        if (d < D && t < T) raw[((size_t)(w0 + w) * D + d) * T + t] = s_out[rw * TTp + tl];
+    // rows (detector, instance) of the tile, lanes along t
+    for (int rw = warp; rw < G * WT; rw += nwarp) {
+        const int d = d0 + rw / WT, w = rw % WT;
+        if (d >= D) continue;
+        float *row = raw + ((size_t)(w0 + w) * D + d) * T;
+        for (int tl = lane; tl < TT; tl += 32)
+            if (t0 + tl < T) row[t0 + tl] = s_out[rw * TTp + tl];
     }
 }
 
 // ---------------------------------------------------------------------------
 // host: table construction at plan creation
 // ---------------------------------------------------------------------------
-// words of the entries region: the entries, then (after the moments) the
-// output tile [G][wt][TT + 1]; a multiple of 4
-int st_ent_region(const Plan &p, int wt) {
-    const int out = p.st_g * wt * (p.st_tt + 1);
-    return (std::max(p.st_ent_cap, out) + 3) & ~3;
+// floats of the image-value / moment region at an instance tile of wt
+int st_x_words(const Plan &p, int wt) {
+    const int NBKp = (p.st_tt + 2 * p.F + 1) | 1;
+    const size_t xs = std::max((size_t)p.st_umax * wt, (size_t)p.st_g * 4 * wt * NBKp);
+    return (int)((xs + 3) & ~(size_t)3);
 }
 
 static inline int floor_div(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
@@ -277,9 +274,7 @@ static inline void st_tile_range(int b, int TT, int F, int n_tiles, int &k0, int
 }
 
 size_t st_smem_bytes(const Plan &p, int wt) {
-    const int NBKp = (p.st_tt + 2 * p.F + 1) | 1;
-    const size_t xs = std::max((size_t)p.st_umax * wt, (size_t)p.st_g * 4 * wt * NBKp);
-    return (size_t)st_ent_region(p, wt) * 4 + (size_t)p.st_off_stride * 4 + 16 + xs * 4;
+    return ((size_t)st_x_words(p, wt) + (size_t)p.st_g * wt * (p.st_tt + 1)) * 4;
 }
 
 namespace {
@@ -348,9 +343,10 @@ int build_fwd_staged_host(const Plan &p, const int32_t *tfx, const int32_t *foff
     const int n_groups_8 = div_up(p.D, 8);
     const int step8 = sample ? std::max(1, n_groups_8 / 32) : 1;
     int best_tt = 0, best_g = 0;
-    // two CTAs per SM (228 KB less 1 KB per CTA), else one; shapes of at
-    // least two warps first
-    const size_t budgets[] = {(size_t)113 * 1024, (size_t)std::max(0, dev_smem - 1024)};
+    // three CTAs per SM (228 KB less 1 KB per CTA), else two, else one;
+    // shapes of at least two warps first
+    const size_t budgets[] = {(size_t)75 * 1024, (size_t)113 * 1024,
+                              (size_t)std::max(0, dev_smem - 1024)};
     for (int min_threads : {64, 1})
         for (size_t budget : budgets) {
             if (best_tt) break;
@@ -363,10 +359,9 @@ int build_fwd_staged_host(const Plan &p, const int32_t *tfx, const int32_t *foff
                     const size_t umax = sample ? (size_t)s.umax * 5 / 4 : (size_t)s.umax;
                     const size_t emax = sample ? (size_t)s.emax * 5 / 4 + 64 : (size_t)s.emax;
                     if (umax >= ((size_t)1 << ib)) continue;
+                    (void)emax;
                     const size_t xs = std::max(umax * 8, (size_t)G * 4 * 8 * (NBK | 1));
-                    const size_t er = std::max(emax, (size_t)G * 8 * (TT + 1));
-                    const size_t need = ((er + 3) & ~(size_t)3) * 4 +
-                                        (size_t)((G * (NBK + 1) + 3) & ~3) * 4 + 16 + xs * 4;
+                    const size_t need = (xs + (size_t)G * 8 * (TT + 1)) * 4;
                     if (need > budget) continue;
                     if (best_cost < 0 || s.cost < best_cost) {
                         best_cost = s.cost;
@@ -498,6 +493,12 @@ int build_fwd_staged(Plan &p, const int32_t *tfx, const int32_t *foff, const int
 // ---------------------------------------------------------------------------
 // host: launch
 // ---------------------------------------------------------------------------
+static int ilog2(int v) {
+    int l = 0;
+    while ((1 << (l + 1)) <= v) ++l;
+    return l;
+}
+
 template <class K>
 static int st_set_smem(K kern, size_t bytes) {
     if (bytes > 48 * 1024) {
@@ -518,9 +519,9 @@ static int st_launch(const Plan &p, const float *xt, float *raw, int W, float sc
     if ((rc = st_set_smem(k_das_fwd_st<WT, F>, smem)) != MSOT_OK) return rc;
     const dim3 grid((unsigned)(p.st_ntiles * p.st_ngroups), (unsigned)(W / WT));
     KLAUNCH(k_das_fwd_st<WT, F><<<grid, p.st_threads, smem, st>>>(
-        p.st_info, p.st_u, p.st_off, p.st_ent, xt, raw, p.P, p.D, p.T, p.st_g, p.st_tt,
-        p.st_ntiles, p.st_off_stride, st_ent_region(p, WT), p.st_ib, p.frac_bits, p.inv_r, p.ce1,
-        p.ce2, scale));
+        p.st_info, p.st_u, p.st_off, p.st_ent, xt, raw, p.P, p.D, p.T, ilog2(p.st_g),
+        ilog2(p.st_tt), p.st_ntiles, p.st_off_stride, st_x_words(p, WT), p.st_ib, p.frac_bits,
+        p.inv_r, p.ce1, p.ce2, scale));
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
 }
@@ -557,21 +558,12 @@ bool fwd_staged_fits(const Plan &p, int wt) {
 int launch_das_forward_staged(const Plan &p, const float *xt, float *raw, int W, int wt,
                               float scale, cudaStream_t st) {
     switch (wt) {
+        case 16: return st_launch_f<16>(p, xt, raw, W, scale, st);
         case 8: return st_launch_f<8>(p, xt, raw, W, scale, st);
         case 4: return st_launch_f<4>(p, xt, raw, W, scale, st);
         case 2: return st_launch_f<2>(p, xt, raw, W, scale, st);
         default: return st_launch_f<1>(p, xt, raw, W, scale, st);
     }
-}
-
-int fwd_staged_error(int clear) {
-    int v = 0;
-    if (cudaMemcpyFromSymbol(&v, g_fwd_st_err, sizeof v) != cudaSuccess) return -1;
-    if (clear && v) {
-        const int z = 0;
-        cudaMemcpyToSymbol(g_fwd_st_err, &z, sizeof z);
-    }
-    return v;
 }
 
 }  // namespace msot

@@ -1070,16 +1070,19 @@ static int das_fwd_f(const Plan &pl, const float *xpm, float *raw, int W, float 
 
 std::atomic<int> g_fwd_staged{1};
 
-int das_fwd_wt(const Plan &pl, int W) {
-    if (pl.tune_fwd_wt && W % pl.tune_fwd_wt == 0) return pl.tune_fwd_wt;
-    return pick_wt(W, 1, 8);
-}
-
 // the staged kernel (das_fwd_staged.cu) where the plan has its tables and
 // they fit shared memory at this instance tile, else k_das_fwd3
 static bool use_staged(const Plan &pl, int wt) {
     const int sel = pl.tune_fwd_staged ? pl.tune_fwd_staged : (g_fwd_staged.load() ? 1 : 2);
     return sel == 1 && fwd_staged_fits(pl, wt);
+}
+
+// 16 instances per CTA only for the staged kernel (k_das_fwd3 takes <= 8)
+int das_fwd_wt(const Plan &pl, int W) {
+    int wt = pick_wt(W, 1, 8);
+    if (pl.tune_fwd_wt && W % pl.tune_fwd_wt == 0) wt = pl.tune_fwd_wt;
+    if (wt > 8 && !use_staged(pl, wt)) wt = pick_wt(W, 1, 8);
+    return wt;
 }
 
 int launch_das_forward(const Plan &pl, const float *xpm, float *raw, int W, float scale,

@@ -13,6 +13,7 @@
 
 #include <map>
 #include <mutex>
+#include <set>
 #include <utility>
 
 #include "common.cuh"
@@ -431,6 +432,14 @@ extern "C" {
 const char *msot_last_error(void) { return g_err; }
 int msot_version(void) { return 1; }
 
+static std::mutex g_live_mu;
+static std::set<const msot_plan *> g_live;  // plans created and not yet destroyed
+
+int msot_plan_valid(msot_plan_t plan) {
+    std::lock_guard<std::mutex> g(g_live_mu);
+    return plan && g_live.count(plan) ? 1 : 0;
+}
+
 int msot_plan_create(const msot_plan_desc *desc, msot_plan_t *out) {
     if (!out) {
         set_error("plan: null output handle");
@@ -445,12 +454,20 @@ int msot_plan_create(const msot_plan_desc *desc, msot_plan_t *out) {
         delete h;
         return rc;
     }
+    {
+        std::lock_guard<std::mutex> g(g_live_mu);
+        g_live.insert(h);
+    }
     *out = h;
     return MSOT_OK;
 }
 
 int msot_plan_destroy(msot_plan_t plan) {
     if (!plan) return MSOT_OK;
+    {
+        std::lock_guard<std::mutex> g(g_live_mu);
+        g_live.erase(plan);
+    }
     free_plan(plan->p);
     delete plan;
     return MSOT_OK;

@@ -73,29 +73,9 @@ __device__ __forceinline__ void cp_async_wait_all() {
     asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
-// packed FP32 pair arithmetic (sm_100 family): each lane rounds as the
-// scalar fmaf / addition does
-__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
-    unsigned long long d;
-    asm("{\n\t.reg .b64 ra, rb, rc;\n\t"
-        "mov.b64 ra, {%1, %2};\n\tmov.b64 rb, {%3, %4};\n\tmov.b64 rc, {%5, %6};\n\t"
-        "fma.rn.f32x2 %0, ra, rb, rc;\n\t}"
-        : "=l"(d)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
-    float2 r;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(d));
-    return r;
-}
-__device__ __forceinline__ float2 fadd2(float2 a, float2 b) {
-    unsigned long long d;
-    asm("{\n\t.reg .b64 ra, rb;\n\t"
-        "mov.b64 ra, {%1, %2};\n\tmov.b64 rb, {%3, %4};\n\t"
-        "add.rn.f32x2 %0, ra, rb;\n\t}"
-        : "=l"(d)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    float2 r;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(d));
-    return r;
-}
+// packed FP32 pair arithmetic (sm_100 family, CUDA's builtins): each lane
+// rounds as the scalar fmaf / addition does
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 fadd2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 
 }  // namespace msot

@@ -1685,8 +1685,8 @@ extern "C" int msot_autotune(msot_plan_t plan, int batch, void *stream, msot_tun
         int pick = 0, pick_kernel = 0;
         for (int kernel : {1, 2}) {
             if (kernel == 1 && !pl.st_tt) continue;
-            for (int wt : {8, 4, 2}) {
-                if (batch % wt) continue;
+            for (int wt : {16, 8, 4, 2}) {
+                if (batch % wt || (wt > 8 && kernel != 1)) continue;
                 if (kernel == 1 && !fwd_staged_fits(pl, wt)) continue;
                 pl.tune_fwd_wt = wt;
                 pl.tune_fwd_staged = kernel;
