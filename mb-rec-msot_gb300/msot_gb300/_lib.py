@@ -75,6 +75,19 @@ class SpmrInfo(C.Structure):
         ("n_dist", C.c_int), ("n_angle", C.c_int), ("n_sir", C.c_int), ("sir_len", C.c_int),
     ]
 
+class ModelFields(C.Structure):
+    """msot_model_fields: the reference model object's fields a plan is
+    built from (MSOTmodel.m:18-48)."""
+    _fields_ = [
+        ("nx", C.c_int), ("nz", C.c_int), ("n_det", C.c_int), ("n_t", C.c_int),
+        ("radius", C.c_double), ("travel", C.POINTER(C.c_double)),
+        ("ir_hat", C.POINTER(C.c_double)), ("n_hat", C.c_int), ("eir_length", C.c_int),
+        ("prefilter", C.POINTER(C.c_double)), ("sir_len", C.c_int), ("n_sir", C.c_int),
+        ("sir", C.POINTER(C.c_double)), ("sir_start_end", C.POINTER(C.c_int32)),
+        ("sir_idx", C.POINTER(C.c_int32)), ("norm", C.c_double), ("max_batch", C.c_int),
+    ]
+
+
 # name: (restype, argtypes)
 SIGNATURES = {
     "msot_last_error": (C.c_char_p, []),
@@ -142,6 +155,16 @@ SIGNATURES = {
     "msot_profile_enable": (C.c_int, [C.c_int]),
     "msot_profile_kernel_name": (C.c_char_p, [C.c_int]),
     "msot_profile_read": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "msot_plan_valid": (C.c_int, [_vp]),
+    "msot_plan_create_from_model": (C.c_int, [C.POINTER(ModelFields), C.POINTER(_vp)]),
+    "msot_plan_norm": (C.c_double, [_vp]),
+    "msot_host_apply": (C.c_int, [_vp, C.c_int, _dp, C.c_int, _dp]),
+    "msot_host_rec_nn_with_L2_reg": (C.c_int, [_vp, _dp, C.c_int, C.c_int, C.c_double,
+                                               C.c_double, _dp, _dp, _dp, _dp]),
+    "msot_host_rec_nn_with_L1_eye_reg": (C.c_int, [_vp, _dp, C.c_int, C.c_int, C.c_double,
+                                                   _dp, _dp, _dp]),
+    "msot_host_rec_nn_with_TV_reg": (C.c_int, [_vp, _dp, C.c_int, C.c_int, C.c_double, _dp,
+                                               _dp, _dp]),
     "msot_mex_forwardDelayAndSum": (C.c_int, [_dp, C.c_int, C.c_int, _dp, C.c_int, C.c_int,
                                               C.c_double, _dp]),
     "msot_mex_transposeDelayAndSum": (C.c_int, [_dp, C.c_int, C.c_int, C.c_int, _dp, C.c_int,
