@@ -453,6 +453,9 @@ typedef struct msot_model_fields {
 int msot_plan_create_from_model(const msot_model_fields *fields, msot_plan_t *plan);
 /* The plan's normalisation factor (0 for an invalid handle). */
 double msot_plan_norm(msot_plan_t plan);
+/* The plan's grid, detectors, samples and largest batch (any pointer may be
+ * NULL); MSOT_EINVAL for an invalid handle.  No device work. */
+int msot_plan_shape(msot_plan_t plan, int *nx, int *nz, int *n_det, int *n_t, int *max_batch);
 
 /* model.Funcs.applyForward (transpose = 0: image Nz x Nx x W -> sinogram
  * T x D x W) and applyTranspose (transpose = 1: the reverse), FP64 host
@@ -464,7 +467,9 @@ int msot_host_apply(msot_plan_t plan, int transpose, const double *in, int W, do
  * stack; rec receives Nz x Nx x W.  rec_nn_with_L2_reg.m:1 (RegL2 the
  * identity weighted by lambdaL2 > 0, RegL2_2 laplacian_per_wavelength
  * weighted by lambdaL2_2 > 0 and used only with lambdaL2 > 0, as the
- * reference does; err_reg2 may be NULL, else it receives ||del2(rec)||^2). */
+ * reference does).  err_reg (may be NULL) receives ||rec||^2 and err_reg2
+ * (may be NULL) ||del2(rec)||^2 whatever the weights, as the reference
+ * evaluates them whenever RegL2 / RegL2_2 are given. */
 int msot_host_rec_nn_with_L2_reg(msot_plan_t plan, const double *data, int W, int num_iter,
                                  double lambdaL2, double lambdaL2_2, double *rec,
                                  double *err_img, double *err_reg, double *err_reg2);

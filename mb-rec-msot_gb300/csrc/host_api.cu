@@ -210,6 +210,20 @@ double msot_plan_norm(msot_plan_t plan) {
     return msot_plan_valid(plan) ? plan->p.norm : 0.0;
 }
 
+int msot_plan_shape(msot_plan_t plan, int *nx, int *nz, int *n_det, int *n_t, int *max_batch) {
+    if (!msot_plan_valid(plan)) {
+        set_error("plan_shape: not a live plan handle");
+        return MSOT_EINVAL;
+    }
+    const Plan &pl = plan->p;
+    if (nx) *nx = pl.nx;
+    if (nz) *nz = pl.nz;
+    if (n_det) *n_det = pl.D;
+    if (n_t) *n_t = pl.T;
+    if (max_batch) *max_batch = pl.max_batch;
+    return MSOT_OK;
+}
+
 int msot_host_apply(msot_plan_t plan, int transpose, const double *in, int W, double *out) {
     int rc = check_host_call(plan, in, out, W, transpose ? "applyTranspose" : "applyForward");
     if (rc) return rc;
@@ -260,10 +274,16 @@ int msot_host_rec_nn_with_L2_reg(msot_plan_t plan, const double *data, int W, in
         e3[0] = s;
     }
     if ((rc = device_copy_out(x, rec, NI))) return rc;
-    double s1 = 0, s2 = 0, s3 = 0;
-    for (int w = 0; w < W; ++w) s1 += e1[w], s2 += e2[w], s3 += e3[w];
+    double s1 = 0, s3 = 0;
+    for (int w = 0; w < W; ++w) s1 += e1[w], s3 += e3[w];
     if (err_img) *err_img = s1;
-    if (err_reg) *err_reg = s2;
+    if (err_reg) {
+        // ||RegL2(rec)||^2 with RegL2 the identity, whatever lambdaL2
+        // (rec_nn_with_L2_reg.m:52-56)
+        double s2 = 0;
+        for (size_t k = 0; k < NI; ++k) s2 += rec[k] * rec[k];
+        *err_reg = s2;
+    }
     if (err_reg2) *err_reg2 = s3;
     return MSOT_OK;
 }

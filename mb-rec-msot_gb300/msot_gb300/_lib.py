@@ -158,6 +158,8 @@ SIGNATURES = {
     "msot_plan_valid": (C.c_int, [_vp]),
     "msot_plan_create_from_model": (C.c_int, [C.POINTER(ModelFields), C.POINTER(_vp)]),
     "msot_plan_norm": (C.c_double, [_vp]),
+    "msot_plan_shape": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                  C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "msot_host_apply": (C.c_int, [_vp, C.c_int, _dp, C.c_int, _dp]),
     "msot_host_rec_nn_with_L2_reg": (C.c_int, [_vp, _dp, C.c_int, C.c_int, C.c_double,
                                                C.c_double, _dp, _dp, _dp, _dp]),
