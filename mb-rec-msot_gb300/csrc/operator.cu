@@ -346,10 +346,15 @@ __global__ void __launch_bounds__(256, 4) k_das_fwd3(const int32_t *__restrict__
 // Adjoint by pixel blocks: CTA = (64x64 pixel block, instance tile of WT,
 // detector group).  For each detector of its group the CTA stages the
 // sinogram samples spanned by the block (plus F+1 on each side) in shared
-// memory, builds the bucket table Q_b = (U_b, V_b, s[b-F], s[b+F+1]) of the
-// span there (each thread filters ADJ_BPT consecutive buckets from a register
-// window), and every thread adds U + f V + e1 s[b-F] + e2 s[b+F+1] to its 16
-// pixels.  Groups write partial images; k_sum_parts adds them in fixed order.
+// memory and builds a bucket table there (each thread filters ADJ_BPT
+// consecutive buckets from a register window).  A pixel of bucket b with
+// fraction f receives v(f) = U + f V + e1(f) s[b-F] + e2(f) s[b+F+1]
+// (U = sum alpha_k s[b+k], V = sum beta_k s[b+k]); as e1 and e2 are linear
+// in f on either side of their kinks at f = r - F and f = F + 1 - r, v is
+// linear on the three pieces between p1 = min(r - F, F + 1 - r) and
+// p2 = max(...), and the table holds (A, B) with v = A + f B per (bucket,
+// piece): one 8-byte load and one FMA per (pixel, detector, instance).
+// Groups write partial images; k_sum_parts adds them in fixed order.
 constexpr int ADJ_BPT = 4;  // buckets per thread when building Q
 std::atomic<int> g_adj_prefetch{1};  // next-detector prefetch in k_das_adj4 (msot_tune_set)
 
@@ -360,12 +365,12 @@ template <int WT, int F, int PF = 0>
 __global__ void __launch_bounds__(BLK_THREADS, 3) k_das_adj4(
     const int32_t *__restrict__ btau, const int2 *__restrict__ bspan,
     const float *__restrict__ s, float *__restrict__ part, int nx, int nz, int nbx, int D,
-    int T, int fb, float inv_r, float ce1, float ce2, int span_max, int det_per_group,
-    size_t part_stride) {
+    int T, int fb, float inv_r, float ce1, float ce2, float p1, float p2, int span_max,
+    int det_per_group, size_t part_stride) {
     extern __shared__ float sm[];
     const int SL = ((span_max + ADJ_BPT - 1) / ADJ_BPT) * ADJ_BPT + 2 * F + 2;
     float *seg = sm;  // [WT][SL]
-    float4 *Q = reinterpret_cast<float4 *>(sm + ((WT * SL + 3) & ~3));  // [WT][span_max]
+    float2 *Q = reinterpret_cast<float2 *>(sm + ((WT * SL + 3) & ~3));  // [WT][3][span_max]
     const int blk = blockIdx.x, w0 = blockIdx.y * WT, grp = blockIdx.z;
     const int t = threadIdx.x;
     const int bxi = blk % nbx, bzi = blk / nbx;
@@ -433,7 +438,18 @@ __global__ void __launch_bounds__(BLK_THREADS, 3) k_das_adj4(
                 U = fmaf(1.f - (float)(k < 0 ? -k : k) * inv_r, g[k], U);
                 V += k <= 0 ? -g[k] : g[k];
             }
-            Q[(size_t)w * span_max + bl] = make_float4(U, V * inv_r, g[-F], g[F + 1]);
+            // pieces f < p1, p1 <= f < p2, f >= p2: e1 = ce1 - f / r below
+            // r - F, e2 = f / r - ce2 above F + 1 - r
+            const float Vr = V * inv_r, sL = g[-F], sH = g[F + 1];
+            const float A0 = fmaf(ce1, sL, U), B0 = fmaf(-inv_r, sL, Vr);
+            const float A2 = fmaf(-ce2, sH, U), B2 = fmaf(inv_r, sH, Vr);
+            const bool lo_first = ce1 <= ce2;  // r - F <= F + 1 - r: e1 ends before e2 starts
+            const float A1 = lo_first ? U : fmaf(-ce2, sH, A0);
+            const float B1 = lo_first ? Vr : fmaf(inv_r, sH, B0);
+            float2 *q = Q + (size_t)w * 3 * span_max + bl;
+            q[0] = make_float2(A0, B0);
+            q[span_max] = make_float2(A1, B1);
+            q[2 * span_max] = make_float2(A2, B2);
         }
         __syncthreads();
         const int32_t *tp = btau + ((size_t)blk * D + d) * BLK + t;
@@ -441,14 +457,12 @@ __global__ void __launch_bounds__(BLK_THREADS, 3) k_das_adj4(
         for (int k = 0; k < BLK_PPT; ++k) {
             const int32_t tau = __ldg(tp + k * BLK_THREADS);
             if (tau == TAU_PAD) continue;
-            const int bl = (tau >> fb) - sp.x;
             const float f = (float)(tau & mask) * step;
-            const float e1 = fmaxf(0.f, fmaf(-f, inv_r, ce1));
-            const float e2 = fmaxf(0.f, fmaf(f, inv_r, -ce2));
+            const int bp = (tau >> fb) - sp.x + ((f >= p1) + (f >= p2)) * span_max;
 #pragma unroll
             for (int i = 0; i < WT; ++i) {
-                const float4 v = Q[(size_t)i * span_max + bl];
-                acc[k][i] = fmaf(e2, v.w, fmaf(e1, v.z, fmaf(f, v.y, acc[k][i] + v.x)));
+                const float2 v = Q[(size_t)i * 3 * span_max + bp];
+                acc[k][i] = fmaf(f, v.y, acc[k][i] + v.x);
             }
         }
         __syncthreads();
@@ -951,6 +965,15 @@ __global__ void __launch_bounds__(1 << (2 * LOG4N - 2)) k_conv_fft(
 // ---------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------
+// kinks of the adjoint's piecewise-linear bucket response in the fraction f:
+// r - F (where e1 reaches zero) and F + 1 - r (where e2 starts)
+static float adj_p1(const Plan &pl) {
+    return (float)std::min(pl.radius - pl.F, pl.F + 1 - pl.radius);
+}
+static float adj_p2(const Plan &pl) {
+    return (float)std::max(pl.radius - pl.F, pl.F + 1 - pl.radius);
+}
+
 static int pick_wt(int W, int T, int max_wt) {
     for (int wt = max_wt; wt > 1; wt >>= 1)
         if (W % wt == 0 && (size_t)wt * T * sizeof(float) <= 160 * 1024) return wt;
@@ -1104,7 +1127,7 @@ static int das_adj_launch(const Plan &pl, const float *raw, float *x, int W, flo
                           cudaStream_t st) {
     const int SL = div_up(pl.blk_span_max, ADJ_BPT) * ADJ_BPT + 2 * F + 2;
     const size_t smem = (size_t)((WT * SL + 3) & ~3) * sizeof(float) +
-                        (size_t)WT * pl.blk_span_max * sizeof(float4);
+                        (size_t)WT * 3 * pl.blk_span_max * sizeof(float2);
     int rc;
     const int base = pl.n_blk * (W / WT);
     int groups = std::max(1, std::min(pl.D, div_up(2 * sm_count(), base)));
@@ -1119,7 +1142,8 @@ static int das_adj_launch(const Plan &pl, const float *raw, float *x, int W, flo
         if ((rc = set_smem(k_das_adj4<WT, F, PFV>, smem)) != MSOT_OK) return rc;           \
         KLAUNCH(k_das_adj4<WT, F, PFV><<<grid, BLK_THREADS, smem, st>>>(                   \
             pl.blk_tau, pl.blk_span, raw, pl.scr_part, pl.nx, pl.nz, pl.n_blk_x, pl.D, pl.T, \
-            pl.frac_bits, pl.inv_r, pl.ce1, pl.ce2, pl.blk_span_max, dpg, stride));        \
+            pl.frac_bits, pl.inv_r, pl.ce1, pl.ce2, adj_p1(pl), adj_p2(pl), pl.blk_span_max, dpg, \
+            stride));                                                                      \
     } while (0)
     // next-detector prefetch when the segment fits PF registers per instance
     if (g_adj_prefetch.load() && SL <= 2 * BLK_THREADS)
@@ -1465,7 +1489,7 @@ static int das_adj_launch_fixed(const Plan &pl, const float *raw, float *x, int 
                                 cudaStream_t st, float *part) {
     const int SL = div_up(pl.blk_span_max, ADJ_BPT) * ADJ_BPT + 2 * F + 2;
     const size_t smem = (size_t)((WT * SL + 3) & ~3) * sizeof(float) +
-                        (size_t)WT * pl.blk_span_max * sizeof(float4);
+                        (size_t)WT * 3 * pl.blk_span_max * sizeof(float2);
     int rc;
     if ((rc = set_smem(k_das_adj4<WT, F>, smem)) != MSOT_OK) return rc;
     const size_t stride = (size_t)W * pl.P;
@@ -1479,7 +1503,8 @@ static int das_adj_launch_fixed(const Plan &pl, const float *raw, float *x, int 
     // k_das_adj4 before k_sum_parts reads it: nothing needs clearing
     KLAUNCH(k_das_adj4<WT, F><<<grid, BLK_THREADS, smem, st>>>(
         pl.blk_tau, pl.blk_span, raw, part, pl.nx, pl.nz, pl.n_blk_x, pl.D, pl.T,
-        pl.frac_bits, pl.inv_r, pl.ce1, pl.ce2, pl.blk_span_max, dpg, stride));
+        pl.frac_bits, pl.inv_r, pl.ce1, pl.ce2, adj_p1(pl), adj_p2(pl), pl.blk_span_max, dpg,
+        stride));
     MSOT_LAUNCH_CHECK();
     KLAUNCH(k_sum_parts<<<(unsigned)std::min<size_t>(4096, div_up((int)stride, 256)), 256, 0,
                           st>>>(part, x, stride, groups, stride, 1.f));
