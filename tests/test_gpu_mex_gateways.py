@@ -77,13 +77,23 @@ def test_apply_forward_and_transpose_match_the_oracle(env, model):
 
 
 def test_normalisation_estimated_when_not_given(env):
+    # [] for the factor: sigma_max by the library's power iteration (100
+    # steps), as MSOTmodel(..., None) of the Python mirror estimates it on
+    # the same geometry
+    from pairs import make_pair
     drv, om, fields = env
     h = _create(drv, om, fields, 0.0, 1)
     out = np.zeros(1)
     msg = C.create_string_buffer(512)
     assert drv.drv_model(b"normalizationFactor", h, None, 0, mexdrv.dptr(out), 1, msg, 512) == 0
-    assert abs(out[0] - om.norm) / om.norm < 1e-3
     assert drv.drv_model(b"destroy", h, None, 0, None, 0, msg, 512) == 0
+    pm, _ = make_pair(n=N, n_det=D, n_samples=T, radius=0.02, fov_half=0.0063, norm=1.0,
+                      max_batch=1)
+    ref = pm.estimate_sigma_max(100)
+    assert abs(out[0] - ref) / ref < 1e-4
+    # power iteration approaches sigma_max from below: within a few per cent
+    # of the oracle's own (shorter) estimate
+    assert abs(out[0] - om.norm) / om.norm < 3e-2
 
 
 def _ops(om, W):
