@@ -359,7 +359,7 @@ int msot_butter_response(int order, int type, double wn1, double wn2, int n, int
  * hot kernels on its own geometry at `batch` instances -- the DAS forward's
  * kernel (image values staged in shared memory per time tile and detector
  * group, or gathered per detector) and instances per CTA (8, 4, 2), the DAS
- * adjoint's instances per CTA (2, 1), the register cap of the
+ * adjoint's instances per CTA (4, 2, 1), the register cap of the
  * IR convolution (1, 3, 4 resident CTAs per SM) and, for square grids, the
  * CTAs per image of the
  * SB_ITV2 cluster kernel (automatic, 1 .. 16) -- and keeps the fastest in
@@ -369,7 +369,7 @@ int msot_butter_response(int order, int type, double wn1, double wn2, int n, int
 typedef struct msot_tuning {
     int fwd_wt, conv_min_blocks, tv_cluster;  /* 0 = the built-in choice */
     double fwd_ms, transpose_ms, tv_prox_ms;  /* per apply of the chosen variant */
-    int adj_wt;                               /* instances per CTA of the DAS adjoint */
+    int adj_wt;                               /* instances per CTA of the DAS adjoint (4, 2, 1) */
     int fwd_staged;                           /* DAS forward: 1 staged, 2 per-detector buckets */
 } msot_tuning;
 int msot_autotune(msot_plan_t plan, int batch, void *stream, msot_tuning *out);

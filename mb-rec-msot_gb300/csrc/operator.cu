@@ -234,7 +234,7 @@ __global__ void k_permute(const float *__restrict__ in, float *__restrict__ out,
 constexpr int FWD_UNR = 2;
 
 template <int WT, int F>
-__global__ void __launch_bounds__(256, 4) k_das_fwd3(const int32_t *__restrict__ off,
+__global__ void __launch_bounds__(256, WT >= 16 ? 2 : 4) k_das_fwd3(const int32_t *__restrict__ off,
                                                   const int2 *__restrict__ ent,
                                                   const float *__restrict__ xpm,
                                                   float *__restrict__ raw, int P, int D, int T,
@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(256, 4) k_das_fwd3(const int32_t *__restrict__
                                                   float ce2, float scale) {
     constexpr int NB = 256;
     constexpr int TB = NB - 2 * F - 2;
-    __shared__ float mom[4 * WT * NB];  // [4][WT][NB], bucket fastest
+    extern __shared__ float mom[];  // [4][WT][NB], bucket fastest (dynamic: 4 KB x WT)
     const int d = blockIdx.y, w0 = blockIdx.z * WT;
     const int t0 = blockIdx.x * TB;
     const int b_lo = t0 - F - 1;
@@ -362,7 +362,7 @@ std::atomic<int> g_adj_prefetch{1};  // next-detector prefetch in k_das_adj4 (ms
 // samples per instance per thread; needs SL <= PF * BLK_THREADS) while the
 // current one is filtered and gathered.
 template <int WT, int F, int PF = 0>
-__global__ void __launch_bounds__(BLK_THREADS, 3) k_das_adj4(
+__global__ void __launch_bounds__(BLK_THREADS, WT >= 4 ? 2 : 3) k_das_adj4(
     const int32_t *__restrict__ btau, const int2 *__restrict__ bspan,
     const float *__restrict__ s, float *__restrict__ part, int nx, int nz, int nbx, int D,
     int T, int fb, float inv_r, float ce1, float ce2, float p1, float p2, int span_max,
@@ -1064,7 +1064,10 @@ static int das_fwd_launch(const Plan &pl, const float *xpm, float *raw, int W, f
                           cudaStream_t st) {
     constexpr int NB = 256, TB = NB - 2 * F - 2;
     dim3 grid(div_up(pl.T, TB), pl.D, W / WT);
-    KLAUNCH(k_das_fwd3<WT, F><<<grid, NB, 0, st>>>(pl.fwd_off, pl.fwd_ent, xpm, raw, pl.P,
+    const size_t smem = (size_t)4 * WT * NB * sizeof(float);
+    int rc;
+    if ((rc = set_smem(k_das_fwd3<WT, F>, smem)) != MSOT_OK) return rc;
+    KLAUNCH(k_das_fwd3<WT, F><<<grid, NB, smem, st>>>(pl.fwd_off, pl.fwd_ent, xpm, raw, pl.P,
                                                       pl.D, pl.T, W, pl.frac_bits, pl.inv_r,
                                                       pl.ce1, pl.ce2, scale));
     MSOT_LAUNCH_CHECK();
@@ -1100,12 +1103,11 @@ static bool use_staged(const Plan &pl, int wt) {
     return sel == 1 && fwd_staged_fits(pl, wt);
 }
 
-// 16 instances per CTA only for the staged kernel (k_das_fwd3 takes <= 8)
+// instances per CTA of the DAS forward: the autotuner's pick (16, 8, 4, 2),
+// else the largest of 8, 4, 2 dividing W
 int das_fwd_wt(const Plan &pl, int W) {
-    int wt = pick_wt(W, 1, 8);
-    if (pl.tune_fwd_wt && W % pl.tune_fwd_wt == 0) wt = pl.tune_fwd_wt;
-    if (wt > 8 && !use_staged(pl, wt)) wt = pick_wt(W, 1, 8);
-    return wt;
+    if (pl.tune_fwd_wt && W % pl.tune_fwd_wt == 0) return pl.tune_fwd_wt;
+    return pick_wt(W, 1, 8);
 }
 
 int launch_das_forward(const Plan &pl, const float *xpm, float *raw, int W, float scale,
@@ -1114,6 +1116,7 @@ int launch_das_forward(const Plan &pl, const float *xpm, float *raw, int W, floa
     const int wt = das_fwd_wt(pl, W);
     if (use_staged(pl, wt)) return launch_das_forward_staged(pl, xpm, raw, W, wt, scale, st);
     switch (wt) {
+        case 16: return das_fwd_f<16>(pl, xpm, raw, W, scale, st);
         case 8: return das_fwd_f<8>(pl, xpm, raw, W, scale, st);
         case 4: return das_fwd_f<4>(pl, xpm, raw, W, scale, st);
         case 2: return das_fwd_f<2>(pl, xpm, raw, W, scale, st);
@@ -1185,6 +1188,7 @@ int launch_das_adjoint(const Plan &pl, const float *raw, float *x, int W, float 
     TimedScope ts_(KID_INTERP_ADJ, st);
     int wt = pick_wt(W, 1, 2);
     if (pl.tune_adj_wt && W % pl.tune_adj_wt == 0) wt = pl.tune_adj_wt;
+    if (wt == 4) return das_adj_f<4>(pl, raw, x, W, scale, st);
     if (wt == 2) return das_adj_f<2>(pl, raw, x, W, scale, st);
     return das_adj_f<1>(pl, raw, x, W, scale, st);
 }

@@ -1686,7 +1686,7 @@ extern "C" int msot_autotune(msot_plan_t plan, int batch, void *stream, msot_tun
         for (int kernel : {1, 2}) {
             if (kernel == 1 && !pl.st_tt) continue;
             for (int wt : {16, 8, 4, 2}) {
-                if (batch % wt || (wt > 8 && kernel != 1)) continue;
+                if (batch % wt) continue;
                 if (kernel == 1 && !fwd_staged_fits(pl, wt)) continue;
                 pl.tune_fwd_wt = wt;
                 pl.tune_fwd_staged = kernel;
@@ -1707,7 +1707,7 @@ extern "C" int msot_autotune(msot_plan_t plan, int batch, void *stream, msot_tun
     {
         double best = 1e30;
         int pick = 0;
-        for (int wt : {2, 1}) {
+        for (int wt : {4, 2, 1}) {
             if (batch % wt) continue;
             pl.tune_adj_wt = wt;
             double ms;
