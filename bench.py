@@ -87,6 +87,10 @@ def parse():
                     help="batched L1-NNLS (rec_nn_with_L1_eye_reg) at 400x400 px, 512-element "
                          "arc over 270 deg, 4096 samples, 64 instances: one JSON line")
     ap.add_argument("--l1-grid", type=int, default=400)
+    ap.add_argument("--l1-bf16", action="store_true",
+                    help="--l1: BF16 storage of the forward's interpolation input")
+    ap.add_argument("--l1-refine", type=int, default=0,
+                    help="--l1 with --l1-bf16: every k-th outer iteration in FP32")
     ap.add_argument("--l1-iters", type=int, default=50)
     ap.add_argument("--l1-check-iters", type=int, default=0,
                     help="iterations of the instance-0 solve compared with the FP64 oracle "
@@ -629,6 +633,8 @@ def run_l1(args):
     amp = y.abs().amax(dim=(1, 2), keepdim=True)
     gen = torch.Generator(device="cuda").manual_seed(405)
     b = (y + 0.01 * amp * torch.randn(y.shape, device="cuda", generator=gen)).contiguous()
+    if args.l1_bf16:  # after the data: the sinograms come from the FP32 operator
+        model.set_storage(True, args.l1_refine)
     L = _lib.load()
     for _ in range(max(1, args.warmup)):
         rec_nn_with_L1_eye_reg(model, b, args.l1_iters, reg)
@@ -651,6 +657,8 @@ def run_l1(args):
         cpu = {"value": 1.0 / acc["cpu_fp64_s"], "unit": "recons/s", "cores": os.cpu_count(),
                "kind": "port", "sample": "instance 0, FP64 oracle solve"}
     return {"mode": "l1_nnls", "metric": "L1-NNLS recons/s", "value": B / (ms_step / 1e3),
+            "storage": ({"interp_input": "bf16", "fp32_every": args.l1_refine}
+                        if args.l1_bf16 else {"interp_input": "fp32"}),
             "cpu_baseline": cpu,
             "unit": "recons/s", "ms_per_step": ms_step, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "gpu_launches_per_step": launches,

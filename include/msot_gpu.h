@@ -97,6 +97,19 @@ int msot_interp_forward(msot_plan_t plan, const float *d_coeffs, float *d_raw, i
 int msot_interp_transpose(msot_plan_t plan, const float *d_raw, float *d_coeffs, int batch,
                           void *stream);
 
+/* Reduced-precision storage (the mixed-precision configuration of the
+ * reference's L1 solve; no counterpart in the reference, which is FP64
+ * throughout).  image_bf16 = 1: the interpolation input of the DAS forward
+ * (the prefiltered image the forwardDelayAndSumMex.cpp:80-100 loop reads per
+ * (pixel, detector) pair) is stored in BF16, round to nearest, and widened
+ * to FP32 for the FP32 accumulation; this halves the bytes the forward
+ * gathers.  refine_every = k > 0: the L1 solver runs every k-th outer
+ * iteration with the FP32 input (the other solvers use the setting as is).
+ * The FP32 default meets the operators' 1e-5 bar; BF16 storage is for solves
+ * judged by their 1e-3 bar against the FP64 oracle.  Plans without SIR only;
+ * drops the plan's captured solver graphs. */
+int msot_plan_set_storage(msot_plan_t plan, int image_bf16, int refine_every);
+
 /* Allocation-free form of msot_interp_transpose for plans without SIR; no
  * counterpart in the reference.  It is for callers that are not allowed to
  * allocate device memory, e.g. a host application whose device memory is

@@ -34,9 +34,20 @@
 #include <algorithm>
 #include <mutex>
 
+#include <cuda_bf16.h>
+
 #include "common.cuh"
 
 namespace msot {
+
+// the interpolation input in [W/wt][P][wt] order, FP32 or (out_bf16) BF16
+// rounded to nearest (the reduced-storage path of msot_plan_set_storage)
+__device__ __forceinline__ void store_interp_input(float *out, size_t i, float v, int out_bf16) {
+    if (out_bf16)
+        reinterpret_cast<__nv_bfloat16 *>(out)[i] = __float2bfloat16_rn(v);
+    else
+        out[i] = v;
+}
 
 __device__ __forceinline__ int tap_lo(int32_t tau, int32_t r_fx, int fb) {
     return -((r_fx - tau) >> fb);
@@ -57,7 +68,8 @@ __device__ __forceinline__ float tri_weight(int t, int32_t tau, int fb, float c1
 __global__ void k_prefilter(const float *__restrict__ in, float *__restrict__ out,
                             const float *__restrict__ taps, int K, int nx, int nz, int W,
                             int along_x, int transpose, float scale,
-                            const int32_t *__restrict__ perm, int out_mode, int wt) {
+                            const int32_t *__restrict__ perm, int out_mode, int wt,
+                            int out_bf16) {
     const int P = nx * nz;
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long)W * P) return;
@@ -83,7 +95,7 @@ __global__ void k_prefilter(const float *__restrict__ in, float *__restrict__ ou
         acc = fmaf(h, __ldg(src + s), acc);
     }
     if (out_mode == 2)
-        out[((size_t)(w / wt) * P + j) * wt + w % wt] = acc * scale;
+        store_interp_input(out, ((size_t)(w / wt) * P + j) * wt + w % wt, acc * scale, out_bf16);
     else
         out[(size_t)w * P + j] = acc * scale;
 }
@@ -108,7 +120,7 @@ template <int KM>
 __global__ void __launch_bounds__(PF_THREADS) k_prefilter2d(
     const float *__restrict__ in, float *__restrict__ out, const float *__restrict__ taps_x,
     const float *__restrict__ taps_z, int Kx, int Kz, int nx, int nz, int W, int transpose,
-    int out_mode, int wt) {
+    int out_mode, int wt, int out_bf16) {
     constexpr int NC = PF_TX + 2 * KM;  // staged columns
     constexpr int NTAP = 2 * KM + 1;
     constexpr int NW = PF_THREADS / 32;
@@ -185,7 +197,8 @@ __global__ void __launch_bounds__(PF_THREADS) k_prefilter2d(
             if (ix >= nx) break;
             const size_t p = (size_t)ix * nz + z;
             if (out_mode == 2)
-                out[((size_t)(w / wt) * nx * nz + p) * wt + w % wt] = acc[j];
+                store_interp_input(out, ((size_t)(w / wt) * nx * nz + p) * wt + w % wt, acc[j],
+                                   out_bf16);
             else
                 out[(size_t)w * nx * nz + p] = acc[j];
         }
@@ -194,11 +207,11 @@ __global__ void __launch_bounds__(PF_THREADS) k_prefilter2d(
 
 // [W][P] -> [W/wt][P][wt] (pixel-major within each tile of wt instances)
 __global__ void k_to_pixmajor(const float *__restrict__ in, float *__restrict__ out, int P,
-                              int W, int wt) {
+                              int W, int wt, int out_bf16) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long)W * P) return;
     const int w = (int)(idx / P), j = (int)(idx % P);
-    out[((size_t)(w / wt) * P + j) * wt + w % wt] = __ldg(in + idx);
+    store_interp_input(out, ((size_t)(w / wt) * P + j) * wt + w % wt, __ldg(in + idx), out_bf16);
 }
 
 // [W][P] -> [W][P] in scatter order (out[w][j] = in[w][perm[j]])
@@ -233,10 +246,49 @@ __global__ void k_permute(const float *__restrict__ in, float *__restrict__ out,
 // applies the (2F+2)-tap filter over the bucket moments.
 constexpr int FWD_UNR = 2;
 
-template <int WT, int F>
+// one pixel's WT instance values of the interpolation input, FP32 or BF16
+// (widened exactly: a BF16 value is the upper half of its FP32 pattern)
+template <int WT>
+__device__ __forceinline__ void load_pixel(const float *xp, float (&xv)[WT]) {
+    if constexpr (WT % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < WT; i += 4) {
+            const float4 v = __ldg(reinterpret_cast<const float4 *>(xp + i));
+            xv[i] = v.x; xv[i + 1] = v.y; xv[i + 2] = v.z; xv[i + 3] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < WT; ++i) xv[i] = __ldg(xp + i);
+    }
+}
+__device__ __forceinline__ float bf16_lo(uint32_t v) { return __uint_as_float(v << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t v) { return __uint_as_float(v & 0xffff0000u); }
+template <int WT>
+__device__ __forceinline__ void load_pixel(const __nv_bfloat16 *xp, float (&xv)[WT]) {
+    if constexpr (WT % 8 == 0) {
+#pragma unroll
+        for (int i = 0; i < WT; i += 8) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4 *>(xp + i));
+            xv[i] = bf16_lo(v.x); xv[i + 1] = bf16_hi(v.x);
+            xv[i + 2] = bf16_lo(v.y); xv[i + 3] = bf16_hi(v.y);
+            xv[i + 4] = bf16_lo(v.z); xv[i + 5] = bf16_hi(v.z);
+            xv[i + 6] = bf16_lo(v.w); xv[i + 7] = bf16_hi(v.w);
+        }
+    } else if constexpr (WT % 2 == 0) {
+#pragma unroll
+        for (int i = 0; i < WT; i += 2) {
+            const uint32_t v = __ldg(reinterpret_cast<const unsigned int *>(xp + i));
+            xv[i] = bf16_lo(v); xv[i + 1] = bf16_hi(v);
+        }
+    } else {
+        xv[0] = __uint_as_float((uint32_t)__ldg(reinterpret_cast<const unsigned short *>(xp)) << 16);
+    }
+}
+
+template <int WT, int F, typename XT = float>
 __global__ void __launch_bounds__(256, WT >= 16 ? 2 : 4) k_das_fwd3(const int32_t *__restrict__ off,
                                                   const int2 *__restrict__ ent,
-                                                  const float *__restrict__ xpm,
+                                                  const XT *__restrict__ xpm,
                                                   float *__restrict__ raw, int P, int D, int T,
                                                   int W, int fb, float inv_r, float ce1,
                                                   float ce2, float scale) {
@@ -283,19 +335,8 @@ __global__ void __launch_bounds__(256, WT >= 16 ? 2 : 4) k_das_fwd3(const int32_
 #pragma unroll
                 for (int u = 0; u < FWD_UNR; ++u) q[u] = qn[u];
 #pragma unroll
-                for (int u = 0; u < FWD_UNR; ++u) {
-                    const float *xp = xpm + ((size_t)blockIdx.z * P + max(q[u].y, 0)) * WT;
-                    if constexpr (WT % 4 == 0) {
-#pragma unroll
-                        for (int i = 0; i < WT; i += 4) {
-                            const float4 v = __ldg(reinterpret_cast<const float4 *>(xp + i));
-                            xv[u][i] = v.x; xv[u][i + 1] = v.y; xv[u][i + 2] = v.z; xv[u][i + 3] = v.w;
-                        }
-                    } else {
-#pragma unroll
-                        for (int i = 0; i < WT; ++i) xv[u][i] = __ldg(xp + i);
-                    }
-                }
+                for (int u = 0; u < FWD_UNR; ++u)
+                    load_pixel<WT>(xpm + ((size_t)blockIdx.z * P + max(q[u].y, 0)) * WT, xv[u]);
 #pragma unroll
                 for (int u = 0; u < FWD_UNR; ++u)
                     qn[u] = j + FWD_UNR + u < j1 ? __ldg(e + j + FWD_UNR + u) : make_int2(0, -1);
@@ -1000,7 +1041,8 @@ int launch_prefilter(const Plan &pl, const float *in, float *out, int W, bool tr
     const long n = (long)W * pl.P;
     const int wt = out_mode == 2 ? das_fwd_wt(pl, W) : 1;
     KLAUNCH(k_prefilter<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
-        in, out, taps, K, pl.nx, pl.nz, W, along_x, transpose, scale, pl.perm, out_mode, wt));
+        in, out, taps, K, pl.nx, pl.nz, W, along_x, transpose, scale, pl.perm, out_mode, wt,
+        out_mode == 2 ? pl.image_bf16 : 0));
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
 }
@@ -1018,7 +1060,7 @@ static int prefilter2d_km(const Plan &pl, const float *in, float *out, int W, bo
     const int wt = out_mode == 2 ? das_fwd_wt(pl, W) : 1;
     KLAUNCH(k_prefilter2d<KM><<<grid, PF_THREADS, smem, st>>>(
         in, out, pl.pre_x, pl.pre_z, pl.Kx, pl.Kz, pl.nx, pl.nz, W, transpose ? 1 : 0, out_mode,
-        wt));
+        wt, out_mode == 2 ? pl.image_bf16 : 0));
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
 }
@@ -1052,8 +1094,8 @@ static int fwd_split(const Plan &pl, int nwt) {
 int launch_to_pixmajor(const Plan &pl, const float *in, float *out, int W, cudaStream_t st) {
     TimedScope ts_(KID_PERMUTE, st);
     const long n = (long)W * pl.P;
-    KLAUNCH(k_to_pixmajor<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, pl.P, W,
-                                                                         das_fwd_wt(pl, W)));
+    KLAUNCH(k_to_pixmajor<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+        in, out, pl.P, W, das_fwd_wt(pl, W), pl.image_bf16));
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
 }
@@ -1066,6 +1108,15 @@ static int das_fwd_launch(const Plan &pl, const float *xpm, float *raw, int W, f
     dim3 grid(div_up(pl.T, TB), pl.D, W / WT);
     const size_t smem = (size_t)4 * WT * NB * sizeof(float);
     int rc;
+    if (pl.image_bf16) {
+        const auto *xb = reinterpret_cast<const __nv_bfloat16 *>(xpm);
+        if ((rc = set_smem(k_das_fwd3<WT, F, __nv_bfloat16>, smem)) != MSOT_OK) return rc;
+        KLAUNCH(k_das_fwd3<WT, F, __nv_bfloat16><<<grid, NB, smem, st>>>(
+            pl.fwd_off, pl.fwd_ent, xb, raw, pl.P, pl.D, pl.T, W, pl.frac_bits, pl.inv_r, pl.ce1,
+            pl.ce2, scale));
+        MSOT_LAUNCH_CHECK();
+        return MSOT_OK;
+    }
     if ((rc = set_smem(k_das_fwd3<WT, F>, smem)) != MSOT_OK) return rc;
     KLAUNCH(k_das_fwd3<WT, F><<<grid, NB, smem, st>>>(pl.fwd_off, pl.fwd_ent, xpm, raw, pl.P,
                                                       pl.D, pl.T, W, pl.frac_bits, pl.inv_r,
@@ -1099,6 +1150,7 @@ std::atomic<int> g_fwd_staged{1};
 // the staged kernel (das_fwd_staged.cu) where the plan has its tables and
 // they fit shared memory at this instance tile, else k_das_fwd3
 static bool use_staged(const Plan &pl, int wt) {
+    if (pl.image_bf16) return false;  // BF16 storage is read by k_das_fwd3 only
     const int sel = pl.tune_fwd_staged ? pl.tune_fwd_staged : (g_fwd_staged.load() ? 1 : 2);
     return sel == 1 && fwd_staged_fits(pl, wt);
 }
@@ -1587,6 +1639,22 @@ int msot_interp_transpose(msot_plan_t plan, const float *d_raw, float *d_coeffs,
     int rc = check_batch(plan, batch, d_raw, d_coeffs);
     if (rc) return rc;
     return interp_adjoint(plan->p, d_raw, d_coeffs, batch, 1.f, (cudaStream_t)stream);
+}
+
+int msot_plan_set_storage(msot_plan_t plan, int image_bf16, int refine_every) {
+    if (!plan || (image_bf16 != 0 && image_bf16 != 1) || refine_every < 0) {
+        set_error("plan_set_storage: image_bf16 must be 0 or 1 and refine_every >= 0");
+        return MSOT_EINVAL;
+    }
+    Plan &pl = plan->p;
+    if (image_bf16 && pl.S) {
+        set_error("plan_set_storage: BF16 storage is for plans without SIR");
+        return MSOT_EINVAL;
+    }
+    pl.storage_bf16 = pl.image_bf16 = image_bf16;
+    pl.refine_every = refine_every;
+    solver_cache_invalidate(pl);  // captured graphs hold the previous kernels
+    return MSOT_OK;
 }
 
 int msot_interp_transpose_noalloc(msot_plan_t plan, const float *d_raw, float *d_coeffs,

@@ -100,6 +100,7 @@ SIGNATURES = {
     "msot_interp_forward": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp]),
     "msot_interp_transpose": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp]),
     "msot_interp_transpose_noalloc": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp]),
+    "msot_plan_set_storage": (C.c_int, [_vp, C.c_int, C.c_int]),
     "msot_estimate_norm": (C.c_int, [_vp, C.c_int, C.c_uint64, _dp, _vp]),
     "msot_rec_nn_with_L2_reg": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_double, _vp,
                                           C.c_int, _dp, _dp, _vp]),

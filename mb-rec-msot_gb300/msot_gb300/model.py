@@ -378,6 +378,13 @@ class MSOTmodel:
                                              _stream_ptr(stream), C.byref(t)))
         return {f: getattr(t, f) for f, _ in t._fields_}
 
+    def set_storage(self, image_bf16: bool = False, refine_every: int = 0) -> None:
+        """msot_plan_set_storage: BF16 storage of the DAS forward's
+        interpolation input (FP32 accumulation), and in the L1 solver every
+        ``refine_every``-th outer iteration with the FP32 input."""
+        _lib.check(_lib.load().msot_plan_set_storage(self.plan, 1 if image_bf16 else 0,
+                                                     int(refine_every)))
+
     def estimate_sigma_max(self, iters: int = 100, seed: int = 0) -> float:
         out = C.c_double()
         _lib.check(_lib.load().msot_estimate_norm(self._plan, int(iters), int(seed),
