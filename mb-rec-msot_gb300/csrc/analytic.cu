@@ -9,7 +9,6 @@
 // operation rounded separately (no contraction into FMA), so it rounds exactly
 // as the FP64 reference does; an index outside the sinogram, where MATLAB
 // raises an error, is reported as MSOT_ERANGE.  Sums over detectors are FP64.
-#include <cublas_v2.h>
 
 #include <cmath>
 #include <vector>
@@ -312,29 +311,16 @@ int msot_backproject_waveeq(const float *d_sig, int W, int D, int T, const doubl
     KLAUNCH(k_psf_same<<<dim3(div_up(T, 128), D, W), 128, 0, st>>>(s1, s2, dpsf, psf_m, psf_n,
                                                                  1.0 / psum, D, T));
     MSOT_LAUNCH_CHECK();
-    // s1 = K(acq, acq) * s2 * dt : one column-major GEMM over all (d, w) columns
-    cublasHandle_t h = nullptr;
-    if (cublasCreate(&h) != CUBLAS_STATUS_SUCCESS) {
-        set_error("backproject_waveeq: cublasCreate failed");
-        return MSOT_ECUDA;
-    }
-    cublasSetStream(h, st);
-    const float alpha = (float)dt, beta = 0.f;
+    // s1 = K(acq, acq) * s2 * dt : one column-major GEMM over all (d, w)
+    // columns, on the tensor cores (gemm_tc.cu)
     const float *Ksub = d_K + (size_t)crop * K_n + crop;
-    cublasStatus_t cs = cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, T, D * W, T, &alpha, Ksub, K_n,
-                                    s2, T, &beta, s1, T);
-    cublasDestroy(h);
-    if (cs != CUBLAS_STATUS_SUCCESS) {
-        set_error("backproject_waveeq: cublasSgemm failed (%d)", (int)cs);
-        return MSOT_ECUDA;
-    }
-    ++g_launch_count;  // the GEMM
+    RC(tc_sgemm(T, D * W, T, (float)dt, Ksub, K_n, s2, T, s1, T, st));
     KLAUNCH(k_bp_gather<<<dim3(div_up(P, 128), W), 128, 0, st>>>(s1, idx, ca, sa, P, D, T, dt * c,
                                                                  fx, fz));
     KLAUNCH(k_div_fliplr<<<dim3(div_up(P, 256), W), 256, 0, st>>>(fx, fz, dx, dz, nx, nz, d_out));
     MSOT_LAUNCH_CHECK();
     MSOT_CUDA_TRY(cudaStreamSynchronize(st));
-    return MSOT_OK;
+    return tc_sgemm_check();
 }
 
 }  // extern "C"

@@ -258,6 +258,14 @@ extern std::atomic<int> g_fwd_staged;
 // laid out [W/wt][P][wt] (pixel-major within an instance tile).  operator.cu
 int das_fwd_wt(const Plan &pl, int W);
 
+// C (M x N) = alpha A (M x K) B (K x N), column-major FP32, on the tensor
+// cores with a 3 x TF32 split (FP32-level accuracy); gemm_tc.cu
+int tc_sgemm(int M, int N, int K, float alpha, const float *A, int lda, const float *B, int ldb,
+             float *C, int ldc, cudaStream_t st);
+// MSOT_ETIMEOUT (and clears the flag) when a tc_sgemm tile's bounded wait ran
+// out since the last check; synchronises the device
+int tc_sgemm_check();
+
 // Streaming multiprocessors of the current device (queried once per device,
 // cached; 1 if the query fails).  Launch heuristics size grids by it.  plan.cu
 int sm_count();

@@ -23,7 +23,6 @@
 // h = ifft(|H|^2) as one FP32 GEMM with the T x T circulant (cuBLAS SGEMM,
 // a plain library GEMM): 2 T^2 flops per column at the SGEMM rate instead of
 // an arbitrary-length FFT.
-#include <cublas_v2.h>
 
 #include <cmath>
 #include <complex>
@@ -143,9 +142,7 @@ struct msot_prep {
     float *win = nullptr;   // [T] window |h|, or null
     float *circ = nullptr;  // [T][T] circulant of ifft(|H|^2) (column-major), or null
     float *work = nullptr;  // [max_cols][T] GEMM input
-    cublasHandle_t blas = nullptr;
     ~msot_prep() {
-        if (blas) cublasDestroy(blas);
         cudaFree(win);
         cudaFree(circ);
         cudaFree(work);
@@ -248,11 +245,6 @@ int msot_prep_create(int T_raw, int n_crop, int window_order, double window_low,
             return fail(e);
         if ((e = cudaMalloc(&pp->work, sizeof(float) * (size_t)max_cols * T)) != cudaSuccess)
             return fail(e);
-        if (cublasCreate(&pp->blas) != CUBLAS_STATUS_SUCCESS) {
-            delete pp;
-            set_error("prep_create: cublasCreate failed");
-            return MSOT_ECUDA;
-        }
     }
     *out = pp;
     return MSOT_OK;
@@ -281,17 +273,10 @@ int msot_prep_apply(msot_prep_t p, const float *d_raw, float *d_out, int n_cols,
     KLAUNCH(k_prep_columns<<<n_cols, 256, sizeof(float) * p->T, st>>>(
         d_raw, p->T_raw, p->n_crop, p->T, p->win, p->demean, dst));
     MSOT_LAUNCH_CHECK();
-    if (p->circ) {
-        const float one = 1.f, zero = 0.f;
-        cublasSetStream(p->blas, st);
-        const cublasStatus_t cs = cublasSgemm(p->blas, CUBLAS_OP_N, CUBLAS_OP_N, p->T, n_cols,
-                                              p->T, &one, p->circ, p->T, p->work, p->T, &zero,
-                                              d_out, p->T);
-        if (cs != CUBLAS_STATUS_SUCCESS) {
-            set_error("prep_apply: cublasSgemm failed (%d)", (int)cs);
-            return MSOT_ECUDA;
-        }
-    }
+    // the zero-phase filter: the T x T circulant times the columns, on the
+    // tensor cores (gemm_tc.cu)
+    if (p->circ) return tc_sgemm(p->T, n_cols, p->T, 1.f, p->circ, p->T, p->work, p->T, d_out,
+                                 p->T, st);
     return MSOT_OK;
 }
 

@@ -65,7 +65,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         list(ex.map(compile_one, zip(srcs, objs)))
     if force or _stale(LIB_PATH, objs):
-        cmd = [nv, *ARCH_FLAGS, "-shared", "-o", LIB_PATH, *objs, "-lcudart", "-lcublas"]
+        cmd = [nv, *ARCH_FLAGS, "-shared", "-o", LIB_PATH, *objs, "-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
