@@ -76,6 +76,10 @@ def parse():
     ap.add_argument("--ws-input-iters", type=int, default=10)
     ap.add_argument("--ws-backprojection", default="transpose", choices=["transpose", "waveeq"],
                     help="network input when --ws-input-iters is 0")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the learned-start arm of the headline line")
+    ap.add_argument("--learned-pairs", type=int, default=1024)
+    ap.add_argument("--learned-steps", type=int, default=1500)
     ap.add_argument("--unet", action="store_true",
                     help="warm-start U-Net alone (4 levels, 32 base channels, batch 16): "
                          "training steps and forward passes: one JSON line")
@@ -411,6 +415,9 @@ def run_ours(args, rank, world):
             "sample": f"{ONE_THREAD_ITERS} of the {N_ITER} outer iterations of instance 0 with "
                       f"the C kernels on one thread; recons/s = ({ONE_THREAD_ITERS}/{N_ITER}) / "
                       "time"}
+    learned = None
+    if not args.no_learned and world == 1:
+        learned = learned_arm(model, args)
     return {
         "metric": METRIC, "value": value, "unit": "recons/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
@@ -418,9 +425,71 @@ def run_ours(args, rank, world):
         "data": "synthetic (seeded disk+vessel phantoms, 1% noise)",
         "config": workload_config(B, world), "clocks": clk.summary(), "e2e": e2e,
         "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
-        "autotune": tuning,
+        "autotune": tuning, "learned": learned,
         "rel_error_vs_fp64": acc, "host": platform.machine(),
     }
+
+
+def learned_arm(model, args, frames=64):
+    """The metric's learned arm on the headline geometry: a U-Net (4 levels,
+    32 base channels; the project's kernels) trained on `learned_pairs` pairs
+    the plain GPU solver generates (input: the plain iterate after
+    ws_input_iters iterations; target: the 200-iteration solution), then on
+    `frames` held-out frames: the accuracy to reach is the headline plain
+    solve's (N_ITER iterations) relative distance to a 1000-iteration solve;
+    the learned solve is the input iterations + network + the fewest warm
+    iterations that reach it (residual-rise fallback included).  Times are
+    CUDA events of the batched calls."""
+    import torch
+    from msot_gb300 import rec_nn_with_L2_reg
+    from msot_gb300.synthetic import phantom_batch
+    from msot_gb300.warmstart import LearnedWarmStart
+    P = args.learned_pairs
+    ws = LearnedWarmStart(model, LAMBDA, levels=4, base_channels=32, max_batch=16,
+                          input_iters=args.ws_input_iters)
+    imgs = phantom_batch(model.Discretization, P + frames, seed=11)
+    (f, t, b), pair_ms = _event_ms(lambda: ws.make_pairs(imgs, 200, seed=12))
+    losses, train_ms = _event_ms(lambda: ws.fit(f[:P], t[:P], args.learned_steps, batch=16,
+                                                lr=2e-3))
+    bt = b[P:P + frames].contiguous()
+    del f, t, b
+    xs = rec_nn_with_L2_reg(model, bt, 1000, LAMBDA)[0]
+    err = lambda x: float((x - xs).norm() / xs.norm())
+    rec_nn_with_L2_reg(model, bt, N_ITER, LAMBDA)  # warm-up
+    xp, plain_ms = _event_ms(lambda: rec_nn_with_L2_reg(model, bt, N_ITER, LAMBDA)[0])
+    target = err(xp)
+    ws.solve(bt, 5)  # warm-up (graph capture of the input and warm iterations)
+    scan, found = [], None
+    for k in (5, 10, 20, 30, 40, 50, 60, 80, 100, 150):
+        (r, fell), ms = _event_ms(lambda: ws.solve(bt, k, restart_iters=N_ITER))
+        e = err(r)
+        scan.append({"warm_iterations": k, "rel_err": e, "ms": ms,
+                     "fallback_instances": int(fell.sum())})
+        if e <= target:
+            found = (k, ms)
+            break
+    out = {"plain": {"iterations": N_ITER, "recons_per_s": frames / (plain_ms / 1e3),
+                     "rel_err_vs_1000_it": target},
+           "accuracy_target": "the plain solve's distance to a 1000-iteration solve",
+           "frames": frames, "warm_scan": scan,
+           "training": {"pairs": P, "pair_generation_s": pair_ms / 1e3,
+                        "steps": len(losses), "batch": 16,
+                        "ms_per_step": train_ms / max(1, len(losses)),
+                        "loss_first": float(np.mean(losses[:20])),
+                        "loss_last": float(np.mean(losses[-100:])),
+                        "input": f"plain iterate after {args.ws_input_iters} iterations",
+                        "grid": list(model.image_shape),
+                        "note": "a subset of the 20k-pair, 256 px training set, sized for "
+                                "the default bench run"}}
+    if found:
+        k, ms = found
+        out.update({"recons_per_s": frames / (ms / 1e3), "ratio_to_plain": plain_ms / ms,
+                    "iterations": {"plain": N_ITER, "learned": args.ws_input_iters + k,
+                                   "saved": N_ITER - args.ws_input_iters - k}})
+    else:
+        out.update({"recons_per_s": None, "ratio_to_plain": None,
+                    "iterations": {"plain": N_ITER, "learned": None, "saved": None}})
+    return out
 
 
 # ----------------------------------------------------------------------------

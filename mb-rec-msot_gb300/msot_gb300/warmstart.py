@@ -11,8 +11,10 @@ x / (kappa s), with s = rms(f) per instance and kappa = median rms(x) /
 rms(f) over the training pairs, so one network serves any data scale; with
 ``residual`` (an iterate as input, kappa = 1) the network predicts the
 correction x / s - f / s.  The plain solver stays
-the fallback: an instance whose prediction has a larger objective
-|A x0 - b|^2 + lambda |x0|^2 than the zero start (|b|^2) is started from zero.
+the fallback, twice: an instance whose prediction has a larger objective
+|A x0 - b|^2 + lambda |x0|^2 than the zero start (|b|^2) is started from
+zero, and (solve) an instance whose data residual |A x - b|^2 rose during the
+warm iterations above that of its start is solved again from zero.
 """
 from __future__ import annotations
 
@@ -216,8 +218,10 @@ class LearnedWarmStart:
         w = self.predict(b) if x0 is None else torch.as_tensor(x0).cuda().to(torch.float32)
         v = torch.empty_like(w)
         fell = torch.zeros(b.shape[0], dtype=torch.bool, device="cuda")
+        res0 = torch.empty(b.shape[0], dtype=torch.float64, device="cuda")
         for i, j in self._chunks(b.shape[0]):
             r = self.model.forward(w[i:j].contiguous()) - b[i:j]
+            res0[i:j] = r.flatten(1).double().pow(2).sum(1)
             obj = r.flatten(1).pow(2).sum(1) + self.lam * w[i:j].flatten(1).pow(2).sum(1)
             fell[i:j] = obj >= b[i:j].flatten(1).pow(2).sum(1)
             g = self.model.transpose(r.contiguous())
@@ -225,13 +229,28 @@ class LearnedWarmStart:
                 g = g + self.lam * w[i:j]
             v[i:j] = torch.where(w[i:j] > 0, torch.zeros_like(g), (g / self.beta).clamp_min(0))
         keep = (~fell).view(-1, 1, 1).to(torch.float32)
+        # data residual of each start (|b|^2 for a zero start), for solve()
+        self.start_residual = torch.where(fell, b.flatten(1).double().pow(2).sum(1), res0)
         return (w * keep).contiguous(), (v * keep).contiguous(), fell
 
-    def solve(self, b, iters, x0=None):
-        """rec_nn_with_L2_reg from the learned start; returns (rec, fallback
-        mask)."""
+    def solve(self, b, iters, x0=None, restart_iters=None):
+        """rec_nn_with_L2_reg from the learned start; an instance whose data
+        residual rose above its start's is solved again from zero with
+        ``restart_iters`` (default ``iters``) plain iterations.  Returns (rec,
+        fallback mask: objective test at the start or residual rise)."""
         b = self._sino(b)
         w, v, fell = self.start(b, x0)
-        recs = [rec_nn_with_L2_reg(self.model, b[i:j], iters, self.lam, x0=w[i:j],
-                                   v0=v[i:j])[0] for i, j in self._chunks(b.shape[0])]
-        return torch.cat(recs), fell
+        recs, res = [], []
+        for i, j in self._chunks(b.shape[0]):
+            out = rec_nn_with_L2_reg(self.model, b[i:j], iters, self.lam, x0=w[i:j], v0=v[i:j])
+            recs.append(out[0])
+            res.append(torch.as_tensor(out[1], dtype=torch.float64, device="cuda"))
+        rec = torch.cat(recs)
+        rose = torch.cat(res) > self.start_residual
+        if bool(rose.any()):
+            idx = torch.nonzero(rose).flatten()
+            again = torch.cat([rec_nn_with_L2_reg(self.model, b[idx[i:j]].contiguous(),
+                                                  restart_iters or iters, self.lam)[0]
+                               for i, j in self._chunks(idx.numel())])
+            rec[idx] = again
+        return rec, fell | rose
