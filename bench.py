@@ -84,6 +84,9 @@ def parse():
                     help="warm-start U-Net alone (4 levels, 32 base channels, batch 16): "
                          "training steps and forward passes: one JSON line")
     ap.add_argument("--unet-side", type=int, default=128)
+    ap.add_argument("--bp", action="store_true",
+                    help="analytic reconstructors: backproject_waveeq and dmas_cf on 256 "
+                         "frames of 256 det x 2030 samples, 128 x 128 px")
     ap.add_argument("--prep", action="store_true",
                     help="raw-sinogram pre-processing (crop 3, Butterworth window, zero-phase "
                          "filter) of 64 x 256 x 2033 samples: one JSON line")
@@ -235,10 +238,11 @@ def oracle_solve(model, b_np, threads, n_iter=None):
 
 
 # DRAM bytes (read + write) per launch of each family's kernel at batch 64,
-# from one ncu --set full capture of `bench.py --op --batch 64`
-NCU_TRAFFIC_B64 = {"interp_forward": 47.80288e6 + 84.551168e6,
-                   "interp_adjoint": 77.48736e6 + 2.382336e6,
-                   "ir_conv": 133.204992e6 + 85.45408e6,
+# from one ncu --set full capture per kernel of `bench.py --op --batch 64`
+# (profiles/das_kernels_128px_b64.md, profiles/eir_conv_fft_128px_b64.md)
+NCU_TRAFFIC_B64 = {"interp_forward": 47.601152e6 + 80.315648e6,
+                   "interp_adjoint": 77.760256e6 + 3.016448e6,
+                   "ir_conv": 133.13664e6 + 83.677184e6,
                    "prefilter": 4.246784e6}
 
 
@@ -740,6 +744,37 @@ def run_l1(args):
                        "batch": B, "grid": [n, n], "n_det": D, "n_t": T}}
 
 
+def run_bp(args):
+    """backproject_waveeq (backproject_waveeq.m:1-50; the K(t, t') product on
+    the tensor-core GEMM) and dmas_cf (dmas_cf.m:19-107) on 256 frames of
+    256 detectors x 2030 samples, 128 x 128 px over the 25.4 mm FOV, psf 1,
+    K = bp_kernel of the acquisition times; CUDA events around the calls."""
+    import torch
+    from msot_gb300.analytic import backproject_waveeq, bp_kernel_device, dmas_cf
+    F, D, T, n = 256, N_DET, N_T, N_GRID
+    g = torch.Generator(device="cuda").manual_seed(9)
+    sig = torch.randn((F, D, T), device="cuda", generator=g)
+    h = 0.2e-3 * 127 / 2
+    x = np.linspace(-h, h, n)
+    K = bp_kernel_device(np.arange(1, T + 1) / 4e7)
+    bp = lambda: backproject_waveeq(sig, x, x, 1500.0, 4e7, 0.0, 135.0, 0.040,
+                                    np.array([[1.0]]), K)
+    dm = lambda: dmas_cf(sig, x, x, 1500.0, 4e7, 0.0, 135.0, 0.040)
+    for _ in range(max(1, args.warmup)):
+        bp(); dm()
+    bp_ms = np.mean([_event_ms(bp)[1] for _ in range(args.steps)])
+    dm_ms = np.mean([_event_ms(dm)[1] for _ in range(args.steps)])
+    flops = 2.0 * T * T * D * F
+    return {"mode": "analytic", "metric": "frames / s", "frames": F,
+            "backproject_waveeq": {"ms_per_256_frames": bp_ms, "frames_per_s": F / (bp_ms / 1e3),
+                                   "gemm_flops": flops,
+                                   "gemm_tflops_fp32_equiv_upper_bound": flops / (bp_ms * 1e9)},
+            "dmas_cf": {"ms_per_256_frames": dm_ms, "frames_per_s": F / (dm_ms / 1e3)},
+            "steps": args.steps, "warmup": args.warmup, "dtype": "f32 (FP64 indices / sums)",
+            "data": "synthetic Gaussian noise sinograms",
+            "config": {"workload": f"{F} frames, {D} det x {T} samples, {n} x {n} px"}}
+
+
 def run_prep(args):
     """Pre-processing of a batch of raw sinograms (64 instances x 256
     detectors x 2033 samples, crop 3 -> 2030): window (order-2 band-pass
@@ -1083,6 +1118,10 @@ def main():
         import torch
         torch.cuda.set_device(0)
         out = run_prep(args)
+    elif args.bp:
+        import torch
+        torch.cuda.set_device(0)
+        out = run_bp(args)
     else:
         if world > 1:
             import torch

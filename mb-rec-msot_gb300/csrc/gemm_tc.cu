@@ -58,10 +58,15 @@ __device__ __forceinline__ float g_tf32(float x) {
 }
 
 // registers of one stage: A rows m = tid % 128, K groups tid / 128 + 2 j;
-// B column n = tid / 2, K groups 4 (tid % 2) + j
+// B column n = g_bcol(tid), K groups 4 g_bhalf(tid) + j.  Eight consecutive
+// threads take eight consecutive columns of the same K group, so that each
+// 8-thread phase of a 16-byte shared store fills one 128-byte core matrix
+// (no bank conflicts).
 struct GRegs {
     float4 a[4], b[4];
 };
+__device__ __forceinline__ int g_bcol(int tid) { return (tid & 7) | ((tid >> 4) << 3); }
+__device__ __forceinline__ int g_bhalf(int tid) { return (tid >> 3) & 1; }
 
 __device__ __forceinline__ void g_load(GRegs &R, const float *A, int lda, const float *B, int ldb,
                                        int M, int N, int K, int m0, int n0, int k0, bool bvec) {
@@ -79,11 +84,11 @@ __device__ __forceinline__ void g_load(GRegs &R, const float *A, int lda, const 
         }
     }
     {
-        const int n = n0 + tid / 2;
+        const int n = n0 + g_bcol(tid);
         const float *col = B + (size_t)n * ldb;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const int k = k0 + 4 * (4 * (tid % 2) + j);
+            const int k = k0 + 4 * (4 * g_bhalf(tid) + j);
             if (n < N && bvec && k + 3 < K) {
                 R.b[j] = __ldg(reinterpret_cast<const float4 *>(col + k));
             } else {
@@ -117,7 +122,8 @@ __device__ __forceinline__ void g_store(const GRegs &R, uint8_t *stage) {
 #pragma unroll
     for (int j = 0; j < 4; ++j) g_split_store(R.a[j], ahi, alo, g_off(tid % GT, tid / GT + 2 * j));
 #pragma unroll
-    for (int j = 0; j < 4; ++j) g_split_store(R.b[j], bhi, blo, g_off(tid / 2, 4 * (tid % 2) + j));
+    for (int j = 0; j < 4; ++j)
+        g_split_store(R.b[j], bhi, blo, g_off(g_bcol(tid), 4 * g_bhalf(tid) + j));
 }
 
 __global__ void __launch_bounds__(G_THREADS, 1) k_gemm_3xtf32(
