@@ -80,6 +80,8 @@ def parse():
                     help="skip the learned-start arm of the headline line")
     ap.add_argument("--learned-pairs", type=int, default=1024)
     ap.add_argument("--learned-steps", type=int, default=1500)
+    ap.add_argument("--learned-target-iters", type=int, default=0,
+                    help="plain iterations of the training targets (0: the headline's)")
     ap.add_argument("--unet", action="store_true",
                     help="warm-start U-Net alone (4 levels, 32 base channels, batch 16): "
                          "training steps and forward passes: one JSON line")
@@ -439,7 +441,8 @@ def learned_arm(model, args, frames=64):
     """The metric's learned arm on the headline geometry: a U-Net (4 levels,
     32 base channels; the project's kernels) trained on `learned_pairs` pairs
     the plain GPU solver generates (input: the plain iterate after
-    ws_input_iters iterations; target: the 200-iteration solution), then on
+    ws_input_iters iterations; target: the solution after
+    learned_target_iters iterations, default the headline's), then on
     `frames` held-out frames: the accuracy to reach is the headline plain
     solve's (N_ITER iterations) relative distance to a 1000-iteration solve;
     the learned solve is the input iterations + network + the fewest warm
@@ -450,10 +453,11 @@ def learned_arm(model, args, frames=64):
     from msot_gb300.synthetic import phantom_batch
     from msot_gb300.warmstart import LearnedWarmStart
     P = args.learned_pairs
+    target_iters = args.learned_target_iters or N_ITER
     ws = LearnedWarmStart(model, LAMBDA, levels=4, base_channels=32, max_batch=16,
                           input_iters=args.ws_input_iters)
     imgs = phantom_batch(model.Discretization, P + frames, seed=11)
-    (f, t, b), pair_ms = _event_ms(lambda: ws.make_pairs(imgs, 200, seed=12))
+    (f, t, b), pair_ms = _event_ms(lambda: ws.make_pairs(imgs, target_iters, seed=12))
     losses, train_ms = _event_ms(lambda: ws.fit(f[:P], t[:P], args.learned_steps, batch=16,
                                                 lr=2e-3))
     bt = b[P:P + frames].contiguous()
@@ -465,8 +469,12 @@ def learned_arm(model, args, frames=64):
     target = err(xp)
     ws.solve(bt, 5)  # warm-up (graph capture of the input and warm iterations)
     scan, found = [], None
-    for k in (5, 10, 20, 30, 40, 50, 60, 80, 100, 150):
-        (r, fell), ms = _event_ms(lambda: ws.solve(bt, k, restart_iters=N_ITER))
+    for k in (0, 2, 5, 10, 20, 30, 40, 50, 60, 80, 100, 150):
+        if k == 0:  # the network's start itself (input iterations + network)
+            (w0, _, fell), ms = _event_ms(lambda: ws.start(bt))
+            r = w0
+        else:
+            (r, fell), ms = _event_ms(lambda: ws.solve(bt, k, restart_iters=N_ITER))
         e = err(r)
         scan.append({"warm_iterations": k, "rel_err": e, "ms": ms,
                      "fallback_instances": int(fell.sum())})
@@ -483,6 +491,7 @@ def learned_arm(model, args, frames=64):
                         "loss_first": float(np.mean(losses[:20])),
                         "loss_last": float(np.mean(losses[-100:])),
                         "input": f"plain iterate after {args.ws_input_iters} iterations",
+                        "target": f"plain solution after {target_iters} iterations",
                         "grid": list(model.image_shape),
                         "note": "a subset of the 20k-pair, 256 px training set, sized for "
                                 "the default bench run"}}
