@@ -78,8 +78,10 @@ def parse():
                     help="network input when --ws-input-iters is 0")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-start arm of the headline line")
-    ap.add_argument("--learned-pairs", type=int, default=1024)
-    ap.add_argument("--learned-steps", type=int, default=1500)
+    ap.add_argument("--learned-pairs", type=int, default=4096)
+    ap.add_argument("--learned-steps", type=int, default=6000)
+    ap.add_argument("--learned-input-iters", type=int, default=5,
+                    help="plain iterations of the learned arm's network input")
     ap.add_argument("--learned-target-iters", type=int, default=0,
                     help="plain iterations of the training targets (0: the headline's)")
     ap.add_argument("--unet", action="store_true",
@@ -441,7 +443,7 @@ def learned_arm(model, args, frames=64):
     """The metric's learned arm on the headline geometry: a U-Net (4 levels,
     32 base channels; the project's kernels) trained on `learned_pairs` pairs
     the plain GPU solver generates (input: the plain iterate after
-    ws_input_iters iterations; target: the solution after
+    learned_input_iters iterations; target: the solution after
     learned_target_iters iterations, default the headline's), then on
     `frames` held-out frames: the accuracy to reach is the headline plain
     solve's (N_ITER iterations) relative distance to a 1000-iteration solve;
@@ -454,8 +456,9 @@ def learned_arm(model, args, frames=64):
     from msot_gb300.warmstart import LearnedWarmStart
     P = args.learned_pairs
     target_iters = args.learned_target_iters or N_ITER
+    ii = args.learned_input_iters
     ws = LearnedWarmStart(model, LAMBDA, levels=4, base_channels=32, max_batch=16,
-                          input_iters=args.ws_input_iters)
+                          input_iters=ii)
     imgs = phantom_batch(model.Discretization, P + frames, seed=11)
     (f, t, b), pair_ms = _event_ms(lambda: ws.make_pairs(imgs, target_iters, seed=12))
     losses, train_ms = _event_ms(lambda: ws.fit(f[:P], t[:P], args.learned_steps, batch=16,
@@ -469,7 +472,8 @@ def learned_arm(model, args, frames=64):
     target = err(xp)
     ws.solve(bt, 5)  # warm-up (graph capture of the input and warm iterations)
     scan, found = [], None
-    for k in (0, 2, 5, 10, 20, 30, 40, 50, 60, 80, 100, 150):
+    for k in (0, 2, 4, 6, 8, 10, 12, 14, 16, 18, 20, 22, 24, 26, 28, 30, 32, 34, 36, 38, 40,
+              45, 50, 60, 80, 100, 150):
         if k == 0:  # the network's start itself (input iterations + network)
             (w0, _, fell), ms = _event_ms(lambda: ws.start(bt))
             r = w0
@@ -490,7 +494,7 @@ def learned_arm(model, args, frames=64):
                         "ms_per_step": train_ms / max(1, len(losses)),
                         "loss_first": float(np.mean(losses[:20])),
                         "loss_last": float(np.mean(losses[-100:])),
-                        "input": f"plain iterate after {args.ws_input_iters} iterations",
+                        "input": f"plain iterate after {ii} iterations",
                         "target": f"plain solution after {target_iters} iterations",
                         "grid": list(model.image_shape),
                         "note": "a subset of the 20k-pair, 256 px training set, sized for "
@@ -498,8 +502,8 @@ def learned_arm(model, args, frames=64):
     if found:
         k, ms = found
         out.update({"recons_per_s": frames / (ms / 1e3), "ratio_to_plain": plain_ms / ms,
-                    "iterations": {"plain": N_ITER, "learned": args.ws_input_iters + k,
-                                   "saved": N_ITER - args.ws_input_iters - k}})
+                    "iterations": {"plain": N_ITER, "learned": ii + k,
+                                   "saved": N_ITER - ii - k}})
     else:
         out.update({"recons_per_s": None, "ratio_to_plain": None,
                     "iterations": {"plain": N_ITER, "learned": None, "saved": None}})
