@@ -59,6 +59,8 @@ def parse():
                          "16 frames): one JSON line")
     ap.add_argument("--tv-grids", default="128,200,256,400",
                     help="grid sizes the --tv instances are drawn from")
+    ap.add_argument("--tv-batch", type=int, default=64,
+                    help="--tv: most instances per solve call")
     ap.add_argument("--tv-concurrent", action="store_true",
                     help="also time the grid sizes solved concurrently (one host thread and "
                          "private stream per grid size)")
@@ -823,12 +825,12 @@ def run_tv(args):
     grid is drawn uniformly from --tv-grids (25.4 mm FOV); each frame has
     2-3 chromophores (disk + vessel phantoms) with random positive spectra;
     1 % noise; lambda_TV = 5e-3, 100 outer iterations.  Instances of one grid
-    size are solved in batches of up to 64; the value is instances / total
+    size are solved in batches of up to --tv-batch; the value is instances / total
     device time of the solves (sinograms resident)."""
     import torch
     from msot_gb300 import Discretization, MSOTmodel, Probe, rec_nn_with_TV_reg
     from msot_gb300.synthetic import gauss_pulse_eir, phantom
-    n_wl, n_fr, n_iter, reg, B = 28, 16, 100, 5e-3, 64
+    n_wl, n_fr, n_iter, reg, B = 28, 16, 100, 5e-3, args.tv_batch
     grids = [int(v) for v in args.tv_grids.split(",")]
     rng = np.random.default_rng(2024)
     grid_of = rng.choice(grids, size=(n_fr, n_wl))
@@ -893,7 +895,7 @@ def run_tv(args):
            "value": n_all / (total_ms / 1e3), "unit": "recons/s", "instances": n_all,
            "iterations": n_iter, "lambda_tv": reg, "per_grid": per_grid, "accuracy": acc,
            "data": "synthetic multispectral disk+vessel phantoms, 1% noise",
-           "note": "batched per grid size (max 64 per call); not one persistent launch"}
+           "note": f"batched per grid size (max {B} per call); not one persistent launch"}
     if args.tv_concurrent:
         # the grid sizes at once: one host thread per grid (the library call
         # releases the interpreter), each solve on its own stream; whole-job

@@ -375,7 +375,8 @@ int msot_butter_response(int order, int type, double wn1, double wn2, int n, int
  * adjoint's instances per CTA (4, 2, 1), the register cap of the
  * IR convolution (1, 3, 4 resident CTAs per SM) and, for square grids, the
  * CTAs per image of the
- * SB_ITV2 cluster kernel (automatic, 1 .. 16) -- and keeps the fastest in
+ * SB_ITV2 cluster kernel (automatic, 1 .. 16, or -1: 16 CTAs with the
+ * vectors in a global-memory workspace) -- and keeps the fastest in
  * the plan (they change results only in float summation order).  Drops the
  * plan's captured solver graphs.  Not concurrent with other calls on the
  * plan.  out (may be NULL) receives the choices and their times. */
@@ -390,7 +391,8 @@ int msot_autotune(msot_plan_t plan, int batch, void *stream, msot_tuning *out);
 /* Kernel tuning knob (no reference counterpart; results change only in
  * float summation order):
  *   "tv_prox_cluster"  CTAs per image of the shared-memory SB_ITV2 kernel
- *                      (1, 2, 4, 8, 16; 0 = automatic).
+ *                      (1, 2, 4, 8, 16; 0 = automatic; -1 = 16 CTAs per
+ *                      image with the vectors in global memory).
  *   "fwd_staged"       1 (default) = the DAS forward stages each CTA's image
  *                      values in shared memory where the plan's tables fit,
  *                      0 = per-detector L2 gathers (plans autotuned keep their pick).

@@ -616,8 +616,21 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
 // ---------------------------------------------------------------------------
 // The same cluster prox with 4 consecutive z-pixels per thread (N % 4 == 0):
 // 128-bit shared-memory accesses; thread t owns group jz = t % (N/4) (pixels
-// 4 jz .. 4 jz + 3) of the columns lc = t / (N/4), ... + G.  Arithmetic is
-// the scalar kernel's, per component.
+// 4 jz .. 4 jz + 3) of the columns lc = t / (N/4), ... + G.  The split-Bregman
+// sweep is the scalar kernel's; its CGS step is the same recurrence written
+// with one CTA barrier less, carrying M p and M q instead of p and uh (M =
+// I + B'B is linear, so M p_new = M uc + beta (M q + beta M p_old) and
+// M uh = M uc + M q, M q = M uc - alpha M vh):
+//   A  uc = r + beta q                                        (local)
+//      __syncthreads
+//   B  Muc = M uc (halo uc from the neighbour's r, q); vh = Muc + beta (Mq +
+//      beta vh); sum rt'vh -> alpha
+//   C  Mvh = M vh (halo vh from the neighbour); q = uc - alpha vh;
+//      Mq = Muc - alpha Mvh; x += alpha (uc + q); r -= alpha (Muc + Mq);
+//      sums r'r, rt'r -> convergence, beta
+// Two stencils and two cluster sums per step, as before; every vector read
+// remotely in a phase was written before the cluster barrier that opened
+// it, and is rewritten only after the next one.
 // ---------------------------------------------------------------------------
 struct F4 {
     float v[4];
@@ -718,8 +731,8 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
     float *S = c.sm;
     int ou = V_U * V, ox = V_X * V;
     const int ob1 = V_B1 * V, ob2 = V_B2 * V, orr = V_R * V, ort = V_RT * V, oq = V_Q * V,
-              ouc = V_UC * V, ouh = V_UH * V, ovh = V_VH * V, oxm = V_XMIN * V;
-    int op = V_P0 * V, opo = V_P1 * V;
+              ouc = V_UC * V, ovh = V_VH * V, oxm = V_XMIN * V;
+    const int omq = V_P0 * V, omuc = V_P1 * V;  // M q and M uc (no p, no uh here)
     int par = 0, n_sweeps = 0, n_cg = 0;
     float A = 0.f, B = 0.f;
     float n2b = 0.f, rho = 0.f, rho1 = 1.f, normrmin = 0.f;
@@ -786,46 +799,43 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
             for (int cit = 0; cit < TV_CG_MAX; ++cit) {
                 ++n_cg;
                 const float beta = beta_next;
-                {
-                    const int t = op;
-                    op = opo;
-                    opo = t;
-                }
+                const bool first = cit == 0;
+                // A: uc = r + beta q
                 TVC4_FOR(c) {
                     const F4 rv = ld4(S + orr + l);
-                    if (cit == 0) {
+                    if (first) {
                         st4(S + ouc + l, rv);
-                        st4(S + op + l, rv);
                     } else {
-                        const F4 qv = ld4(S + oq + l), pv = ld4(S + opo + l);
-                        F4 uv, pn;
+                        const F4 qv = ld4(S + oq + l);
+                        F4 uv;
 #pragma unroll
-                        for (int k = 0; k < 4; ++k) {
-                            uv.v[k] = fmaf(beta, qv.v[k], rv.v[k]);
-                            pn.v[k] = fmaf(beta, fmaf(beta, pv.v[k], qv.v[k]), uv.v[k]);
-                        }
+                        for (int k = 0; k < 4; ++k) uv.v[k] = fmaf(beta, qv.v[k], rv.v[k]);
                         st4(S + ouc + l, uv);
-                        st4(S + op + l, pn);
                     }
                 }
                 __syncthreads();
-                const bool first = cit == 0;
-                const int opo_ = opo;
-                auto halo_p = [=](const float *b, int k) {
+                // B: Muc = M uc (halo uc from the neighbour's r and q);
+                //    vh = M p_new = Muc + beta (Mq + beta vh_old)
+                auto halo_uc = [=](const float *b, int k) {
                     const F4 rv = ld4n<GM>(b + orr + k);
                     if (first) return rv;
-                    const F4 qv = ld4n<GM>(b + oq + k), pv = ld4n<GM>(b + opo_ + k);
+                    const F4 qv = ld4n<GM>(b + oq + k);
                     F4 o;
 #pragma unroll
-                    for (int m = 0; m < 4; ++m) {
-                        const float uv = fmaf(beta, qv.v[m], rv.v[m]);
-                        o.v[m] = fmaf(beta, fmaf(beta, pv.v[m], qv.v[m]), uv);
-                    }
+                    for (int m = 0; m < 4; ++m) o.v[m] = fmaf(beta, qv.v[m], rv.v[m]);
                     return o;
                 };
                 float a_rtvh = 0.f;
                 TVC4_FOR(c) {
-                    const F4 vh = tvc4_M(c, op, lc, l, halo_p);
+                    const F4 muc = tvc4_M(c, ouc, lc, l, halo_uc);
+                    st4(S + omuc + l, muc);
+                    F4 vh = muc;
+                    if (!first) {
+                        const F4 mq = ld4(S + omq + l), vo = ld4(S + ovh + l);
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            vh.v[k] = fmaf(beta, fmaf(beta, vo.v[k], mq.v[k]), muc.v[k]);
+                    }
                     st4(S + ovh + l, vh);
                     const F4 rt = ld4(S + ort + l);
 #pragma unroll
@@ -834,38 +844,27 @@ __global__ void __launch_bounds__(TVC_THREADS, 2)
                 tvc_reduce(a_rtvh, 0.f, A, B, wsum, red, par, C, rank);
                 if (A == 0.f || !isfinite(A)) break;
                 const float alpha = rho / A;
+                // C: Mvh = M vh (halo vh read from the neighbour); q = uc - alpha vh,
+                //    Mq = Muc - alpha Mvh, x += alpha (uc + q), r -= alpha (Muc + Mq)
+                auto halo_vh = [=](const float *b, int k) { return ld4n<GM>(b + ovh + k); };
+                float a_rr = 0.f, a_rtr = 0.f;
                 TVC4_FOR(c) {
-                    const F4 uv = ld4(S + ouc + l), vh = ld4(S + ovh + l), xv = ld4(S + ox + l);
-                    F4 q, uh, xn;
+                    const F4 mv = tvc4_M(c, ovh, lc, l, halo_vh);
+                    const F4 uv = ld4(S + ouc + l), vh = ld4(S + ovh + l), muc = ld4(S + omuc + l);
+                    const F4 xv = ld4(S + ox + l), rv = ld4(S + orr + l), rt = ld4(S + ort + l);
+                    F4 q, mq, xn, rn;
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
                         q.v[k] = fmaf(-alpha, vh.v[k], uv.v[k]);
-                        uh.v[k] = uv.v[k] + q.v[k];
-                        xn.v[k] = fmaf(alpha, uh.v[k], xv.v[k]);
-                    }
-                    st4(S + oq + l, q);
-                    st4(S + ouh + l, uh);
-                    st4(S + ox + l, xn);
-                }
-                __syncthreads();
-                auto halo_uh = [=](const float *b, int k) {
-                    const F4 uv = ld4n<GM>(b + ouc + k), vh = ld4n<GM>(b + ovh + k);
-                    F4 o;
-#pragma unroll
-                    for (int m = 0; m < 4; ++m) o.v[m] = uv.v[m] + fmaf(-alpha, vh.v[m], uv.v[m]);
-                    return o;
-                };
-                float a_rr = 0.f, a_rtr = 0.f;
-                TVC4_FOR(c) {
-                    const F4 mv = tvc4_M(c, ouh, lc, l, halo_uh);
-                    const F4 rv = ld4(S + orr + l), rt = ld4(S + ort + l);
-                    F4 rn;
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        rn.v[k] = fmaf(-alpha, mv.v[k], rv.v[k]);
+                        mq.v[k] = fmaf(-alpha, mv.v[k], muc.v[k]);
+                        xn.v[k] = fmaf(alpha, uv.v[k] + q.v[k], xv.v[k]);
+                        rn.v[k] = fmaf(-alpha, muc.v[k] + mq.v[k], rv.v[k]);
                         a_rr = fmaf(rn.v[k], rn.v[k], a_rr);
                         a_rtr = fmaf(rt.v[k], rn.v[k], a_rtr);
                     }
+                    st4(S + oq + l, q);
+                    st4(S + omq + l, mq);
+                    st4(S + ox + l, xn);
                     st4(S + orr + l, rn);
                 }
                 tvc_reduce(a_rr, a_rtr, A, B, wsum, red, par, C, rank);
@@ -1180,12 +1179,15 @@ struct TvcGeom {
     size_t smem = 0;
 };
 
-std::atomic<int> g_tv_cluster{0};  // forced cluster size (msot_tune_set), 0 = automatic
+// forced cluster size (msot_tune_set), 0 = automatic, -1 = the 16-CTA
+// cluster with its vectors in the global-memory workspace
+std::atomic<int> g_tv_cluster{0};
 
 TvcGeom tvc_geometry(int N, int force = 0) {
     TvcGeom g;
     if (N > TVC_THREADS) return g;
     if (const int Cf = force ? force : g_tv_cluster.load()) {
+        if (Cf < 0) return g;  // no shared-memory geometry: the global-memory form
         const int nloc = (N + Cf - 1) / Cf;
         const size_t bytes = (size_t)TVC_NV * nloc * N * sizeof(float);
         if (bytes <= 225 * 1024) {
@@ -1405,7 +1407,8 @@ int msot_tune_set(const char *key, int value) {
         return MSOT_OK;
     }
     if (key && std::strcmp(key, "tv_prox_cluster") == 0 &&
-        (value == 0 || value == 1 || value == 2 || value == 4 || value == 8 || value == 16)) {
+        (value == -1 || value == 0 || value == 1 || value == 2 || value == 4 || value == 8 ||
+         value == 16)) {
         g_tv_cluster.store(value);
         return MSOT_OK;
     }
@@ -1735,14 +1738,17 @@ extern "C" int msot_autotune(msot_plan_t plan, int batch, void *stream, msot_tun
         res.conv_min_blocks = pick;
         res.transpose_ms = best;
     }
-    // SB_ITV2 cluster size (square grids): the automatic choice and every forced
-    // size whose vectors fit in shared memory
+    // SB_ITV2 cluster size (square grids): the automatic choice, every forced
+    // size whose vectors fit in shared memory, and (-1) the 16-CTA cluster on
+    // the global-memory workspace, which holds more images at once than
+    // 16-CTA clusters of one CTA per SM (a cluster stays inside one GPC)
     res.tv_cluster = 0;
     if (tv_ok) {
         double best = 1e30;
         int pick = 0;
-        for (int C : {0, 1, 2, 4, 8, 16}) {
-            if (C && !tvc_geometry(pl.nx, C).C) continue;
+        for (int C : {0, 1, 2, 4, 8, 16, -1}) {
+            if (C > 0 && !tvc_geometry(pl.nx, C).C) continue;
+            if (C < 0 && pl.nx % 4 != 0) continue;
             double ms;
             if ((rc = tune_time(st, 2, ms, [&] {
                      return tv_prox(img, nullptr, 0.05, 1, img2, work, batch, pl.nx, st, C);
