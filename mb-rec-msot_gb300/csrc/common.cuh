@@ -94,6 +94,11 @@ struct Plan {
     float2 *fft_tw = nullptr;    // [N] exp(-2 pi i t / N)
     float2 *fft_hf = nullptr;    // [N] spectrum of ir_fwd / N
     float2 *fft_ha = nullptr;    // [N] spectrum of ir_adj / N
+    // the same for the split-complex 1024-point kernel (N = 1024 only): per
+    // register pair m and lane, (re a, re b, im a, im b) of w^(lane k1) for
+    // k1 = brev5(2m), brev5(2m + 1); conj w^(lane n) for n = 2m, 2m + 1; and
+    // H[lane + 32 k2] for k2 = brev5(2m), brev5(2m + 1)  ([16][32] each)
+    float4 *fft_twb = nullptr, *fft_twn = nullptr, *fft_hfb = nullptr, *fft_hab = nullptr;
     // prefilter
     int Kx = -1, Kz = -1;   // -1: no prefilter along that axis
     float *pre_x = nullptr, *pre_z = nullptr;
@@ -123,6 +128,7 @@ cudaError_t raise_max_dynamic_smem(const void *func, size_t bytes);
 extern std::atomic<int> g_unet_tc;
 // register cap (minimum resident CTAs per SM) of the IR convolution; operator.cu
 extern std::atomic<int> g_conv_min_blocks;
+extern std::atomic<int> g_conv_packed;
 // next-detector register prefetch of the DAS adjoint on (1) or off (0); operator.cu
 extern std::atomic<int> g_adj_prefetch;
 

@@ -821,6 +821,127 @@ __device__ __forceinline__ void fft32(float2 (&v)[32]) {
     for (int i = 0; i < 32; ++i) v[i] = t[i];
 }
 
+// Split-complex 32-point FFTs on packed FP32x2 arithmetic.  A lane's 32
+// complex values are held as R[m] = (re[2m], re[2m+1]), I[m] = (im[2m],
+// im[2m+1]), so one packed add / multiply / fma works on two butterflies.
+// Radix-2 decimation in frequency (natural order in, bit-reversed out) and
+// in time (bit-reversed in, natural out); every stage but the one pairing
+// neighbouring elements (half = 1) is packed.  The bit-reversed orders never
+// move data: the callers index registers through brev5() at compile time.
+// c_p2r / c_p2i hold the stage twiddle pairs (w32^t0, w32^t1), t = j * step
+// for the pairs j, j + 1 of the stages half = 16, 8, 4, 2 (15 pairs); c_p2n
+// is -c_p2i (the conjugate's imaginary part).
+#define MSOT_W32P(a, b) {c_w32r[a], c_w32r[b]}
+#define MSOT_W32I(a, b) {c_w32i[a], c_w32i[b]}
+#define MSOT_W32N(a, b) {-c_w32i[a], -c_w32i[b]}
+constexpr float c_w32r[16] = {1.000000000e+00f,  9.807852804e-01f,  9.238795325e-01f,
+                              8.314696123e-01f,  7.071067812e-01f,  5.555702330e-01f,
+                              3.826834324e-01f,  1.950903220e-01f,  0.000000000e+00f,
+                              -1.950903220e-01f, -3.826834324e-01f, -5.555702330e-01f,
+                              -7.071067812e-01f, -8.314696123e-01f, -9.238795325e-01f,
+                              -9.807852804e-01f};
+constexpr float c_w32i[16] = {0.000000000e+00f,  -1.950903220e-01f, -3.826834324e-01f,
+                              -5.555702330e-01f, -7.071067812e-01f, -8.314696123e-01f,
+                              -9.238795325e-01f, -9.807852804e-01f, -1.000000000e+00f,
+                              -9.807852804e-01f, -9.238795325e-01f, -8.314696123e-01f,
+                              -7.071067812e-01f, -5.555702330e-01f, -3.826834324e-01f,
+                              -1.950903220e-01f};
+#define MSOT_W32_PAIRS(M)                                                                  \
+    M(0, 1), M(2, 3), M(4, 5), M(6, 7), M(8, 9), M(10, 11), M(12, 13), M(14, 15), M(0, 2),    \
+        M(4, 6), M(8, 10), M(12, 14), M(0, 4), M(8, 12), M(0, 8)
+__constant__ float2 c_p2r[15] = {MSOT_W32_PAIRS(MSOT_W32P)};
+__constant__ float2 c_p2i[15] = {MSOT_W32_PAIRS(MSOT_W32I)};
+__constant__ float2 c_p2n[15] = {MSOT_W32_PAIRS(MSOT_W32N)};
+#undef MSOT_W32_PAIRS
+#undef MSOT_W32P
+#undef MSOT_W32I
+#undef MSOT_W32N
+
+// index of the twiddle pair of stage `half`, butterflies j, j + 1
+__host__ __device__ constexpr int p2_index(int half, int j) {
+    return (half == 16 ? 0 : half == 8 ? 8 : half == 4 ? 12 : 14) + j / 2;
+}
+
+__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) {
+    return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
+// (R, I) <- (R, I) * (WR, WI) for two complex values; NI = -WI
+__device__ __forceinline__ void cmul2(float2 &R, float2 &I, float2 WR, float2 WI, float2 NI) {
+    const float2 r = __ffma2_rn(I, NI, __fmul2_rn(R, WR));
+    const float2 i = __ffma2_rn(I, WR, __fmul2_rn(R, WI));
+    R = r;
+    I = i;
+}
+// the same with a table pair q = (re a, re b, im a, im b)
+__device__ __forceinline__ void cmul2q(float2 &R, float2 &I, float4 q) {
+    cmul2(R, I, make_float2(q.x, q.y), make_float2(q.z, q.w), make_float2(-q.z, -q.w));
+}
+
+// SIGN = -1: forward (w32^t), +1: inverse (conjugate twiddles)
+template <int SIGN>
+__device__ __forceinline__ void fft32_dif2(float2 (&R)[16], float2 (&I)[16]) {
+#pragma unroll
+    for (int half = 16; half >= 2; half >>= 1) {
+#pragma unroll
+        for (int b = 0; b < 32; b += 2 * half) {
+#pragma unroll
+            for (int j = 0; j < half; j += 2) {
+                const int a = (b + j) >> 1, c = (b + j + half) >> 1, q = p2_index(half, j);
+                const float2 uR = R[a], uI = I[a], wR = R[c], wI = I[c];
+                R[a] = f2add(uR, wR);
+                I[a] = f2add(uI, wI);
+                float2 dR = f2sub(uR, wR), dI = f2sub(uI, wI);
+                if (SIGN < 0)
+                    cmul2(dR, dI, c_p2r[q], c_p2i[q], c_p2n[q]);
+                else
+                    cmul2(dR, dI, c_p2r[q], c_p2n[q], c_p2i[q]);
+                R[c] = dR;
+                I[c] = dI;
+            }
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {  // half = 1: the two elements of a pair
+        const float2 r = R[m], i = I[m];
+        R[m] = make_float2(r.x + r.y, r.x - r.y);
+        I[m] = make_float2(i.x + i.y, i.x - i.y);
+    }
+}
+
+template <int SIGN>
+__device__ __forceinline__ void fft32_dit2(float2 (&R)[16], float2 (&I)[16]) {
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {  // half = 1
+        const float2 r = R[m], i = I[m];
+        R[m] = make_float2(r.x + r.y, r.x - r.y);
+        I[m] = make_float2(i.x + i.y, i.x - i.y);
+    }
+#pragma unroll
+    for (int half = 2; half <= 16; half <<= 1) {
+#pragma unroll
+        for (int b = 0; b < 32; b += 2 * half) {
+#pragma unroll
+            for (int j = 0; j < half; j += 2) {
+                const int a = (b + j) >> 1, c = (b + j + half) >> 1, q = p2_index(half, j);
+                float2 tR = R[c], tI = I[c];
+                if (SIGN < 0)
+                    cmul2(tR, tI, c_p2r[q], c_p2i[q], c_p2n[q]);
+                else
+                    cmul2(tR, tI, c_p2r[q], c_p2n[q], c_p2i[q]);
+                const float2 uR = R[a], uI = I[a];
+                R[a] = f2add(uR, tR);
+                I[a] = f2add(uI, tI);
+                R[c] = f2sub(uR, tR);
+                I[c] = f2sub(uI, tI);
+            }
+        }
+    }
+}
+
+// element e (0 .. 31) of a split-complex register array
+__device__ __forceinline__ float &ev(float2 (&A)[16], int e) { return (e & 1) ? A[e >> 1].y : A[e >> 1].x; }
+
 // Epilogue of the convolution for the LSQR sinogram update (EPI 1: u =
 // sl*b - sl*y, EPI 2: u = sl*y - gamma*u) with per-CTA partial sums of u^2.
 struct ConvEpi {
@@ -931,6 +1052,151 @@ __global__ void __launch_bounds__(32 * FPC, MINB) k_conv_fft1k(const float *__re
                     } else {
                         a = done ? l1[j] : fmaf(sl, v[n2].x, -g * l1[j]);
                         bb = done ? l2[j] : fmaf(sl, v[n2].y, -g * l2[j]);
+                    }
+                    y1[t] = a;
+                    if (has2) y2[t] = bb;
+                    acc = fmaf(a, a, acc);
+                    acc = fmaf(bb, bb, acc);
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        __shared__ float wacc[FPC];
+        if (lane == 0) wacc[warp] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double sum = 0.0;
+#pragma unroll
+            for (int k = 0; k < FPC; ++k) sum += (double)wacc[k];
+            const int per_inst = epi.D / (2 * FPC);  // CTAs (along y) per instance
+            const int slot = (blockIdx.y - w * per_inst) * gridDim.x + blockIdx.x;
+            epi.part[(size_t)w * epi.nparts + slot] = sum;
+        }
+    }
+}
+
+// k_conv_fft1k on the split-complex packed FFTs (same four-step
+// decomposition, same epilogues).  Tables, each [16 pairs][32 lanes] of
+// (re a, re b, im a, im b): twb = w1024^(lane k1) for the register pair of
+// k1 = brev5(2m), brev5(2m + 1); twn = conj w1024^(lane n) for n = 2m,
+// 2m + 1; Hb = H[lane + 32 k2] for k2 = brev5(2m), brev5(2m + 1).
+template <int FPC, int EPI = 0, int MINB = 1>
+__global__ void __launch_bounds__(32 * FPC, MINB) k_conv_fft1k2(
+    const float *__restrict__ in, float *__restrict__ out, const float4 *__restrict__ twb,
+    const float4 *__restrict__ twn, const float4 *__restrict__ Hb, int C, int T, int L,
+    ConvEpi epi = {}) {
+    __shared__ __align__(16) float SR[FPC][32][34];
+    __shared__ __align__(16) float SI[FPC][32][34];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int pair = blockIdx.y * FPC + warp;
+    const int c1 = 2 * pair, c2 = c1 + 1;
+    if (c1 >= C) return;  // whole warp; no CTA-wide barriers below
+    const bool has2 = c2 < C;
+    const int V = 1024 - L + 1;
+    const int t0 = blockIdx.x * V;
+    const int u0 = t0 + L / 2 - (L - 1);
+    const float *x1 = in + (size_t)c1 * T;
+    const float *x2 = in + (size_t)(has2 ? c2 : c1) * T;
+    float2 R[16], I[16];
+    if (u0 >= 0 && u0 + 1023 < T) {
+#pragma unroll
+        for (int n1 = 0; n1 < 32; ++n1) {
+            const int u = u0 + 32 * n1 + lane;
+            ev(R, n1) = __ldg(x1 + u);
+            ev(I, n1) = has2 ? __ldg(x2 + u) : 0.f;
+        }
+    } else {
+#pragma unroll
+        for (int n1 = 0; n1 < 32; ++n1) {
+            const int u = u0 + 32 * n1 + lane;
+            const bool ok = u >= 0 && u < T;
+            ev(R, n1) = ok ? __ldg(x1 + u) : 0.f;
+            ev(I, n1) = (ok && has2) ? __ldg(x2 + u) : 0.f;
+        }
+    }
+    fft32_dif2<-1>(R, I);  // over n1 (this lane is n2); register e holds k1 = brev5(e)
+#pragma unroll
+    for (int m = 0; m < 16; ++m) cmul2q(R[m], I[m], __ldg(twb + m * 32 + lane));
+    float(*Sr)[34] = SR[warp];
+    float(*Si)[34] = SI[warp];
+#pragma unroll
+    for (int e = 0; e < 32; ++e) {
+        Sr[brev5(e)][lane] = ev(R, e);
+        Si[brev5(e)][lane] = ev(I, e);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {  // this lane is k1 now, n2 in natural order
+        R[m] = *reinterpret_cast<const float2 *>(&Sr[lane][2 * m]);
+        I[m] = *reinterpret_cast<const float2 *>(&Si[lane][2 * m]);
+    }
+    __syncwarp();
+    fft32_dif2<-1>(R, I);  // over n2: register e holds X[k1 + 32 k2], k2 = brev5(e)
+#pragma unroll
+    for (int m = 0; m < 16; ++m) cmul2q(R[m], I[m], __ldg(Hb + m * 32 + lane));
+    fft32_dit2<1>(R, I);  // inverse over k2: register e holds n1' = e
+#pragma unroll
+    for (int m = 0; m < 16; ++m) cmul2q(R[m], I[m], __ldg(twn + m * 32 + lane));
+#pragma unroll
+    for (int e = 0; e < 32; ++e) {
+        Sr[e][lane] = ev(R, e);
+        Si[e][lane] = ev(I, e);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {  // this lane is n1', k1 in natural order
+        R[m] = *reinterpret_cast<const float2 *>(&Sr[lane][2 * m]);
+        I[m] = *reinterpret_cast<const float2 *>(&Si[lane][2 * m]);
+    }
+    fft32_dif2<1>(R, I);  // inverse over k1: register e holds y[n1' + 32 n2'], n2' = brev5(e)
+    float *y1 = out + (size_t)c1 * T, *y2 = out + (size_t)c2 * T;
+    if constexpr (EPI == 0) {
+#pragma unroll
+        for (int e = 0; e < 32; ++e) {
+            const int n = lane + 32 * brev5(e);
+            const int t = t0 + n - (L - 1);
+            if (n >= L - 1 && t < T) {
+                y1[t] = ev(R, e);
+                if (has2) y2[t] = ev(I, e);
+            }
+        }
+    } else {
+        const int w = c1 / epi.D;
+        const Scal &q = epi.sc[epi.coupled ? 0 : w];
+        const float g = (float)q.gamma, sl = epi.sl;
+        const bool done = EPI == 2 && q.done;
+        const float *b1 = epi.b + (size_t)c1 * T, *b2 = epi.b + (size_t)c2 * T;
+        float acc = 0.f;
+        // chunks of 8 outputs: all loads of a chunk are issued before its
+        // stores (the stores could alias the loads of later iterations)
+        constexpr int CH = 8;
+#pragma unroll
+        for (int c0 = 0; c0 < 32; c0 += CH) {
+            float l1[CH], l2[CH];
+#pragma unroll
+            for (int j = 0; j < CH; ++j) {
+                const int n = lane + 32 * (c0 + j);
+                const int t = t0 + n - (L - 1);
+                const bool ok = n >= L - 1 && t < T;
+                const float *s1 = EPI == 1 ? b1 : y1, *s2 = EPI == 1 ? b2 : y2;
+                l1[j] = ok ? s1[t] : 0.f;
+                l2[j] = (ok && has2) ? s2[t] : 0.f;
+            }
+#pragma unroll
+            for (int j = 0; j < CH; ++j) {
+                const int n2 = c0 + j, e = brev5(n2);
+                const int n = lane + 32 * n2;
+                const int t = t0 + n - (L - 1);
+                if (n >= L - 1 && t < T) {
+                    const float vr = ev(R, e), vi = ev(I, e);
+                    float a, bb;
+                    if (EPI == 1) {
+                        a = fmaf(sl, l1[j], -sl * vr);
+                        bb = has2 ? fmaf(sl, l2[j], -sl * vi) : 0.f;
+                    } else {
+                        a = done ? l1[j] : fmaf(sl, vr, -g * l1[j]);
+                        bb = done ? l2[j] : fmaf(sl, vi, -g * l2[j]);
                     }
                     y1[t] = a;
                     if (has2) y2[t] = bb;
@@ -1311,6 +1577,8 @@ constexpr int CONV_FPC = 4;
 // cap): 1 = unconstrained (172 registers, 2 CTAs fit), 3 (168 registers, no
 // spills), 4 (128 registers, small spills); msot_tune_set("conv_min_blocks")
 std::atomic<int> g_conv_min_blocks{3};
+// 1 (default): the split-complex packed FFT kernel; 0: complex-per-register
+std::atomic<int> g_conv_packed{1};
 static int conv_min_blocks(const Plan &pl) {
     return pl.tune_conv_mb ? pl.tune_conv_mb : g_conv_min_blocks.load();
 }
@@ -1328,6 +1596,24 @@ int launch_conv(const Plan &pl, const float *in, float *out, int W, bool transpo
         if (pl.fft_log4n == 5) {
             constexpr int FPC = CONV_FPC;
             dim3 g1(div_up(pl.T, V), div_up(div_up(C, 2), FPC));
+            if (g_conv_packed.load() && pl.fft_twb) {
+                const float4 *Hb = transpose ? pl.fft_hab : pl.fft_hfb;
+                switch (conv_min_blocks(pl)) {
+                case 3:
+                    KLAUNCH(k_conv_fft1k2<FPC, 0, 3><<<g1, 32 * FPC, 0, st>>>(
+                        in, out, pl.fft_twb, pl.fft_twn, Hb, C, pl.T, pl.L));
+                    break;
+                case 4:
+                    KLAUNCH(k_conv_fft1k2<FPC, 0, 4><<<g1, 32 * FPC, 0, st>>>(
+                        in, out, pl.fft_twb, pl.fft_twn, Hb, C, pl.T, pl.L));
+                    break;
+                default:
+                    KLAUNCH(k_conv_fft1k2<FPC><<<g1, 32 * FPC, 0, st>>>(
+                        in, out, pl.fft_twb, pl.fft_twn, Hb, C, pl.T, pl.L));
+                }
+                MSOT_LAUNCH_CHECK();
+                return MSOT_OK;
+            }
             switch (conv_min_blocks(pl)) {
             case 3:
                 KLAUNCH(k_conv_fft1k<FPC, 0, 3><<<g1, 32 * FPC, 0, st>>>(in, out, pl.fft_tw, H, C,
@@ -1458,8 +1744,14 @@ int apply_forward_update(const Plan &pl, const float *img, float *u, const float
     *nparts = e.nparts;
     const int mb = conv_min_blocks(pl);
 #define CONV_EPI_LAUNCH(EPI, MB)                                                           \
-    KLAUNCH(k_conv_fft1k<CONV_FPC, EPI, MB><<<g1, 32 * CONV_FPC, 0, st>>>(                 \
-        pl.scr_sino, u, pl.fft_tw, pl.fft_hf, C, pl.T, pl.L, e))
+    do {                                                                                   \
+        if (g_conv_packed.load() && pl.fft_twb)                                            \
+            KLAUNCH(k_conv_fft1k2<CONV_FPC, EPI, MB><<<g1, 32 * CONV_FPC, 0, st>>>(        \
+                pl.scr_sino, u, pl.fft_twb, pl.fft_twn, pl.fft_hfb, C, pl.T, pl.L, e));    \
+        else                                                                               \
+            KLAUNCH(k_conv_fft1k<CONV_FPC, EPI, MB><<<g1, 32 * CONV_FPC, 0, st>>>(         \
+                pl.scr_sino, u, pl.fft_tw, pl.fft_hf, C, pl.T, pl.L, e));                  \
+    } while (0)
     if (mode == 0) {
         if (mb == 3) CONV_EPI_LAUNCH(1, 3);
         else if (mb == 4) CONV_EPI_LAUNCH(1, 4);

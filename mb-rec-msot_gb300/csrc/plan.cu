@@ -96,8 +96,8 @@ static void free_plan(Plan &p) {
     void *ptrs[] = {p.tau_tiles, p.tau_pi, p.perm, p.ir_fwd, p.ir_adj, p.pre_x, p.pre_z,
                     p.sir, p.sir_se, p.sir_tiles, p.sir_pi, p.scr_img0, p.scr_img1,
                     p.scr_sino, p.fwd_off, p.fwd_ent, p.blk_tau, p.blk_span,
-                    p.scr_part, p.fft_tw, p.fft_hf, p.fft_ha, p.st_info, p.st_u,
-                    p.st_off, p.st_ent};
+                    p.scr_part, p.fft_tw, p.fft_hf, p.fft_ha, p.fft_twb, p.fft_twn,
+                    p.fft_hfb, p.fft_hab, p.st_info, p.st_u, p.st_off, p.st_ent};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     p = Plan();
@@ -350,6 +350,28 @@ static int build(const msot_plan_desc *d, Plan &p) {
             fha[f] = make_float2((float)(ar / N), (float)(ai / N));
         }
     }
+    std::vector<float4> ftwb, ftwn, fhfb, fhab;
+    if (p.fft_log4n == 5) {
+        auto brev5 = [](int i) {
+            return ((i & 1) << 4) | ((i & 2) << 2) | (i & 4) | ((i & 8) >> 2) | ((i & 16) >> 4);
+        };
+        ftwb.resize(512);
+        ftwn.resize(512);
+        fhfb.resize(512);
+        fhab.resize(512);
+        for (int m = 0; m < 16; ++m)
+            for (int lane = 0; lane < 32; ++lane) {
+                const int i = m * 32 + lane, ka = brev5(2 * m), kb = brev5(2 * m + 1);
+                const float2 a = ftw[lane * ka], b = ftw[lane * kb];
+                ftwb[i] = make_float4(a.x, b.x, a.y, b.y);
+                const float2 c = ftw[lane * 2 * m], d = ftw[lane * (2 * m + 1)];
+                ftwn[i] = make_float4(c.x, d.x, -c.y, -d.y);
+                const float2 hf = fhf[lane + 32 * ka], hg = fhf[lane + 32 * kb];
+                fhfb[i] = make_float4(hf.x, hg.x, hf.y, hg.y);
+                const float2 ha = fha[lane + 32 * ka], hb = fha[lane + 32 * kb];
+                fhab[i] = make_float4(ha.x, hb.x, ha.y, hb.y);
+            }
+    }
     std::vector<float> px, pz;
     if (d->pre_len_x > 0) {
         if (d->pre_len_x % 2 == 0 || !d->pre_x || d->pre_len_x > 2 * p.nx - 1) {
@@ -398,6 +420,12 @@ static int build(const msot_plan_desc *d, Plan &p) {
         UP(p.fft_tw, ftw);
         UP(p.fft_hf, fhf);
         UP(p.fft_ha, fha);
+    }
+    if (p.fft_log4n == 5) {
+        UP(p.fft_twb, ftwb);
+        UP(p.fft_twn, ftwn);
+        UP(p.fft_hfb, fhfb);
+        UP(p.fft_hab, fhab);
     }
     if (p.Kx >= 0) {
         std::vector<float> v(px.begin(), px.end());
