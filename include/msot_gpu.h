@@ -403,7 +403,7 @@ int msot_autotune(msot_plan_t plan, int batch, void *stream, msot_tuning *out);
  *   "adj_prefetch"     1 (default) = the DAS adjoint loads the next detector's
  *                      samples into registers during the current one; 0 = off.
  *   "conv_min_blocks"  register cap of the IR convolution, as resident CTAs
- *                      per SM: 3 (default), 4, or 1 (uncapped).
+ *                      per SM: 4 (default), 3, or 1 (uncapped).
  *   "unet_tensor_cores" 1 (default) = U-Net 3x3 convolutions on the tensor
  *                      cores where the shape allows, 0 = CUDA cores only
  *                      (FP32 activations, no TF32 rounding). */

@@ -128,7 +128,6 @@ cudaError_t raise_max_dynamic_smem(const void *func, size_t bytes);
 extern std::atomic<int> g_unet_tc;
 // register cap (minimum resident CTAs per SM) of the IR convolution; operator.cu
 extern std::atomic<int> g_conv_min_blocks;
-extern std::atomic<int> g_conv_packed;
 // next-detector register prefetch of the DAS adjoint on (1) or off (0); operator.cu
 extern std::atomic<int> g_adj_prefetch;
 

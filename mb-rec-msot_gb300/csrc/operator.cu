@@ -769,56 +769,9 @@ __device__ __forceinline__ void radix4_stage(const float2 *__restrict__ A, float
     o[3 * L] = make_float2(t1.x - t3.x, t1.y - t3.y);
 }
 
-// 32-point FFT in registers: radix-2 decimation in frequency, then the
-// bit-reversal permutation (register renaming).  w32[k] = exp(-2 pi i k/32).
-__constant__ float2 c_w32[16] = {
-    {1.000000000e+00f, 0.000000000e+00f},   {9.807852804e-01f, -1.950903220e-01f},
-    {9.238795325e-01f, -3.826834324e-01f},  {8.314696123e-01f, -5.555702330e-01f},
-    {7.071067812e-01f, -7.071067812e-01f},  {5.555702330e-01f, -8.314696123e-01f},
-    {3.826834324e-01f, -9.238795325e-01f},  {1.950903220e-01f, -9.807852804e-01f},
-    {0.000000000e+00f, -1.000000000e+00f},  {-1.950903220e-01f, -9.807852804e-01f},
-    {-3.826834324e-01f, -9.238795325e-01f}, {-5.555702330e-01f, -8.314696123e-01f},
-    {-7.071067812e-01f, -7.071067812e-01f}, {-8.314696123e-01f, -5.555702330e-01f},
-    {-9.238795325e-01f, -3.826834324e-01f}, {-9.807852804e-01f, -1.950903220e-01f}};
-
+// bit reversal of a 5-bit index
 __host__ __device__ constexpr int brev5(int i) {
     return ((i & 1) << 4) | ((i & 2) << 2) | (i & 4) | ((i & 8) >> 2) | ((i & 16) >> 4);
-}
-
-__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
-    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
-}
-
-template <int SIGN>
-__device__ __forceinline__ void fft32(float2 (&v)[32]) {
-#pragma unroll
-    for (int len = 32; len >= 2; len >>= 1) {
-        const int half = len >> 1, step = 32 / len;
-#pragma unroll
-        for (int b = 0; b < 32; b += len) {
-#pragma unroll
-            for (int j = 0; j < half; ++j) {
-                const float2 u = v[b + j], w = v[b + j + half];
-                v[b + j] = make_float2(u.x + w.x, u.y + w.y);
-                const float2 d = make_float2(u.x - w.x, u.y - w.y);
-                const int ti = j * step;
-                if (ti == 0) {
-                    v[b + j + half] = d;
-                } else if (ti == 8) {
-                    v[b + j + half] = SIGN < 0 ? make_float2(d.y, -d.x) : make_float2(-d.y, d.x);
-                } else {
-                    float2 tw = c_w32[ti];
-                    if (SIGN > 0) tw.y = -tw.y;
-                    v[b + j + half] = cmul(d, tw);
-                }
-            }
-        }
-    }
-    float2 t[32];
-#pragma unroll
-    for (int i = 0; i < 32; ++i) t[i] = v[brev5(i)];
-#pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = t[i];
 }
 
 // Split-complex 32-point FFTs on packed FP32x2 arithmetic.  A lane's 32
@@ -953,136 +906,16 @@ struct ConvEpi {
 };
 
 // 1024-point overlap-save convolution by the four-step FFT 1024 = 32 x 32:
-// one warp per transform (two real columns), 32-point FFTs in registers and
-// two warp-local transposes through padded shared memory per direction.
-// EPI != 0 requires every CTA's columns to lie in one instance.
-template <int FPC, int EPI = 0, int MINB = 1>
-__global__ void __launch_bounds__(32 * FPC, MINB) k_conv_fft1k(const float *__restrict__ in,
-                                                         float *__restrict__ out,
-                                                         const float2 *__restrict__ tw,
-                                                         const float2 *__restrict__ H, int C,
-                                                         int T, int L, ConvEpi epi = {}) {
-    __shared__ float2 S[FPC][32][33];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int pair = blockIdx.y * FPC + warp;
-    const int c1 = 2 * pair, c2 = c1 + 1;
-    if (c1 >= C) return;  // whole warp; no CTA-wide barriers below
-    const bool has2 = c2 < C;
-    const int V = 1024 - L + 1;
-    const int t0 = blockIdx.x * V;
-    const int u0 = t0 + L / 2 - (L - 1);
-    const float *x1 = in + (size_t)c1 * T;
-    const float *x2 = in + (size_t)(has2 ? c2 : c1) * T;
-    float2 v[32];
-#pragma unroll
-    for (int n1 = 0; n1 < 32; ++n1) {
-        const int u = u0 + 32 * n1 + lane;
-        const bool ok = u >= 0 && u < T;
-        v[n1] = make_float2(ok ? __ldg(x1 + u) : 0.f, (ok && has2) ? __ldg(x2 + u) : 0.f);
-    }
-    fft32<-1>(v);  // over n1, this lane is n2
-#pragma unroll
-    for (int k1 = 1; k1 < 32; ++k1) v[k1] = cmul(v[k1], __ldg(tw + lane * k1));
-    float2(*Sw)[33] = S[warp];
-#pragma unroll
-    for (int k1 = 0; k1 < 32; ++k1) Sw[k1][lane] = v[k1];
-    __syncwarp();
-#pragma unroll
-    for (int n2 = 0; n2 < 32; ++n2) v[n2] = Sw[lane][n2];
-    __syncwarp();
-    fft32<-1>(v);  // over n2, this lane is k1: v[k2] = X[k1 + 32 k2]
-#pragma unroll
-    for (int k2 = 0; k2 < 32; ++k2) v[k2] = cmul(v[k2], __ldg(H + lane + 32 * k2));
-    fft32<1>(v);  // over k2: v[n1'] for this k1
-#pragma unroll
-    for (int n1 = 1; n1 < 32; ++n1) {
-        float2 w = __ldg(tw + lane * n1);
-        w.y = -w.y;
-        v[n1] = cmul(v[n1], w);
-    }
-#pragma unroll
-    for (int n1 = 0; n1 < 32; ++n1) Sw[n1][lane] = v[n1];
-    __syncwarp();
-#pragma unroll
-    for (int k1 = 0; k1 < 32; ++k1) v[k1] = Sw[lane][k1];
-    fft32<1>(v);  // over k1, this lane is n1': v[n2'] = y[n1' + 32 n2']
-    float *y1 = out + (size_t)c1 * T, *y2 = out + (size_t)c2 * T;
-    if constexpr (EPI == 0) {
-#pragma unroll
-        for (int n2 = 0; n2 < 32; ++n2) {
-            const int n = lane + 32 * n2;
-            const int t = t0 + n - (L - 1);
-            if (n >= L - 1 && t < T) {
-                y1[t] = v[n2].x;
-                if (has2) y2[t] = v[n2].y;
-            }
-        }
-    } else {
-        const int w = c1 / epi.D;
-        const Scal &q = epi.sc[epi.coupled ? 0 : w];
-        const float g = (float)q.gamma, sl = epi.sl;
-        const bool done = EPI == 2 && q.done;
-        const float *b1 = epi.b + (size_t)c1 * T, *b2 = epi.b + (size_t)c2 * T;
-        float acc = 0.f;
-        // chunks of 8 outputs: all loads of a chunk are issued before its
-        // stores (the stores could alias the loads of later iterations)
-        constexpr int CH = 8;
-#pragma unroll
-        for (int c0 = 0; c0 < 32; c0 += CH) {
-            float l1[CH], l2[CH];
-#pragma unroll
-            for (int j = 0; j < CH; ++j) {
-                const int n = lane + 32 * (c0 + j);
-                const int t = t0 + n - (L - 1);
-                const bool ok = n >= L - 1 && t < T;
-                const float *s1 = EPI == 1 ? b1 : y1, *s2 = EPI == 1 ? b2 : y2;
-                l1[j] = ok ? s1[t] : 0.f;
-                l2[j] = (ok && has2) ? s2[t] : 0.f;
-            }
-#pragma unroll
-            for (int j = 0; j < CH; ++j) {
-                const int n2 = c0 + j;
-                const int n = lane + 32 * n2;
-                const int t = t0 + n - (L - 1);
-                if (n >= L - 1 && t < T) {
-                    float a, bb;
-                    if (EPI == 1) {
-                        a = fmaf(sl, l1[j], -sl * v[n2].x);
-                        bb = has2 ? fmaf(sl, l2[j], -sl * v[n2].y) : 0.f;
-                    } else {
-                        a = done ? l1[j] : fmaf(sl, v[n2].x, -g * l1[j]);
-                        bb = done ? l2[j] : fmaf(sl, v[n2].y, -g * l2[j]);
-                    }
-                    y1[t] = a;
-                    if (has2) y2[t] = bb;
-                    acc = fmaf(a, a, acc);
-                    acc = fmaf(bb, bb, acc);
-                }
-            }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-        __shared__ float wacc[FPC];
-        if (lane == 0) wacc[warp] = acc;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double sum = 0.0;
-#pragma unroll
-            for (int k = 0; k < FPC; ++k) sum += (double)wacc[k];
-            const int per_inst = epi.D / (2 * FPC);  // CTAs (along y) per instance
-            const int slot = (blockIdx.y - w * per_inst) * gridDim.x + blockIdx.x;
-            epi.part[(size_t)w * epi.nparts + slot] = sum;
-        }
-    }
-}
-
-// k_conv_fft1k on the split-complex packed FFTs (same four-step
-// decomposition, same epilogues).  Tables, each [16 pairs][32 lanes] of
+// one warp per transform (two real columns as one complex sequence), the
+// split-complex packed 32-point FFTs above in registers and two warp-local
+// transposes through padded shared memory (re and im planes) per direction.
+// EPI != 0 requires every CTA's columns to lie in one instance.  Tables, each
+// [16 pairs][32 lanes] of
 // (re a, re b, im a, im b): twb = w1024^(lane k1) for the register pair of
 // k1 = brev5(2m), brev5(2m + 1); twn = conj w1024^(lane n) for n = 2m,
 // 2m + 1; Hb = H[lane + 32 k2] for k2 = brev5(2m), brev5(2m + 1).
 template <int FPC, int EPI = 0, int MINB = 1>
-__global__ void __launch_bounds__(32 * FPC, MINB) k_conv_fft1k2(
+__global__ void __launch_bounds__(32 * FPC, MINB) k_conv_fft1k(
     const float *__restrict__ in, float *__restrict__ out, const float4 *__restrict__ twb,
     const float4 *__restrict__ twn, const float4 *__restrict__ Hb, int C, int T, int L,
     ConvEpi epi = {}) {
@@ -1574,11 +1407,10 @@ int launch_sir_adjoint(const Plan &pl, const float *raw, float *x, int W, float 
 
 constexpr int CONV_FPC = 4;
 // minimum resident CTAs per SM the convolution is compiled for (register
-// cap): 1 = unconstrained (172 registers, 2 CTAs fit), 3 (168 registers, no
-// spills), 4 (128 registers, small spills); msot_tune_set("conv_min_blocks")
-std::atomic<int> g_conv_min_blocks{3};
-// 1 (default): the split-complex packed FFT kernel; 0: complex-per-register
-std::atomic<int> g_conv_packed{1};
+// cap): 1 = unconstrained (about 155 registers, 3 CTAs fit), 3 (the same),
+// 4 (128 registers, no spills; the fastest on GB300);
+// msot_tune_set("conv_min_blocks")
+std::atomic<int> g_conv_min_blocks{4};
 static int conv_min_blocks(const Plan &pl) {
     return pl.tune_conv_mb ? pl.tune_conv_mb : g_conv_min_blocks.load();
 }
@@ -1596,36 +1428,20 @@ int launch_conv(const Plan &pl, const float *in, float *out, int W, bool transpo
         if (pl.fft_log4n == 5) {
             constexpr int FPC = CONV_FPC;
             dim3 g1(div_up(pl.T, V), div_up(div_up(C, 2), FPC));
-            if (g_conv_packed.load() && pl.fft_twb) {
-                const float4 *Hb = transpose ? pl.fft_hab : pl.fft_hfb;
-                switch (conv_min_blocks(pl)) {
-                case 3:
-                    KLAUNCH(k_conv_fft1k2<FPC, 0, 3><<<g1, 32 * FPC, 0, st>>>(
-                        in, out, pl.fft_twb, pl.fft_twn, Hb, C, pl.T, pl.L));
-                    break;
-                case 4:
-                    KLAUNCH(k_conv_fft1k2<FPC, 0, 4><<<g1, 32 * FPC, 0, st>>>(
-                        in, out, pl.fft_twb, pl.fft_twn, Hb, C, pl.T, pl.L));
-                    break;
-                default:
-                    KLAUNCH(k_conv_fft1k2<FPC><<<g1, 32 * FPC, 0, st>>>(
-                        in, out, pl.fft_twb, pl.fft_twn, Hb, C, pl.T, pl.L));
-                }
-                MSOT_LAUNCH_CHECK();
-                return MSOT_OK;
-            }
+            const float4 *Hb = transpose ? pl.fft_hab : pl.fft_hfb;
             switch (conv_min_blocks(pl)) {
             case 3:
-                KLAUNCH(k_conv_fft1k<FPC, 0, 3><<<g1, 32 * FPC, 0, st>>>(in, out, pl.fft_tw, H, C,
-                                                                         pl.T, pl.L));
+                KLAUNCH(k_conv_fft1k<FPC, 0, 3><<<g1, 32 * FPC, 0, st>>>(
+                    in, out, pl.fft_twb, pl.fft_twn, Hb, C, pl.T, pl.L));
                 break;
             case 4:
-                KLAUNCH(k_conv_fft1k<FPC, 0, 4><<<g1, 32 * FPC, 0, st>>>(in, out, pl.fft_tw, H, C,
-                                                                         pl.T, pl.L));
+                KLAUNCH(k_conv_fft1k<FPC, 0, 4><<<g1, 32 * FPC, 0, st>>>(
+                    in, out, pl.fft_twb, pl.fft_twn, Hb, C, pl.T, pl.L));
                 break;
             default:
-                KLAUNCH(k_conv_fft1k<FPC><<<g1, 32 * FPC, 0, st>>>(in, out, pl.fft_tw, H, C, pl.T,
-                                                                   pl.L));
+                KLAUNCH(k_conv_fft1k<FPC><<<g1, 32 * FPC, 0, st>>>(in, out, pl.fft_twb,
+                                                                    pl.fft_twn, Hb, C, pl.T,
+                                                                    pl.L));
             }
         } else {
             if ((rc = set_smem(k_conv_fft<6>, smem)) != MSOT_OK) return rc;
@@ -1744,14 +1560,8 @@ int apply_forward_update(const Plan &pl, const float *img, float *u, const float
     *nparts = e.nparts;
     const int mb = conv_min_blocks(pl);
 #define CONV_EPI_LAUNCH(EPI, MB)                                                           \
-    do {                                                                                   \
-        if (g_conv_packed.load() && pl.fft_twb)                                            \
-            KLAUNCH(k_conv_fft1k2<CONV_FPC, EPI, MB><<<g1, 32 * CONV_FPC, 0, st>>>(        \
-                pl.scr_sino, u, pl.fft_twb, pl.fft_twn, pl.fft_hfb, C, pl.T, pl.L, e));    \
-        else                                                                               \
-            KLAUNCH(k_conv_fft1k<CONV_FPC, EPI, MB><<<g1, 32 * CONV_FPC, 0, st>>>(         \
-                pl.scr_sino, u, pl.fft_tw, pl.fft_hf, C, pl.T, pl.L, e));                  \
-    } while (0)
+    KLAUNCH(k_conv_fft1k<CONV_FPC, EPI, MB><<<g1, 32 * CONV_FPC, 0, st>>>(                \
+        pl.scr_sino, u, pl.fft_twb, pl.fft_twn, pl.fft_hfb, C, pl.T, pl.L, e))
     if (mode == 0) {
         if (mb == 3) CONV_EPI_LAUNCH(1, 3);
         else if (mb == 4) CONV_EPI_LAUNCH(1, 4);

@@ -1406,10 +1406,6 @@ int msot_tune_set(const char *key, int value) {
         msot::g_st_force_g.store(value);
         return MSOT_OK;
     }
-    if (key && std::strcmp(key, "conv_packed") == 0 && (value == 0 || value == 1)) {
-        msot::g_conv_packed.store(value);
-        return MSOT_OK;
-    }
     if (key && std::strcmp(key, "tv_prox_cluster") == 0 &&
         (value == -1 || value == 0 || value == 1 || value == 2 || value == 4 || value == 8 ||
          value == 16)) {
