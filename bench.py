@@ -84,6 +84,8 @@ def parse():
     ap.add_argument("--learned-steps", type=int, default=6000)
     ap.add_argument("--learned-input-iters", type=int, default=5,
                     help="plain iterations of the learned arm's network input")
+    ap.add_argument("--learned-trajectory", type=int, default=0,
+                    help="learned arm: also feed the last m steps x_k - x_(k-m) (0: off)")
     ap.add_argument("--learned-target-iters", type=int, default=0,
                     help="plain iterations of the training targets (0: the headline's)")
     ap.add_argument("--unet", action="store_true",
@@ -460,7 +462,7 @@ def learned_arm(model, args, frames=64):
     target_iters = args.learned_target_iters or N_ITER
     ii = args.learned_input_iters
     ws = LearnedWarmStart(model, LAMBDA, levels=4, base_channels=32, max_batch=16,
-                          input_iters=ii)
+                          input_iters=ii, trajectory=args.learned_trajectory)
     imgs = phantom_batch(model.Discretization, P + frames, seed=11)
     (f, t, b), pair_ms = _event_ms(lambda: ws.make_pairs(imgs, target_iters, seed=12))
     losses, train_ms = _event_ms(lambda: ws.fit(f[:P], t[:P], args.learned_steps, batch=16,
@@ -496,7 +498,9 @@ def learned_arm(model, args, frames=64):
                         "ms_per_step": train_ms / max(1, len(losses)),
                         "loss_first": float(np.mean(losses[:20])),
                         "loss_last": float(np.mean(losses[-100:])),
-                        "input": f"plain iterate after {ii} iterations",
+                        "input": f"plain iterate after {ii} iterations" + (
+                            f", and its last {args.learned_trajectory} steps"
+                            if args.learned_trajectory else ""),
                         "target": f"plain solution after {target_iters} iterations",
                         "grid": list(model.image_shape),
                         "note": "a subset of the 20k-pair, 256 px training set, sized for "

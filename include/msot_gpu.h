@@ -240,6 +240,17 @@ int msot_rec_nn_with_L2_reg_warm(msot_plan_t plan, const float *d_b, float *d_re
                                  const float *d_v0, int coupled, double *err_img,
                                  double *err_reg, void *stream);
 
+/* The same iteration with its whole state in and out: starts from (d_w0,
+ * d_v0) (both NULL: the zero start of rec_nn_with_L2_reg; d_v0 NULL with a
+ * d_w0: v = 0) and writes the final image to d_rec and the final multiplier
+ * v to d_v, so that num_iter = k1 followed by a call from (d_rec, d_v) with
+ * k2 iterations is the k1 + k2 iteration solve.  No reference counterpart
+ * (the reference keeps v inside nnls_L2_less.m). */
+int msot_rec_nn_with_L2_reg_state(msot_plan_t plan, const float *d_b, float *d_rec, float *d_v,
+                                  int batch, int num_iter, double lambdaL2, const float *d_w0,
+                                  const float *d_v0, int coupled, double *err_img,
+                                  double *err_reg, void *stream);
+
 /* rec_nn_with_L2_reg.m:1 with both regularisers of the reference's overview
  * script (reconstruction_overview_script.m:46-54): RegL2 = identity weighted
  * by lambdaL2 and RegL2_2 = RegL2T_2 = laplacian_per_wavelength (MATLAB
@@ -317,6 +328,10 @@ int msot_backproject_waveeq(const float *d_sig, int W, int D, int T, const doubl
 typedef struct msot_unet *msot_unet_t;
 int msot_unet_create(int levels, int base_channels, int side, int max_batch, uint64_t seed,
                      msot_unet_t *net);
+/* The same with in_channels (1 .. 8) input channels, [n][in_channels][side]
+ * [side]; msot_unet_create is in_channels = 1.  The output has one channel. */
+int msot_unet_create_ch(int levels, int base_channels, int in_channels, int side, int max_batch,
+                        uint64_t seed, msot_unet_t *net);
 int msot_unet_destroy(msot_unet_t net);
 int msot_unet_param_count(msot_unet_t net, size_t *n);
 int msot_unet_get_params(msot_unet_t net, float *host_params);

@@ -588,7 +588,8 @@ static long count_kernel_nodes(cudaGraph_t g) {
 static int solve_l2(Plan &pl, const float *b_in, float *rec, int W, int num_iter,
                     double lambdaL2, const float *x0, const float *v0, int coupled,
                     double *err_img, double *err_reg, cudaStream_t user,
-                    double lambdaL2_2 = 0.0, double *err_reg2 = nullptr) {
+                    double lambdaL2_2 = 0.0, double *err_reg2 = nullptr,
+                    float *v_out = nullptr) {
     int rc;
     SolverCache *sc = cache_for(pl, W, rc);
     if (rc) return rc;
@@ -675,6 +676,7 @@ static int solve_l2(Plan &pl, const float *b_in, float *rec, int W, int num_iter
             if (rc) break;
         }
         KLAUNCH(k_copy<<<256, 256, 0, st>>>(wv, rec, NI));
+        if (v_out) KLAUNCH(k_copy<<<256, 256, 0, st>>>(vm, v_out, NI));
         if (err_img || err_reg) {
             std::vector<double> e;
             if ((rc = apply_forward(pl, rec, wk.s2, W, st))) break;
@@ -1090,6 +1092,24 @@ extern "C" int msot_rec_nn_with_L2_reg_warm(msot_plan_t plan, const float *d_b, 
     if (int rc = check_plan_device(plan->p, "solver")) return rc;
     return solve_l2(plan->p, d_b, d_rec, batch, num_iter, lambdaL2, d_w0, d_v0,
                     coupled ? 1 : 0, err_img, err_reg, (cudaStream_t)stream);
+}
+
+extern "C" int msot_rec_nn_with_L2_reg_state(msot_plan_t plan, const float *d_b, float *d_rec,
+                                             float *d_v, int batch, int num_iter,
+                                             double lambdaL2, const float *d_w0,
+                                             const float *d_v0, int coupled, double *err_img,
+                                             double *err_reg, void *stream) {
+    if (!plan || !d_b || !d_rec || !d_v || batch <= 0 || num_iter < 0 || (!d_w0 && d_v0)) {
+        set_error("rec_nn_with_L2_reg_state: bad arguments (a v0 needs its w0)");
+        return MSOT_EINVAL;
+    }
+    if (batch > plan->p.max_batch) {
+        set_error("batch %d exceeds the plan's max_batch %d", batch, plan->p.max_batch);
+        return MSOT_EINVAL;
+    }
+    if (int rc = check_plan_device(plan->p, "solver")) return rc;
+    return solve_l2(plan->p, d_b, d_rec, batch, num_iter, lambdaL2, d_w0, d_v0,
+                    coupled ? 1 : 0, err_img, err_reg, (cudaStream_t)stream, 0.0, nullptr, d_v);
 }
 
 extern "C" int msot_rec_nn_with_L2_reg_2(msot_plan_t plan, const float *d_b, float *d_rec,

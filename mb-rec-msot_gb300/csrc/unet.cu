@@ -1075,9 +1075,16 @@ extern "C" {
 
 int msot_unet_create(int levels, int base_channels, int side, int max_batch, uint64_t seed,
                      msot_unet_t *out) {
+    return msot_unet_create_ch(levels, base_channels, 1, side, max_batch, seed, out);
+}
+
+int msot_unet_create_ch(int levels, int base_channels, int in_channels, int side, int max_batch,
+                        uint64_t seed, msot_unet_t *out) {
     if (!out || levels < 1 || levels > 6 || base_channels < 1 || base_channels > 256 ||
-        max_batch < 1 || side < 1 || side % (1 << (levels - 1)) != 0) {
-        set_error("unet_create: bad arguments (side must be divisible by 2^(levels-1))");
+        in_channels < 1 || in_channels > 8 || max_batch < 1 || side < 1 ||
+        side % (1 << (levels - 1)) != 0) {
+        set_error("unet_create: bad arguments (side must be divisible by 2^(levels-1), "
+                  "1 .. 8 input channels)");
         return MSOT_EINVAL;
     }
     auto *u = new msot_unet();
@@ -1098,7 +1105,7 @@ int msot_unet_create(int levels, int base_channels, int side, int max_batch, uin
     u->dec_c.resize(levels);
     u->dec_d.resize(levels);
     for (int l = 0; l < levels; ++l) {
-        add(u->enc_a, l == 0 ? 1 : u->ch[l - 1], u->ch[l], u->side[l]);
+        add(u->enc_a, l == 0 ? in_channels : u->ch[l - 1], u->ch[l], u->side[l]);
         add(u->enc_b, u->ch[l], u->ch[l], u->side[l]);
     }
     for (int l = levels - 2; l >= 0; --l) {

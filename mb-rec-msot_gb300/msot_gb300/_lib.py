@@ -106,6 +106,8 @@ SIGNATURES = {
                                           C.c_int, _dp, _dp, _vp]),
     "msot_rec_nn_with_L2_reg_warm": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_double,
                                                _vp, _vp, C.c_int, _dp, _dp, _vp]),
+    "msot_rec_nn_with_L2_reg_state": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int,
+                                                C.c_double, _vp, _vp, C.c_int, _dp, _dp, _vp]),
     "msot_rec_nn_with_L1_eye_reg": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_double, _vp,
                                               C.c_int, _dp, _dp, _vp]),
     "msot_rec_nn_with_TV_reg": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_double, C.c_int,
@@ -122,6 +124,8 @@ SIGNATURES = {
     "msot_spmr_tables": (C.c_int, [C.POINTER(SpmrSpec), _dp, _ip, _ip]),
     "msot_unet_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64,
                                    C.POINTER(C.c_void_p)]),
+    "msot_unet_create_ch": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64,
+                                      C.POINTER(C.c_void_p)]),
     "msot_unet_destroy": (C.c_int, [_vp]),
     "msot_unet_param_count": (C.c_int, [_vp, C.POINTER(C.c_size_t)]),
     "msot_unet_get_params": (C.c_int, [_vp, C.POINTER(C.c_float)]),

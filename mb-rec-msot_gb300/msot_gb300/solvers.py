@@ -56,9 +56,13 @@ def kkt_multiplier(model: MSOTmodel, data_filt, w0, lambdaL2: float = 0.0, beta:
 
 def rec_nn_with_L2_reg(model: MSOTmodel, data_filt, num_iter_nn_outer: int, lambdaL2: float = 0.0,
                        RegL2="identity", RegL2T="identity", lambdaL2_2=None, RegL2_2=None,
-                       RegL2T_2=None, *, x0=None, v0=None, coupled: bool = False, stream=None):
+                       RegL2T_2=None, *, x0=None, v0=None, v_out=None, coupled: bool = False,
+                       stream=None):
     """rec_nn_with_L2_reg.m:1.  Returns (rec_img, lCurveErrImg, lCurveErrReg,
-    lCurveErrReg_2, err, t) like the reference.  RegL2 is the identity;
+    lCurveErrReg_2, err, t) like the reference.  x0 / v0 start the splitting
+    from an image and multiplier; v_out (a CUDA tensor of the image batch's
+    size) receives the final multiplier, so a solve can be continued from
+    (rec_img, v_out).  RegL2 is the identity;
     RegL2_2 / RegL2T_2 (with lambdaL2_2 > 0 and lambdaL2 > 0, as the reference
     requires) is laplacian_per_wavelength.  lCurveErr* are per-instance
     numpy arrays (one value when coupled), err is empty (the reference only
@@ -75,14 +79,31 @@ def rec_nn_with_L2_reg(model: MSOTmodel, data_filt, num_iter_nn_outer: int, lamb
     e3 = np.zeros(W)
     t0 = time.perf_counter()
     if two:
-        if v0 is not None:
-            raise NotImplementedError("v0 with the second regulariser")
+        if v0 is not None or v_out is not None:
+            raise NotImplementedError("v0 / v_out with the second regulariser")
         _lib.check(_lib.load().msot_rec_nn_with_L2_reg_2(
             model.plan, C.c_void_p(b.data_ptr()), C.c_void_p(rec.data_ptr()), W,
             int(num_iter_nn_outer), float(lambdaL2 or 0.0), float(lambdaL2_2),
             C.c_void_p(x0p.data_ptr()) if x0p is not None else None, 1 if coupled else 0,
             e1.ctypes.data_as(C.POINTER(C.c_double)), e2.ctypes.data_as(C.POINTER(C.c_double)),
             e3.ctypes.data_as(C.POINTER(C.c_double)), _stream_ptr(stream)))
+    elif v_out is not None:
+        if not (v_out.is_cuda and v_out.dtype == torch.float32 and v_out.is_contiguous()
+                and v_out.numel() == rec.numel()):
+            raise ValueError("v_out: a contiguous float32 CUDA tensor of the images' size")
+        if v0 is not None and x0p is None:
+            raise ValueError("v0 needs x0")
+        v0p = None
+        if v0 is not None:
+            v0p = torch.as_tensor(v0).to(device=b.device, dtype=torch.float32)
+            v0p = v0p.reshape(W, *model.image_shape).contiguous()
+        _lib.check(_lib.load().msot_rec_nn_with_L2_reg_state(
+            model.plan, C.c_void_p(b.data_ptr()), C.c_void_p(rec.data_ptr()),
+            C.c_void_p(v_out.data_ptr()), W, int(num_iter_nn_outer), float(lambdaL2 or 0.0),
+            C.c_void_p(x0p.data_ptr()) if x0p is not None else None,
+            C.c_void_p(v0p.data_ptr()) if v0p is not None else None, 1 if coupled else 0,
+            e1.ctypes.data_as(C.POINTER(C.c_double)), e2.ctypes.data_as(C.POINTER(C.c_double)),
+            _stream_ptr(stream)))
     elif v0 is not None:
         if x0p is None:
             raise ValueError("v0 needs x0")

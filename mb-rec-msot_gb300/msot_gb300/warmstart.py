@@ -29,13 +29,16 @@ from .solvers import rec_nn_with_L2_reg
 
 
 class UNet:
-    """msot_unet_create(levels, base_channels, side, max_batch, seed)."""
+    """msot_unet_create_ch(levels, base_channels, in_channels, side, max_batch,
+    seed): input (n, in_channels, side, side), output (n, 1, side, side)."""
 
-    def __init__(self, levels=4, base_channels=32, side=128, max_batch=16, seed=0):
+    def __init__(self, levels=4, base_channels=32, side=128, max_batch=16, seed=0,
+                 in_channels=1):
         self.levels, self.base, self.side, self.max_batch = levels, base_channels, side, max_batch
+        self.in_channels = int(in_channels)
         h = C.c_void_p()
-        _lib.check(_lib.load().msot_unet_create(levels, base_channels, side, max_batch, seed,
-                                                C.byref(h)))
+        _lib.check(_lib.load().msot_unet_create_ch(levels, base_channels, self.in_channels, side,
+                                                   max_batch, seed, C.byref(h)))
         self._h = h
         n = C.c_size_t()
         _lib.check(_lib.load().msot_unet_param_count(h, C.byref(n)))
@@ -63,15 +66,17 @@ class UNet:
         _lib.check(_lib.load().msot_unet_set_params(self._h, p.ctypes.data_as(
             C.POINTER(C.c_float))))
 
-    def _dev(self, x):
+    def _dev(self, x, channels=None):
         t = torch.as_tensor(x)
         if not t.is_cuda:
             t = t.cuda()
-        return t.to(torch.float32).reshape(-1, 1, self.side, self.side).contiguous()
+        c = self.in_channels if channels is None else channels
+        return t.to(torch.float32).reshape(-1, c, self.side, self.side).contiguous()
 
     def forward(self, x, stream=None):
         x = self._dev(x)
-        out = torch.empty_like(x)
+        out = torch.empty((x.shape[0], 1, self.side, self.side), device=x.device,
+                          dtype=torch.float32)
         for c0 in range(0, x.shape[0], self.max_batch):
             xs = x[c0:c0 + self.max_batch]
             _lib.check(_lib.load().msot_unet_forward(self._h, C.c_void_p(xs.data_ptr()),
@@ -80,7 +85,7 @@ class UNet:
         return out
 
     def gradients(self, x, target, stream=None):
-        x, t = self._dev(x), self._dev(target)
+        x, t = self._dev(x), self._dev(target, 1)
         loss = C.c_double()
         g = np.empty(self.n_params, dtype=np.float32)
         _lib.check(_lib.load().msot_unet_gradients(self._h, C.c_void_p(x.data_ptr()),
@@ -91,7 +96,7 @@ class UNet:
         return loss.value, g
 
     def train_step(self, x, target, lr=1e-3, stream=None):
-        x, t = self._dev(x), self._dev(target)
+        x, t = self._dev(x), self._dev(target, 1)
         loss = C.c_double()
         _lib.check(_lib.load().msot_unet_gradients(self._h, C.c_void_p(x.data_ptr()),
                                                    C.c_void_p(t.data_ptr()), x.shape[0],
@@ -108,12 +113,16 @@ class LearnedWarmStart:
 
     def __init__(self, model, lambdaL2: float = 0.0, net: UNet | None = None, levels=4,
                  base_channels=32, max_batch=16, seed=0, beta=1e-3, input_iters=0,
-                 residual=None, backprojection: str = "transpose"):
+                 residual=None, backprojection: str = "transpose", trajectory: int = 0):
         nx, nz = model.image_shape
         if nx != nz:
             raise ValueError("the warm-start network needs a square grid")
         self.model, self.lam, self.beta = model, float(lambdaL2 or 0.0), beta
-        self.net = net or UNet(levels, base_channels, nx, max_batch, seed)
+        self.trajectory = int(trajectory)
+        if self.trajectory and not 0 < self.trajectory < int(input_iters):
+            raise ValueError("the trajectory input needs 0 < trajectory < input_iters")
+        self.net = net or UNet(levels, base_channels, nx, max_batch, seed,
+                               in_channels=2 if self.trajectory else 1)
         self.input_iters = int(input_iters)
         self.residual = bool(self.input_iters > 0 if residual is None else residual)
         if self.residual and self.input_iters <= 0:
@@ -136,9 +145,25 @@ class LearnedWarmStart:
 
     def features(self, b):
         """(f / s as (W, 1, n, n), s (W,)); f = the plain iterate, A'b or the
-        backproject_waveeq image (see the module docstring)."""
+        backproject_waveeq image (see the module docstring).  With
+        ``trajectory`` = m a second channel holds (x_k - x_{k-m}) / s, the last
+        m steps of the plain iteration (k = input_iters; the solve runs k - m
+        iterations, keeps its multiplier, and continues for m: k in all)."""
         b = self._sino(b)
-        if self.input_iters > 0:
+        d = None
+        if self.input_iters > 0 and self.trajectory:
+            fs, ds = [], []
+            for i, j in self._chunks(b.shape[0]):
+                v = torch.empty((j - i, *self.model.image_shape), device=b.device,
+                                dtype=torch.float32)
+                wa = rec_nn_with_L2_reg(self.model, b[i:j], self.input_iters - self.trajectory,
+                                        self.lam, v_out=v)[0]
+                wk = rec_nn_with_L2_reg(self.model, b[i:j], self.trajectory, self.lam, x0=wa,
+                                        v0=v.clone(), v_out=v)[0]
+                fs.append(wk)
+                ds.append(wk - wa)
+            f, d = torch.cat(fs), torch.cat(ds)
+        elif self.input_iters > 0:
             f = torch.cat([rec_nn_with_L2_reg(self.model, b[i:j], self.input_iters, self.lam)[0]
                            for i, j in self._chunks(b.shape[0])])
         elif self.backprojection == "waveeq":
@@ -146,7 +171,10 @@ class LearnedWarmStart:
         else:
             f = torch.cat([self.model.transpose(b[i:j]) for i, j in self._chunks(b.shape[0])])
         s = f.flatten(1).pow(2).mean(1).sqrt().clamp_min(1e-30)
-        return (f / s.view(-1, 1, 1)).unsqueeze(1).contiguous(), s
+        feat = (f / s.view(-1, 1, 1)).unsqueeze(1)
+        if d is not None:
+            feat = torch.cat([feat, (d / s.view(-1, 1, 1)).unsqueeze(1)], dim=1)
+        return feat.contiguous(), s
 
     def _waveeq(self, b):
         """backproject_waveeq of b on the model's grid and probe (psf = 1),
@@ -184,7 +212,7 @@ class LearnedWarmStart:
             self.kappa = float(ratio.median())
         t = (rec / (self.kappa * s.view(-1, 1, 1))).unsqueeze(1)
         if self.residual:
-            t = t - f
+            t = t - f[:, :1]
         return f, t.contiguous(), b
 
     def fit(self, inputs, targets, steps, batch=16, lr=1e-3, lr_final=1e-5, seed=0):
@@ -208,7 +236,7 @@ class LearnedWarmStart:
         f, s = self.features(b)
         out = self.net.forward(f)
         if self.residual:
-            out = out + f
+            out = out + f[:, :1]
         return (out.squeeze(1).clamp_min(0) * (self.kappa * s.view(-1, 1, 1))).contiguous()
 
     def start(self, b, x0=None):
