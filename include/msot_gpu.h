@@ -99,16 +99,20 @@ int msot_interp_transpose(msot_plan_t plan, const float *d_raw, float *d_coeffs,
 
 /* Reduced-precision storage (the mixed-precision configuration of the
  * reference's L1 solve; no counterpart in the reference, which is FP64
- * throughout).  image_bf16 = 1: the interpolation input of the DAS forward
- * (the prefiltered image the forwardDelayAndSumMex.cpp:80-100 loop reads per
- * (pixel, detector) pair) is stored in BF16, round to nearest, and widened
- * to FP32 for the FP32 accumulation; this halves the bytes the forward
- * gathers.  refine_every = k > 0: the L1 solver runs every k-th outer
- * iteration with the FP32 input (the other solvers use the setting as is).
- * The FP32 default meets the operators' 1e-5 bar; BF16 storage is for solves
- * judged by their 1e-3 bar against the FP64 oracle.  Plans without SIR only;
- * drops the plan's captured solver graphs. */
-int msot_plan_set_storage(msot_plan_t plan, int image_bf16, int refine_every);
+ * throughout).  The interpolation input of the DAS forward (the prefiltered
+ * image the forwardDelayAndSumMex.cpp:80-100 loop reads per (pixel,
+ * detector) pair) is stored in 16 bits and widened to FP32 for the FP32
+ * accumulation, which halves the bytes the forward gathers:
+ * image_format = 1: BF16, round to nearest; 2: FP16, round to nearest, of
+ * the values times a power-of-two scale per instance (from the instance's
+ * largest magnitude and the prefilter's gain, so that the stored values
+ * stay below 2^14; the forward's output is multiplied back by the inverse,
+ * exactly); 0: FP32 (default).  refine_every = k > 0: the L1 solver runs
+ * every k-th outer iteration with the FP32 input (the other solvers use the
+ * setting as is).  The FP32 default meets the operators' 1e-5 bar; 16-bit
+ * storage is for solves judged by their 1e-3 bar against the FP64 oracle.
+ * Plans without SIR only; drops the plan's captured solver graphs. */
+int msot_plan_set_storage(msot_plan_t plan, int image_format, int refine_every);
 
 /* Allocation-free form of msot_interp_transpose for plans without SIR; no
  * counterpart in the reference.  It is for callers that are not allowed to

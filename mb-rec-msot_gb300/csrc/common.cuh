@@ -80,11 +80,14 @@ struct Plan {
     int tune_tv_cluster = 0;  // CTAs per image of the SB_ITV2 cluster kernel
     int tune_fwd_staged = 0;  // DAS forward kernel: 1 staged, 2 k_das_fwd3, 0 = g_fwd_staged
     // reduced storage (msot_plan_set_storage): the interpolation input of the
-    // DAS forward in BF16 (FP32 accumulation); mutable so that a solver can
-    // run its full-precision refinement iterations with it off
-    mutable int image_bf16 = 0;  // in effect now
-    int storage_bf16 = 0;        // requested
+    // DAS forward in BF16 (1) or FP16 with a power-of-two scale per instance
+    // (2), FP32 accumulation; mutable so that a solver can run its
+    // full-precision refinement iterations with it off
+    mutable int image_fmt = 0;   // in effect now: 0 FP32, 1 BF16, 2 FP16
+    int storage_fmt = 0;         // requested
     int refine_every = 0;        // L1 solver: every refine_every-th outer iteration in FP32
+    float *h16_sc = nullptr;     // FP16: [max_batch] scales s, then [max_batch] 1 / s
+    float pre_gain_x = 1.f, pre_gain_z = 1.f;  // sum |taps| of the prefilter axes
     // IR
     int L = 0, Lh = 0;
     float *ir_fwd = nullptr, *ir_adj = nullptr;

@@ -35,18 +35,49 @@
 #include <mutex>
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include "common.cuh"
 
 namespace msot {
 
-// the interpolation input in [W/wt][P][wt] order, FP32 or (out_bf16) BF16
-// rounded to nearest (the reduced-storage path of msot_plan_set_storage)
-__device__ __forceinline__ void store_interp_input(float *out, size_t i, float v, int out_bf16) {
-    if (out_bf16)
+// the interpolation input in [W/wt][P][wt] order: FP32 (fmt 0), BF16
+// rounded to nearest (1), or FP16 of v times the instance's power-of-two
+// scale hsc[w] (2) -- the reduced-storage paths of msot_plan_set_storage
+__device__ __forceinline__ void store_interp_input(float *out, size_t i, float v, int fmt,
+                                                   const float *hsc, int w) {
+    if (fmt == 1)
         reinterpret_cast<__nv_bfloat16 *>(out)[i] = __float2bfloat16_rn(v);
+    else if (fmt == 2)
+        reinterpret_cast<__half *>(out)[i] = __float2half_rn(v * __ldg(hsc + w));
     else
         out[i] = v;
+}
+
+// FP16 storage: the power-of-two scale of each instance, s = 2^(14 - e) with
+// gain * max |in| < 2^e, so that every stored value stays below 2^14 (FP16
+// holds 65504) and keeps 11 significant bits down to 2^-24 of that; writes
+// s to hsc[w] and 1 / s to hsc[stride + w].  One CTA per instance.
+__global__ void __launch_bounds__(256) k_h16_scale(const float *__restrict__ in, int P,
+                                                   float gain, float *__restrict__ hsc,
+                                                   int stride) {
+    __shared__ float red[8];
+    const float *x = in + (size_t)blockIdx.x * P;
+    float m = 0.f;
+    for (int i = threadIdx.x; i < P; i += 256) m = fmaxf(m, fabsf(__ldg(x + i)));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < 8; ++k) m = fmaxf(m, red[k]);
+        const float g = m * gain;
+        int e = 0;
+        if (g > 0.f && isfinite(g)) frexpf(g, &e);
+        e = max(-100, min(100, e));
+        hsc[blockIdx.x] = ldexpf(1.f, 14 - e);
+        hsc[stride + blockIdx.x] = ldexpf(1.f, e - 14);
+    }
 }
 
 __device__ __forceinline__ int tap_lo(int32_t tau, int32_t r_fx, int fb) {
@@ -68,8 +99,8 @@ __device__ __forceinline__ float tri_weight(int t, int32_t tau, int fb, float c1
 __global__ void k_prefilter(const float *__restrict__ in, float *__restrict__ out,
                             const float *__restrict__ taps, int K, int nx, int nz, int W,
                             int along_x, int transpose, float scale,
-                            const int32_t *__restrict__ perm, int out_mode, int wt,
-                            int out_bf16) {
+                            const int32_t *__restrict__ perm, int out_mode, int wt, int fmt,
+                            const float *__restrict__ hsc) {
     const int P = nx * nz;
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long)W * P) return;
@@ -95,7 +126,8 @@ __global__ void k_prefilter(const float *__restrict__ in, float *__restrict__ ou
         acc = fmaf(h, __ldg(src + s), acc);
     }
     if (out_mode == 2)
-        store_interp_input(out, ((size_t)(w / wt) * P + j) * wt + w % wt, acc * scale, out_bf16);
+        store_interp_input(out, ((size_t)(w / wt) * P + j) * wt + w % wt, acc * scale, fmt, hsc,
+                           w);
     else
         out[(size_t)w * P + j] = acc * scale;
 }
@@ -120,7 +152,7 @@ template <int KM>
 __global__ void __launch_bounds__(PF_THREADS) k_prefilter2d(
     const float *__restrict__ in, float *__restrict__ out, const float *__restrict__ taps_x,
     const float *__restrict__ taps_z, int Kx, int Kz, int nx, int nz, int W, int transpose,
-    int out_mode, int wt, int out_bf16) {
+    int out_mode, int wt, int fmt, const float *__restrict__ hsc) {
     constexpr int NC = PF_TX + 2 * KM;  // staged columns
     constexpr int NTAP = 2 * KM + 1;
     constexpr int NW = PF_THREADS / 32;
@@ -198,7 +230,7 @@ __global__ void __launch_bounds__(PF_THREADS) k_prefilter2d(
             const size_t p = (size_t)ix * nz + z;
             if (out_mode == 2)
                 store_interp_input(out, ((size_t)(w / wt) * nx * nz + p) * wt + w % wt, acc[j],
-                                   out_bf16);
+                                   fmt, hsc, w);
             else
                 out[(size_t)w * nx * nz + p] = acc[j];
         }
@@ -207,11 +239,12 @@ __global__ void __launch_bounds__(PF_THREADS) k_prefilter2d(
 
 // [W][P] -> [W/wt][P][wt] (pixel-major within each tile of wt instances)
 __global__ void k_to_pixmajor(const float *__restrict__ in, float *__restrict__ out, int P,
-                              int W, int wt, int out_bf16) {
+                              int W, int wt, int fmt, const float *__restrict__ hsc) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long)W * P) return;
     const int w = (int)(idx / P), j = (int)(idx % P);
-    store_interp_input(out, ((size_t)(w / wt) * P + j) * wt + w % wt, __ldg(in + idx), out_bf16);
+    store_interp_input(out, ((size_t)(w / wt) * P + j) * wt + w % wt, __ldg(in + idx), fmt, hsc,
+                       w);
 }
 
 // [W][P] -> [W][P] in scatter order (out[w][j] = in[w][perm[j]])
@@ -285,13 +318,40 @@ __device__ __forceinline__ void load_pixel(const __nv_bfloat16 *xp, float (&xv)[
     }
 }
 
+template <int WT>
+__device__ __forceinline__ void load_pixel(const __half *xp, float (&xv)[WT]) {
+    if constexpr (WT % 8 == 0) {
+#pragma unroll
+        for (int i = 0; i < WT; i += 8) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4 *>(xp + i));
+            const uint32_t u[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float2 f = __half22float2(*reinterpret_cast<const __half2 *>(&u[k]));
+                xv[i + 2 * k] = f.x;
+                xv[i + 2 * k + 1] = f.y;
+            }
+        }
+    } else if constexpr (WT % 2 == 0) {
+#pragma unroll
+        for (int i = 0; i < WT; i += 2) {
+            const float2 f = __half22float2(__ldg(reinterpret_cast<const __half2 *>(xp + i)));
+            xv[i] = f.x;
+            xv[i + 1] = f.y;
+        }
+    } else {
+        xv[0] = __half2float(__ldg(xp));
+    }
+}
+
 template <int WT, int F, typename XT = float>
 __global__ void __launch_bounds__(256, WT >= 16 ? 2 : 4) k_das_fwd3(const int32_t *__restrict__ off,
                                                   const int2 *__restrict__ ent,
                                                   const XT *__restrict__ xpm,
                                                   float *__restrict__ raw, int P, int D, int T,
                                                   int W, int fb, float inv_r, float ce1,
-                                                  float ce2, float scale) {
+                                                  float ce2, float scale,
+                                                  const float *__restrict__ inv_s = nullptr) {
     constexpr int NB = 256;
     constexpr int TB = NB - 2 * F - 2;
     extern __shared__ float mom[];  // [4][WT][NB], bucket fastest (dynamic: 4 KB x WT)
@@ -380,7 +440,7 @@ __global__ void __launch_bounds__(256, WT >= 16 ? 2 : 4) k_das_fwd3(const int32_
             acc = fmaf(a, M0[-k], acc);
             acc = fmaf(k <= 0 ? -inv_r : inv_r, M1[-k], acc);
         }
-        raw[((size_t)(w0 + i) * D + d) * T + t] = acc * scale;
+        raw[((size_t)(w0 + i) * D + d) * T + t] = acc * (inv_s ? scale * __ldg(inv_s + w0 + i) : scale);
     }
 }
 
@@ -1139,9 +1199,14 @@ int launch_prefilter(const Plan &pl, const float *in, float *out, int W, bool tr
     const float *taps = along_x ? pl.pre_x : pl.pre_z;
     const long n = (long)W * pl.P;
     const int wt = out_mode == 2 ? das_fwd_wt(pl, W) : 1;
+    const int fmt = out_mode == 2 ? pl.image_fmt : 0;
+    if (fmt == 2)
+        KLAUNCH(k_h16_scale<<<W, 256, 0, st>>>(
+            in, pl.P, std::fabs(scale) * (along_x ? pl.pre_gain_x : pl.pre_gain_z), pl.h16_sc,
+            pl.max_batch));
     KLAUNCH(k_prefilter<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
-        in, out, taps, K, pl.nx, pl.nz, W, along_x, transpose, scale, pl.perm, out_mode, wt,
-        out_mode == 2 ? pl.image_bf16 : 0));
+        in, out, taps, K, pl.nx, pl.nz, W, along_x, transpose, scale, pl.perm, out_mode, wt, fmt,
+        pl.h16_sc));
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
 }
@@ -1157,9 +1222,13 @@ static int prefilter2d_km(const Plan &pl, const float *in, float *out, int W, bo
     MSOT_CUDA_TRY(raise_max_dynamic_smem((const void *)k_prefilter2d<KM>, smem));
     const dim3 grid((unsigned)((pl.nx + PF_TX - 1) / PF_TX), (unsigned)W);
     const int wt = out_mode == 2 ? das_fwd_wt(pl, W) : 1;
+    const int fmt = out_mode == 2 ? pl.image_fmt : 0;
+    if (fmt == 2)
+        KLAUNCH(k_h16_scale<<<W, 256, 0, st>>>(in, pl.P, pl.pre_gain_x * pl.pre_gain_z,
+                                               pl.h16_sc, pl.max_batch));
     KLAUNCH(k_prefilter2d<KM><<<grid, PF_THREADS, smem, st>>>(
         in, out, pl.pre_x, pl.pre_z, pl.Kx, pl.Kz, pl.nx, pl.nz, W, transpose ? 1 : 0, out_mode,
-        wt, out_mode == 2 ? pl.image_bf16 : 0));
+        wt, fmt, pl.h16_sc));
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
 }
@@ -1193,8 +1262,10 @@ static int fwd_split(const Plan &pl, int nwt) {
 int launch_to_pixmajor(const Plan &pl, const float *in, float *out, int W, cudaStream_t st) {
     TimedScope ts_(KID_PERMUTE, st);
     const long n = (long)W * pl.P;
+    if (pl.image_fmt == 2)
+        KLAUNCH(k_h16_scale<<<W, 256, 0, st>>>(in, pl.P, 1.f, pl.h16_sc, pl.max_batch));
     KLAUNCH(k_to_pixmajor<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
-        in, out, pl.P, W, das_fwd_wt(pl, W), pl.image_bf16));
+        in, out, pl.P, W, das_fwd_wt(pl, W), pl.image_fmt, pl.h16_sc));
     MSOT_LAUNCH_CHECK();
     return MSOT_OK;
 }
@@ -1207,12 +1278,21 @@ static int das_fwd_launch(const Plan &pl, const float *xpm, float *raw, int W, f
     dim3 grid(div_up(pl.T, TB), pl.D, W / WT);
     const size_t smem = (size_t)4 * WT * NB * sizeof(float);
     int rc;
-    if (pl.image_bf16) {
+    if (pl.image_fmt == 1) {
         const auto *xb = reinterpret_cast<const __nv_bfloat16 *>(xpm);
         if ((rc = set_smem(k_das_fwd3<WT, F, __nv_bfloat16>, smem)) != MSOT_OK) return rc;
         KLAUNCH(k_das_fwd3<WT, F, __nv_bfloat16><<<grid, NB, smem, st>>>(
             pl.fwd_off, pl.fwd_ent, xb, raw, pl.P, pl.D, pl.T, W, pl.frac_bits, pl.inv_r, pl.ce1,
             pl.ce2, scale));
+        MSOT_LAUNCH_CHECK();
+        return MSOT_OK;
+    }
+    if (pl.image_fmt == 2) {
+        const auto *xh = reinterpret_cast<const __half *>(xpm);
+        if ((rc = set_smem(k_das_fwd3<WT, F, __half>, smem)) != MSOT_OK) return rc;
+        KLAUNCH(k_das_fwd3<WT, F, __half><<<grid, NB, smem, st>>>(
+            pl.fwd_off, pl.fwd_ent, xh, raw, pl.P, pl.D, pl.T, W, pl.frac_bits, pl.inv_r, pl.ce1,
+            pl.ce2, scale, pl.h16_sc + pl.max_batch));
         MSOT_LAUNCH_CHECK();
         return MSOT_OK;
     }
@@ -1249,7 +1329,7 @@ std::atomic<int> g_fwd_staged{1};
 // the staged kernel (das_fwd_staged.cu) where the plan has its tables and
 // they fit shared memory at this instance tile, else k_das_fwd3
 static bool use_staged(const Plan &pl, int wt) {
-    if (pl.image_bf16) return false;  // BF16 storage is read by k_das_fwd3 only
+    if (pl.image_fmt) return false;  // 16-bit storage is read by k_das_fwd3 only
     const int sel = pl.tune_fwd_staged ? pl.tune_fwd_staged : (g_fwd_staged.load() ? 1 : 2);
     return sel == 1 && fwd_staged_fits(pl, wt);
 }
@@ -1743,17 +1823,18 @@ int msot_interp_transpose(msot_plan_t plan, const float *d_raw, float *d_coeffs,
     return interp_adjoint(plan->p, d_raw, d_coeffs, batch, 1.f, (cudaStream_t)stream);
 }
 
-int msot_plan_set_storage(msot_plan_t plan, int image_bf16, int refine_every) {
-    if (!plan || (image_bf16 != 0 && image_bf16 != 1) || refine_every < 0) {
-        set_error("plan_set_storage: image_bf16 must be 0 or 1 and refine_every >= 0");
+int msot_plan_set_storage(msot_plan_t plan, int image_format, int refine_every) {
+    if (!plan || image_format < 0 || image_format > 2 || refine_every < 0) {
+        set_error("plan_set_storage: image_format must be 0 (FP32), 1 (BF16) or 2 (FP16) and "
+                  "refine_every >= 0");
         return MSOT_EINVAL;
     }
     Plan &pl = plan->p;
-    if (image_bf16 && pl.S) {
-        set_error("plan_set_storage: BF16 storage is for plans without SIR");
+    if (image_format && pl.S) {
+        set_error("plan_set_storage: 16-bit storage is for plans without SIR");
         return MSOT_EINVAL;
     }
-    pl.storage_bf16 = pl.image_bf16 = image_bf16;
+    pl.storage_fmt = pl.image_fmt = image_format;
     pl.refine_every = refine_every;
     solver_cache_invalidate(pl);  // captured graphs hold the previous kernels
     return MSOT_OK;

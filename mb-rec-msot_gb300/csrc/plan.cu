@@ -97,7 +97,8 @@ static void free_plan(Plan &p) {
                     p.sir, p.sir_se, p.sir_tiles, p.sir_pi, p.scr_img0, p.scr_img1,
                     p.scr_sino, p.fwd_off, p.fwd_ent, p.blk_tau, p.blk_span,
                     p.scr_part, p.fft_tw, p.fft_hf, p.fft_ha, p.fft_twb, p.fft_twn,
-                    p.fft_hfb, p.fft_hab, p.st_info, p.st_u, p.st_off, p.st_ent};
+                    p.fft_hfb, p.fft_hab, p.st_info, p.st_u, p.st_off, p.st_ent,
+                    p.h16_sc};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     p = Plan();
@@ -440,6 +441,18 @@ static int build(const msot_plan_desc *d, Plan &p) {
     if ((rc = alloc(&p.scr_img0, W * p.P, B)) != MSOT_OK) return rc;
     if ((rc = alloc(&p.scr_img1, W * p.P, B)) != MSOT_OK) return rc;
     if ((rc = alloc(&p.scr_sino, W * p.D * p.T, B)) != MSOT_OK) return rc;
+    if ((rc = alloc(&p.h16_sc, 2 * W, B)) != MSOT_OK) return rc;
+    p.pre_gain_x = p.pre_gain_z = 1.f;  // bounds of |prefiltered| / max |input|
+    if (!px.empty()) {
+        double g = 0;
+        for (float t : px) g += std::fabs((double)t);
+        p.pre_gain_x = (float)g;
+    }
+    if (!pz.empty()) {
+        double g = 0;
+        for (float t : pz) g += std::fabs((double)t);
+        p.pre_gain_z = (float)g;
+    }
     if (!has_sir) {
         // detector groups of the adjoint: enough CTAs to fill the GPU twice,
         // at most 512 partial images in flight

@@ -931,9 +931,11 @@ static int solve_l1(const Plan &pl, const float *b, float *rec, int W, int num_i
         for (int it = 0; it < num_iter && rc == MSOT_OK; ++it) {
             // reduced storage: every refine_every-th outer iteration runs its
             // operators with the FP32 interpolation input, which corrects the
-            // drift the BF16 iterations leave in u and the Bregman variable
-            pl.image_bf16 = pl.storage_bf16 && !(pl.refine_every > 0 &&
-                                                 (it + 1) % pl.refine_every == 0);
+            // drift the reduced-storage iterations leave in u and the Bregman
+            // variable
+            pl.image_fmt = (pl.refine_every > 0 && (it + 1) % pl.refine_every == 0)
+                               ? 0
+                               : pl.storage_fmt;
             KLAUNCH(k_l1_rhs<<<gi, RED_THREADS, 0, st>>>(u, bp, atb, dv, rhs, x, r, rt, xmin, ni, lam, eta,
                                                  c.P(0)));
             KLAUNCH(k_cgs_scalar<<<1, 1024, 0, st>>>(wk.sc, 0, c.P(0), c.nbi, W, coupled, 1e-8));
@@ -960,7 +962,7 @@ static int solve_l1(const Plan &pl, const float *b, float *rec, int W, int num_i
                 rc = MSOT_ECUDA;
             }
         }
-        pl.image_bf16 = 0;  // lCurveErrImg with the FP32 operator
+        pl.image_fmt = 0;  // lCurveErrImg with the FP32 operator
         if (rc) break;
         KLAUNCH(k_copy<<<256, 256, 0, st>>>(u, rec, NI));
         if (err_img || err_reg) {
@@ -993,7 +995,7 @@ static int solve_l1(const Plan &pl, const float *b, float *rec, int W, int num_i
             rc = MSOT_ECUDA;
         }
     } while (0);
-    pl.image_bf16 = pl.storage_bf16;
+    pl.image_fmt = pl.storage_fmt;
     if (rc == MSOT_OK && nonfinite >= 0) {
         set_error("rec_nn_with_L1_eye_reg: non-finite residual ||A x - b||^2 for instance %d "
                   "(NaN or Inf in the data or the start)", nonfinite);

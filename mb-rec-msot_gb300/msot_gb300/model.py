@@ -378,11 +378,16 @@ class MSOTmodel:
                                              _stream_ptr(stream), C.byref(t)))
         return {f: getattr(t, f) for f, _ in t._fields_}
 
-    def set_storage(self, image_bf16: bool = False, refine_every: int = 0) -> None:
-        """msot_plan_set_storage: BF16 storage of the DAS forward's
-        interpolation input (FP32 accumulation), and in the L1 solver every
-        ``refine_every``-th outer iteration with the FP32 input."""
-        _lib.check(_lib.load().msot_plan_set_storage(self.plan, 1 if image_bf16 else 0,
+    def set_storage(self, image_format=False, refine_every: int = 0) -> None:
+        """msot_plan_set_storage: 16-bit storage of the DAS forward's
+        interpolation input (FP32 accumulation) -- image_format "bf16" (or
+        True), "fp16" (scaled per instance), or "fp32" (or False) -- and in
+        the L1 solver every ``refine_every``-th outer iteration with the FP32
+        input."""
+        fmts = {False: 0, "fp32": 0, True: 1, "bf16": 1, "fp16": 2}
+        if image_format not in fmts:
+            raise ValueError("image_format: 'fp32', 'bf16' or 'fp16'")
+        _lib.check(_lib.load().msot_plan_set_storage(self.plan, fmts[image_format],
                                                      int(refine_every)))
 
     def estimate_sigma_max(self, iters: int = 100, seed: int = 0) -> float:
