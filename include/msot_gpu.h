@@ -403,7 +403,8 @@ typedef struct msot_tuning {
     int fwd_wt, conv_min_blocks, tv_cluster;  /* 0 = the built-in choice */
     double fwd_ms, transpose_ms, tv_prox_ms;  /* per apply of the chosen variant */
     int adj_wt;                               /* instances per CTA of the DAS adjoint (4, 2, 1) */
-    int fwd_staged;                           /* DAS forward: 1 staged, 2 per-detector buckets */
+    int fwd_staged;                           /* DAS forward: 1 staged, 2 per-detector buckets,
+                                                 4 per-detector buckets, interleaved entries */
 } msot_tuning;
 int msot_autotune(msot_plan_t plan, int batch, void *stream, msot_tuning *out);
 
@@ -415,6 +416,8 @@ int msot_autotune(msot_plan_t plan, int batch, void *stream, msot_tuning *out);
  *   "fwd_staged"       1 (default) = the DAS forward stages each CTA's image
  *                      values in shared memory where the plan's tables fit,
  *                      0 = per-detector L2 gathers (plans autotuned keep their pick).
+ *   "fwd_ell"          1 = plans not autotuned run the DAS forward on the
+ *                      interleaved (per-warp) copy of its entry table; 0 (default) = off.
  *   "fwd_staged_tile", "fwd_staged_group"  time samples per CTA (8 .. 64) and
  *                      detectors per CTA (1 .. 16) of the staged forward's
  *                      tables in plans created afterwards; 0 (default) = the

@@ -53,6 +53,14 @@ struct Plan {
     float ce1 = 0.f, ce2 = 0.f;    // (r - F)/r and (F + 1 - r)/r
     int32_t *fwd_off = nullptr;    // [D][T+1] CSR offsets of bucket b = floor(tau)
     int2 *fwd_ent = nullptr;       // [D][P] (tau fixed point, pixel) sorted by bucket
+    // the same entries per (detector, time tile of the forward, warp of 32
+    // buckets), interleaved: row k holds the k-th entry of each of the warp's
+    // buckets ((0, -1) past a bucket's end), so that a warp's entry load is
+    // 256 contiguous bytes; fwd_ell_off[(d * ntiles + tile) * 8 + warp] is a
+    // block's first entry (the next block's start ends it)
+    int2 *fwd_ell = nullptr;
+    int32_t *fwd_ell_off = nullptr;
+    int fwd_ell_tiles = 0;
     // staged forward (das_fwd_staged.cu): CTA = (time tile of st_tt samples,
     // group of st_g detectors); st_tt == 0 when the plan has no such tables
     int st_tt = 0, st_g = 0, st_ntiles = 0, st_ngroups = 0, st_ib = 0;
@@ -78,7 +86,7 @@ struct Plan {
     int tune_adj_wt = 0;      // instances per CTA of the DAS adjoint (2, 1)
     int tune_conv_mb = 0;     // register cap of the IR convolution (1, 3, 4)
     int tune_tv_cluster = 0;  // CTAs per image of the SB_ITV2 cluster kernel
-    int tune_fwd_staged = 0;  // DAS forward kernel: 1 staged, 2 k_das_fwd3, 0 = g_fwd_staged
+    int tune_fwd_staged = 0;  // DAS forward kernel: 1 staged, 2 k_das_fwd3 (CSR), 4 k_das_fwd3 (ELL), 0 = knobs
     // reduced storage (msot_plan_set_storage): the interpolation input of the
     // DAS forward in BF16 (1) or FP16 with a power-of-two scale per instance
     // (2), FP32 accumulation; mutable so that a solver can run its
@@ -130,6 +138,8 @@ cudaError_t raise_max_dynamic_smem(const void *func, size_t bytes);
 // tensor-core convolutions of the warm-start U-Net on (1) or off (0); unet.cu
 extern std::atomic<int> g_unet_tc;
 // register cap (minimum resident CTAs per SM) of the IR convolution; operator.cu
+// DAS forward on the interleaved entry table for plans not autotuned; operator.cu
+extern std::atomic<int> g_fwd_ell;
 extern std::atomic<int> g_conv_min_blocks;
 // next-detector register prefetch of the DAS adjoint on (1) or off (0); operator.cu
 extern std::atomic<int> g_adj_prefetch;

@@ -344,14 +344,20 @@ __device__ __forceinline__ void load_pixel(const __half *xp, float (&xv)[WT]) {
     }
 }
 
-template <int WT, int F, typename XT = float>
+// ELL: the entries come from the interleaved table (Plan::fwd_ell; `ent`
+// and `ell_off` are it and its block offsets): a warp's load of the k-th
+// entries of its 32 buckets is 256 contiguous bytes instead of 32 separate
+// lines, which the L1 data pipe -- this kernel's bound -- serves in two
+// wavefronts.  Same entries in the same order per bucket: the same result.
+template <int WT, int F, typename XT = float, bool ELL = false>
 __global__ void __launch_bounds__(256, WT >= 16 ? 2 : 4) k_das_fwd3(const int32_t *__restrict__ off,
                                                   const int2 *__restrict__ ent,
                                                   const XT *__restrict__ xpm,
                                                   float *__restrict__ raw, int P, int D, int T,
                                                   int W, int fb, float inv_r, float ce1,
                                                   float ce2, float scale,
-                                                  const float *__restrict__ inv_s = nullptr) {
+                                                  const float *__restrict__ inv_s = nullptr,
+                                                  const int32_t *__restrict__ ell_off = nullptr) {
     constexpr int NB = 256;
     constexpr int TB = NB - 2 * F - 2;
     extern __shared__ float mom[];  // [4][WT][NB], bucket fastest (dynamic: 4 KB x WT)
@@ -377,10 +383,25 @@ __global__ void __launch_bounds__(256, WT >= 16 ? 2 : 4) k_das_fwd3(const int32_
 #pragma unroll
         for (int i = 0; i < WT; ++i) m0[i] = m1[i] = m2[i] = m3[i] = 0.f;
         const int b = b_lo + (int)threadIdx.x;
-        if (b >= 0 && b < T) {
-            const int32_t *o = off + (size_t)d * (T + 1);
-            const int j0 = __ldg(o + b), j1 = __ldg(o + b + 1);
-            const int2 *e = ent + (size_t)d * P;
+        int j0 = 0, j1 = 0;
+        const int2 *e;
+        constexpr int ES = ELL ? 32 : 1;  // stride between a thread's entries
+        if constexpr (ELL) {
+            // the CTA's tiles are the table's: blockIdx.x = tile, warp = 32 buckets
+            const int blk = (d * (int)gridDim.x + (int)blockIdx.x) * (NB / 32) +
+                            ((int)threadIdx.x >> 5);
+            const int s0 = __ldg(ell_off + blk), s1 = __ldg(ell_off + blk + 1);
+            j1 = (s1 - s0) >> 5;
+            e = ent + s0 + ((int)threadIdx.x & 31);
+        } else {
+            if (b >= 0 && b < T) {
+                const int32_t *o = off + (size_t)d * (T + 1);
+                j0 = __ldg(o + b);
+                j1 = __ldg(o + b + 1);
+            }
+            e = ent + (size_t)d * P;
+        }
+        if (j0 < j1) {
             const int mask = (1 << fb) - 1;
             const float step = __int_as_float((127 - fb) << 23);  // 2^-fb
             // the entries of the next group load while this group's gathers
@@ -388,7 +409,7 @@ __global__ void __launch_bounds__(256, WT >= 16 ? 2 : 4) k_das_fwd3(const int32_
             int2 qn[FWD_UNR];
 #pragma unroll
             for (int u = 0; u < FWD_UNR; ++u)
-                qn[u] = j0 + u < j1 ? __ldg(e + j0 + u) : make_int2(0, -1);
+                qn[u] = j0 + u < j1 ? __ldg(e + (size_t)(j0 + u) * ES) : make_int2(0, -1);
             for (int j = j0; j < j1; j += FWD_UNR) {
                 int2 q[FWD_UNR];
                 float xv[FWD_UNR][WT];
@@ -399,7 +420,8 @@ __global__ void __launch_bounds__(256, WT >= 16 ? 2 : 4) k_das_fwd3(const int32_
                     load_pixel<WT>(xpm + ((size_t)blockIdx.z * P + max(q[u].y, 0)) * WT, xv[u]);
 #pragma unroll
                 for (int u = 0; u < FWD_UNR; ++u)
-                    qn[u] = j + FWD_UNR + u < j1 ? __ldg(e + j + FWD_UNR + u) : make_int2(0, -1);
+                    qn[u] = j + FWD_UNR + u < j1 ? __ldg(e + (size_t)(j + FWD_UNR + u) * ES)
+                                                 : make_int2(0, -1);
 #pragma unroll
                 for (int u = 0; u < FWD_UNR; ++u) {
                     if (q[u].y < 0) break;
@@ -1271,37 +1293,53 @@ int launch_to_pixmajor(const Plan &pl, const float *in, float *out, int W, cudaS
 }
 
 // DAS forward by bucket moments; xpm is [W/WT][P][WT].
-template <int WT, int F>
-static int das_fwd_launch(const Plan &pl, const float *xpm, float *raw, int W, float scale,
-                          cudaStream_t st) {
+std::atomic<int> g_fwd_staged{1};
+std::atomic<int> g_fwd_ell{0};
+
+// the DAS forward kernel: the autotuner's pick, else 4 (interleaved entry
+// table) when msot_tune_set("fwd_ell") is on, else 1 (staged) or 2
+// (k_das_fwd3 on the CSR table) by msot_tune_set("fwd_staged")
+static int fwd_kernel(const Plan &pl) {
+    if (pl.tune_fwd_staged) return pl.tune_fwd_staged;
+    if (g_fwd_ell.load()) return 4;
+    return g_fwd_staged.load() ? 1 : 2;
+}
+
+template <int WT, int F, typename XT, bool ELL>
+static int das_fwd_launch_t(const Plan &pl, const XT *xpm, float *raw, int W, float scale,
+                            const float *inv_s, cudaStream_t st) {
     constexpr int NB = 256, TB = NB - 2 * F - 2;
     dim3 grid(div_up(pl.T, TB), pl.D, W / WT);
     const size_t smem = (size_t)4 * WT * NB * sizeof(float);
     int rc;
+    if ((rc = set_smem(k_das_fwd3<WT, F, XT, ELL>, smem)) != MSOT_OK) return rc;
+    KLAUNCH(k_das_fwd3<WT, F, XT, ELL><<<grid, NB, smem, st>>>(
+        pl.fwd_off, ELL ? pl.fwd_ell : pl.fwd_ent, xpm, raw, pl.P, pl.D, pl.T, W, pl.frac_bits,
+        pl.inv_r, pl.ce1, pl.ce2, scale, inv_s, ELL ? pl.fwd_ell_off : nullptr));
+    MSOT_LAUNCH_CHECK();
+    return MSOT_OK;
+}
+
+// DAS forward by bucket moments; xpm is [W/WT][P][WT] in the plan's storage
+// format; the interleaved entry table where the autotuner picked it
+template <int WT, int F>
+static int das_fwd_launch(const Plan &pl, const float *xpm, float *raw, int W, float scale,
+                          cudaStream_t st) {
+    const bool ell = fwd_kernel(pl) == 4 && pl.fwd_ell_off;
     if (pl.image_fmt == 1) {
         const auto *xb = reinterpret_cast<const __nv_bfloat16 *>(xpm);
-        if ((rc = set_smem(k_das_fwd3<WT, F, __nv_bfloat16>, smem)) != MSOT_OK) return rc;
-        KLAUNCH(k_das_fwd3<WT, F, __nv_bfloat16><<<grid, NB, smem, st>>>(
-            pl.fwd_off, pl.fwd_ent, xb, raw, pl.P, pl.D, pl.T, W, pl.frac_bits, pl.inv_r, pl.ce1,
-            pl.ce2, scale));
-        MSOT_LAUNCH_CHECK();
-        return MSOT_OK;
+        return ell ? das_fwd_launch_t<WT, F, __nv_bfloat16, true>(pl, xb, raw, W, scale, nullptr, st)
+                   : das_fwd_launch_t<WT, F, __nv_bfloat16, false>(pl, xb, raw, W, scale, nullptr,
+                                                                   st);
     }
     if (pl.image_fmt == 2) {
         const auto *xh = reinterpret_cast<const __half *>(xpm);
-        if ((rc = set_smem(k_das_fwd3<WT, F, __half>, smem)) != MSOT_OK) return rc;
-        KLAUNCH(k_das_fwd3<WT, F, __half><<<grid, NB, smem, st>>>(
-            pl.fwd_off, pl.fwd_ent, xh, raw, pl.P, pl.D, pl.T, W, pl.frac_bits, pl.inv_r, pl.ce1,
-            pl.ce2, scale, pl.h16_sc + pl.max_batch));
-        MSOT_LAUNCH_CHECK();
-        return MSOT_OK;
+        const float *inv = pl.h16_sc + pl.max_batch;
+        return ell ? das_fwd_launch_t<WT, F, __half, true>(pl, xh, raw, W, scale, inv, st)
+                   : das_fwd_launch_t<WT, F, __half, false>(pl, xh, raw, W, scale, inv, st);
     }
-    if ((rc = set_smem(k_das_fwd3<WT, F>, smem)) != MSOT_OK) return rc;
-    KLAUNCH(k_das_fwd3<WT, F><<<grid, NB, smem, st>>>(pl.fwd_off, pl.fwd_ent, xpm, raw, pl.P,
-                                                      pl.D, pl.T, W, pl.frac_bits, pl.inv_r,
-                                                      pl.ce1, pl.ce2, scale));
-    MSOT_LAUNCH_CHECK();
-    return MSOT_OK;
+    return ell ? das_fwd_launch_t<WT, F, float, true>(pl, xpm, raw, W, scale, nullptr, st)
+               : das_fwd_launch_t<WT, F, float, false>(pl, xpm, raw, W, scale, nullptr, st);
 }
 
 template <int WT>
@@ -1324,14 +1362,11 @@ static int das_fwd_f(const Plan &pl, const float *xpm, float *raw, int W, float 
     }
 }
 
-std::atomic<int> g_fwd_staged{1};
-
 // the staged kernel (das_fwd_staged.cu) where the plan has its tables and
 // they fit shared memory at this instance tile, else k_das_fwd3
 static bool use_staged(const Plan &pl, int wt) {
     if (pl.image_fmt) return false;  // 16-bit storage is read by k_das_fwd3 only
-    const int sel = pl.tune_fwd_staged ? pl.tune_fwd_staged : (g_fwd_staged.load() ? 1 : 2);
-    return sel == 1 && fwd_staged_fits(pl, wt);
+    return fwd_kernel(pl) == 1 && fwd_staged_fits(pl, wt);
 }
 
 // instances per CTA of the DAS forward: the autotuner's pick (16, 8, 4, 2),

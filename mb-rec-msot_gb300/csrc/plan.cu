@@ -98,7 +98,7 @@ static void free_plan(Plan &p) {
                     p.scr_sino, p.fwd_off, p.fwd_ent, p.blk_tau, p.blk_span,
                     p.scr_part, p.fft_tw, p.fft_hf, p.fft_ha, p.fft_twb, p.fft_twn,
                     p.fft_hfb, p.fft_hab, p.st_info, p.st_u, p.st_off, p.st_ent,
-                    p.h16_sc};
+                    p.h16_sc, p.fwd_ell, p.fwd_ell_off};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     p = Plan();
@@ -206,6 +206,48 @@ static int build(const msot_plan_desc *d, Plan &p) {
             int2 *e = fent.data() + (size_t)det * p.P;
             for (int q = 0; q < p.P; ++q) e[fill[tf[q] >> fb]++] = make_int2(tf[q], q);
         }
+    }
+    // interleaved (ELL) copy of the forward table per (detector, time tile of
+    // k_das_fwd3: 256 buckets from tile * (256 - 2F - 2) - F - 1, warp)
+    std::vector<int2> fell;
+    std::vector<int32_t> felloff;
+    if (!has_sir && p.F <= 8) {
+        const int TB = 256 - 2 * p.F - 2;
+        p.fwd_ell_tiles = div_up(p.T, TB);
+        felloff.reserve((size_t)p.D * p.fwd_ell_tiles * 8 + 1);
+        fell.reserve((size_t)PD + PD / 2);
+        const int nblk = p.fwd_ell_tiles * 8;
+        std::vector<int> Ks(nblk);
+        for (int det = 0; det < p.D; ++det) {
+            const int32_t *o = foff.data() + (size_t)det * (p.T + 1);
+            const int2 *e = fent.data() + (size_t)det * p.P;
+            size_t add = 0;
+            for (int i = 0; i < nblk; ++i) {
+                const int b0 = (i / 8) * TB - p.F - 1 + 32 * (i % 8);
+                int K = 0;
+                for (int l = 0; l < 32; ++l) {
+                    const int b = b0 + l;
+                    if (b >= 0 && b < p.T) K = std::max(K, o[b + 1] - o[b]);
+                }
+                Ks[i] = K;
+                add += (size_t)K * 32;
+            }
+            if (fell.size() + add > (size_t)INT32_MAX) {
+                set_error("plan: interleaved forward table above 2^31 entries");
+                return MSOT_EINVAL;
+            }
+            for (int i = 0; i < nblk; ++i) {
+                felloff.push_back((int32_t)fell.size());
+                const int b0 = (i / 8) * TB - p.F - 1 + 32 * (i % 8);
+                for (int k = 0; k < Ks[i]; ++k)
+                    for (int l = 0; l < 32; ++l) {
+                        const int b = b0 + l;
+                        const bool in = b >= 0 && b < p.T && k < o[b + 1] - o[b];
+                        fell.push_back(in ? e[o[b] + k] : make_int2(0, -1));
+                    }
+            }
+        }
+        felloff.push_back((int32_t)fell.size());
     }
 
     // --- adjoint blocks: 64x64 pixels, travel times and bucket span per detector --------
@@ -404,6 +446,8 @@ static int build(const msot_plan_desc *d, Plan &p) {
             return rc;
         UP(p.fwd_off, foff);
         UP(p.fwd_ent, fent);
+        UP(p.fwd_ell, fell);
+        UP(p.fwd_ell_off, felloff);
         UP(p.blk_tau, btau);
         UP(p.blk_span, bspan);
     }

@@ -1406,6 +1406,10 @@ int msot_tune_set(const char *key, int value) {
         msot::g_st_force_g.store(value);
         return MSOT_OK;
     }
+    if (key && std::strcmp(key, "fwd_ell") == 0 && (value == 0 || value == 1)) {
+        msot::g_fwd_ell.store(value);
+        return MSOT_OK;
+    }
     if (key && std::strcmp(key, "tv_prox_cluster") == 0 &&
         (value == -1 || value == 0 || value == 1 || value == 2 || value == 4 || value == 8 ||
          value == 16)) {
@@ -1681,13 +1685,15 @@ extern "C" int msot_autotune(msot_plan_t plan, int batch, void *stream, msot_tun
     MSOT_LAUNCH_CHECK();
     int rc;
     msot_tuning res{};
-    // DAS forward: kernel (staged / per-detector buckets) and instances per
-    // CTA (apply_forward: prefilter, forward, conv)
+    // DAS forward: kernel (1 staged, 2 per-detector buckets on the CSR table,
+    // 4 the same on the interleaved table) and instances per CTA
+    // (apply_forward: prefilter, forward, conv)
     {
         double best = 1e30;
         int pick = 0, pick_kernel = 0;
-        for (int kernel : {1, 2}) {
+        for (int kernel : {1, 2, 4}) {
             if (kernel == 1 && !pl.st_tt) continue;
+            if (kernel == 4 && !pl.fwd_ell_off) continue;
             for (int wt : {16, 8, 4, 2}) {
                 if (batch % wt) continue;
                 if (kernel == 1 && !fwd_staged_fits(pl, wt)) continue;

@@ -215,3 +215,25 @@ def test_model_tables_from_disk_cache(cuda, tmp_path):
     assert np.array_equal(m1.travel, m2.travel)
     x = torch.rand((1, 32, 32))
     assert torch.equal(m1.forward(x), m2.forward(x))
+
+
+@pytest.mark.parametrize("W,fmt", [(8, "fp32"), (4, "fp32"), (16, "fp16"), (2, "fp32")])
+def test_interleaved_entry_table_forward_is_bit_identical(cuda, W, fmt):
+    # k_das_fwd3 on the per-warp interleaved entry table reads the same
+    # entries of each bucket in the same order as on the CSR table
+    import torch
+    from msot_gb300 import _lib
+    L = _lib.load()
+    pm, _ = make_pair(n=64, n_det=128, n_samples=1200, radius=0.02, fov_half=0.0063,
+                      max_batch=W)
+    pm.set_storage(fmt)
+    x = torch.rand((W, 64, 64), device="cuda", generator=torch.Generator("cuda").manual_seed(9))
+    _lib.check(L.msot_tune_set(b"fwd_staged", 0))
+    try:
+        y_csr = pm.forward(x).cpu().numpy()
+        _lib.check(L.msot_tune_set(b"fwd_ell", 1))
+        y_ell = pm.forward(x).cpu().numpy()
+    finally:
+        _lib.check(L.msot_tune_set(b"fwd_ell", 0))
+        _lib.check(L.msot_tune_set(b"fwd_staged", 1))
+    assert np.array_equal(y_csr, y_ell)
