@@ -283,7 +283,15 @@ constexpr int FWD_UNR = 2;
 // (widened exactly: a BF16 value is the upper half of its FP32 pattern)
 template <int WT>
 __device__ __forceinline__ void load_pixel(const float *xp, float (&xv)[WT]) {
-    if constexpr (WT % 4 == 0) {
+    if constexpr (WT % 8 == 0) {
+        // one 256-bit load per 8 values (xp is 32-byte aligned: [W/WT][P][WT])
+#pragma unroll
+        for (int i = 0; i < WT; i += 8)
+            asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                : "=f"(xv[i]), "=f"(xv[i + 1]), "=f"(xv[i + 2]), "=f"(xv[i + 3]),
+                  "=f"(xv[i + 4]), "=f"(xv[i + 5]), "=f"(xv[i + 6]), "=f"(xv[i + 7])
+                : "l"(xp + i));
+    } else if constexpr (WT % 4 == 0) {
 #pragma unroll
         for (int i = 0; i < WT; i += 4) {
             const float4 v = __ldg(reinterpret_cast<const float4 *>(xp + i));
@@ -294,11 +302,29 @@ __device__ __forceinline__ void load_pixel(const float *xp, float (&xv)[WT]) {
         for (int i = 0; i < WT; ++i) xv[i] = __ldg(xp + i);
     }
 }
+// eight 32-bit words of a 32-byte aligned address in one 256-bit load
+__device__ __forceinline__ void ld256(const void *p, uint32_t (&u)[8]) {
+    asm("ld.global.nc.v8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]),
+          "=r"(u[7])
+        : "l"(p));
+}
 __device__ __forceinline__ float bf16_lo(uint32_t v) { return __uint_as_float(v << 16); }
 __device__ __forceinline__ float bf16_hi(uint32_t v) { return __uint_as_float(v & 0xffff0000u); }
 template <int WT>
 __device__ __forceinline__ void load_pixel(const __nv_bfloat16 *xp, float (&xv)[WT]) {
-    if constexpr (WT % 8 == 0) {
+    if constexpr (WT % 16 == 0) {
+#pragma unroll
+        for (int i = 0; i < WT; i += 16) {
+            uint32_t u[8];
+            ld256(xp + i, u);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                xv[i + 2 * k] = bf16_lo(u[k]);
+                xv[i + 2 * k + 1] = bf16_hi(u[k]);
+            }
+        }
+    } else if constexpr (WT % 8 == 0) {
 #pragma unroll
         for (int i = 0; i < WT; i += 8) {
             const uint4 v = __ldg(reinterpret_cast<const uint4 *>(xp + i));
@@ -320,7 +346,19 @@ __device__ __forceinline__ void load_pixel(const __nv_bfloat16 *xp, float (&xv)[
 
 template <int WT>
 __device__ __forceinline__ void load_pixel(const __half *xp, float (&xv)[WT]) {
-    if constexpr (WT % 8 == 0) {
+    if constexpr (WT % 16 == 0) {
+#pragma unroll
+        for (int i = 0; i < WT; i += 16) {
+            uint32_t u[8];
+            ld256(xp + i, u);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const float2 f = __half22float2(*reinterpret_cast<const __half2 *>(&u[k]));
+                xv[i + 2 * k] = f.x;
+                xv[i + 2 * k + 1] = f.y;
+            }
+        }
+    } else if constexpr (WT % 8 == 0) {
 #pragma unroll
         for (int i = 0; i < WT; i += 8) {
             const uint4 v = __ldg(reinterpret_cast<const uint4 *>(xp + i));
