@@ -531,7 +531,9 @@ __global__ void __launch_bounds__(BLK_THREADS, WT >= 4 ? 2 : 3) k_das_adj4(
     extern __shared__ float sm[];
     const int SL = ((span_max + ADJ_BPT - 1) / ADJ_BPT) * ADJ_BPT + 2 * F + 2;
     float *seg = sm;  // [WT][SL]
-    float2 *Q = reinterpret_cast<float2 *>(sm + ((WT * SL + 3) & ~3));  // [WT][3][span_max]
+    // [3][span_max][WT]: a bucket's (A, B) pairs of the CTA's instances side
+    // by side, so that one 128-bit load gathers two instances
+    float2 *Q = reinterpret_cast<float2 *>(sm + ((WT * SL + 3) & ~3));
     const int blk = blockIdx.x, w0 = blockIdx.y * WT, grp = blockIdx.z;
     const int t = threadIdx.x;
     const int bxi = blk % nbx, bzi = blk / nbx;
@@ -607,10 +609,10 @@ __global__ void __launch_bounds__(BLK_THREADS, WT >= 4 ? 2 : 3) k_das_adj4(
             const bool lo_first = ce1 <= ce2;  // r - F <= F + 1 - r: e1 ends before e2 starts
             const float A1 = lo_first ? U : fmaf(-ce2, sH, A0);
             const float B1 = lo_first ? Vr : fmaf(inv_r, sH, B0);
-            float2 *q = Q + (size_t)w * 3 * span_max + bl;
+            float2 *q = Q + (size_t)bl * WT + w;
             q[0] = make_float2(A0, B0);
-            q[span_max] = make_float2(A1, B1);
-            q[2 * span_max] = make_float2(A2, B2);
+            q[(size_t)span_max * WT] = make_float2(A1, B1);
+            q[(size_t)2 * span_max * WT] = make_float2(A2, B2);
         }
         __syncthreads();
         const int32_t *tp = btau + ((size_t)blk * D + d) * BLK + t;
@@ -620,10 +622,20 @@ __global__ void __launch_bounds__(BLK_THREADS, WT >= 4 ? 2 : 3) k_das_adj4(
             if (tau == TAU_PAD) continue;
             const float f = (float)(tau & mask) * step;
             const int bp = (tau >> fb) - sp.x + ((f >= p1) + (f >= p2)) * span_max;
+            const float2 *qv = Q + (size_t)bp * WT;
+            if constexpr (WT % 2 == 0) {
 #pragma unroll
-            for (int i = 0; i < WT; ++i) {
-                const float2 v = Q[(size_t)i * 3 * span_max + bp];
-                acc[k][i] = fmaf(f, v.y, acc[k][i] + v.x);
+                for (int i = 0; i < WT; i += 2) {
+                    const float4 v = *reinterpret_cast<const float4 *>(qv + i);
+                    acc[k][i] = fmaf(f, v.y, acc[k][i] + v.x);
+                    acc[k][i + 1] = fmaf(f, v.w, acc[k][i + 1] + v.z);
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < WT; ++i) {
+                    const float2 v = qv[i];
+                    acc[k][i] = fmaf(f, v.y, acc[k][i] + v.x);
+                }
             }
         }
         __syncthreads();
