@@ -253,7 +253,7 @@ def oracle_solve(model, b_np, threads, n_iter=None):
 # DRAM bytes (read + write) per launch of each family's kernel at batch 64,
 # from one ncu --set full capture per kernel of `bench.py --op --batch 64`
 # (profiles/das_kernels_128px_b64.md, profiles/eir_conv_fft_128px_b64.md)
-NCU_TRAFFIC_B64 = {"interp_forward": 47.601152e6 + 80.315648e6,
+NCU_TRAFFIC_B64 = {"interp_forward": 84.3648e6 + 97.833984e6,
                    "interp_adjoint": 77.760256e6 + 3.016448e6,
                    "ir_conv": 133.13664e6 + 83.677184e6,
                    "prefilter": 4.246784e6}
