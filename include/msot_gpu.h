@@ -413,11 +413,14 @@ int msot_autotune(msot_plan_t plan, int batch, void *stream, msot_tuning *out);
  *   "tv_prox_cluster"  CTAs per image of the shared-memory SB_ITV2 kernel
  *                      (1, 2, 4, 8, 16; 0 = automatic; -1 = 16 CTAs per
  *                      image with the vectors in global memory).
- *   "fwd_staged"       1 (default) = the DAS forward stages each CTA's image
- *                      values in shared memory where the plan's tables fit,
- *                      0 = per-detector L2 gathers (plans autotuned keep their pick).
- *   "fwd_ell"          1 = plans not autotuned run the DAS forward on the
- *                      interleaved (per-warp) copy of its entry table; 0 (default) = off.
+ *   "fwd_ell"          1 (default) = plans not autotuned run the DAS forward on
+ *                      the interleaved (per-warp) copy of its entry table;
+ *                      0 = the choice "fwd_staged" makes.
+ *   "fwd_staged"       with "fwd_ell" 0: 1 (default) = the DAS forward stages
+ *                      each CTA's image values in shared memory where the
+ *                      plan's tables fit, 0 = per-detector gathers on the CSR
+ *                      table (plans autotuned keep their pick; all forms give
+ *                      the same sums).
  *   "fwd_staged_tile", "fwd_staged_group"  time samples per CTA (8 .. 64) and
  *                      detectors per CTA (1 .. 16) of the staged forward's
  *                      tables in plans created afterwards; 0 (default) = the

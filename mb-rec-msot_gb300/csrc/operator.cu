@@ -1344,14 +1344,15 @@ int launch_to_pixmajor(const Plan &pl, const float *in, float *out, int W, cudaS
 
 // DAS forward by bucket moments; xpm is [W/WT][P][WT].
 std::atomic<int> g_fwd_staged{1};
-std::atomic<int> g_fwd_ell{0};
+std::atomic<int> g_fwd_ell{1};
 
-// the DAS forward kernel: the autotuner's pick, else 4 (interleaved entry
-// table) when msot_tune_set("fwd_ell") is on, else 1 (staged) or 2
-// (k_das_fwd3 on the CSR table) by msot_tune_set("fwd_staged")
+// the DAS forward kernel: the autotuner's pick, else 4 (the interleaved
+// entry table, the fastest on GB300) when msot_tune_set("fwd_ell") is on
+// (default) and the plan has the table, else 1 (staged) or 2 (k_das_fwd3 on
+// the CSR table) by msot_tune_set("fwd_staged"); all give the same sums
 static int fwd_kernel(const Plan &pl) {
     if (pl.tune_fwd_staged) return pl.tune_fwd_staged;
-    if (g_fwd_ell.load()) return 4;
+    if (g_fwd_ell.load() && pl.fwd_ell_off) return 4;
     return g_fwd_staged.load() ? 1 : 2;
 }
 

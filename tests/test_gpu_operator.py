@@ -229,11 +229,33 @@ def test_interleaved_entry_table_forward_is_bit_identical(cuda, W, fmt):
     pm.set_storage(fmt)
     x = torch.rand((W, 64, 64), device="cuda", generator=torch.Generator("cuda").manual_seed(9))
     _lib.check(L.msot_tune_set(b"fwd_staged", 0))
+    _lib.check(L.msot_tune_set(b"fwd_ell", 0))
     try:
         y_csr = pm.forward(x).cpu().numpy()
         _lib.check(L.msot_tune_set(b"fwd_ell", 1))
         y_ell = pm.forward(x).cpu().numpy()
     finally:
-        _lib.check(L.msot_tune_set(b"fwd_ell", 0))
+        _lib.check(L.msot_tune_set(b"fwd_ell", 1))
         _lib.check(L.msot_tune_set(b"fwd_staged", 1))
     assert np.array_equal(y_csr, y_ell)
+
+
+def test_staged_forward_matches_the_per_detector_forward(cuda):
+    # the staged kernel (pixel unions in shared memory, packed FMAs) sums the
+    # same bucket moments as k_das_fwd3 on the CSR table
+    import torch
+    from msot_gb300 import _lib
+    L = _lib.load()
+    pm, _ = make_pair(n=64, n_det=128, n_samples=1200, radius=0.02, fov_half=0.0063,
+                      max_batch=8)
+    x = torch.rand((8, 64, 64), device="cuda", generator=torch.Generator("cuda").manual_seed(4))
+    _lib.check(L.msot_tune_set(b"fwd_ell", 0))
+    try:
+        _lib.check(L.msot_tune_set(b"fwd_staged", 0))
+        y_csr = pm.forward(x).cpu().numpy()
+        _lib.check(L.msot_tune_set(b"fwd_staged", 1))
+        y_st = pm.forward(x).cpu().numpy()
+    finally:
+        _lib.check(L.msot_tune_set(b"fwd_staged", 1))
+        _lib.check(L.msot_tune_set(b"fwd_ell", 1))
+    assert rel(y_st, y_csr) <= 1e-6
