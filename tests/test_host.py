@@ -210,6 +210,18 @@ def test_new_entry_points_reject_bad_arguments_without_a_device():
         (lambda: L.msot_l2_gather_probe(1024, ctypes.cast(out, D)), b"l2_gather_probe"),
         (lambda: L.msot_tune_set(b"no_such_knob", 1), b"tune_set"),
         (lambda: L.msot_tune_set(b"conv_min_blocks", 2), b"tune_set"),
+        (lambda: L.msot_tune_set(b"fwd_ell", 2), b"tune_set"),
+        (lambda: L.msot_tune_set(b"tv_prox_cluster", -2), b"tune_set"),
+        # storage format outside 0 .. 2, no plan
+        (lambda: L.msot_plan_set_storage(None, 3, 0), b"plan_set_storage"),
+        (lambda: L.msot_plan_set_storage(None, 2, 0), b"plan_set_storage"),
+        # the state-returning L2 solve: no plan / no v output / v0 without w0
+        (lambda: L.msot_rec_nn_with_L2_reg_state(None, None, None, None, 1, 1, 1e-2, None,
+                                                 None, 0, None, None, None),
+         b"rec_nn_with_L2_reg_state"),
+        # U-Net input channels 1 .. 8
+        (lambda: L.msot_unet_create_ch(3, 8, 0, 32, 4, 0, ctypes.byref(h)), b"unet_create"),
+        (lambda: L.msot_unet_create_ch(3, 8, 9, 32, 4, 0, ctypes.byref(h)), b"unet_create"),
     ]
     for call, where in cases:
         rc = call()
@@ -507,3 +519,25 @@ def test_model_struct_views_run_reference_style_code(monkeypatch):
     assert args[8:13] == (1480.0, probe.fs, 13.0, 135.0, 0.02)
     A.reconstruct_dmas_cf(model, sinogram)
     assert fake.calls[-1][1][8:13] == args[8:13]
+
+
+def test_storage_and_warm_start_wrappers(monkeypatch):
+    """set_storage maps 'fp32' / 'bf16' / 'fp16' (and the booleans) to the
+    library's formats 0 / 1 / 2 and rejects anything else; the trajectory
+    input of the learned warm start needs 0 < m < input_iters, checked before
+    any network is built."""
+    from msot_gb300 import MSOTmodel, Discretization, Probe
+    from msot_gb300.warmstart import LearnedWarmStart
+    fake = _host_only(monkeypatch)
+    probe = Probe(n_det=16, radius=0.02, angular_coverage=135.0, n_samples=400, eir_length=33)
+    disc = Discretization([-0.002, 0.002], 16)
+    m = MSOTmodel(probe, disc, 1500.0, False, True, 0, 1e5, 12e6, 2.5, max_batch=2)
+    for arg, code in (("fp32", 0), (False, 0), ("bf16", 1), (True, 1), ("fp16", 2)):
+        m.set_storage(arg, 3)
+        name, args = fake.calls[-1]
+        assert name == "msot_plan_set_storage" and args[1:] == (code, 3)
+    with pytest.raises(ValueError):
+        m.set_storage("fp8")
+    for traj, iters in ((5, 5), (3, 0), (-1, 4)):
+        with pytest.raises(ValueError, match="trajectory"):
+            LearnedWarmStart(m, 1e-2, input_iters=iters, trajectory=traj)
