@@ -134,6 +134,27 @@ const char *set_error(const char *fmt, ...);
 // different sizes used from several threads must not shrink it between
 // another thread's setting and launch.  Thread-safe.  plan.cu
 cudaError_t raise_max_dynamic_smem(const void *func, size_t bytes);
+// a kernel's dynamic shared memory limit raised to `bytes` where above 48 KB
+template <class K>
+inline int set_smem(K kern, size_t bytes) {
+    if (bytes > 48 * 1024) {
+        cudaError_t e = raise_max_dynamic_smem((const void *)kern, bytes);
+        if (e != cudaSuccess) {
+            set_error("cudaFuncSetAttribute(smem=%zu): %s", bytes, cudaGetErrorString(e));
+            return MSOT_ECUDA;
+        }
+    }
+    return MSOT_OK;
+}
+// k_das_fwd3 launches per storage format of the interpolation input (xpm of
+// FP32, BF16 or FP16 values; inv_s: the FP16 inverse scales, else null)
+int das_fwd_run_f32(const Plan &pl, const void *xpm, float *raw, int W, float scale,
+                    const float *inv_s, bool ell, int wt, cudaStream_t st);
+int das_fwd_run_bf16(const Plan &pl, const void *xpm, float *raw, int W, float scale,
+                     const float *inv_s, bool ell, int wt, cudaStream_t st);
+int das_fwd_run_f16(const Plan &pl, const void *xpm, float *raw, int W, float scale,
+                    const float *inv_s, bool ell, int wt, cudaStream_t st);
+
 
 // tensor-core convolutions of the warm-start U-Net on (1) or off (0); unet.cu
 extern std::atomic<int> g_unet_tc;
