@@ -8,11 +8,12 @@
 //                  and the SIR path's pixel order.
 //   k_to_pixmajor / k_permute  instance-major image -> the pixel-major (and,
 //                  with SIR, tile-permuted) order the interpolation gathers.
-//   k_das_fwd3     forwardDelayAndSumMex.cpp:72-103 restated exactly by the
-//                  bucket decomposition of the tri taps: per (time tile,
-//                  detector, instances) CTA, bucket moments over the pixels
-//                  whose travel time falls in each sample, then the 2F+2-tap
-//                  filter over the moments; no atomics.
+//   k_das_fwd3     (das_fwd.cuh, launched from here) forwardDelayAndSumMex.cpp:
+//                  72-103 restated exactly by the bucket decomposition of the
+//                  tri taps: per (time tile, detector, instances) CTA, bucket
+//                  moments over the pixels whose travel time falls in each
+//                  sample, then the 2F+2-tap filter over the moments; no
+//                  atomics.
 //   k_das_adj4 + k_sum_parts  transposeDelayAndSumMex.cpp:67-97: per 64x64
 //                  pixel block and detector group, the block's sinogram span
 //                  filtered once into bucket tables in shared memory; groups'
@@ -22,7 +23,8 @@
 //   k_sir_adj     transposeMex.cpp:115-158 (its exact adjoint).
 //   k_conv_fft1k  convolve_with_IR / transpose_convolve_with_IR
 //                 (MSOTmodel.m:259-269) by overlap-save with 1024-point FFTs,
-//                 two real columns per complex transform; with EPI set it also
+//                 two real columns per complex transform, split-complex
+//                 packed FP32x2 butterflies; with EPI set it also
 //                 writes the L2 solver's LSQR sinogram update (IRs up to 513
 //                 taps).  k_conv_fft (4096 points) takes IRs of 514-2049
 //                 taps, the direct FIR k_conv longer ones.
