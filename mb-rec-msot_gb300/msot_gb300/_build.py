@@ -62,7 +62,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
             print(" ".join(cmd))
         return obj
 
-    with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+    with ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 8))) as ex:
         list(ex.map(compile_one, zip(srcs, objs)))
     if force or _stale(LIB_PATH, objs):
         cmd = [nv, *ARCH_FLAGS, "-shared", "-o", LIB_PATH, *objs, "-lcudart"]
