@@ -110,7 +110,7 @@ int msot_interp_transpose(msot_plan_t plan, const float *d_raw, float *d_coeffs,
  * exactly); 0: FP32 (default).  refine_every = k > 0: the L1 solver runs
  * every k-th outer iteration with the FP32 input (the other solvers use the
  * setting as is).  The FP32 default meets the operators' 1e-5 bar; 16-bit
- * storage is for solves judged by their 1e-3 bar against the FP64 oracle.
+ * storage is for solves held to their 1e-3 bar against the FP64 oracle.
  * Plans without SIR only; drops the plan's captured solver graphs. */
 int msot_plan_set_storage(msot_plan_t plan, int image_format, int refine_every);
 
